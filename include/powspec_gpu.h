@@ -1,0 +1,158 @@
+/*
+ * powspec_gpu.h -- C ABI of the GB300 (sm_103a) periodic-box P_l(k) path.
+ *
+ * Drop-in boundary for powspec's hot path.  The reference computes it in two
+ * calls from main (src/powspec.c:47,55):
+ *
+ *   MESH *genr_mesh(const CONF *conf, CATA *cat);          src/genr_mesh.c:874
+ *   PK   *powspec(const CONF *conf, const CATA *cat, MESH *mesh);
+ *                                                          src/multipole.c:1179
+ *
+ * Here the same work is an opaque context driven by plain pointers and sizes:
+ * ps_gpu_create (mesh_init + powspec_init + powspec_precomp),
+ * ps_gpu_assign_* (one catalogue's part of gen_dens), ps_gpu_execute
+ * (dens_k0 + count_mode + normalisation) and ps_gpu_destroy (mesh_destroy +
+ * powspec_destroy).  Every entry point returns 0 or a negative status whose
+ * values extend the reference's POWSPEC_ERR_* codes (src/define.h:112-124);
+ * none of them exits the process.  One context per host thread; each
+ * context owns one CUDA stream.  There is no CPU fallback: without a usable
+ * GPU every call that needs one fails with PS_GPU_ERR_CUDA.
+ */
+#ifndef POWSPEC_GPU_H
+#define POWSPEC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PS_GPU_ABI_VERSION 1
+
+/* Status codes.  The first block mirrors src/define.h:112-124. */
+#define PS_GPU_OK 0
+#define PS_GPU_ERR_MEMORY (-1)  /* POWSPEC_ERR_MEMORY: host or device allocation */
+#define PS_GPU_ERR_ARG (-2)     /* POWSPEC_ERR_ARG: invalid argument */
+#define PS_GPU_ERR_CATA (-11)   /* POWSPEC_ERR_CATA: particle outside [0, BOX_SIZE) */
+#define PS_GPU_ERR_MESH (-13)   /* POWSPEC_ERR_MESH */
+#define PS_GPU_ERR_PK (-14)     /* POWSPEC_ERR_PK: bin definition (src/multipole.c:344-356) */
+#define PS_GPU_ERR_CUDA (-20)   /* CUDA runtime error or no usable device */
+#define PS_GPU_ERR_STATE (-21)  /* call order: execute before every catalogue was assigned */
+#define PS_GPU_ERR_RANGE (-22)  /* total |weight| too large for the fixed-point mesh */
+
+/* Particle assignment schemes (src/genr_mesh.h:37-42). */
+#define PS_ASSIGN_NGP 0
+#define PS_ASSIGN_CIC 1
+#define PS_ASSIGN_TSC 2
+#define PS_ASSIGN_PCS 3
+
+/* Estimator settings.  Every field has the meaning of the CONF field of the
+ * same role after load_conf (src/load_conf.h:40-117); in particular kmin and
+ * kmax are log10 values when logscale is set (src/load_conf.c:1352-1354) and
+ * kmax <= 0 means "unset" (POWSPEC_KMAX_ISSET, src/define.h:68). */
+typedef struct {
+  int ng;            /* GRID_SIZE: even, with ng/2 a product of 2, 3 and 5 */
+  double box[3];     /* BOX_SIZE */
+  int assign;        /* PARTICLE_ASSIGN */
+  int interlace;     /* GRID_INTERLACE */
+  int ncat;          /* number of data catalogues: 1 or 2 */
+  int isauto[2];     /* auto spectra wanted (OUTPUT_AUTO set) */
+  int iscross;       /* cross spectrum wanted (OUTPUT_CROSS set, ncat == 2) */
+  double los[3];     /* LINE_OF_SIGHT */
+  double kmin, kmax; /* KMIN, KMAX */
+  double dk;         /* BIN_SIZE */
+  int logscale;      /* LOG_SCALE */
+  int npole;         /* number of multipoles */
+  int poles[7];      /* MULTIPOLE: sorted, unique, 0..6 */
+  int device;        /* CUDA device ordinal */
+} ps_gpu_params;
+
+/* Outputs of ps_gpu_execute; arrays are caller-owned and sized with
+ * ps_gpu_nbin().  Field names follow PK (src/multipole.h:38-61). */
+typedef struct {
+  int nbin;          /* out */
+  double *k;         /* [nbin]   bin centres */
+  double *kedge;     /* [nbin+1] bin edges */
+  double *km;        /* [nbin]   mean |k| of the modes in each bin */
+  uint64_t *cnt;     /* [nbin]   mode counts (bit-exact with the reference) */
+  double *lcnt;      /* [npole*nbin] sum of weight * L_l(mu) per bin */
+  double *pl;        /* [2][npole][nbin] auto multipoles (NULL: not copied) */
+  double *xpl;       /* [npole][nbin] cross multipoles (NULL: not copied) */
+  double shot[2];    /* out: V / W (src/genr_mesh.c:907) */
+  double norm[2];    /* out: W^2 / V (src/genr_mesh.c:908) */
+  double wdata[2];   /* out: W = sum of weights */
+} ps_gpu_result;
+
+typedef struct ps_gpu_ctx ps_gpu_ctx;
+
+/* Validates the settings, defines the bins (src/multipole.c:334-394),
+ * allocates the device meshes, and builds the geometry tables: bin of every
+ * squared lattice vector, mode counts, mean |k| and the multipole mode
+ * weights (src/multipole.c:111-257, which depend on the geometry only). */
+int ps_gpu_create(const ps_gpu_params *params, ps_gpu_ctx **ctx);
+
+/* Frees everything the context owns (src/genr_mesh.c:615, src/multipole.c:270). */
+void ps_gpu_destroy(ps_gpu_ctx *ctx);
+
+/* Number of k bins; < 0 on error. */
+int ps_gpu_nbin(const ps_gpu_ctx *ctx);
+
+/* Assigns catalogue `cat` (0 or 1) to its mesh(es) with the configured
+ * scheme (src/genr_mesh.c:793-848 for CUBIC_SIM).  Positions must lie in
+ * [0, BOX_SIZE) (src/genr_mesh.c:523-531).
+ *   _aos:  xyzw = n records {double x, y, z, w} -- the reference DATA
+ *          layout (src/read_cata.h:42-45).
+ *   _soa:  four float arrays x[n], y[n], z[n], w[n] (w may be NULL: unit
+ *          weights).
+ * on_device = 0: host pointers (copied through a pinned staging buffer);
+ * on_device = 1: pointers already in this device's memory.  Asynchronous on
+ * the context stream; errors from out-of-range particles are reported by
+ * ps_gpu_execute. */
+int ps_gpu_assign_aos(ps_gpu_ctx *ctx, int cat, const double *xyzw, size_t n,
+                      int on_device);
+int ps_gpu_assign_soa(ps_gpu_ctx *ctx, int cat, const float *x,
+                      const float *y, const float *z, const float *w,
+                      size_t n, int on_device);
+
+/* FFTs, interlace combine, window compensation, binning and normalisation
+ * (src/multipole.c:435-505, :778-1087, :1267-1274).  Blocks until the
+ * results are on the host. */
+int ps_gpu_execute(ps_gpu_ctx *ctx, ps_gpu_result *res);
+
+/* Last error message of this context (never NULL). */
+const char *ps_gpu_last_error(const ps_gpu_ctx *ctx);
+
+/* Device time in milliseconds of the phases of the last execute, measured
+ * with CUDA events on the context stream: [0] assignment (all catalogues),
+ * [1] z transform, [2] y transform, [3] x transform + combine + binning,
+ * [4] reduction, [5] total.  Returns the number of entries written. */
+int ps_gpu_last_timings(const ps_gpu_ctx *ctx, float *ms, int nmax);
+
+/* Number of kernel launches issued by the last assign+execute cycle. */
+int ps_gpu_last_launches(const ps_gpu_ctx *ctx);
+
+/* ---- Stage-level entry points (checked against the oracle stage by stage) */
+
+/* Copies mesh m (0: Fr, 1: Frl) of catalogue cat to the host as doubles,
+ * row-major [ng][ng][ng].  Valid between assign and execute. */
+int ps_gpu_read_mesh(ps_gpu_ctx *ctx, int cat, int m, double *out);
+
+/* Standalone r2c 3-D FFT of a real FP32 cube [ng][ng][ng] (host memory)
+ * into the FFTW half-complex layout [ng][ng][ng/2+1] of interleaved FP32
+ * (re, im) (host memory).  Uses ctx's device buffers of mesh 0 of
+ * catalogue 0. */
+int ps_gpu_fft_r2c_host(ps_gpu_ctx *ctx, const float *in, float *out);
+
+/* Binning sweep alone over given half-complex FP32 field(s) in FFTW layout
+ * (host memory), with the window of the configured scheme: f1 == f2 gives
+ * an auto spectrum.  Writes the unnormalised sums
+ * pl[npole][nbin] = sum p L_l(mu) (src/multipole.c:815-880). */
+int ps_gpu_bin_fields_host(ps_gpu_ctx *ctx, const float *f1, const float *f2,
+                           double *pl);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,274 @@
+"""powspec_gb300 -- GB300 (sm_103a) periodic-box P_l(k) estimator.
+
+Python view of the C ABI in ``include/powspec_gpu.h`` (libpowspec_gpu.so),
+used by the tests and the benchmark.  The estimator itself runs entirely in
+the CUDA library; there is no CPU fallback: loading fails loudly when the
+library is missing, and every call fails when no GPU is usable.
+
+The two reference entry points map onto one context:
+
+* ``genr_mesh(conf, cat)``   (src/genr_mesh.c:874) -> ``Estimator.assign``
+* ``powspec(conf, cat, mesh)`` (src/multipole.c:1179) -> ``Estimator.execute``
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpowspec_gpu.so")
+
+# status codes (include/powspec_gpu.h)
+ERRORS = {
+    -1: "PS_GPU_ERR_MEMORY", -2: "PS_GPU_ERR_ARG", -11: "PS_GPU_ERR_CATA",
+    -13: "PS_GPU_ERR_MESH", -14: "PS_GPU_ERR_PK", -20: "PS_GPU_ERR_CUDA",
+    -21: "PS_GPU_ERR_STATE", -22: "PS_GPU_ERR_RANGE",
+}
+ASSIGN = {"NGP": 0, "CIC": 1, "TSC": 2, "PCS": 3}
+
+EXPORTED = [
+    "ps_gpu_create", "ps_gpu_destroy", "ps_gpu_nbin", "ps_gpu_assign_aos",
+    "ps_gpu_assign_soa", "ps_gpu_execute", "ps_gpu_last_error",
+    "ps_gpu_last_timings", "ps_gpu_last_launches", "ps_gpu_read_mesh",
+    "ps_gpu_fft_r2c_host", "ps_gpu_bin_fields_host",
+]
+
+
+class PowspecError(RuntimeError):
+    def __init__(self, code, msg=""):
+        self.code = code
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("ng", ctypes.c_int),
+        ("box", ctypes.c_double * 3),
+        ("assign", ctypes.c_int),
+        ("interlace", ctypes.c_int),
+        ("ncat", ctypes.c_int),
+        ("isauto", ctypes.c_int * 2),
+        ("iscross", ctypes.c_int),
+        ("los", ctypes.c_double * 3),
+        ("kmin", ctypes.c_double),
+        ("kmax", ctypes.c_double),
+        ("dk", ctypes.c_double),
+        ("logscale", ctypes.c_int),
+        ("npole", ctypes.c_int),
+        ("poles", ctypes.c_int * 7),
+        ("device", ctypes.c_int),
+    ]
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class Result(ctypes.Structure):
+    _fields_ = [
+        ("nbin", ctypes.c_int),
+        ("k", _dp),
+        ("kedge", _dp),
+        ("km", _dp),
+        ("cnt", ctypes.POINTER(ctypes.c_uint64)),
+        ("lcnt", _dp),
+        ("pl", _dp),
+        ("xpl", _dp),
+        ("shot", ctypes.c_double * 2),
+        ("norm", ctypes.c_double * 2),
+        ("wdata", ctypes.c_double * 2),
+    ]
+
+
+_lib = None
+
+
+def build(verbose=False):
+    from . import buildlib
+    return buildlib.build(verbose=verbose)
+
+
+def lib():
+    """Load libpowspec_gpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} not built: run powspec_gb300.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        L.ps_gpu_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_void_p)]
+        L.ps_gpu_destroy.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_destroy.restype = None
+        L.ps_gpu_nbin.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_assign_aos.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.c_int]
+        L.ps_gpu_assign_soa.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4 + [
+            ctypes.c_size_t, ctypes.c_int]
+        L.ps_gpu_execute.argtypes = [ctypes.c_void_p, ctypes.POINTER(Result)]
+        L.ps_gpu_last_error.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_last_error.restype = ctypes.c_char_p
+        L.ps_gpu_last_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.ps_gpu_last_launches.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_read_mesh.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.ps_gpu_fft_r2c_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.ps_gpu_bin_fields_host.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
+        _lib = L
+    return _lib
+
+
+@dataclass
+class Spectrum:
+    nbin: int
+    k: np.ndarray
+    kedge: np.ndarray
+    km: np.ndarray
+    cnt: np.ndarray
+    lcnt: np.ndarray
+    pl: np.ndarray    # [2, npole, nbin]
+    xpl: np.ndarray   # [npole, nbin]
+    shot: np.ndarray
+    norm: np.ndarray
+    wdata: np.ndarray
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Estimator:
+    """One GPU context: settings with the meaning of the reference's CONF."""
+
+    def __init__(self, ng, box=1000.0, assign=1, interlace=False, ncat=1,
+                 poles=(0, 2, 4), los=(0.0, 0.0, 1.0), kmin=0.0, kmax=-1.0, dk=0.005,
+                 logscale=False, isauto=(True, True), iscross=True, device=0):
+        L = lib()
+        if isinstance(assign, str):
+            assign = ASSIGN[assign.upper()]
+        p = Params()
+        p.ng = int(ng)
+        b = box if isinstance(box, (tuple, list)) else (box, box, box)
+        p.box = (ctypes.c_double * 3)(*[float(x) for x in b])
+        p.assign = int(assign)
+        p.interlace = int(bool(interlace))
+        p.ncat = int(ncat)
+        p.isauto = (ctypes.c_int * 2)(*[int(bool(x)) for x in isauto])
+        p.iscross = int(bool(iscross) and ncat == 2)
+        p.los = (ctypes.c_double * 3)(*[float(x) for x in los])
+        p.kmin, p.kmax, p.dk = float(kmin), float(kmax), float(dk)
+        p.logscale = int(bool(logscale))
+        poles = sorted(set(int(x) for x in poles))
+        p.npole = len(poles)
+        p.poles = (ctypes.c_int * 7)(*poles)
+        p.device = int(device)
+        self.params = p
+        self.poles = poles
+        self.ncat = int(ncat)
+        self._ctx = ctypes.c_void_p()
+        rc = L.ps_gpu_create(ctypes.byref(p), ctypes.byref(self._ctx))
+        if rc:
+            msg = self.last_error()
+            self.close()
+            raise PowspecError(rc, msg)
+        self.nbin = L.ps_gpu_nbin(self._ctx)
+
+    def last_error(self):
+        if not self._ctx:
+            return "context not created"
+        return lib().ps_gpu_last_error(self._ctx).decode()
+
+    def close(self):
+        if self._ctx:
+            lib().ps_gpu_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise PowspecError(rc, self.last_error())
+
+    # -- gen_dens for one catalogue
+    def assign(self, cat, particles=None, *, x=None, y=None, z=None, w=None, on_device=False,
+               n=None):
+        """AoS float64 [N,4] (host numpy or device pointer with n=...) or SoA float32."""
+        L = lib()
+        if particles is not None:
+            if on_device:
+                self._check(L.ps_gpu_assign_aos(self._ctx, cat, ctypes.c_void_p(particles), n, 1))
+            else:
+                a = np.ascontiguousarray(particles, dtype=np.float64)
+                self._keep = a
+                self._check(L.ps_gpu_assign_aos(self._ctx, cat, _ptr(a), len(a), 0))
+        else:
+            if on_device:
+                self._check(L.ps_gpu_assign_soa(self._ctx, cat, ctypes.c_void_p(x), ctypes.c_void_p(y),
+                                                ctypes.c_void_p(z),
+                                                ctypes.c_void_p(w) if w else None, n, 1))
+            else:
+                arrs = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+                wa = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+                self._keep = (arrs, wa)
+                self._check(L.ps_gpu_assign_soa(self._ctx, cat, _ptr(arrs[0]), _ptr(arrs[1]),
+                                                _ptr(arrs[2]), _ptr(wa), len(arrs[0]), 0))
+
+    def execute(self) -> Spectrum:
+        nb, npole = self.nbin, len(self.poles)
+        out = dict(k=np.zeros(nb), kedge=np.zeros(nb + 1), km=np.zeros(nb),
+                   cnt=np.zeros(nb, np.uint64), lcnt=np.zeros((npole, nb)),
+                   pl=np.zeros((2, npole, nb)), xpl=np.zeros((npole, nb)))
+        r = Result()
+        r.k = out["k"].ctypes.data_as(_dp)
+        r.kedge = out["kedge"].ctypes.data_as(_dp)
+        r.km = out["km"].ctypes.data_as(_dp)
+        r.cnt = out["cnt"].ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+        r.lcnt = out["lcnt"].ctypes.data_as(_dp)
+        r.pl = out["pl"].ctypes.data_as(_dp)
+        r.xpl = out["xpl"].ctypes.data_as(_dp)
+        self._check(lib().ps_gpu_execute(self._ctx, ctypes.byref(r)))
+        return Spectrum(nbin=r.nbin, shot=np.array(r.shot[:]), norm=np.array(r.norm[:]),
+                        wdata=np.array(r.wdata[:]), **out)
+
+    def run(self, cats):
+        for i, c in enumerate(cats):
+            self.assign(i, c)
+        return self.execute()
+
+    def timings(self):
+        t = np.zeros(6, np.float32)
+        lib().ps_gpu_last_timings(self._ctx, _ptr(t), 6)
+        return t
+
+    def launches(self):
+        return lib().ps_gpu_last_launches(self._ctx)
+
+    # -- stage-level entry points
+    def read_mesh(self, cat=0, m=0):
+        ng = self.params.ng
+        out = np.zeros((ng, ng, ng))
+        self._check(lib().ps_gpu_read_mesh(self._ctx, cat, m, _ptr(out)))
+        return out
+
+    def fft_r2c(self, real):
+        ng = self.params.ng
+        a = np.ascontiguousarray(real, dtype=np.float32)
+        out = np.zeros((ng, ng, ng // 2 + 1), np.complex64)
+        self._check(lib().ps_gpu_fft_r2c_host(self._ctx, _ptr(a), _ptr(out)))
+        return out
+
+    def bin_fields(self, f1, f2=None):
+        a = np.ascontiguousarray(f1, dtype=np.complex64)
+        b = a if f2 is None else np.ascontiguousarray(f2, dtype=np.complex64)
+        out = np.zeros((len(self.poles), self.nbin))
+        self._check(lib().ps_gpu_bin_fields_host(self._ctx, _ptr(a), _ptr(b), _ptr(out)))
+        return out

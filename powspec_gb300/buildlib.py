@@ -1,0 +1,103 @@
+"""Build recipe of libpowspec_gpu.so (sm_103a only) and the C host CLI.
+
+Compiles every CUDA translation unit of ``powspec_gb300/csrc`` in parallel
+with ``nvcc -gencode arch=compute_103a,code=sm_103a`` and links the shared
+library in-tree (``powspec_gb300/libpowspec_gpu.so``).  No cmake, no torch.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+HOST = os.path.join(HERE, "host")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libpowspec_gpu.so")
+CLI = os.path.join(HERE, "powspec_gpu")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+
+
+def nvcc():
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(exe):
+        raise RuntimeError("nvcc not found")
+    return exe
+
+
+def _sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def _headers():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    hs.append(os.path.join(ROOT, "include", "powspec_gpu.h"))
+    return hs
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(src, verbose=False):
+    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+    if not _stale(obj, [src] + _headers()):
+        return obj
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+    if verbose:
+        cmd.append("-Xptxas=-v")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")
+    if verbose and r.stderr:
+        sys.stderr.write(r.stderr)
+    return obj
+
+
+def build_lib(verbose=False, jobs=None):
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = _sources()
+    with cf.ThreadPoolExecutor(max_workers=jobs or len(srcs)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
+    if _stale(LIB, objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"link failed:\n{r.stderr}")
+    return LIB
+
+
+def build_cli():
+    """The C host program (powspec.conf / CLI / output format)."""
+    srcs = sorted(os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".c")) \
+        if os.path.isdir(HOST) else []
+    if not srcs:
+        return None
+    deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")] + [LIB]
+    if _stale(CLI, deps):
+        cmd = ["gcc", "-std=c99", "-O2", "-Wall", "-o", CLI] + srcs + [
+            "-I" + os.path.join(ROOT, "include"), "-I" + HOST,
+            "-L" + HERE, "-lpowspec_gpu", "-Wl,-rpath,$ORIGIN", "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"host CLI build failed:\n{r.stderr}")
+    return CLI
+
+
+def build(verbose=False):
+    lib = build_lib(verbose=verbose)
+    build_cli()
+    return lib
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,414 @@
+// ps_bin.cu -- last FFT pass fused with the interlace combine, the window
+// compensation and the Legendre-weighted binning; plus the stand-alone
+// binning sweep, the geometry sweep and the partial-sum reduction.
+//
+// Reference: dens_k0's interlace combine (src/multipole.c:462-487),
+// count_mode_sim_lin/_log (src/multipole.c:778-1031) and the mode counting
+// of powspec_precomp (src/multipole.c:111-257).
+//
+// Accumulation: every thread walks a run of consecutive modes along x, whose
+// |k| grows monotonically, and keeps the run's sums in registers while the
+// bin stays the same; on a bin change it adds them to FP32 per-tile
+// accumulators in shared memory.  After each tile the touched bins are added
+// into this CTA's FP64 slice of a partial-sum array in global memory, which
+// a final kernel reduces over CTAs in a fixed order.
+#include "ps_internal.h"
+
+namespace ps {
+namespace {
+
+constexpr int kRun = 8;  // consecutive modes per thread
+
+template <int NSPEC>
+struct RunAcc {
+  int bin;
+  float v[NSPEC][kMaxPole];
+};
+
+template <int NSPEC>
+__device__ __forceinline__ void run_flush(RunAcc<NSPEC>& ra, float* tacc, int npole, int nbin,
+                                          int& lo, int& hi) {
+  if (ra.bin < 0) return;
+#pragma unroll
+  for (int s = 0; s < NSPEC; s++)
+#pragma unroll
+    for (int l = 0; l < kMaxPole; l++)
+      if (l < npole) {
+        if (ra.v[s][l] != 0.f) atomicAdd(&tacc[(s * npole + l) * nbin + ra.bin], ra.v[s][l]);
+        ra.v[s][l] = 0.f;
+      }
+  lo = min(lo, ra.bin);
+  hi = max(hi, ra.bin);
+}
+
+// Adds one mode with power p[s] (already windowed and weighted) at mu.
+template <int NSPEC>
+__device__ __forceinline__ void run_add(RunAcc<NSPEC>& ra, const ModeGeom& g, int b,
+                                        const float (&p)[NSPEC], float mu, bool skip_odd,
+                                        float* tacc, int& lo, int& hi) {
+  if (b != ra.bin) {
+    run_flush<NSPEC>(ra, tacc, g.npole, g.nbin, lo, hi);
+    ra.bin = b;
+  }
+#pragma unroll
+  for (int l = 0; l < kMaxPole; l++) {
+    if (l < g.npole) {
+      const int ell = g.poles[l];
+      if (skip_odd && (ell & 1)) continue;  // cancels between half-spaces (src/multipole.c:844)
+      const float L = legendre(ell, mu);
+#pragma unroll
+      for (int s = 0; s < NSPEC; s++) ra.v[s][l] = fmaf(p[s], L, ra.v[s][l]);
+    }
+  }
+}
+
+// Merge the FP32 tile accumulators of the touched bin range into the CTA's
+// FP64 slice and clear them.  Ends with a barrier.
+__device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int nbin, int lo,
+                           int hi) {
+  // block-wide min/max of the touched range
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&srange[0], lo);
+    atomicMax(&srange[1], hi);
+  }
+  __syncthreads();
+  const int blo = srange[0], bhi = srange[1];
+  if (bhi >= blo) {
+    const int w = bhi - blo + 1;
+    for (int e = threadIdx.x; e < nacc * w; e += blockDim.x) {
+      const int q = e / w;
+      const int idx = q * nbin + blo + (e - q * w);
+      part[idx] += (double)tacc[idx];
+      tacc[idx] = 0.f;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    srange[0] = 0x7fffffff;
+    srange[1] = -1;
+  }
+  __syncthreads();
+}
+
+// Pass C.  Lines of tile: field f, row r -> smem line f * nl + r.
+template <int NSPEC, bool STORE>
+__global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ PassCArgs a) {
+  extern __shared__ float2 sm[];
+  const int ng = a.ng, ngk = (ng >> 1) + 1, ls = ng + 1, h = ng >> 1;
+  const int nty = (ng + a.ty - 1) / a.ty;
+  const int ntile = ngk * nty;
+  const ModeGeom& g = a.geom;
+  const int nacc = NSPEC * g.npole;
+  const size_t tile_elems = (size_t)a.nfield * a.ty * ls;
+  float2* sm2 = sm + tile_elems;  // second FFT buffer (ping-pong)
+  float* tacc = reinterpret_cast<float*>(sm + 2 * tile_elems);
+  __shared__ int srange[2];
+  double* part = STORE ? nullptr : a.partials + (size_t)blockIdx.x * nacc * g.nbin;
+  if (!STORE) {
+    for (int e = threadIdx.x; e < nacc * g.nbin; e += blockDim.x) tacc[e] = 0.f;
+    if (threadIdx.x == 0) {
+      srange[0] = 0x7fffffff;
+      srange[1] = -1;
+    }
+    __syncthreads();
+  }
+  const int mpc = a.interlace ? 2 : 1;  // meshes per catalogue
+  const bool interlace = a.interlace != 0, two_cat = a.ncat > 1;
+  int spec_a[NSPEC], spec_b[NSPEC];
+#pragma unroll
+  for (int s = 0; s < NSPEC; s++) {
+    spec_a[s] = a.spec_a[s];
+    spec_b[s] = a.spec_b[s];
+  }
+
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int kz = tile / nty;
+    const int ky0 = (tile - kz * nty) * a.ty;
+    const int nl = min(a.ty, ng - ky0);
+    for (int f = 0; f < a.nfield; f++) {
+      const float2* src = a.in[f] + ((size_t)kz * ng + ky0) * ng;
+      for (int e = threadIdx.x; e < nl * h; e += blockDim.x) {
+        const int r = e / h, m = e - r * h;
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(src + (size_t)r * ng) + m);
+        float2* L = sm + (f * nl + r) * ls;
+        L[2 * m] = make_float2(v.x, v.y);
+        L[2 * m + 1] = make_float2(v.z, v.w);
+      }
+    }
+    __syncthreads();
+    const float2* X = fft_lines_pp(sm, sm2, a.plan_full, a.nfield * nl, ls, a.tw_full);
+
+    if (STORE) {
+      // FFTW layout [x][y][kz]; strided stores (diagnostic path only).
+      for (int e = threadIdx.x; e < nl * ng; e += blockDim.x) {
+        const int r = e / ng, i = e - r * ng;
+        a.store[((size_t)i * ng + ky0 + r) * ngk + kz] = X[r * ls + i];
+      }
+      __syncthreads();
+      continue;
+    }
+
+    const bool twice = !(kz == 0 || 2 * kz == ng);
+    const float wk = twice ? 2.f : 1.f;
+    const float kzf = g.vec[2] * (float)kz;
+    const int chunks = (ng + kRun - 1) / kRun;
+    int lo = 0x7fffffff, hi = -1;
+    for (int e = threadIdx.x; e < nl * chunks; e += blockDim.x) {
+      const int r = e / chunks;
+      const int i0 = (e - r * chunks) * kRun;
+      const int ky = ky0 + r;
+      const int jp = dsigned(ky, ng), ja = abs(jp);
+      const float wjk = __ldg(&g.win[ng + ky]) * __ldg(&g.win[2 * ng + kz]) * wk;
+      const float kyf = g.vec[1] * (float)jp;
+      const float mu_yz = kyf * g.los[1] + kzf * g.los[2];
+      const float k2_yz = kyf * kyf + kzf * kzf;
+      const int n_yz = ja * ja + kz * kz;
+      RunAcc<NSPEC> ra;
+      ra.bin = -1;
+#pragma unroll
+      for (int s = 0; s < NSPEC; s++)
+#pragma unroll
+        for (int l = 0; l < kMaxPole; l++) ra.v[s][l] = 0.f;
+      const int iend = min(i0 + kRun, ng);
+      for (int i = i0; i < iend; i++) {
+        const int ip = dsigned(i, ng), ia = abs(ip);
+        const int n = ia * ia + n_yz;
+        if (n == 0) continue;  // DC (src/multipole.c:806)
+        const int b = mode_bin(g, ia, ja, kz, n);
+        if (b < 0) continue;
+        // combined field of each catalogue: (F0 + exp(i theta) F1) / 2
+        float2 G0 = X[r * ls + i], G1 = G0;
+        if (interlace) {
+          const float2 ph = __ldg(&g.phase[ip + jp + kz + ng]);
+          const float2 t = cmul(ph, X[(nl + r) * ls + i]);
+          G0 = make_float2(0.5f * (G0.x + t.x), 0.5f * (G0.y + t.y));
+        }
+        if (two_cat) {
+          G1 = X[(mpc * nl + r) * ls + i];
+          if (interlace) {
+            const float2 ph = __ldg(&g.phase[ip + jp + kz + ng]);
+            const float2 t = cmul(ph, X[((mpc + 1) * nl + r) * ls + i]);
+            G1 = make_float2(0.5f * (G1.x + t.x), 0.5f * (G1.y + t.y));
+          }
+        }
+        const float wwin = __ldg(&g.win[i]) * wjk;
+        float p[NSPEC];
+#pragma unroll
+        for (int s = 0; s < NSPEC; s++) {
+          const float2 A = spec_a[s] ? G1 : G0;
+          const float2 B = spec_b[s] ? G1 : G0;
+          p[s] = (A.x * B.x + A.y * B.y) * wwin;
+        }
+        const float kxf = g.vec[0] * (float)ip;
+        const float mu = (kxf * g.los[0] + mu_yz) * rsqrtf(kxf * kxf + k2_yz);
+        run_add<NSPEC>(ra, g, b, p, mu, twice, tacc, lo, hi);
+      }
+      run_flush<NSPEC>(ra, tacc, g.npole, g.nbin, lo, hi);
+    }
+    __syncthreads();
+    merge_tile(tacc, srange, part, nacc, g.nbin, lo, hi);
+  }
+}
+
+// Stand-alone binning of FFTW-layout fields [x][y][kz]: one line per (x, y).
+__global__ void __launch_bounds__(kFftThreads) k_bin_fields(const __grid_constant__ BinFieldArgs a) {
+  extern __shared__ float smf[];
+  const int ng = a.ng, ngk = (ng >> 1) + 1;
+  const ModeGeom& g = a.geom;
+  const int nacc = g.npole;
+  float* tacc = smf;
+  __shared__ int srange[2];
+  double* part = a.partials + (size_t)blockIdx.x * nacc * g.nbin;
+  for (int e = threadIdx.x; e < nacc * g.nbin; e += blockDim.x) tacc[e] = 0.f;
+  if (threadIdx.x == 0) {
+    srange[0] = 0x7fffffff;
+    srange[1] = -1;
+  }
+  __syncthreads();
+  const int chunks = (ngk + kRun - 1) / kRun;
+  const int rows_per_tile = max(1, kFftThreads / chunks);
+  const int nrows = ng * ng;
+  for (int row0 = blockIdx.x * rows_per_tile; row0 < nrows; row0 += gridDim.x * rows_per_tile) {
+    int lo = 0x7fffffff, hi = -1;
+    for (int e = threadIdx.x; e < rows_per_tile * chunks; e += blockDim.x) {
+      const int rr = e / chunks;
+      const int row = row0 + rr;
+      if (row >= nrows) continue;
+      const int i = row / ng, j = row - i * ng;
+      const int k0 = (e - rr * chunks) * kRun;
+      const int ip = dsigned(i, ng), jp = dsigned(j, ng);
+      const int ia = abs(ip), ja = abs(jp);
+      const float kxf = g.vec[0] * (float)ip, kyf = g.vec[1] * (float)jp;
+      const float wij = __ldg(&g.win[i]) * __ldg(&g.win[ng + j]);
+      RunAcc<1> ra;
+      ra.bin = -1;
+#pragma unroll
+      for (int l = 0; l < kMaxPole; l++) ra.v[0][l] = 0.f;
+      const int kend = min(k0 + kRun, ngk);
+      for (int k = k0; k < kend; k++) {
+        const int n = ia * ia + ja * ja + k * k;
+        if (n == 0) continue;
+        const int b = mode_bin(g, ia, ja, k, n);
+        if (b < 0) continue;
+        const bool twice = !(k == 0 || 2 * k == ng);
+        const size_t idx = (size_t)row * ngk + k;
+        const float2 A = a.f1[idx], B = a.f2[idx];
+        const float wv = wij * __ldg(&g.win[2 * ng + k]) * (twice ? 2.f : 1.f);
+        float p[1] = {(A.x * B.x + A.y * B.y) * wv};
+        const float kzf = g.vec[2] * (float)k;
+        const float mu = (kxf * g.los[0] + kyf * g.los[1] + kzf * g.los[2]) *
+                         rsqrtf(kxf * kxf + kyf * kyf + kzf * kzf);
+        run_add<1>(ra, g, b, p, mu, twice, tacc, lo, hi);
+      }
+      run_flush<1>(ra, tacc, g.npole, g.nbin, lo, hi);
+    }
+    __syncthreads();
+    merge_tile(tacc, srange, part, nacc, g.nbin, lo, hi);
+  }
+}
+
+// Geometry sweep (FP64, once per context): counts with weight 1 on the k = 0
+// and Nyquist planes and 2 between (DC included, src/multipole.c:144-239),
+// sum of weight * |k|, and sum of weight * L_l(mu) without DC
+// (src/multipole.c:806-880), mu = (k . los) / |k| in FP64 as the reference.
+__global__ void __launch_bounds__(256) k_geometry(const __grid_constant__ GeomArgs a) {
+  extern __shared__ double smd[];
+  const ModeGeom& g = a.geom;
+  const int ng = a.ng, ngk = (ng >> 1) + 1, h = ngk;
+  const int nbin = g.nbin, npole = g.npole;
+  double* s_ks = smd;                           // [nbin]
+  double* s_lc = smd + nbin;                    // [npole][nbin]
+  unsigned long long* s_cnt =
+      reinterpret_cast<unsigned long long*>(smd + (size_t)(1 + npole) * nbin);  // [nbin]
+  for (int e = threadIdx.x; e < (2 + npole) * nbin; e += blockDim.x) smd[e] = 0.0;
+  __syncthreads();
+  const size_t nmodes = (size_t)ng * ng * ngk;
+  for (size_t m = (size_t)blockIdx.x * blockDim.x + threadIdx.x; m < nmodes;
+       m += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(m % ngk);
+    const size_t row = m / ngk;
+    const int i = (int)(row / ng), j = (int)(row % ng);
+    const int ip = dsigned(i, ng), jp = dsigned(j, ng);
+    const int ia = abs(ip), ja = abs(jp);
+    const int n = ia * ia + ja * ja + k * k;
+    const int b = mode_bin(g, ia, ja, k, n);
+    if (b < 0) continue;
+    const bool twice = !(k == 0 || 2 * k == ng);
+    const double w = twice ? 2.0 : 1.0;
+    double km2 = __dadd_rn(g.ksq[ia], g.ksq[h + ja]);
+    if (k) km2 = __dadd_rn(km2, g.ksq[2 * h + k]);
+    const double kmod = __dsqrt_rn(km2);
+    atomicAdd(&s_cnt[b], twice ? 2ull : 1ull);
+    atomicAdd(&s_ks[b], w * (g.logscale ? 0.5 * log10(km2) : kmod));
+    if (n == 0) continue;
+    const double ki = __dmul_rn(a.vec[0], (double)ip), kj = __dmul_rn(a.vec[1], (double)jp);
+    const double kk = __dmul_rn(a.vec[2], (double)k);
+    double num = __dadd_rn(__dmul_rn(ki, a.los[0]), __dmul_rn(kj, a.los[1]));
+    if (k) num = __dadd_rn(num, __dmul_rn(kk, a.los[2]));
+    const double mu = __ddiv_rn(num, kmod);
+    const double x2 = mu * mu;
+    for (int l = 0; l < npole; l++) {
+      const int ell = g.poles[l];
+      if (twice && (ell & 1)) continue;
+      double L;
+      switch (ell) {
+        case 0: L = 1.0; break;
+        case 1: L = mu; break;
+        case 2: L = 1.5 * x2 - 0.5; break;
+        case 3: L = 2.5 * mu * (x2 - 0.6); break;
+        case 4: L = 4.375 * x2 * x2 - 3.75 * x2 + 0.375; break;
+        case 5: L = 8.75 * mu * (0.9 * x2 * x2 - x2 + 0.21428571428571427); break;
+        default: L = 14.4375 * x2 * x2 * x2 - 19.6875 * x2 * x2 + 6.5625 * x2 - 0.3125; break;
+      }
+      atomicAdd(&s_lc[l * nbin + b], w * L);
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbin; b += blockDim.x) {
+    if (s_cnt[b]) {
+      atomicAdd(&a.cnt[b], s_cnt[b]);
+      atomicAdd(&a.ksum[b], s_ks[b]);
+    }
+    for (int l = 0; l < npole; l++)
+      if (s_lc[l * nbin + b] != 0.0) atomicAdd(&a.lcnt[l * nbin + b], s_lc[l * nbin + b]);
+  }
+}
+
+__global__ void k_reduce(const double* __restrict__ part, int grid, int width,
+                         double* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= width) return;
+  double s = 0.0;
+  for (int gi = 0; gi < grid; gi++) s += part[(size_t)gi * width + j];
+  out[j] = s;
+}
+
+}  // namespace
+
+size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin) {
+  return 2 * (size_t)nfield * ty * (ng + 1) * sizeof(float2) + (size_t)nacc * nbin * sizeof(float);
+}
+
+int launch_pass_c(const PassCArgs& a, cudaStream_t s) {
+  const int ngk = a.ng / 2 + 1;
+  const int nty = (a.ng + a.ty - 1) / a.ty;
+  const int ntile = ngk * nty;
+  if (a.store) {
+    const size_t smem = pass_c_smem(a.ng, a.ty, a.nfield, 0, 0);
+    cudaFuncSetAttribute(k_pass_c<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    k_pass_c<1, true><<<(unsigned)ntile, kFftThreads, smem, s>>>(a);
+    return 1;
+  }
+  const size_t smem = pass_c_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole, a.geom.nbin);
+  switch (a.nspec) {
+    case 1:
+      cudaFuncSetAttribute(k_pass_c<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+      k_pass_c<1, false><<<(unsigned)a.grid, kFftThreads, smem, s>>>(a);
+      break;
+    case 2:
+      cudaFuncSetAttribute(k_pass_c<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+      k_pass_c<2, false><<<(unsigned)a.grid, kFftThreads, smem, s>>>(a);
+      break;
+    default:
+      cudaFuncSetAttribute(k_pass_c<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+      k_pass_c<3, false><<<(unsigned)a.grid, kFftThreads, smem, s>>>(a);
+      break;
+  }
+  return 1;
+}
+
+int launch_bin_fields(const BinFieldArgs& a, cudaStream_t s) {
+  const size_t smem = (size_t)a.geom.npole * a.geom.nbin * sizeof(float);
+  cudaFuncSetAttribute(k_bin_fields, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_bin_fields<<<(unsigned)a.grid, kFftThreads, smem, s>>>(a);
+  return 1;
+}
+
+int launch_geometry(const GeomArgs& a, cudaStream_t s) {
+  const size_t smem = (size_t)(2 + a.geom.npole) * a.geom.nbin * sizeof(double);
+  cudaFuncSetAttribute(k_geometry, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t nmodes = (size_t)a.ng * a.ng * (a.ng / 2 + 1);
+  size_t blocks = (nmodes + 255) / 256;
+  if (blocks > (size_t)nsm * 4) blocks = (size_t)nsm * 4;
+  k_geometry<<<(unsigned)blocks, 256, smem, s>>>(a);
+  return 1;
+}
+
+int launch_reduce(const double* part, int grid, int width, double* out, cudaStream_t s) {
+  k_reduce<<<(width + 255) / 256, 256, 0, s>>>(part, grid, width, out);
+  return 1;
+}
+
+}  // namespace ps

@@ -1,0 +1,697 @@
+// ps_capi.cu -- context, host-side tables and the extern "C" entry points of
+// libpowspec_gpu.so (declared in include/powspec_gpu.h).
+//
+// Host work here is O(ng) or O(nbin) per call plus one O(ng^2) table per
+// context; every O(ng^3) or O(N) loop runs on the GPU.
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "powspec_gpu.h"
+#include "ps_internal.h"
+
+using namespace ps;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+// 1-D window / alias factor (src/multipole.c:46-100), FP64.  Note that the
+// reference passes the SIGNED frequency: for negative arguments the x > 0.01
+// test fails and the Taylor branch is taken, which the tables reproduce.
+double alias_corr(int interlace, int assign, double pik) {
+  double fac;
+  if (interlace) {
+    if (pik > 0.01) {
+      fac = pik / sin(pik);
+    } else {
+      const double t = pik * pik;
+      fac = 1 + 0x1.5555555555555p-3 * t + 0x1.3e93e93e93e94p-6 * t * t +
+            0x1.0cbb766210cbbp-9 * t * t * t;
+    }
+    fac *= fac;
+    switch (assign) {
+      case 0: return fac;
+      case 1: return fac * fac;
+      case 2: return fac * fac * fac;
+      default: fac *= fac; return fac * fac;
+    }
+  }
+  if (pik > 0.01) {
+    fac = sin(pik);
+  } else {
+    const double t = pik * pik;
+    fac = (1 - 0x1.5555555555555p-3 * t + 0x1.1111111111111p-7 * t * t -
+           0x1.a01a01a01a01ap-13 * t * t * t) * pik;
+  }
+  fac *= fac;
+  switch (assign) {
+    case 0: return 1;
+    case 1: return 1 / (1 - 0x1.5555555555555p-1 * fac);
+    case 2: return 1 / (1 - fac + 0x1.1111111111111p-3 * fac * fac);
+    default:
+      return 1 / (1 - 0x1.5555555555555p+0 * fac + 0.4 * fac * fac -
+                  0x1.a01a01a01a01ap-7 * fac * fac * fac);
+  }
+}
+
+bool make_plan(int n, FftPlan& p) {
+  p.n = n;
+  p.npass = 0;
+  int m = n, e = 0;
+  while (m % 2 == 0) { m /= 2; e++; }
+  while (e > 0) {
+    int r;
+    if (e == 4) r = 4;
+    else if (e >= 3) r = 8;
+    else if (e == 2) r = 4;
+    else r = 2;
+    if (p.npass >= kMaxPlan) return false;
+    p.radix[p.npass++] = r;
+    e -= (r == 8) ? 3 : (r == 4) ? 2 : 1;
+  }
+  while (m % 3 == 0) { if (p.npass >= kMaxPlan) return false; p.radix[p.npass++] = 3; m /= 3; }
+  while (m % 5 == 0) { if (p.npass >= kMaxPlan) return false; p.radix[p.npass++] = 5; m /= 5; }
+  return m == 1;
+}
+
+std::vector<float2> twiddles(int n) {
+  std::vector<float2> t(n);
+  for (int m = 0; m < n; m++) {
+    // angle reduced to [0, pi] for accuracy, sign restored
+    const int mm = (2 * m <= n) ? m : n - m;
+    const double a = 2.0 * kPi * (double)mm / (double)n;
+    const double s = (2 * m <= n) ? -sin(a) : sin(a);
+    t[m] = make_float2((float)cos(a), (float)s);
+  }
+  return t;
+}
+
+}  // namespace
+
+struct ps_gpu_ctx {
+  ps_gpu_params p;
+  int ng = 0, ngk = 0, nbin = 0, nfield = 0, mpc = 1, nsm = 0;
+  size_t ntot = 0, ncx = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<double> kedge, kcen, km, lcnt;
+  std::vector<uint64_t> cnt;
+  unsigned long long* grid[4] = {nullptr, nullptr, nullptr, nullptr};
+  float2* cbuf[4] = {nullptr, nullptr, nullptr, nullptr};
+  short* d_bintab = nullptr;
+  double* d_ksq = nullptr;
+  float* d_win = nullptr;
+  float2* d_phase = nullptr;
+  float2* d_tw_full = nullptr;
+  float2* d_tw_half = nullptr;
+  FftPlan plan_full{}, plan_half{};
+  ModeGeom geom{};
+  int nspec = 0, spec_a[3] = {0, 0, 0}, spec_b[3] = {0, 0, 0}, spec_cat[3] = {0, 0, 0};
+  int ty_a = 1, tx_b = 1, ty_c = 1, grid_c = 1;
+  double* d_part = nullptr;
+  double* d_sums = nullptr;
+  double* d_wsum = nullptr;  // [2 cats][2]
+  int* d_err = nullptr;      // [2 cats]
+  double* h_out = nullptr;   // pinned: sums + wsum + err
+  void* d_stage = nullptr;
+  size_t stage_bytes = 0;
+  int assigned[2] = {0, 0};
+  cudaEvent_t ev[8] = {};
+  bool assign_started = false;
+  float timings[6] = {0, 0, 0, 0, 0, 0};
+  int launches = 0;
+  char err[512] = {0};
+};
+
+namespace {
+
+int fail(ps_gpu_ctx* c, int code, const char* fmt, ...) {
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof c->err, fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+#define CU(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(c, PS_GPU_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+int upload(ps_gpu_ctx* c, T** dst, const std::vector<T>& v) {
+  CU(cudaMalloc((void**)dst, sizeof(T) * (v.empty() ? 1 : v.size())));
+  if (!v.empty()) CU(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// Bin of a squared wave number with the reference's FP64 sequence
+// (src/multipole.c:147-158).
+int ref_bin(const ps_gpu_ctx* c, double km2) {
+  const double kmod = c->p.logscale ? 0.5 * log10(km2) : sqrt(km2);
+  if (kmod < c->kedge[0] || kmod >= c->kedge[c->nbin]) return -1;
+  const int b = (int)((kmod - c->kedge[0]) / c->p.dk);
+  return (b < 0 || b >= c->nbin) ? -1 : b;
+}
+
+int validate(ps_gpu_ctx* c, const ps_gpu_params* p) {
+  if (p->ng < 4 || p->ng % 2) return fail(c, PS_GPU_ERR_ARG, "GRID_SIZE must be even and >= 4: %d", p->ng);
+  if (p->assign < 0 || p->assign > 3) return fail(c, PS_GPU_ERR_ARG, "invalid PARTICLE_ASSIGN: %d", p->assign);
+  if (p->ncat < 1 || p->ncat > 2) return fail(c, PS_GPU_ERR_ARG, "number of catalogues must be 1 or 2");
+  for (int d = 0; d < 3; d++)
+    if (!(p->box[d] > 0)) return fail(c, PS_GPU_ERR_ARG, "BOX_SIZE must be positive");
+  if (!(p->dk > 0)) return fail(c, PS_GPU_ERR_ARG, "BIN_SIZE must be positive");
+  if (p->npole < 1 || p->npole > kMaxPole) return fail(c, PS_GPU_ERR_ARG, "invalid number of multipoles");
+  for (int l = 0; l < p->npole; l++) {
+    if (p->poles[l] < 0 || p->poles[l] > 6) return fail(c, PS_GPU_ERR_ARG, "MULTIPOLE must be between 0 and 6");
+    if (l && p->poles[l] <= p->poles[l - 1]) return fail(c, PS_GPU_ERR_ARG, "MULTIPOLE must be sorted and unique");
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
+  if (!params || !out) return PS_GPU_ERR_ARG;
+  *out = nullptr;
+  ps_gpu_ctx* c = new (std::nothrow) ps_gpu_ctx();
+  if (!c) return PS_GPU_ERR_MEMORY;
+  c->p = *params;
+  const ps_gpu_params& p = c->p;
+  int rc = validate(c, &p);
+  if (rc) { *out = c; return rc; }
+  *out = c;
+  c->ng = p.ng;
+  c->ngk = p.ng / 2 + 1;
+  c->ntot = (size_t)p.ng * p.ng * p.ng;
+  c->ncx = (size_t)p.ng * p.ng * c->ngk;
+  c->mpc = p.interlace ? 2 : 1;
+  c->nfield = p.ncat * c->mpc;
+  if (!make_plan(p.ng, c->plan_full) || !make_plan(p.ng / 2, c->plan_half))
+    return fail(c, PS_GPU_ERR_ARG, "GRID_SIZE/2 must be a product of 2, 3 and 5: %d", p.ng);
+  if ((size_t)c->nfield * p.ng > (size_t)2 * kPassCElems)
+    return fail(c, PS_GPU_ERR_ARG, "GRID_SIZE %d too large for %d fields", p.ng, c->nfield);
+
+  // spectra: autos, then the cross (src/multipole.c:1221-1226)
+  for (int k = 0; k < p.ncat; k++)
+    if (p.isauto[k]) { c->spec_a[c->nspec] = k; c->spec_b[c->nspec] = k; c->spec_cat[c->nspec] = k; c->nspec++; }
+  if (p.ncat == 2 && p.iscross) { c->spec_a[c->nspec] = 0; c->spec_b[c->nspec] = 1; c->spec_cat[c->nspec] = -1; c->nspec++; }
+  if (!c->nspec) return fail(c, PS_GPU_ERR_ARG, "no auto or cross spectrum requested");
+
+  // bins (src/multipole.c:334-394)
+  {
+    double bmax = (p.box[0] > p.box[1]) ? p.box[0] : p.box[1];
+    if (bmax < p.box[2]) bmax = p.box[2];
+    double kny = kPi * p.ng / bmax;
+    if (p.logscale) kny = log10(kny);
+    double kmax = kny;
+    if (p.kmax > 0 && kmax > p.kmax) kmax = p.kmax;
+    const double nb = round((kmax - p.kmin) / p.dk);
+    if (!(nb < 2147483647.0)) return fail(c, PS_GPU_ERR_PK, "too many wave number bins");
+    int nbin = (int)nb;
+    if (p.kmin + p.dk * nbin > kny) nbin -= 1;
+    if (nbin < 1) return fail(c, PS_GPU_ERR_PK, "not enough k bins given the Nyquist frequency and the bin size");
+    c->nbin = nbin;
+    c->kedge.resize(nbin + 1);
+    c->kcen.resize(nbin);
+    for (int i = 0; i <= nbin; i++) c->kedge[i] = p.kmin + p.dk * i;
+    for (int i = 0; i < nbin; i++) c->kcen[i] = (c->kedge[i] + c->kedge[i + 1]) * 0.5;
+  }
+
+  int dcount = 0;
+  if (cudaGetDeviceCount(&dcount) != cudaSuccess || dcount < 1)
+    return fail(c, PS_GPU_ERR_CUDA, "no CUDA device available");
+  if (p.device < 0 || p.device >= dcount) return fail(c, PS_GPU_ERR_ARG, "invalid device %d", p.device);
+  CU(cudaSetDevice(p.device));
+  CU(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, p.device));
+  CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  for (auto& e : c->ev) CU(cudaEventCreate(&e));
+
+  // ---- geometry tables (FP64 on the host)
+  const int ng = p.ng, h = c->ngk;
+  double vec[3];
+  for (int d = 0; d < 3; d++) vec[d] = 2 * kPi / p.box[d];
+  std::vector<double> ksq(3 * h);
+  for (int d = 0; d < 3; d++)
+    for (int m = 0; m < h; m++) {
+      const double kv = m * vec[d];
+      ksq[d * h + m] = kv * kv;
+    }
+  std::vector<float> win(3 * ng);
+  const double fac = kPi / ng;
+  for (int d = 0; d < 3; d++)
+    for (int i = 0; i < ng; i++)
+      win[d * ng + i] = (float)alias_corr(p.interlace, p.assign, signed_index(i, ng) * fac);
+  std::vector<float2> phase(3 * ng);
+  for (int m = 0; m < 3 * ng; m++) {
+    const double a = kPi * (double)(m - ng) / ng;
+    phase[m] = make_float2((float)cos(a), (float)sin(a));
+  }
+  const bool cubic = (p.box[0] == p.box[1] && p.box[1] == p.box[2]);
+  const int nmax = 3 * (ng / 2) * (ng / 2);
+  if (cubic && c->nbin < 32000) {
+    std::vector<short> tab(nmax + 1);
+    const double v2 = vec[0] * vec[0];
+    for (int n = 0; n <= nmax; n++) {
+      const double t = (double)n * v2;
+      const int blo = ref_bin(c, t * (1 - 1e-12)), bhi = ref_bin(c, t * (1 + 1e-12));
+      tab[n] = (short)((blo == bhi) ? blo : -2);
+    }
+    if ((rc = upload(c, &c->d_bintab, tab))) return rc;
+  }
+  if ((rc = upload(c, &c->d_ksq, ksq))) return rc;
+  if ((rc = upload(c, &c->d_win, win))) return rc;
+  if ((rc = upload(c, &c->d_phase, phase))) return rc;
+  if ((rc = upload(c, &c->d_tw_full, twiddles(ng)))) return rc;
+  if ((rc = upload(c, &c->d_tw_half, twiddles(ng / 2)))) return rc;
+
+  ModeGeom& g = c->geom;
+  g.ng = ng;
+  g.nbin = c->nbin;
+  g.npole = p.npole;
+  for (int l = 0; l < kMaxPole; l++) g.poles[l] = (l < p.npole) ? p.poles[l] : 0;
+  g.logscale = p.logscale;
+  g.nmax = nmax;
+  g.bintab = c->d_bintab;
+  g.ksq = c->d_ksq;
+  g.win = c->d_win;
+  g.phase = c->d_phase;
+  g.kedge0 = c->kedge[0];
+  g.kedgeN = c->kedge[c->nbin];
+  g.dk = p.dk;
+  for (int d = 0; d < 3; d++) {
+    g.vec[d] = (float)vec[d];
+    g.los[d] = (float)p.los[d];
+  }
+
+  // ---- tiles and persistent grid of the binning pass
+  c->ty_a = std::min({ng, 16, kCtaElems / (ng / 2)});
+  c->tx_b = std::min({ng, 16, kCtaElems / ng});
+  c->ty_c = std::max(1, std::min(ng, kPassCElems / (c->nfield * ng)));
+  const int nacc = c->nspec * p.npole;
+  const size_t smem_c = pass_c_smem(ng, c->ty_c, c->nfield, nacc, c->nbin);
+  if (smem_c > 227 * 1024)
+    return fail(c, PS_GPU_ERR_ARG, "too many bins (%d) for the binning pass", c->nbin);
+  const int per_sm = std::max(1, std::min(4, (int)((228 * 1024) / (smem_c + 2048))));
+  const int ntile_c = c->ngk * ((ng + c->ty_c - 1) / c->ty_c);
+  c->grid_c = std::min(ntile_c, c->nsm * per_sm);
+
+  // ---- device memory
+  size_t freeb = 0, totalb = 0;
+  CU(cudaMemGetInfo(&freeb, &totalb));
+  const size_t need = (size_t)c->nfield * (c->ntot * 8 + c->ncx * 8) +
+                      (size_t)c->grid_c * nacc * c->nbin * 8 + (64u << 20);
+  if (need > freeb)
+    return fail(c, PS_GPU_ERR_MEMORY, "need %.1f GB of device memory, %.1f GB free", need / 1e9, freeb / 1e9);
+  for (int f = 0; f < c->nfield; f++) {
+    CU(cudaMalloc(&c->grid[f], c->ntot * sizeof(unsigned long long)));
+    CU(cudaMalloc(&c->cbuf[f], c->ncx * sizeof(float2)));
+  }
+  CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)c->grid_c * nacc * c->nbin));
+  CU(cudaMalloc(&c->d_sums, sizeof(double) * (size_t)nacc * c->nbin));
+  CU(cudaMalloc(&c->d_wsum, sizeof(double) * 4));
+  CU(cudaMalloc(&c->d_err, sizeof(int) * 2));
+  CU(cudaMemset(c->d_wsum, 0, sizeof(double) * 4));
+  CU(cudaMemset(c->d_err, 0, sizeof(int) * 2));
+  CU(cudaMallocHost(&c->h_out, sizeof(double) * ((size_t)nacc * c->nbin + 8)));
+
+  // ---- geometry sweep: counts, mean |k|, multipole mode weights
+  {
+    unsigned long long* d_cnt = nullptr;
+    double *d_ks = nullptr, *d_lc = nullptr;
+    CU(cudaMalloc(&d_cnt, sizeof(unsigned long long) * c->nbin));
+    CU(cudaMalloc(&d_ks, sizeof(double) * c->nbin));
+    CU(cudaMalloc(&d_lc, sizeof(double) * (size_t)p.npole * c->nbin));
+    CU(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * c->nbin, c->stream));
+    CU(cudaMemsetAsync(d_ks, 0, sizeof(double) * c->nbin, c->stream));
+    CU(cudaMemsetAsync(d_lc, 0, sizeof(double) * (size_t)p.npole * c->nbin, c->stream));
+    GeomArgs ga;
+    ga.ng = ng;
+    ga.geom = g;
+    for (int d = 0; d < 3; d++) { ga.vec[d] = vec[d]; ga.los[d] = p.los[d]; }
+    ga.cnt = d_cnt;
+    ga.ksum = d_ks;
+    ga.lcnt = d_lc;
+    launch_geometry(ga, c->stream);
+    CU(cudaGetLastError());
+    c->cnt.resize(c->nbin);
+    c->km.resize(c->nbin);
+    c->lcnt.resize((size_t)p.npole * c->nbin);
+    std::vector<unsigned long long> cnt(c->nbin);
+    CU(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(unsigned long long) * c->nbin, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(c->km.data(), d_ks, sizeof(double) * c->nbin, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(c->lcnt.data(), d_lc, sizeof(double) * (size_t)p.npole * c->nbin, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    cudaFree(d_cnt);
+    cudaFree(d_ks);
+    cudaFree(d_lc);
+    for (int b = 0; b < c->nbin; b++) {
+      c->cnt[b] = cnt[b];
+      if (cnt[b]) c->km[b] /= (double)cnt[b];
+    }
+  }
+  return 0;
+}
+
+void ps_gpu_destroy(ps_gpu_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int f = 0; f < 4; f++) {
+    if (c->grid[f]) cudaFree(c->grid[f]);
+    if (c->cbuf[f]) cudaFree(c->cbuf[f]);
+  }
+  void* bufs[] = {c->d_bintab, c->d_ksq, c->d_win, c->d_phase, c->d_tw_full, c->d_tw_half,
+                  c->d_part, c->d_sums, c->d_wsum, c->d_err, c->d_stage};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int ps_gpu_nbin(const ps_gpu_ctx* c) { return c ? c->nbin : PS_GPU_ERR_ARG; }
+
+const char* ps_gpu_last_error(const ps_gpu_ctx* c) { return c ? c->err : "null context"; }
+
+int ps_gpu_last_timings(const ps_gpu_ctx* c, float* ms, int nmax) {
+  if (!c || !ms) return 0;
+  int n = std::min(nmax, 6);
+  for (int i = 0; i < n; i++) ms[i] = c->timings[i];
+  return n;
+}
+
+int ps_gpu_last_launches(const ps_gpu_ctx* c) { return c ? c->launches : 0; }
+
+}  // extern "C"
+
+namespace {
+
+int ensure_stage(ps_gpu_ctx* c, size_t bytes) {
+  if (bytes <= c->stage_bytes) return 0;
+  if (c->d_stage) {
+    CU(cudaStreamSynchronize(c->stream));
+    cudaFree(c->d_stage);
+    c->d_stage = nullptr;
+    c->stage_bytes = 0;
+  }
+  CU(cudaMalloc(&c->d_stage, bytes));
+  c->stage_bytes = bytes;
+  return 0;
+}
+
+int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
+  CU(cudaSetDevice(c->p.device));
+  if (!c->assign_started) {
+    CU(cudaEventRecord(c->ev[6], c->stream));
+    c->assign_started = true;
+    c->launches = 0;
+  }
+  for (int m = 0; m < c->mpc; m++)
+    CU(cudaMemsetAsync(c->grid[cat * c->mpc + m], 0, c->ntot * sizeof(unsigned long long), c->stream));
+  CU(cudaMemsetAsync(c->d_wsum + 2 * cat, 0, sizeof(double) * 2, c->stream));
+  CU(cudaMemsetAsync(c->d_err + cat, 0, sizeof(int), c->stream));
+  AssignArgs a;
+  a.ng = c->ng;
+  a.assign = c->p.assign;
+  for (int d = 0; d < 3; d++) a.box[d] = c->p.box[d];
+  a.mesh0 = c->grid[cat * c->mpc];
+  a.mesh1 = c->p.interlace ? c->grid[cat * c->mpc + 1] : nullptr;
+  a.wsum = c->d_wsum + 2 * cat;
+  a.err = c->d_err + cat;
+  if (pt.n) c->launches += launch_assign(pt, a, c->stream);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[7], c->stream));
+  c->assigned[cat] = 1;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ps_gpu_assign_aos(ps_gpu_ctx* c, int cat, const double* xyzw, size_t n, int on_device) {
+  if (!c || cat < 0 || cat >= c->p.ncat || (!xyzw && n)) return fail(c, PS_GPU_ERR_ARG, "invalid assign arguments");
+  Particles pt{};
+  pt.n = n;
+  if (on_device) {
+    pt.aos = xyzw;
+  } else {
+    int rc = ensure_stage(c, n * 4 * sizeof(double));
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(c->d_stage, xyzw, n * 4 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    pt.aos = (const double*)c->d_stage;
+  }
+  return assign_common(c, cat, pt);
+}
+
+int ps_gpu_assign_soa(ps_gpu_ctx* c, int cat, const float* x, const float* y, const float* z,
+                      const float* w, size_t n, int on_device) {
+  if (!c || cat < 0 || cat >= c->p.ncat || ((!x || !y || !z) && n))
+    return fail(c, PS_GPU_ERR_ARG, "invalid assign arguments");
+  Particles pt{};
+  pt.n = n;
+  if (on_device) {
+    pt.x = x; pt.y = y; pt.z = z; pt.w = w;
+  } else {
+    const int na = w ? 4 : 3;
+    int rc = ensure_stage(c, n * na * sizeof(float));
+    if (rc) return rc;
+    float* s = (float*)c->d_stage;
+    const float* src[4] = {x, y, z, w};
+    for (int k = 0; k < na; k++)
+      CU(cudaMemcpyAsync(s + k * n, src[k], n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    pt.x = s; pt.y = s + n; pt.z = s + 2 * n; pt.w = w ? s + 3 * n : nullptr;
+  }
+  return assign_common(c, cat, pt);
+}
+
+int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
+  if (!c || !r) return fail(c, PS_GPU_ERR_ARG, "null argument");
+  const ps_gpu_params& p = c->p;
+  for (int k = 0; k < p.ncat; k++)
+    if (!c->assigned[k]) return fail(c, PS_GPU_ERR_STATE, "catalogue %d not assigned", k);
+  CU(cudaSetDevice(p.device));
+  cudaStream_t s = c->stream;
+  const int ng = c->ng, npole = p.npole, nbin = c->nbin;
+  const int nacc = c->nspec * npole;
+
+  CU(cudaEventRecord(c->ev[0], s));
+  for (int f = 0; f < c->nfield; f++) {
+    PassAArgs a;
+    a.ng = ng;
+    a.ty = c->ty_a;
+    a.grid = (const long long*)c->grid[f];
+    a.fgrid = nullptr;
+    a.out = c->cbuf[f];
+    a.wsum = c->d_wsum + 2 * (f / c->mpc);
+    a.tw_half = c->d_tw_half;
+    a.tw_full = c->d_tw_full;
+    a.plan_half = c->plan_half;
+    c->launches += launch_pass_a(a, s);
+  }
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[1], s));
+  for (int f = 0; f < c->nfield; f++) {
+    PassBArgs b;
+    b.ng = ng;
+    b.tx = c->tx_b;
+    b.in = c->cbuf[f];
+    b.out = (float2*)c->grid[f];
+    b.tw_full = c->d_tw_full;
+    b.plan_full = c->plan_full;
+    c->launches += launch_pass_b(b, s);
+  }
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[2], s));
+  CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)c->grid_c * nacc * nbin, s));
+  PassCArgs pc;
+  memset(&pc, 0, sizeof pc);
+  pc.ng = ng;
+  pc.ty = c->ty_c;
+  pc.nfield = c->nfield;
+  pc.interlace = p.interlace;
+  pc.ncat = p.ncat;
+  pc.nspec = c->nspec;
+  for (int k = 0; k < 3; k++) { pc.spec_a[k] = c->spec_a[k]; pc.spec_b[k] = c->spec_b[k]; }
+  for (int f = 0; f < c->nfield; f++) pc.in[f] = (const float2*)c->grid[f];
+  pc.store = nullptr;
+  pc.tw_full = c->d_tw_full;
+  pc.plan_full = c->plan_full;
+  pc.geom = c->geom;
+  pc.partials = c->d_part;
+  pc.grid = c->grid_c;
+  c->launches += launch_pass_c(pc, s);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[3], s));
+  c->launches += launch_reduce(c->d_part, c->grid_c, nacc * nbin, c->d_sums, s);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[4], s));
+  double* h = c->h_out;
+  CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nbin, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h + (size_t)nacc * nbin, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h + (size_t)nacc * nbin + 4, c->d_err, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  float t = 0;
+  if (c->assign_started && cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess) c->timings[0] = t;
+  for (int i = 0; i < 4; i++)
+    if (cudaEventElapsedTime(&t, c->ev[i], c->ev[i + 1]) == cudaSuccess) c->timings[1 + i] = t;
+  if (cudaEventElapsedTime(&t, c->ev[0], c->ev[4]) == cudaSuccess) c->timings[5] = t + c->timings[0];
+  c->assign_started = false;
+  c->assigned[0] = c->assigned[1] = 0;
+
+  const double* sums = h;
+  const double* wsum = h + (size_t)nacc * nbin;
+  const int* errs = (const int*)(h + (size_t)nacc * nbin + 4);
+  for (int k = 0; k < p.ncat; k++) {
+    if (errs[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: coordinate outside [0, BOX_SIZE)", k);
+    if (!(wsum[2 * k + 1] < kFixMaxWeight))
+      return fail(c, PS_GPU_ERR_RANGE, "catalogue %d: total |weight| %g exceeds the fixed-point range", k, wsum[2 * k + 1]);
+  }
+
+  // epilogue (src/genr_mesh.c:904-910, src/multipole.c:1047-1087)
+  const double vol = p.box[0] * p.box[1] * p.box[2];
+  for (int k = 0; k < 2; k++) {
+    r->wdata[k] = (k < p.ncat) ? wsum[2 * k] : 0;
+    r->shot[k] = (k < p.ncat) ? vol / r->wdata[k] : 0;
+    r->norm[k] = (k < p.ncat) ? r->wdata[k] * r->wdata[k] / vol : 0;
+  }
+  r->nbin = nbin;
+  for (int s2 = 0; s2 < c->nspec; s2++) {
+    const int cat = c->spec_cat[s2];
+    double* dst = (cat >= 0) ? (r->pl ? r->pl + (size_t)cat * npole * nbin : nullptr) : r->xpl;
+    if (!dst) continue;
+    for (int l = 0; l < npole; l++) {
+      for (int i = 0; i < nbin; i++) {
+        double v = sums[((size_t)s2 * npole + l) * nbin + i];
+        const double cn = (double)c->cnt[i];
+        if (cat >= 0) {
+          if (c->cnt[i]) {
+            v /= r->norm[cat] * cn;
+            v -= r->shot[cat] * c->lcnt[(size_t)l * nbin + i] / cn;
+          }
+        } else if (c->cnt[i]) {
+          v /= sqrt(r->norm[0] * r->norm[1]) * cn;
+        }
+        v *= 2 * p.poles[l] + 1;
+        dst[(size_t)l * nbin + i] = v;
+      }
+    }
+  }
+  for (int i = 0; i < nbin; i++) {
+    if (r->k) r->k[i] = c->kcen[i];
+    if (r->km) r->km[i] = c->km[i];
+    if (r->kedge) r->kedge[i] = c->kedge[i];
+    if (r->cnt) r->cnt[i] = c->cnt[i];
+  }
+  if (r->kedge) r->kedge[nbin] = c->kedge[nbin];
+  if (r->lcnt) memcpy(r->lcnt, c->lcnt.data(), sizeof(double) * (size_t)npole * nbin);
+  // log bins: src/multipole.c:1267-1274, including its reuse of the rescaled k
+  if (p.logscale) {
+    for (int i = 0; i < nbin; i++) {
+      const double kc = pow(10, c->kcen[i]);
+      if (r->k) r->k[i] = kc;
+      if (r->km) r->km[i] = pow(10, kc);
+      if (r->kedge) r->kedge[i] = pow(10, kc);
+    }
+    if (r->kedge) r->kedge[nbin] = pow(10, c->kedge[nbin]);
+  }
+  return 0;
+}
+
+int ps_gpu_read_mesh(ps_gpu_ctx* c, int cat, int m, double* out) {
+  if (!c || !out || cat < 0 || cat >= c->p.ncat || m < 0 || m >= c->mpc)
+    return fail(c, PS_GPU_ERR_ARG, "invalid read_mesh arguments");
+  CU(cudaSetDevice(c->p.device));
+  std::vector<long long> q(c->ntot);
+  CU(cudaMemcpyAsync(q.data(), c->grid[cat * c->mpc + m], c->ntot * 8, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  for (size_t i = 0; i < c->ntot; i++) out[i] = (double)q[i] * kFixInv;
+  return 0;
+}
+
+int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
+  if (!c || !in || !out) return fail(c, PS_GPU_ERR_ARG, "null argument");
+  CU(cudaSetDevice(c->p.device));
+  cudaStream_t s = c->stream;
+  const int ng = c->ng;
+  float* d_in = (float*)c->grid[0];  // ntot floats fit in the int64 grid
+  CU(cudaMemcpyAsync(d_in, in, c->ntot * sizeof(float), cudaMemcpyHostToDevice, s));
+  PassAArgs a;
+  a.ng = ng;
+  a.ty = c->ty_a;
+  a.grid = nullptr;
+  a.fgrid = d_in;
+  a.out = c->cbuf[0];
+  a.wsum = nullptr;
+  a.tw_half = c->d_tw_half;
+  a.tw_full = c->d_tw_full;
+  a.plan_half = c->plan_half;
+  launch_pass_a(a, s);
+  PassBArgs b;
+  b.ng = ng;
+  b.tx = c->tx_b;
+  b.in = c->cbuf[0];
+  b.out = (float2*)c->grid[0];
+  b.tw_full = c->d_tw_full;
+  b.plan_full = c->plan_full;
+  launch_pass_b(b, s);
+  PassCArgs pc;
+  memset(&pc, 0, sizeof pc);
+  pc.ng = ng;
+  pc.ty = std::max(1, std::min(ng, kPassCElems / ng));
+  pc.nfield = 1;
+  pc.ncat = 1;
+  pc.nspec = 1;
+  pc.in[0] = (const float2*)c->grid[0];
+  pc.store = c->cbuf[0];
+  pc.tw_full = c->d_tw_full;
+  pc.plan_full = c->plan_full;
+  pc.geom = c->geom;
+  launch_pass_c(pc, s);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(out, c->cbuf[0], c->ncx * sizeof(float2), cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int ps_gpu_bin_fields_host(ps_gpu_ctx* c, const float* f1, const float* f2, double* pl) {
+  if (!c || !f1 || !f2 || !pl) return fail(c, PS_GPU_ERR_ARG, "null argument");
+  CU(cudaSetDevice(c->p.device));
+  cudaStream_t s = c->stream;
+  const int npole = c->p.npole, nbin = c->nbin;
+  float2* d1 = c->cbuf[0];
+  float2* d2 = (float2*)c->grid[0];
+  CU(cudaMemcpyAsync(d1, f1, c->ncx * sizeof(float2), cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(d2, f2, c->ncx * sizeof(float2), cudaMemcpyHostToDevice, s));
+  CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)c->grid_c * npole * nbin, s));
+  BinFieldArgs b;
+  b.ng = c->ng;
+  b.f1 = d1;
+  b.f2 = d2;
+  b.geom = c->geom;
+  b.partials = c->d_part;
+  b.grid = c->grid_c;
+  launch_bin_fields(b, s);
+  launch_reduce(c->d_part, c->grid_c, npole * nbin, c->d_sums, s);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(pl, c->d_sums, sizeof(double) * (size_t)npole * nbin, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+}  // extern "C"

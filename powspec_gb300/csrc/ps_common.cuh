@@ -1,0 +1,307 @@
+// ps_common.cuh -- shared device code of the GB300 P_l(k) path: fixed-point
+// mesh format, the in-shared-memory mixed-radix FFT engine, and the per-mode
+// geometry (bin lookup, window, Legendre) used by the binning sweeps.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "powspec_gpu.h"
+
+namespace ps {
+
+// ---------------------------------------------------------------- limits
+constexpr int kMaxPole = 7;        // ell = 0..6 (src/define.h:96)
+constexpr int kMaxPlan = 24;       // radix passes per transform length
+constexpr int kFftThreads = 256;   // threads of every FFT-pass CTA
+constexpr int kElemsPerThread = 32;  // complex values a thread stages per pass
+constexpr int kCtaElems = kFftThreads * kElemsPerThread;  // 8192 complex = 64 KB
+constexpr int kPassCElems = 4096;  // complex per ping-pong buffer of the binning pass
+
+// Fixed-point mesh: every stencil node adds llrint(w_node * 2^32) to an int64
+// cell with an integer atomic.  Integer addition is associative, so the mesh
+// is bit-identical whatever the order of the atomics.
+constexpr float kFixScale = 4294967296.0f;         // 2^32
+constexpr double kFixInv = 2.3283064365386963e-10;  // 2^-32
+constexpr double kFixMaxWeight = 2147483648.0;      // |cell| < 2^31 weight units
+
+// Radix plan of one transform length (product of 8, 4, 2, 3, 5).
+struct FftPlan {
+  int n;
+  int npass;
+  int radix[kMaxPlan];
+};
+
+// --------------------------------------------------------------- complex
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  return make_float2(a.x - b.x, a.y - b.y);
+}
+// a * (-i)
+__device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
+
+// ------------------------------------------------- forward DFT butterflies
+// out[q] = sum_r v[r] exp(-2 pi i r q / R), natural order, in place.
+template <int R>
+__device__ __forceinline__ void dft(float2 (&v)[R]);
+
+template <>
+__device__ __forceinline__ void dft<2>(float2 (&v)[2]) {
+  float2 a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+
+template <>
+__device__ __forceinline__ void dft<4>(float2 (&v)[4]) {
+  float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+  float2 t2 = cadd(v[1], v[3]), t3 = cmul_mi(csub(v[1], v[3]));
+  v[0] = cadd(t0, t2);
+  v[2] = csub(t0, t2);
+  v[1] = cadd(t1, t3);
+  v[3] = csub(t1, t3);
+}
+
+template <>
+__device__ __forceinline__ void dft<8>(float2 (&v)[8]) {
+  const float h = 0.70710678118654752440f;  // sqrt(1/2)
+  float2 e[4] = {v[0], v[2], v[4], v[6]};
+  float2 o[4] = {v[1], v[3], v[5], v[7]};
+  dft<4>(e);
+  dft<4>(o);
+  // twiddles W8^q, q = 0..3: 1, h(1-i), -i, -h(1+i)
+  float2 o1 = make_float2(h * (o[1].x + o[1].y), h * (o[1].y - o[1].x));
+  float2 o2 = cmul_mi(o[2]);
+  float2 o3 = make_float2(h * (o[3].y - o[3].x), -h * (o[3].x + o[3].y));
+  v[0] = cadd(e[0], o[0]);
+  v[4] = csub(e[0], o[0]);
+  v[1] = cadd(e[1], o1);
+  v[5] = csub(e[1], o1);
+  v[2] = cadd(e[2], o2);
+  v[6] = csub(e[2], o2);
+  v[3] = cadd(e[3], o3);
+  v[7] = csub(e[3], o3);
+}
+
+template <>
+__device__ __forceinline__ void dft<3>(float2 (&v)[3]) {
+  const float h = 0.86602540378443864676f;  // sqrt(3)/2
+  float2 s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+  float2 a = make_float2(v[0].x - 0.5f * s.x, v[0].y - 0.5f * s.y);
+  // -i h d = (h d.y, -h d.x)
+  float2 t = make_float2(h * d.y, -h * d.x);
+  v[0] = cadd(v[0], s);
+  v[1] = cadd(a, t);
+  v[2] = csub(a, t);
+}
+
+template <>
+__device__ __forceinline__ void dft<5>(float2 (&v)[5]) {
+  const float c1 = 0.30901699437494742410f;   // cos(2pi/5)
+  const float c2 = -0.80901699437494742410f;  // cos(4pi/5)
+  const float s1 = 0.95105651629515357212f;   // sin(2pi/5)
+  const float s2 = 0.58778525229247312917f;   // sin(4pi/5)
+  float2 a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
+  float2 a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+  float2 x0 = v[0];
+  float2 r1 = make_float2(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
+  float2 r2 = make_float2(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
+  // i1 = s1 b1 + s2 b2 ; i2 = s2 b1 - s1 b2 ; out = r -/+ i * i_
+  float2 i1 = make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
+  float2 i2 = make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
+  v[0] = make_float2(x0.x + a1.x + a2.x, x0.y + a1.y + a2.y);
+  v[1] = cadd(r1, cmul_mi(i1));
+  v[4] = csub(r1, cmul_mi(i1));
+  v[2] = cadd(r2, cmul_mi(i2));
+  v[3] = csub(r2, cmul_mi(i2));
+}
+
+// One Stockham radix-R pass over `nlines` lines of length n held in shared
+// memory (line stride ls complex), in place: every thread first stages the
+// inputs of its butterflies in registers, the block synchronises, then the
+// outputs go to their autosorted positions.  tw[m] = exp(-2 pi i m / n).
+// Requires nlines * n <= kCtaElems (checked on the host).
+template <int R>
+__device__ __forceinline__ void fft_pass(float2* buf, int n, int nlines, int ls,
+                                         int Ns, const float2* __restrict__ tw) {
+  constexpr int BPT = (kElemsPerThread + R - 1) / R;
+  const int m = n / R;
+  const int total = nlines * m;
+  const int tws = n / (Ns * R);
+  float2 v[BPT][R];
+#pragma unroll
+  for (int t = 0; t < BPT; t++) {
+    const int b = threadIdx.x + t * blockDim.x;
+    if (b < total) {
+      const int line = b / m;
+      const int j = b - line * m;
+      const int k = j % Ns;
+      const float2* src = buf + line * ls;
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        float2 x = src[j + r * m];
+        if (r > 0 && k > 0) x = cmul(x, __ldg(&tw[r * k * tws]));
+        v[t][r] = x;
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < BPT; t++) {
+    const int b = threadIdx.x + t * blockDim.x;
+    if (b < total) {
+      const int line = b / m;
+      const int j = b - line * m;
+      const int k = j % Ns;
+      dft<R>(v[t]);
+      float2* dst = buf + line * ls + (j / Ns) * Ns * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) dst[r * Ns] = v[t][r];
+    }
+  }
+  __syncthreads();
+}
+
+// Full forward transform of every line in shared memory.  The plan lists
+// its passes grouped by radix (8s, 4s, 2s, 3s, 5s; any order of the factors
+// is a valid Stockham sequence); one loop per radix keeps every inlined
+// butterfly body in its own region, which the register allocator handles
+// far better than a switch inside a single loop.
+__device__ __forceinline__ void fft_lines(float2* buf, const FftPlan& plan, int nlines,
+                                          int ls, const float2* __restrict__ tw) {
+  int Ns = 1, p = 0;
+  const int np = plan.npass;
+  for (; p < np && plan.radix[p] == 8; p++, Ns *= 8) fft_pass<8>(buf, plan.n, nlines, ls, Ns, tw);
+  for (; p < np && plan.radix[p] == 4; p++, Ns *= 4) fft_pass<4>(buf, plan.n, nlines, ls, Ns, tw);
+  for (; p < np && plan.radix[p] == 2; p++, Ns *= 2) fft_pass<2>(buf, plan.n, nlines, ls, Ns, tw);
+  for (; p < np && plan.radix[p] == 3; p++, Ns *= 3) fft_pass<3>(buf, plan.n, nlines, ls, Ns, tw);
+  for (; p < np && plan.radix[p] == 5; p++, Ns *= 5) fft_pass<5>(buf, plan.n, nlines, ls, Ns, tw);
+}
+
+// Ping-pong variant for kernels that transform many tiles in a loop: every
+// butterfly goes from buffer `src` to buffer `dst` with only its R inputs in
+// registers, so register use stays that of a single butterfly however many
+// passes are inlined.  Returns the buffer holding the result.
+template <int R>
+__device__ __forceinline__ void fft_pass_pp(const float2* src, float2* dst, int n, int nlines,
+                                            int ls, int Ns, const float2* __restrict__ tw) {
+  const int m = n / R;
+  const int total = nlines * m;
+  const int tws = n / (Ns * R);
+  for (int b = threadIdx.x; b < total; b += blockDim.x) {
+    const int line = b / m;
+    const int j = b - line * m;
+    const int k = j % Ns;
+    const float2* s = src + line * ls + j;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      float2 x = s[r * m];
+      if (r > 0 && k > 0) x = cmul(x, __ldg(&tw[r * k * tws]));
+      v[r] = x;
+    }
+    dft<R>(v);
+    float2* d = dst + line * ls + (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) d[r * Ns] = v[r];
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ float2* fft_lines_pp(float2* a, float2* b, const FftPlan& plan,
+                                                int nlines, int ls,
+                                                const float2* __restrict__ tw) {
+  int Ns = 1, p = 0;
+  const int np = plan.npass;
+  for (; p < np && plan.radix[p] == 8; p++, Ns *= 8) {
+    fft_pass_pp<8>(a, b, plan.n, nlines, ls, Ns, tw);
+    float2* t = a; a = b; b = t;
+  }
+  for (; p < np && plan.radix[p] == 4; p++, Ns *= 4) {
+    fft_pass_pp<4>(a, b, plan.n, nlines, ls, Ns, tw);
+    float2* t = a; a = b; b = t;
+  }
+  for (; p < np && plan.radix[p] == 2; p++, Ns *= 2) {
+    fft_pass_pp<2>(a, b, plan.n, nlines, ls, Ns, tw);
+    float2* t = a; a = b; b = t;
+  }
+  for (; p < np && plan.radix[p] == 3; p++, Ns *= 3) {
+    fft_pass_pp<3>(a, b, plan.n, nlines, ls, Ns, tw);
+    float2* t = a; a = b; b = t;
+  }
+  for (; p < np && plan.radix[p] == 5; p++, Ns *= 5) {
+    fft_pass_pp<5>(a, b, plan.n, nlines, ls, Ns, tw);
+    float2* t = a; a = b; b = t;
+  }
+  return a;
+}
+
+// Fixed-point cell (minus a constant offset) -> float.  d = hi * 2^32 + lo,
+// value = d * 2^-32 = hi + lo * 2^-32, using two 32-bit conversions.
+__device__ __forceinline__ float fix_to_float(long long d) {
+  const int hi = (int)(d >> 32);
+  const unsigned lo = (unsigned)(d & 0xffffffffull);
+  return (float)hi + (float)lo * 2.3283064365386963e-10f;
+}
+
+// ---------------------------------------------------------- mode geometry
+// Everything a binning sweep needs to turn a lattice vector into a bin,
+// window factor and mu.  Tables are built on the host in FP64 (see the
+// host code for their definitions).
+struct ModeGeom {
+  int ng;
+  int nbin;
+  int npole;
+  int poles[kMaxPole];
+  int logscale;
+  int nmax;                  // n = i'^2 + j'^2 + k^2 <= nmax
+  const short* bintab;       // [nmax+1]: bin, -1 out of range, -2 ambiguous; NULL: none
+  const double* ksq;         // [3][ng/2+1]: fl(fl(vec_d * m)^2)
+  const float* win;          // [3][ng]: window factor per signed index (FP64 -> FP32)
+  const float2* phase;       // [3*ng]: exp(i pi (m - ng) / ng), m = i'+j'+k+ng
+  double kedge0, kedgeN, dk;
+  float vec[3];              // 2 pi / L per axis (FP32, for mu only)
+  float los[3];
+};
+
+// Bin of a mode with |i'| = ia, |j'| = ja, k = ka, n = ia^2+ja^2+ka^2.
+// Unambiguous n come from the table; the rest run the reference's exact FP64
+// sequence kmod = sqrt((ki^2 + kj^2) + kk^2), (int)((kmod - kedge0) / dk)
+// (src/multipole.c:132-158, :593-605) with correctly rounded intrinsics.
+__device__ __forceinline__ int mode_bin(const ModeGeom& g, int ia, int ja, int ka, int n) {
+  if (g.bintab) {
+    const int t = __ldg(&g.bintab[n]);
+    if (t != -2) return t;
+  }
+  const int h = g.ng / 2 + 1;
+  double km2 = __dadd_rn(__ldg(&g.ksq[ia]), __ldg(&g.ksq[h + ja]));
+  if (ka) km2 = __dadd_rn(km2, __ldg(&g.ksq[2 * h + ka]));
+  const double kmod = g.logscale ? 0.5 * log10(km2) : __dsqrt_rn(km2);
+  if (kmod < g.kedge0 || kmod >= g.kedgeN) return -1;
+  const int b = (int)__ddiv_rn(__dsub_rn(kmod, g.kedge0), g.dk);
+  return (b < 0 || b >= g.nbin) ? -1 : b;
+}
+
+// Legendre polynomial P_ell(x) (math/legpoly.h:47-62), FP32.
+__device__ __forceinline__ float legendre(int ell, float x) {
+  const float x2 = x * x;
+  switch (ell) {
+    case 0: return 1.f;
+    case 1: return x;
+    case 2: return 1.5f * x2 - 0.5f;
+    case 3: return 2.5f * x * (x2 - 0.6f);
+    case 4: return (4.375f * x2 - 3.75f) * x2 + 0.375f;
+    case 5: return 8.75f * x * ((0.9f * x2 - 1.f) * x2 + 0.21428571428571428f);
+    default: return ((14.4375f * x2 - 19.6875f) * x2 + 6.5625f) * x2 - 0.3125f;
+  }
+}
+
+inline int signed_index(int i, int ng) { return (i <= (ng >> 1)) ? i : i - ng; }
+__device__ __forceinline__ int dsigned(int i, int ng) { return (i <= (ng >> 1)) ? i : i - ng; }
+
+}  // namespace ps

@@ -1,0 +1,110 @@
+// ps_internal.h -- launch wrappers shared by the translation units of
+// libpowspec_gpu.so.  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "ps_common.cuh"
+
+namespace ps {
+
+// Particle source for the assignment kernels.
+struct Particles {
+  const double* aos;  // {x, y, z, w} records, or NULL
+  const float* x;     // SoA arrays when aos == NULL
+  const float* y;
+  const float* z;
+  const float* w;     // NULL: unit weights
+  size_t n;
+};
+
+struct AssignArgs {
+  int ng;
+  int assign;
+  double box[3];
+  unsigned long long* mesh0;  // plain grid (lower corner 0)
+  unsigned long long* mesh1;  // half-cell shifted grid, or NULL
+  double* wsum;               // [2]: sum w, sum |w| (accumulated)
+  int* err;                   // bit 0: particle outside [0, L)
+};
+
+// Returns the number of kernel launches issued.
+int launch_assign(const Particles& p, const AssignArgs& a, cudaStream_t s);
+
+// z transform: fixed-point grid [x][y][z] -> A[x][kz][y] (complex).
+struct PassAArgs {
+  int ng;
+  int ty;                       // y rows per CTA
+  const long long* grid;        // fixed-point input, or NULL
+  const float* fgrid;           // FP32 input when grid == NULL
+  float2* out;
+  const double* wsum;           // mean offset source: wsum[0] = W
+  const float2* tw_half;        // length ng/2 twiddles
+  const float2* tw_full;        // length ng twiddles (r2c split)
+  FftPlan plan_half;
+};
+int launch_pass_a(const PassAArgs& a, cudaStream_t s);
+
+// y transform: A[x][kz][y] -> B[kz][ky][x].
+struct PassBArgs {
+  int ng;
+  int tx;
+  const float2* in;
+  float2* out;
+  const float2* tw_full;
+  FftPlan plan_full;
+};
+int launch_pass_b(const PassBArgs& a, cudaStream_t s);
+
+// x transform of B[kz][ky][x] rows, then either stored in the FFTW layout
+// [x][y][kz] (store mode) or combined, windowed and binned (bin mode).
+struct PassCArgs {
+  int ng;
+  int ty;
+  int nfield;                   // 1, 2 (interlace or 2 catalogues) or 4
+  int interlace;
+  int ncat;
+  int nspec;                    // spectra accumulated: pairs (sa, sb)
+  int spec_a[3], spec_b[3];     // catalogue indices of each spectrum
+  const float2* in[4];          // field f = cat * (interlace ? 2 : 1) + mesh
+  float2* store;                // store mode target (FFTW layout), or NULL
+  const float2* tw_full;
+  FftPlan plan_full;
+  ModeGeom geom;
+  double* partials;             // [grid][nspec*npole*nbin] FP64
+  int grid;                     // persistent CTAs (bin mode)
+};
+int launch_pass_c(const PassCArgs& a, cudaStream_t s);
+
+// Binning of standard-layout half-complex fields [x][y][kz].
+struct BinFieldArgs {
+  int ng;
+  const float2* f1;
+  const float2* f2;
+  ModeGeom geom;
+  double* partials;             // [grid][npole*nbin]
+  int grid;
+};
+int launch_bin_fields(const BinFieldArgs& a, cudaStream_t s);
+
+// Geometry-only sweep: mode counts, sum of |k| and sum of w L_l(mu) per bin
+// (FP64), accumulated into cnt[nbin], ksum[nbin], lcnt[npole*nbin].
+struct GeomArgs {
+  int ng;
+  ModeGeom geom;
+  double vec[3];
+  double los[3];
+  unsigned long long* cnt;
+  double* ksum;
+  double* lcnt;
+};
+int launch_geometry(const GeomArgs& a, cudaStream_t s);
+
+// Deterministic reduction of per-CTA partials: out[j] = sum_g part[g][j].
+int launch_reduce(const double* part, int grid, int width, double* out, cudaStream_t s);
+
+// Minimum shared memory per CTA the passes need (bytes).
+size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin);
+
+}  // namespace ps

@@ -1,0 +1,126 @@
+"""Generate the golden fixtures of tests/golden/ from the REFERENCE itself.
+
+Runs the unmodified reference sources (compiled from source into
+oracle/_ref by ``make -C oracle ref``, linked against the FFTW-API shim)
+with one OpenMP thread so that every output is deterministic, and stores
+inputs + outputs as .npz files.  The reference publishes no test vectors, so
+these are the pins of the oracle and of the GPU path:
+
+* ``ref_cases.npz``: seeded catalogues (float64 x, y, z, w) and the
+  reference outputs k, kedge, km, cnt, lcnt, pl, xpl, shot, norm for a grid
+  of settings (every scheme, interlacing on/off, linear and log bins, all
+  poles, auto + cross, KMAX set, tilted line of sight, non-cubic box).
+* ``ref_meshes.npz``: the reference density meshes Fr / Frl at Ng = 16 for
+  every scheme, interlaced.
+* ``cli/``: an ASCII catalogue, a powspec.conf and the reference POWSPEC
+  output file for it (the output-format pin).
+
+Usage (in a tree that has the reference sources):  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from powspec_gb300 import catalog  # noqa: E402
+
+CASES = [
+    # name, ng, assign, interlace, poles, dk, log, kmin, kmax, ncat, box, los, npart, kind
+    ("ngp_lin", 16, 0, 0, (0, 2, 4), 0.01, 0, 0.0, -1, 1, 1000.0, (0, 0, 1), 3000, "lognormal"),
+    ("cic_lin", 16, 1, 0, (0, 2, 4), 0.01, 0, 0.0, -1, 1, 1000.0, (0, 0, 1), 3000, "lognormal"),
+    ("tsc_il", 16, 2, 1, (0, 2, 4), 0.01, 0, 0.0, -1, 1, 1000.0, (0, 0, 1), 3000, "lognormal"),
+    ("pcs_il", 16, 3, 1, (0, 2, 4), 0.01, 0, 0.0, -1, 1, 1000.0, (0, 0, 1), 3000, "lognormal"),
+    ("cic_il_allpoles", 24, 1, 1, (0, 1, 2, 3, 4, 5, 6), 0.008, 0, 0.0, -1, 1, 1000.0, (0, 0, 1), 4000, "lognormal"),
+    ("tsc_cross", 32, 2, 0, (0, 2, 4), 0.01, 0, 0.0, -1, 2, 1000.0, (0, 0, 1), 5000, "lognormal"),
+    ("pcs_il_cross", 32, 3, 1, (0, 2, 4), 0.01, 0, 0.0, -1, 2, 1000.0, (0, 0, 1), 5000, "lognormal"),
+    ("cic_log", 32, 1, 1, (0, 2), 0.1, 1, np.log10(0.008), -1, 1, 1000.0, (0, 0, 1), 4000, "lognormal"),
+    ("tsc_kmax_los", 32, 2, 1, (0, 2, 4), 0.006, 0, 0.01, 0.07, 1, 1000.0, (0.6, 0, 0.8), 4000, "lognormal"),
+    ("cic_kf_edges", 32, 1, 0, (0, 2, 4), 2 * np.pi / 1000.0, 0, 0.0, -1, 1, 1000.0, (0, 0, 1), 4000, "uniform"),
+    ("cic_noncubic", 16, 1, 0, (0, 2), 0.01, 0, 0.0, -1, 1, (1000.0, 800.0, 1200.0), (0, 0, 1), 3000, "uniform"),
+    ("pcs_weights", 32, 3, 1, (0, 2, 4), 0.01, 0, 0.0, -1, 1, 1000.0, (0, 0, 1), 4000, "weighted"),
+]
+
+
+def make_cat(kind, n, box, seed):
+    b = np.array(box if isinstance(box, tuple) else (box,) * 3)
+    if kind == "uniform":
+        c = catalog.uniform(n, box=1.0, seed=seed)
+        c[:, :3] = np.minimum(c[:, :3] * b, np.nextafter(b, 0))
+        return c
+    if kind == "weighted":
+        c = catalog.lognormal(n, box=float(b[0]), seed=seed, ngen=32, weights=(0.5, 1.5))
+        return c
+    return catalog.lognormal(n, box=float(b[0]), seed=seed, ngen=32)
+
+
+def main():
+    if oracle.build_ref() is None:
+        raise SystemExit("reference sources not found: cannot generate fixtures")
+    oracle.build_port()
+    oracle.set_threads(1)
+    out = {}
+    for ci, (name, ng, a, il, poles, dk, lg, kmin, kmax, ncat, box, los, npart, kind) in enumerate(CASES):
+        cats = [make_cat(kind, npart, box, 100 + 10 * ci + j) for j in range(ncat)]
+        spec = oracle.Spec(ng=ng, box=box, assign=a, interlace=bool(il), poles=poles, los=los,
+                           kmin=kmin, kmax=kmax, dk=dk, logscale=bool(lg),
+                           isauto=(True, True), iscross=ncat == 2)
+        r = oracle.run("ref", spec, cats)
+        pre = f"{name}/"
+        for j, c in enumerate(cats):
+            out[pre + f"cat{j}"] = c
+        out[pre + "settings"] = np.array([ng, a, il, dk, lg, kmin, kmax, ncat], dtype=np.float64)
+        out[pre + "box"] = np.array(spec.box3())
+        out[pre + "los"] = np.array(los, dtype=np.float64)
+        out[pre + "poles"] = np.array(poles, dtype=np.int64)
+        for f in ("k", "kedge", "km", "cnt", "lcnt", "pl", "xpl", "shot", "norm"):
+            out[pre + f] = getattr(r, f)
+        print(f"{name}: nbin={r.nbin} N={[len(c) for c in cats]}")
+    np.savez_compressed(os.path.join(HERE, "ref_cases.npz"), **out)
+
+    meshes = {}
+    cat = make_cat("lognormal", 2000, 1000.0, 7)
+    meshes["cat"] = cat
+    for a in range(4):
+        m0, m1 = oracle.assign("ref", cat, 16, 1000.0, a, 1)
+        meshes[f"fr_{a}"] = m0
+        meshes[f"frl_{a}"] = m1
+    np.savez_compressed(os.path.join(HERE, "ref_meshes.npz"), **meshes)
+
+    # CLI / output-format pin
+    cli = os.path.join(HERE, "cli")
+    os.makedirs(cli, exist_ok=True)
+    cat = make_cat("lognormal", 1500, 500.0, 11)
+    np.savetxt(os.path.join(cli, "data.txt"), cat, fmt="%.8f")
+    conf = """DATA_CATALOG    = data.txt
+DATA_FORMATTER  = "%lf %lf %lf %lf"
+DATA_POSITION   = [$1, $2, $3]
+DATA_WT_COMP    = $4
+CUBIC_SIM       = T
+BOX_SIZE        = 500
+GRID_SIZE       = 32
+PARTICLE_ASSIGN = 2
+GRID_INTERLACE  = T
+MULTIPOLE       = [0, 2, 4]
+BIN_SIZE        = 0.02
+OUTPUT_AUTO     = ref_auto.txt
+OVERWRITE       = 1
+VERBOSE         = F
+"""
+    with open(os.path.join(cli, "powspec.conf"), "w") as f:
+        f.write(conf)
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.run([oracle.REF_CLI, "-c", "powspec.conf"], cwd=cli, check=True, env=env,
+                   stdout=subprocess.DEVNULL)
+    print("cli fixture written")
+
+
+if __name__ == "__main__":
+    main()
