@@ -132,6 +132,10 @@ int ps_gpu_last_timings(const ps_gpu_ctx *ctx, float *ms, int nmax);
 /* Number of kernel launches issued by the last assign+execute cycle. */
 int ps_gpu_last_launches(const ps_gpu_ctx *ctx);
 
+/* The context's CUDA stream (a cudaStream_t), so that callers can order
+ * their own work or record CUDA events around the context's launches. */
+void *ps_gpu_stream(const ps_gpu_ctx *ctx);
+
 /* ---- Stage-level entry points (checked against the oracle stage by stage) */
 
 /* Copies mesh m (0: Fr, 1: Frl) of catalogue cat to the host as doubles,

@@ -33,7 +33,7 @@ EXPORTED = [
     "ps_gpu_create", "ps_gpu_destroy", "ps_gpu_nbin", "ps_gpu_assign_aos",
     "ps_gpu_assign_soa", "ps_gpu_execute", "ps_gpu_last_error",
     "ps_gpu_last_timings", "ps_gpu_last_launches", "ps_gpu_read_mesh",
-    "ps_gpu_fft_r2c_host", "ps_gpu_bin_fields_host",
+    "ps_gpu_fft_r2c_host", "ps_gpu_bin_fields_host", "ps_gpu_stream",
 ]
 
 
@@ -110,6 +110,8 @@ def lib():
         L.ps_gpu_last_error.restype = ctypes.c_char_p
         L.ps_gpu_last_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.ps_gpu_last_launches.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_stream.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_stream.restype = ctypes.c_void_p
         L.ps_gpu_read_mesh.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.ps_gpu_fft_r2c_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ps_gpu_bin_fields_host.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
@@ -251,6 +253,10 @@ class Estimator:
 
     def launches(self):
         return lib().ps_gpu_last_launches(self._ctx)
+
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        return lib().ps_gpu_stream(self._ctx) or 0
 
     # -- stage-level entry points
     def read_mesh(self, cat=0, m=0):

@@ -21,6 +21,7 @@ constexpr int kAssignThreads = 256;
 struct Stencil {
   int node[4];
   float w[4];
+  int big;  // index of the largest weight (>= 1/2 CIC, 1/2 TSC, 0.48 PCS)
 };
 
 // Reference FP64 grid coordinate of one axis; returns the truncated cell and
@@ -46,12 +47,14 @@ __device__ __forceinline__ void stencil_1d(int i0, double d, int ng, Stencil& st
   if (S == 1) {  // NGP: round up at d >= 0.5 (src/genr_mesh.c:64-66)
     st.node[0] = (d >= 0.5) ? ((i0 == ng - 1) ? 0 : i0 + 1) : i0;
     st.w[0] = 1.f;
+    st.big = 0;
   } else if (S == 2) {  // CIC (src/genr_mesh.c:98-108)
     const float f = (float)d;
     st.node[0] = i0;
     st.node[1] = (i0 == ng - 1) ? 0 : i0 + 1;
     st.w[0] = 1.f - f;
     st.w[1] = f;
+    st.big = (f < 0.5f) ? 0 : 1;
   } else if (S == 3) {  // TSC (src/genr_mesh.c:153-173)
     if (d < 0.5) {
       const float f = (float)d;
@@ -71,6 +74,7 @@ __device__ __forceinline__ void stencil_1d(int i0, double d, int ng, Stencil& st
       st.w[1] = 0.75f - f * f;
     }
     st.w[2] = 1.f - st.w[0] - st.w[1];
+    st.big = 1;
   } else {  // PCS: cubic B-spline on nodes i0-1 .. i0+2 (src/genr_mesh.c:257-270)
     const float f = (float)d;
     st.node[1] = i0;
@@ -83,6 +87,7 @@ __device__ __forceinline__ void stencil_1d(int i0, double d, int ng, Stencil& st
     st.w[2] = (1.f + 3.f * (f + f2 - f3)) * s;
     st.w[1] = (4.f - 6.f * f2 + 3.f * f3) * s;
     st.w[0] = 1.f - st.w[1] - st.w[2] - st.w[3];
+    st.big = (f < 0.5f) ? 1 : 2;
   }
 }
 
@@ -93,7 +98,7 @@ __device__ __forceinline__ void red_add(unsigned long long* cell, long long v) {
 template <int S, bool AOS>
 __global__ void __launch_bounds__(kAssignThreads)
     k_assign(Particles p, int ng, double L0, double L1, double L2,
-             unsigned long long* __restrict__ mesh, int shift, double* wsum, int* err) {
+             unsigned long long* __restrict__ mesh, int shift, double* wpart, int* err) {
   const double L[3] = {L0, L1, L2};
   double ws = 0.0, wa = 0.0;
   int bad = 0;
@@ -131,7 +136,16 @@ __global__ void __launch_bounds__(kAssignThreads)
       red_add(mesh + cell, __double2ll_rn(w * 4294967296.0));
       continue;
     }
+    // Every node gets its FP32 share rounded to fixed point, except the
+    // stencil's largest node, which gets the remainder: the particle's
+    // quantised weight llrint(w 2^32) is conserved exactly.
+    const long long qtot = __double2ll_rn(w * 4294967296.0);
     const float wf = (float)w * kFixScale;
+    long long qsum = 0;
+    size_t acell = 0;
+    int anc[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) anc[d] = st[d].big;
 #pragma unroll
     for (int a = 0; a < S; a++) {
       const float wx = st[0].w[a] * wf;
@@ -141,10 +155,18 @@ __global__ void __launch_bounds__(kAssignThreads)
         const size_t row = ((size_t)st[0].node[a] * ng + st[1].node[b]) * ng;
 #pragma unroll
         for (int c = 0; c < S; c++) {
-          red_add(mesh + row + st[2].node[c], __float2ll_rn(wxy * st[2].w[c]));
+          const size_t cell = row + st[2].node[c];
+          if (a == anc[0] && b == anc[1] && c == anc[2]) {
+            acell = cell;
+            continue;
+          }
+          const long long q = __float2ll_rn(wxy * st[2].w[c]);
+          qsum += q;
+          red_add(mesh + cell, q);
         }
       }
     }
+    red_add(mesh + acell, qtot - qsum);
   }
   // Block reduction of the weight sums (plain grid only).
   if (!shift) {
@@ -166,11 +188,24 @@ __global__ void __launch_bounds__(kAssignThreads)
         t0 += sws[k];
         t1 += swa[k];
       }
-      atomicAdd(&wsum[0], t0);
-      atomicAdd(&wsum[1], t1);
+      // per-block partials, summed in block order by k_wsum: deterministic
+      wpart[2 * blockIdx.x] = t0;
+      wpart[2 * blockIdx.x + 1] = t1;
     }
   }
   if (bad) atomicOr(err, 1);
+}
+
+__global__ void k_wsum(const double* __restrict__ wpart, int nblocks, double* wsum) {
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0;
+    for (int b = 0; b < nblocks; b++) {
+      t0 += wpart[2 * b];
+      t1 += wpart[2 * b + 1];
+    }
+    wsum[0] = t0;
+    wsum[1] = t1;
+  }
 }
 
 template <int S>
@@ -179,7 +214,7 @@ int launch_s(const Particles& p, const AssignArgs& a, cudaStream_t s) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   size_t blocks = (p.n + kAssignThreads - 1) / kAssignThreads;
-  const size_t cap = (size_t)nsm * 8;
+  const size_t cap = (size_t)kAssignMaxBlocks;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   int n = 0;
@@ -187,11 +222,15 @@ int launch_s(const Particles& p, const AssignArgs& a, cudaStream_t s) {
     unsigned long long* mesh = m ? a.mesh1 : a.mesh0;
     if (p.aos)
       k_assign<S, true><<<(unsigned)blocks, kAssignThreads, 0, s>>>(
-          p, a.ng, a.box[0], a.box[1], a.box[2], mesh, m, a.wsum, a.err);
+          p, a.ng, a.box[0], a.box[1], a.box[2], mesh, m, a.wpart, a.err);
     else
       k_assign<S, false><<<(unsigned)blocks, kAssignThreads, 0, s>>>(
-          p, a.ng, a.box[0], a.box[1], a.box[2], mesh, m, a.wsum, a.err);
+          p, a.ng, a.box[0], a.box[1], a.box[2], mesh, m, a.wpart, a.err);
     n++;
+    if (m == 0) {
+      k_wsum<<<1, 32, 0, s>>>(a.wpart, (int)blocks, a.wsum);
+      n++;
+    }
   }
   return n;
 }

@@ -17,7 +17,8 @@
 namespace ps {
 namespace {
 
-constexpr int kRun = 8;  // consecutive modes per thread
+constexpr int kRun = 8;          // consecutive modes per thread
+constexpr int kMergeEvery = 8;   // tiles between FP32 -> FP64 merges
 
 template <int NSPEC>
 struct RunAcc {
@@ -62,20 +63,22 @@ __device__ __forceinline__ void run_add(RunAcc<NSPEC>& ra, const ModeGeom& g, in
   }
 }
 
-// Merge the FP32 tile accumulators of the touched bin range into the CTA's
-// FP64 slice and clear them.  Ends with a barrier.
-__device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int nbin, int lo,
-                           int hi) {
-  // block-wide min/max of the touched range
+// Record a thread's touched bin range [lo, hi] into the block's range.
+__device__ __forceinline__ void note_range(int* srange, int lo, int hi) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
     hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
   }
-  if ((threadIdx.x & 31) == 0) {
+  if ((threadIdx.x & 31) == 0 && hi >= lo) {
     atomicMin(&srange[0], lo);
     atomicMax(&srange[1], hi);
   }
+}
+
+// Merge the FP32 accumulators of the touched bin range into the CTA's FP64
+// slice and clear them.  Starts and ends with a barrier.
+__device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int nbin) {
   __syncthreads();
   const int blo = srange[0], bhi = srange[1];
   if (bhi >= blo) {
@@ -96,15 +99,15 @@ __device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int
 }
 
 // Pass C.  Lines of tile: field f, row r -> smem line f * nl + r.
-template <int NSPEC, bool STORE>
+template <int NSPEC, bool STORE, bool P2>
 __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ PassCArgs a) {
   extern __shared__ float2 sm[];
-  const int ng = a.ng, ngk = (ng >> 1) + 1, ls = ng + 1, h = ng >> 1;
+  const int ng = a.ng, ngk = (ng >> 1) + 1, ls = line_stride(ng, P2), h = ng >> 1;
   const int nty = (ng + a.ty - 1) / a.ty;
   const int ntile = ngk * nty;
   const ModeGeom& g = a.geom;
   const int nacc = NSPEC * g.npole;
-  const size_t tile_elems = (size_t)a.nfield * a.ty * ls;
+  const size_t tile_elems = (size_t)a.nfield * a.ty * ls;  // one ping-pong buffer
   float2* sm2 = sm + tile_elems;  // second FFT buffer (ping-pong)
   float* tacc = reinterpret_cast<float*>(sm + 2 * tile_elems);
   __shared__ int srange[2];
@@ -126,6 +129,7 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
     spec_b[s] = a.spec_b[s];
   }
 
+  int ntiles_acc = 0;
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const int kz = tile / nty;
     const int ky0 = (tile - kz * nty) * a.ty;
@@ -136,18 +140,19 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
         const int r = e / h, m = e - r * h;
         const float4 v = __ldcs(reinterpret_cast<const float4*>(src + (size_t)r * ng) + m);
         float2* L = sm + (f * nl + r) * ls;
-        L[2 * m] = make_float2(v.x, v.y);
-        L[2 * m + 1] = make_float2(v.z, v.w);
+        L[lidx<P2>(2 * m)] = make_float2(v.x, v.y);
+        L[lidx<P2>(2 * m + 1)] = make_float2(v.z, v.w);
       }
     }
     __syncthreads();
-    const float2* X = fft_lines_pp(sm, sm2, a.plan_full, a.nfield * nl, ls, a.tw_full);
+    const float2* X = P2 ? fft2_lines_pp<4>(sm, sm2, a.plan_full.logn, a.nfield * nl, ls, a.tw_full)
+                         : fft_lines_pp(sm, sm2, a.plan_full, a.nfield * nl, ls, a.tw_full);
 
     if (STORE) {
       // FFTW layout [x][y][kz]; strided stores (diagnostic path only).
       for (int e = threadIdx.x; e < nl * ng; e += blockDim.x) {
         const int r = e / ng, i = e - r * ng;
-        a.store[((size_t)i * ng + ky0 + r) * ngk + kz] = X[r * ls + i];
+        a.store[((size_t)i * ng + ky0 + r) * ngk + kz] = X[r * ls + lidx<P2>(i)];
       }
       __syncthreads();
       continue;
@@ -182,17 +187,18 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
         const int b = mode_bin(g, ia, ja, kz, n);
         if (b < 0) continue;
         // combined field of each catalogue: (F0 + exp(i theta) F1) / 2
-        float2 G0 = X[r * ls + i], G1 = G0;
+        const int li = lidx<P2>(i);
+        float2 G0 = X[r * ls + li], G1 = G0;
         if (interlace) {
           const float2 ph = __ldg(&g.phase[ip + jp + kz + ng]);
-          const float2 t = cmul(ph, X[(nl + r) * ls + i]);
+          const float2 t = cmul(ph, X[(nl + r) * ls + li]);
           G0 = make_float2(0.5f * (G0.x + t.x), 0.5f * (G0.y + t.y));
         }
         if (two_cat) {
-          G1 = X[(mpc * nl + r) * ls + i];
+          G1 = X[(mpc * nl + r) * ls + li];
           if (interlace) {
             const float2 ph = __ldg(&g.phase[ip + jp + kz + ng]);
-            const float2 t = cmul(ph, X[((mpc + 1) * nl + r) * ls + i]);
+            const float2 t = cmul(ph, X[((mpc + 1) * nl + r) * ls + li]);
             G1 = make_float2(0.5f * (G1.x + t.x), 0.5f * (G1.y + t.y));
           }
         }
@@ -210,9 +216,15 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
       }
       run_flush<NSPEC>(ra, tacc, g.npole, g.nbin, lo, hi);
     }
-    __syncthreads();
-    merge_tile(tacc, srange, part, nacc, g.nbin, lo, hi);
+    note_range(srange, lo, hi);
+    if (++ntiles_acc == kMergeEvery) {
+      merge_tile(tacc, srange, part, nacc, g.nbin);
+      ntiles_acc = 0;
+    } else {
+      __syncthreads();
+    }
   }
+  if (!STORE && ntiles_acc) merge_tile(tacc, srange, part, nacc, g.nbin);
 }
 
 // Stand-alone binning of FFTW-layout fields [x][y][kz]: one line per (x, y).
@@ -267,8 +279,8 @@ __global__ void __launch_bounds__(kFftThreads) k_bin_fields(const __grid_constan
       }
       run_flush<1>(ra, tacc, g.npole, g.nbin, lo, hi);
     }
-    __syncthreads();
-    merge_tile(tacc, srange, part, nacc, g.nbin, lo, hi);
+    note_range(srange, lo, hi);
+    merge_tile(tacc, srange, part, nacc, g.nbin);
   }
 }
 
@@ -350,39 +362,41 @@ __global__ void k_reduce(const double* __restrict__ part, int grid, int width,
 
 }  // namespace
 
-size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin) {
-  return 2 * (size_t)nfield * ty * (ng + 1) * sizeof(float2) + (size_t)nacc * nbin * sizeof(float);
+size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin, bool pow2) {
+  return 2 * (size_t)nfield * ty * line_stride(ng, pow2) * sizeof(float2) +
+         (size_t)nacc * nbin * sizeof(float);
 }
 
-int launch_pass_c(const PassCArgs& a, cudaStream_t s) {
+namespace {
+template <int NSPEC, bool STORE, bool P2>
+void launch_c(const PassCArgs& a, unsigned grid, size_t smem, cudaStream_t s) {
+  cudaFuncSetAttribute(k_pass_c<NSPEC, STORE, P2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  k_pass_c<NSPEC, STORE, P2><<<grid, kFftThreads, smem, s>>>(a);
+}
+template <bool P2>
+void launch_c_p(const PassCArgs& a, cudaStream_t s) {
   const int ngk = a.ng / 2 + 1;
   const int nty = (a.ng + a.ty - 1) / a.ty;
   const int ntile = ngk * nty;
   if (a.store) {
-    const size_t smem = pass_c_smem(a.ng, a.ty, a.nfield, 0, 0);
-    cudaFuncSetAttribute(k_pass_c<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    k_pass_c<1, true><<<(unsigned)ntile, kFftThreads, smem, s>>>(a);
-    return 1;
+    launch_c<1, true, P2>(a, (unsigned)ntile, pass_c_smem(a.ng, a.ty, a.nfield, 0, 0, P2), s);
+    return;
   }
-  const size_t smem = pass_c_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole, a.geom.nbin);
+  const size_t smem = pass_c_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole, a.geom.nbin, P2);
   switch (a.nspec) {
-    case 1:
-      cudaFuncSetAttribute(k_pass_c<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
-      k_pass_c<1, false><<<(unsigned)a.grid, kFftThreads, smem, s>>>(a);
-      break;
-    case 2:
-      cudaFuncSetAttribute(k_pass_c<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
-      k_pass_c<2, false><<<(unsigned)a.grid, kFftThreads, smem, s>>>(a);
-      break;
-    default:
-      cudaFuncSetAttribute(k_pass_c<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
-      k_pass_c<3, false><<<(unsigned)a.grid, kFftThreads, smem, s>>>(a);
-      break;
+    case 1: launch_c<1, false, P2>(a, (unsigned)a.grid, smem, s); break;
+    case 2: launch_c<2, false, P2>(a, (unsigned)a.grid, smem, s); break;
+    default: launch_c<3, false, P2>(a, (unsigned)a.grid, smem, s); break;
   }
+}
+}  // namespace
+
+int launch_pass_c(const PassCArgs& a, cudaStream_t s) {
+  if (a.plan_full.logn >= 0)
+    launch_c_p<true>(a, s);
+  else
+    launch_c_p<false>(a, s);
   return 1;
 }
 

@@ -65,6 +65,12 @@ double alias_corr(int interlace, int assign, double pik) {
 bool make_plan(int n, FftPlan& p) {
   p.n = n;
   p.npass = 0;
+  p.logn = -1;
+  if ((n & (n - 1)) == 0) {
+    int l = 0;
+    while ((1 << l) < n) l++;
+    p.logn = l;
+  }
   int m = n, e = 0;
   while (m % 2 == 0) { m /= 2; e++; }
   while (e > 0) {
@@ -115,14 +121,17 @@ struct ps_gpu_ctx {
   ModeGeom geom{};
   int nspec = 0, spec_a[3] = {0, 0, 0}, spec_b[3] = {0, 0, 0}, spec_cat[3] = {0, 0, 0};
   int ty_a = 1, tx_b = 1, ty_c = 1, grid_c = 1;
+  int ty_ap = 1, tx_bp = 1;  // tiles of the pipelined passes
   double* d_part = nullptr;
   double* d_sums = nullptr;
   double* d_wsum = nullptr;  // [2 cats][2]
+  double* d_wpart = nullptr; // [2 * kAssignMaxBlocks]
   int* d_err = nullptr;      // [2 cats]
   double* h_out = nullptr;   // pinned: sums + wsum + err
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
   int assigned[2] = {0, 0};
+  size_t npart[2] = {0, 0};
   cudaEvent_t ev[8] = {};
   bool assign_started = false;
   float timings[6] = {0, 0, 0, 0, 0, 0};
@@ -300,9 +309,12 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   // ---- tiles and persistent grid of the binning pass
   c->ty_a = std::min({ng, 16, kCtaElems / (ng / 2)});
   c->tx_b = std::min({ng, 16, kCtaElems / ng});
+  // pipelined passes: 64 KB staged per tile (int64 rows for z, complex for y)
+  c->ty_ap = std::max(1, std::min(ng, 8192 / ng));
+  c->tx_bp = std::max(1, std::min(ng, 8192 / ng));
   c->ty_c = std::max(1, std::min(ng, kPassCElems / (c->nfield * ng)));
   const int nacc = c->nspec * p.npole;
-  const size_t smem_c = pass_c_smem(ng, c->ty_c, c->nfield, nacc, c->nbin);
+  const size_t smem_c = pass_c_smem(ng, c->ty_c, c->nfield, nacc, c->nbin, c->plan_full.logn >= 0);
   if (smem_c > 227 * 1024)
     return fail(c, PS_GPU_ERR_ARG, "too many bins (%d) for the binning pass", c->nbin);
   const int per_sm = std::max(1, std::min(4, (int)((228 * 1024) / (smem_c + 2048))));
@@ -323,9 +335,10 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)c->grid_c * nacc * c->nbin));
   CU(cudaMalloc(&c->d_sums, sizeof(double) * (size_t)nacc * c->nbin));
   CU(cudaMalloc(&c->d_wsum, sizeof(double) * 4));
-  CU(cudaMalloc(&c->d_err, sizeof(int) * 2));
+  CU(cudaMalloc(&c->d_wpart, sizeof(double) * 2 * kAssignMaxBlocks));
+  CU(cudaMalloc(&c->d_err, sizeof(int) * 4));
   CU(cudaMemset(c->d_wsum, 0, sizeof(double) * 4));
-  CU(cudaMemset(c->d_err, 0, sizeof(int) * 2));
+  CU(cudaMemset(c->d_err, 0, sizeof(int) * 4));
   CU(cudaMallocHost(&c->h_out, sizeof(double) * ((size_t)nacc * c->nbin + 8)));
 
   // ---- geometry sweep: counts, mean |k|, multipole mode weights
@@ -374,7 +387,7 @@ void ps_gpu_destroy(ps_gpu_ctx* c) {
     if (c->cbuf[f]) cudaFree(c->cbuf[f]);
   }
   void* bufs[] = {c->d_bintab, c->d_ksq, c->d_win, c->d_phase, c->d_tw_full, c->d_tw_half,
-                  c->d_part, c->d_sums, c->d_wsum, c->d_err, c->d_stage};
+                  c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -396,6 +409,8 @@ int ps_gpu_last_timings(const ps_gpu_ctx* c, float* ms, int nmax) {
 }
 
 int ps_gpu_last_launches(const ps_gpu_ctx* c) { return c ? c->launches : 0; }
+
+void* ps_gpu_stream(const ps_gpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 }  // extern "C"
 
@@ -432,11 +447,13 @@ int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
   a.mesh0 = c->grid[cat * c->mpc];
   a.mesh1 = c->p.interlace ? c->grid[cat * c->mpc + 1] : nullptr;
   a.wsum = c->d_wsum + 2 * cat;
+  a.wpart = c->d_wpart;
   a.err = c->d_err + cat;
   if (pt.n) c->launches += launch_assign(pt, a, c->stream);
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[7], c->stream));
   c->assigned[cat] = 1;
+  c->npart[cat] = pt.n;
   return 0;
 }
 
@@ -490,11 +507,15 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   const int ng = c->ng, npole = p.npole, nbin = c->nbin;
   const int nacc = c->nspec * npole;
 
+  const bool pipe = c->plan_full.logn >= 0 && !getenv("PS_GPU_NO_PIPELINE");
+  CU(cudaMemsetAsync(c->d_err + 2, 0, sizeof(int), s));
   CU(cudaEventRecord(c->ev[0], s));
   for (int f = 0; f < c->nfield; f++) {
     PassAArgs a;
     a.ng = ng;
-    a.ty = c->ty_a;
+    a.ty = pipe ? c->ty_ap : c->ty_a;
+    a.pipe_grid = pipe ? c->nsm : 0;
+    a.err = c->d_err + 2;
     a.grid = (const long long*)c->grid[f];
     a.fgrid = nullptr;
     a.out = c->cbuf[f];
@@ -509,7 +530,9 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   for (int f = 0; f < c->nfield; f++) {
     PassBArgs b;
     b.ng = ng;
-    b.tx = c->tx_b;
+    b.tx = pipe ? c->tx_bp : c->tx_b;
+    b.pipe_grid = pipe ? c->nsm : 0;
+    b.err = c->d_err + 2;
     b.in = c->cbuf[f];
     b.out = (float2*)c->grid[f];
     b.tw_full = c->d_tw_full;
@@ -544,7 +567,7 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   double* h = c->h_out;
   CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nbin, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nbin, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
-  CU(cudaMemcpyAsync(h + (size_t)nacc * nbin + 4, c->d_err, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h + (size_t)nacc * nbin + 4, c->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   float t = 0;
   if (c->assign_started && cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess) c->timings[0] = t;
@@ -557,7 +580,10 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   const double* sums = h;
   const double* wsum = h + (size_t)nacc * nbin;
   const int* errs = (const int*)(h + (size_t)nacc * nbin + 4);
+  if (errs[2]) return fail(c, PS_GPU_ERR_CUDA, "pipelined pass: bulk-copy wait timed out (flags %d)", errs[2]);
   for (int k = 0; k < p.ncat; k++) {
+    // an empty catalogue has no coordinate range (src/genr_mesh.c:518-521)
+    if (!c->npart[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: no objects", k);
     if (errs[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: coordinate outside [0, BOX_SIZE)", k);
     if (!(wsum[2 * k + 1] < kFixMaxWeight))
       return fail(c, PS_GPU_ERR_RANGE, "catalogue %d: total |weight| %g exceeds the fixed-point range", k, wsum[2 * k + 1]);
@@ -641,6 +667,8 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   a.tw_half = c->d_tw_half;
   a.tw_full = c->d_tw_full;
   a.plan_half = c->plan_half;
+  a.pipe_grid = 0;
+  a.err = c->d_err + 2;
   launch_pass_a(a, s);
   PassBArgs b;
   b.ng = ng;
@@ -649,6 +677,8 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   b.out = (float2*)c->grid[0];
   b.tw_full = c->d_tw_full;
   b.plan_full = c->plan_full;
+  b.pipe_grid = 0;
+  b.err = c->d_err + 2;
   launch_pass_b(b, s);
   PassCArgs pc;
   memset(&pc, 0, sizeof pc);

@@ -30,6 +30,7 @@ struct FftPlan {
   int n;
   int npass;
   int radix[kMaxPlan];
+  int logn;  // log2(n) when n is a power of two, else -1
 };
 
 // --------------------------------------------------------------- complex
@@ -119,6 +120,204 @@ __device__ __forceinline__ void dft<5>(float2 (&v)[5]) {
   v[4] = csub(r1, cmul_mi(i1));
   v[2] = cadd(r2, cmul_mi(i2));
   v[3] = csub(r2, cmul_mi(i2));
+}
+
+// x * exp(-2 pi i e / 32) for a compile-time e (folds to constants).
+__device__ __forceinline__ float2 rot32(float2 x, int e) {
+  e &= 31;
+  if (e == 0) return x;
+  if (e == 8) return make_float2(x.y, -x.x);
+  if (e == 16) return make_float2(-x.x, -x.y);
+  if (e == 24) return make_float2(-x.y, x.x);
+  // cos, sin of 2 pi r / 32, r = 0..7
+  const float C[8] = {1.000000000f, 0.980785280f, 0.923879533f, 0.831469612f,
+                      0.707106781f, 0.555570233f, 0.382683432f, 0.195090322f};
+  const float S[8] = {0.000000000f, 0.195090322f, 0.382683432f, 0.555570233f,
+                      0.707106781f, 0.831469612f, 0.923879533f, 0.980785280f};
+  const int q = e >> 3, r = e & 7;
+  // rotate by exp(-i 2 pi r / 32) first, then by (-i)^q
+  float2 y = make_float2(x.x * C[r] + x.y * S[r], x.y * C[r] - x.x * S[r]);
+  if (q == 1) y = make_float2(y.y, -y.x);
+  else if (q == 2) y = make_float2(-y.x, -y.y);
+  else if (q == 3) y = make_float2(-y.y, y.x);
+  return y;
+}
+
+// 16-point DFT as 4 x 4 (input n = 4 n1 + n2, output k = k1 + 4 k2).
+template <>
+__device__ __forceinline__ void dft<16>(float2 (&x)[16]) {
+  float2 y[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; n2++) {
+    float2 t[4] = {x[n2], x[4 + n2], x[8 + n2], x[12 + n2]};
+    dft<4>(t);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) y[n2][k1] = rot32(t[k1], 2 * n2 * k1);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    float2 t[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    dft<4>(t);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) x[k1 + 4 * k2] = t[k2];
+  }
+}
+
+// 32-point DFT as 4 x 8 (input n = 8 n1 + n2, output k = k1 + 4 k2).
+template <>
+__device__ __forceinline__ void dft<32>(float2 (&x)[32]) {
+  float2 y[8][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 8; n2++) {
+    float2 t[4] = {x[n2], x[8 + n2], x[16 + n2], x[24 + n2]};
+    dft<4>(t);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) y[n2][k1] = rot32(t[k1], n2 * k1);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    float2 t[8] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1],
+                   y[4][k1], y[5][k1], y[6][k1], y[7][k1]};
+    dft<8>(t);
+#pragma unroll
+    for (int k2 = 0; k2 < 8; k2++) x[k1 + 4 * k2] = t[k2];
+  }
+}
+
+// Twiddle load that the compiler may not hoist out of a persistent tile
+// loop (hoisting 31 loop-invariant twiddles would pin 62 registers).
+__device__ __forceinline__ float2 ldtw(const float2* p) {
+  float2 v;
+  asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  return v;
+}
+
+// ---------------------------------------------------- power-of-two engine
+// Lines of n = 2^logn complex in shared memory use a padded layout: element
+// e of a line sits at e + e/32, so the stride-32 writes of a radix-32 pass
+// fall in distinct banks.  Radix-32 passes run first (no twiddles in the
+// first, conflict-free strides in all), then one remainder pass of radix
+// 2, 4, 8 or 16.  All index arithmetic is shifts and masks.
+__device__ __forceinline__ int pidx(int e) { return e + (e >> 5); }
+
+// Element e of a line in either layout.
+template <bool PAD>
+__device__ __forceinline__ int lidx(int e) { return PAD ? e + (e >> 5) : e; }
+
+// Line stride (complex) of lines holding `slots` elements: odd, so that
+// reading one element from each of 16 consecutive lines is conflict-free.
+__host__ __device__ inline int line_stride(int slots, bool pad) {
+  int s = pad ? (slots - 1) + ((slots - 1) >> 5) + 1 : slots;
+  return (s & 1) ? s : s + 1;
+}
+
+// In place: every thread stages 32 complex values (one radix-32 butterfly,
+// or 32/R smaller ones), the block synchronises, then stores.
+// Requires nlines << logn <= kCtaElems.
+template <int R, int LOGR>
+__device__ __forceinline__ void fft2_pass(float2* buf, int logn, int nlines, int ls, int logNs,
+                                          const float2* __restrict__ tw, int tid = threadIdx.x) {
+  constexpr int BPT = 32 / R;
+  const int logm = logn - LOGR;
+  const int mmask = (1 << logm) - 1, nsmask = (1 << logNs) - 1;
+  const int total = nlines << logm;
+  const int tws = logn - logNs - LOGR;
+  float2 v[BPT][R];
+#pragma unroll
+  for (int t = 0; t < BPT; t++) {
+    const int b = tid + t * blockDim.x;
+    if (b < total) {
+      const int line = b >> logm, j = b & mmask, k = j & nsmask;
+      const float2* src = buf + line * ls;
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int e = j + (r << logm);
+        float2 x = src[pidx(e)];
+        if (r > 0 && k > 0) x = cmul(x, ldtw(&tw[(r * k) << tws]));
+        v[t][r] = x;
+      }
+      dft<R>(v[t]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < BPT; t++) {
+    const int b = tid + t * blockDim.x;
+    if (b < total) {
+      const int line = b >> logm, j = b & mmask, k = j & nsmask;
+      float2* dst = buf + line * ls;
+      const int e0 = ((j >> logNs) << (logNs + LOGR)) + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) dst[pidx(e0 + (r << logNs))] = v[t][r];
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void fft2_lines(float2* buf, int logn, int nlines, int ls,
+                                           const float2* __restrict__ tw) {
+  int logNs = 0;
+  for (; logn - logNs >= 5; logNs += 5) fft2_pass<32, 5>(buf, logn, nlines, ls, logNs, tw);
+  switch (logn - logNs) {
+    case 4: fft2_pass<16, 4>(buf, logn, nlines, ls, logNs, tw); break;
+    case 3: fft2_pass<8, 3>(buf, logn, nlines, ls, logNs, tw); break;
+    case 2: fft2_pass<4, 2>(buf, logn, nlines, ls, logNs, tw); break;
+    case 1: fft2_pass<2, 1>(buf, logn, nlines, ls, logNs, tw); break;
+    default: break;
+  }
+}
+
+// Ping-pong variant (one butterfly in registers at a time) for persistent
+// kernels that loop over tiles.  Returns the buffer holding the result.
+template <int R, int LOGR>
+__device__ __forceinline__ void fft2_pass_pp(const float2* src, float2* dst, int logn,
+                                             int nlines, int ls, int logNs,
+                                             const float2* __restrict__ tw, int tid = threadIdx.x) {
+  const int logm = logn - LOGR;
+  const int mmask = (1 << logm) - 1, nsmask = (1 << logNs) - 1;
+  const int total = nlines << logm;
+  const int tws = logn - logNs - LOGR;
+  for (int b = tid; b < total; b += blockDim.x) {
+    const int line = b >> logm, j = b & mmask, k = j & nsmask;
+    const float2* s = src + line * ls;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      float2 x = s[pidx(j + (r << logm))];
+      if (r > 0 && k > 0) x = cmul(x, ldtw(&tw[(r * k) << tws]));
+      v[r] = x;
+    }
+    dft<R>(v);
+    float2* d = dst + line * ls;
+    const int e0 = ((j >> logNs) << (logNs + LOGR)) + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) d[pidx(e0 + (r << logNs))] = v[r];
+  }
+  __syncthreads();
+}
+
+// MAXLOG = 5: radix-32 passes; MAXLOG = 4: radix-16 passes (twice the
+// butterflies per pass, for tiles too small to occupy every thread).
+template <int MAXLOG = 5>
+__device__ __forceinline__ float2* fft2_lines_pp(float2* a, float2* b, int logn, int nlines,
+                                                 int ls, const float2* __restrict__ tw) {
+  int logNs = 0;
+  for (; logn - logNs >= MAXLOG; logNs += MAXLOG) {
+    if (MAXLOG == 5) fft2_pass_pp<32, 5>(a, b, logn, nlines, ls, logNs, tw);
+    else fft2_pass_pp<16, 4>(a, b, logn, nlines, ls, logNs, tw);
+    float2* t = a; a = b; b = t;
+  }
+  const int rem = logn - logNs;
+  if (rem) {
+    switch (rem) {
+      case 4: fft2_pass_pp<16, 4>(a, b, logn, nlines, ls, logNs, tw); break;
+      case 3: fft2_pass_pp<8, 3>(a, b, logn, nlines, ls, logNs, tw); break;
+      case 2: fft2_pass_pp<4, 2>(a, b, logn, nlines, ls, logNs, tw); break;
+      default: fft2_pass_pp<2, 1>(a, b, logn, nlines, ls, logNs, tw); break;
+    }
+    float2* t = a; a = b; b = t;
+  }
+  return a;
 }
 
 // One Stockham radix-R pass over `nlines` lines of length n held in shared
@@ -248,6 +447,198 @@ __device__ __forceinline__ float fix_to_float(long long d) {
   const unsigned lo = (unsigned)(d & 0xffffffffull);
   return (float)hi + (float)lo * 2.3283064365386963e-10f;
 }
+
+
+// ------------------------------------------------ async bulk copies (TMA)
+// One-dimensional cp.async.bulk global -> shared with mbarrier completion.
+// Addresses and sizes must be multiples of 16 bytes.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after `limit` polls (each poll may suspend the
+// thread for a hardware-defined time) and reports failure.
+constexpr long long kWaitLimit = 1ll << 24;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long i = 0; i < kWaitLimit; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// First radix pass of a pipelined transform: reads lines of n = 2^logn
+// from an unpadded staging buffer (line stride sstride), writes the padded
+// FFT buffer (line stride ls).
+template <int R, int LOGR>
+__device__ __forceinline__ void fft2_first_pass(const float2* src, int sstride, float2* dst,
+                                                int logn, int nlines, int ls,
+                                                int tid = threadIdx.x) {
+  const int logm = logn - LOGR;
+  const int mmask = (1 << logm) - 1;
+  const int total = nlines << logm;
+  for (int b = tid; b < total; b += blockDim.x) {
+    const int line = b >> logm, j = b & mmask;
+    const float2* s = src + line * sstride + j;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = s[r << logm];
+    dft<R>(v);
+    float2* d = dst + line * ls;
+#pragma unroll
+    for (int r = 0; r < R; r++) d[pidx(j * R + r)] = v[r];
+  }
+  __syncthreads();
+}
+
+// Same, for a first pass that reads fixed-point int64 cells (two per
+// complex input value) and subtracts a constant offset while converting.
+template <int R, int LOGR>
+__device__ __forceinline__ void fft2_first_pass_fix(const long long* src, int sstride,
+                                                    long long off, float2* dst, int logn,
+                                                    int nlines, int ls, int tid = threadIdx.x) {
+  const int logm = logn - LOGR;
+  const int mmask = (1 << logm) - 1;
+  const int total = nlines << logm;
+  for (int b = tid; b < total; b += blockDim.x) {
+    const int line = b >> logm, j = b & mmask;
+    const longlong2* s = reinterpret_cast<const longlong2*>(src + (size_t)line * sstride) + j;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const longlong2 q = s[r << logm];
+      v[r] = make_float2(fix_to_float(q.x - off), fix_to_float(q.y - off));
+    }
+    dft<R>(v);
+    float2* d = dst + line * ls;
+#pragma unroll
+    for (int r = 0; r < R; r++) d[pidx(j * R + r)] = v[r];
+  }
+  __syncthreads();
+}
+
+// Remaining in-place passes after a first pass of radix 2^first.
+__device__ __forceinline__ void fft2_rest(float2* buf, int logn, int first, int nlines, int ls,
+                                          const float2* __restrict__ tw, int tid = threadIdx.x) {
+  int logNs = first;
+  for (; logn - logNs >= 5; logNs += 5) fft2_pass<32, 5>(buf, logn, nlines, ls, logNs, tw, tid);
+  switch (logn - logNs) {
+    case 4: fft2_pass<16, 4>(buf, logn, nlines, ls, logNs, tw, tid); break;
+    case 3: fft2_pass<8, 3>(buf, logn, nlines, ls, logNs, tw, tid); break;
+    case 2: fft2_pass<4, 2>(buf, logn, nlines, ls, logNs, tw, tid); break;
+    case 1: fft2_pass<2, 1>(buf, logn, nlines, ls, logNs, tw, tid); break;
+    default: break;
+  }
+}
+
+// Ping-pong transform of lines staged unpadded in `stage` (line stride
+// sstride): first pass stage -> F, then F <-> stage (the stage buffer is
+// free once the first pass has read it; it must hold nlines * ls complex).
+// Returns the buffer holding the padded result.  `fix` != NULL: the staged
+// lines are int64 fixed-point cells minus `off` (the first pass converts).
+template <bool FIX>
+__device__ __forceinline__ float2* fft2_pp_from(void* stage, int sstride, long long off,
+                                                float2* F, int logn, int nlines, int ls,
+                                                const float2* __restrict__ tw) {
+  int first;
+  if (logn >= 5) {
+    if (FIX) fft2_first_pass_fix<32, 5>((const long long*)stage, sstride, off, F, logn, nlines, ls);
+    else fft2_first_pass<32, 5>((const float2*)stage, sstride, F, logn, nlines, ls);
+    first = 5;
+  } else {
+    switch (logn) {
+      case 4:
+        if (FIX) fft2_first_pass_fix<16, 4>((const long long*)stage, sstride, off, F, logn, nlines, ls);
+        else fft2_first_pass<16, 4>((const float2*)stage, sstride, F, logn, nlines, ls);
+        break;
+      case 3:
+        if (FIX) fft2_first_pass_fix<8, 3>((const long long*)stage, sstride, off, F, logn, nlines, ls);
+        else fft2_first_pass<8, 3>((const float2*)stage, sstride, F, logn, nlines, ls);
+        break;
+      case 2:
+        if (FIX) fft2_first_pass_fix<4, 2>((const long long*)stage, sstride, off, F, logn, nlines, ls);
+        else fft2_first_pass<4, 2>((const float2*)stage, sstride, F, logn, nlines, ls);
+        break;
+      default:
+        if (FIX) fft2_first_pass_fix<2, 1>((const long long*)stage, sstride, off, F, logn, nlines, ls);
+        else fft2_first_pass<2, 1>((const float2*)stage, sstride, F, logn, nlines, ls);
+        break;
+    }
+    first = logn;
+  }
+  float2* a = F;
+  float2* b = (float2*)stage;
+  int logNs = first;
+  for (; logn - logNs >= 5; logNs += 5) {
+    fft2_pass_pp<32, 5>(a, b, logn, nlines, ls, logNs, tw);
+    float2* t = a; a = b; b = t;
+  }
+  const int rem = logn - logNs;
+  if (rem) {
+    switch (rem) {
+      case 4: fft2_pass_pp<16, 4>(a, b, logn, nlines, ls, logNs, tw); break;
+      case 3: fft2_pass_pp<8, 3>(a, b, logn, nlines, ls, logNs, tw); break;
+      case 2: fft2_pass_pp<4, 2>(a, b, logn, nlines, ls, logNs, tw); break;
+      default: fft2_pass_pp<2, 1>(a, b, logn, nlines, ls, logNs, tw); break;
+    }
+    float2* t = a; a = b; b = t;
+  }
+  return a;
+}
+
+// The thread index as an opaque per-call value: index arithmetic derived
+// from it cannot be hoisted out of a persistent tile loop (which would pin
+// the 64 addresses of every inlined radix-32 pass in registers).
+__device__ __forceinline__ int opaque_tid() {
+  int t;
+  asm volatile("mov.u32 %0, %%tid.x;" : "=r"(t));
+  return t;
+}
+
+// Whole transform of lines staged unpadded in `src`, result padded in `dst`.
+__device__ __forceinline__ void fft2_lines_from(const float2* src, int sstride, float2* dst,
+                                                int logn, int nlines, int ls,
+                                                const float2* __restrict__ tw) {
+  if (logn >= 5) {
+    fft2_first_pass<32, 5>(src, sstride, dst, logn, nlines, ls, opaque_tid());
+    fft2_rest(dst, logn, 5, nlines, ls, tw, opaque_tid());
+    return;
+  }
+  const int tid = opaque_tid();
+  switch (logn) {
+    case 4: fft2_first_pass<16, 4>(src, sstride, dst, logn, nlines, ls, tid); break;
+    case 3: fft2_first_pass<8, 3>(src, sstride, dst, logn, nlines, ls, tid); break;
+    case 2: fft2_first_pass<4, 2>(src, sstride, dst, logn, nlines, ls, tid); break;
+    default: fft2_first_pass<2, 1>(src, sstride, dst, logn, nlines, ls, tid); break;
+  }
+}
+
 
 // ---------------------------------------------------------- mode geometry
 // Everything a binning sweep needs to turn a lattice vector into a bin,

@@ -18,12 +18,11 @@
 namespace ps {
 namespace {
 
-__device__ __forceinline__ int odd_stride(int n) { return (n & 1) ? n : n + 1; }
-
-__global__ void __launch_bounds__(kFftThreads) k_pass_a(const __grid_constant__ PassAArgs a) {
+template <bool P2>
+__global__ void __launch_bounds__(kFftThreads, 2) k_pass_a(const __grid_constant__ PassAArgs a) {
   extern __shared__ float2 sm[];
   const int ng = a.ng, M = ng >> 1, ngk = M + 1;
-  const int ls = odd_stride(M + 1);
+  const int ls = line_stride(M + 1, P2);
   const int nty = (ng + a.ty - 1) / a.ty;
   const int x = blockIdx.x / nty;
   const int y0 = (blockIdx.x - x * nty) * a.ty;
@@ -37,17 +36,20 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_a(const __grid_constant__ 
     for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
       const int r = e / M, m = e - r * M;
       const longlong2 q = __ldcs(reinterpret_cast<const longlong2*>(base + (size_t)r * ng) + m);
-      sm[r * ls + m] = make_float2(fix_to_float(q.x - off), fix_to_float(q.y - off));
+      sm[r * ls + lidx<P2>(m)] = make_float2(fix_to_float(q.x - off), fix_to_float(q.y - off));
     }
   } else {
     const float* base = a.fgrid + ((size_t)x * ng + y0) * ng;
     for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
       const int r = e / M, m = e - r * M;
-      sm[r * ls + m] = __ldcs(reinterpret_cast<const float2*>(base + (size_t)r * ng) + m);
+      sm[r * ls + lidx<P2>(m)] = __ldcs(reinterpret_cast<const float2*>(base + (size_t)r * ng) + m);
     }
   }
   __syncthreads();
-  fft_lines(sm, a.plan_half, nl, ls, a.tw_half);
+  if (P2)
+    fft2_lines(sm, a.plan_half.logn, nl, ls, a.tw_half);
+  else
+    fft_lines(sm, a.plan_half, nl, ls, a.tw_half);
 
   // Real-to-complex split of each line: Z = FFT_M(x[2m] + i x[2m+1]);
   // X[k] = E + W^k O with E = (Z[k] + conj Z[M-k]) / 2,
@@ -59,17 +61,18 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_a(const __grid_constant__ 
     if (k == 0) {
       const float2 z = L[0];
       L[0] = make_float2(z.x + z.y, 0.f);
-      L[M] = make_float2(z.x - z.y, 0.f);
+      L[lidx<P2>(M)] = make_float2(z.x - z.y, 0.f);
     } else {
-      const float2 A = L[k], B = L[M - k];
+      const int ik = lidx<P2>(k), imk = lidx<P2>(M - k);
+      const float2 A = L[ik], B = L[imk];
       const float2 E = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
       const float2 O = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
       const float2 W = __ldg(&a.tw_full[k]);
       const float2 WO = cmul(W, O);
       // W^(M-k) = -conj(W)
       const float2 W2O = cmul(make_float2(-W.x, W.y), make_float2(O.x, -O.y));
-      L[k] = cadd(E, WO);
-      L[M - k] = make_float2(E.x + W2O.x, -E.y + W2O.y);
+      L[ik] = cadd(E, WO);
+      L[imk] = make_float2(E.x + W2O.x, -E.y + W2O.y);
     }
   }
   __syncthreads();
@@ -77,14 +80,15 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_a(const __grid_constant__ 
   float2* ob = a.out + (size_t)x * ngk * ng + y0;
   for (int e = threadIdx.x; e < ngk * nl; e += blockDim.x) {
     const int kz = e / nl, r = e - kz * nl;
-    ob[(size_t)kz * ng + r] = sm[r * ls + kz];
+    ob[(size_t)kz * ng + r] = sm[r * ls + lidx<P2>(kz)];
   }
 }
 
-__global__ void __launch_bounds__(kFftThreads) k_pass_b(const __grid_constant__ PassBArgs a) {
+template <bool P2>
+__global__ void __launch_bounds__(kFftThreads, 2) k_pass_b(const __grid_constant__ PassBArgs a) {
   extern __shared__ float2 sm[];
   const int ng = a.ng, ngk = (ng >> 1) + 1;
-  const int ls = ng + 1;
+  const int ls = line_stride(ng, P2);
   const int ntx = (ng + a.tx - 1) / a.tx;
   const int kz = blockIdx.x / ntx;
   const int x0 = (blockIdx.x - kz * ntx) * a.tx;
@@ -94,15 +98,171 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_b(const __grid_constant__ 
     const int r = e / h, m = e - r * h;
     const float4 v = __ldcs(reinterpret_cast<const float4*>(
                                a.in + ((size_t)(x0 + r) * ngk + kz) * ng) + m);
-    sm[r * ls + 2 * m] = make_float2(v.x, v.y);
-    sm[r * ls + 2 * m + 1] = make_float2(v.z, v.w);
+    sm[r * ls + lidx<P2>(2 * m)] = make_float2(v.x, v.y);
+    sm[r * ls + lidx<P2>(2 * m + 1)] = make_float2(v.z, v.w);
   }
   __syncthreads();
-  fft_lines(sm, a.plan_full, nl, ls, a.tw_full);
+  if (P2)
+    fft2_lines(sm, a.plan_full.logn, nl, ls, a.tw_full);
+  else
+    fft_lines(sm, a.plan_full, nl, ls, a.tw_full);
   float2* ob = a.out + (size_t)kz * ng * ng + x0;
   for (int e = threadIdx.x; e < ng * nl; e += blockDim.x) {
     const int ky = e / nl, r = e - ky * nl;
-    ob[(size_t)ky * ng + r] = sm[r * ls + ky];
+    ob[(size_t)ky * ng + r] = sm[r * ls + lidx<P2>(ky)];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined power-of-two passes.  Persistent CTAs (one per SM); thread 0
+// issues the bulk copies of tile t+1's input rows into the other half of a
+// double-buffered staging area while all threads transform tile t.  The
+// first radix pass reads the staging buffer, later passes work in place on
+// the padded FFT buffer.  Waits are bounded: on time-out the CTA raises
+// err[0] |= 2 and stops.
+
+struct Pipe {
+  uint64_t* bar;  // [2]
+  int it;
+};
+
+__device__ __forceinline__ bool pipe_wait(uint64_t* bar, int it, int* err, int* s_abort) {
+  if (!mbar_wait(&bar[it & 1], (uint32_t)((it >> 1) & 1))) {
+    atomicOr(err, 2);
+    *s_abort = 1;
+  }
+  __syncthreads();
+  return *s_abort == 0;
+}
+
+__global__ void __launch_bounds__(kFftThreads, 1) k_pass_a_tma(const __grid_constant__ PassAArgs a) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ int s_abort;
+  const int ng = a.ng, M = ng >> 1, ngk = M + 1;
+  const int logm = a.plan_half.logn;
+  const int ls = line_stride(M + 1, true);
+  const int nty = (ng + a.ty - 1) / a.ty;
+  const int ntile = ng * nty;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
+  long long* stage[2];
+  stage[0] = reinterpret_cast<long long*>(smraw + 128);
+  stage[1] = stage[0] + (size_t)a.ty * ng;
+  float2* F = reinterpret_cast<float2*>(stage[1] + (size_t)a.ty * ng);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    s_abort = 0;
+  }
+  __syncthreads();
+  const double W = *a.wsum;
+  const long long off = __double2ll_rn(W * 4294967296.0 / ((double)ng * ng * ng));
+  auto issue = [&](int tile, int s) {
+    const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
+    const int nl = min(a.ty, ng - y0);
+    mbar_expect_tx(&bar[s], (uint32_t)(nl * ng * 8));
+    const long long* src = a.grid + ((size_t)x * ng + y0) * ng;
+    for (int r = 0; r < nl; r++)
+      bulk_g2s(stage[s] + (size_t)r * ng, src + (size_t)r * ng, (uint32_t)(ng * 8), &bar[s]);
+  };
+  if (threadIdx.x == 0 && (int)blockIdx.x < ntile) issue(blockIdx.x, 0);
+  int it = 0;
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x, it++) {
+    const int s = it & 1;
+    if (threadIdx.x == 0 && tile + (int)gridDim.x < ntile) {
+      fence_proxy_async();
+      issue(tile + gridDim.x, s ^ 1);
+    }
+    if (!pipe_wait(bar, it, a.err, &s_abort)) break;
+    const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
+    const int nl = min(a.ty, ng - y0);
+    float2* X = fft2_pp_from<true>(stage[s], ng, off, F, logm, nl, ls, a.tw_half);
+    const int half = (M >> 1) + 1;
+    for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {
+      const int r = e / half, k = e - r * half;
+      float2* L = X + r * ls;
+      if (k == 0) {
+        const float2 z = L[0];
+        L[0] = make_float2(z.x + z.y, 0.f);
+        L[pidx(M)] = make_float2(z.x - z.y, 0.f);
+      } else {
+        const int ik = pidx(k), imk = pidx(M - k);
+        const float2 A = L[ik], B = L[imk];
+        const float2 E = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
+        const float2 O = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
+        const float2 Wk = __ldg(&a.tw_full[k]);
+        const float2 WO = cmul(Wk, O);
+        const float2 W2O = cmul(make_float2(-Wk.x, Wk.y), make_float2(O.x, -O.y));
+        L[ik] = cadd(E, WO);
+        L[imk] = make_float2(E.x + W2O.x, -E.y + W2O.y);
+      }
+    }
+    __syncthreads();
+    float2* ob = a.out + (size_t)x * ngk * ng + y0;
+    for (int e = threadIdx.x; e < ngk * nl; e += blockDim.x) {
+      const int kz = e / nl, r = e - kz * nl;
+      ob[(size_t)kz * ng + r] = X[r * ls + pidx(kz)];
+    }
+    __syncthreads();
+  }
+  // drain: never exit with a bulk copy in flight into this CTA's memory
+  if (threadIdx.x == 0 && s_abort) {
+    mbar_wait(&bar[0], 0);
+    mbar_wait(&bar[1], 0);
+  }
+}
+
+__global__ void __launch_bounds__(kFftThreads, 1) k_pass_b_tma(const __grid_constant__ PassBArgs a) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ int s_abort;
+  const int ng = a.ng, ngk = (ng >> 1) + 1;
+  const int logn = a.plan_full.logn;
+  const int ls = line_stride(ng, true);
+  const int ntx = (ng + a.tx - 1) / a.tx;
+  const int ntile = ngk * ntx;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
+  const size_t selems = ((size_t)a.tx * ls + 1) & ~(size_t)1;  // 16-byte aligned
+  float2* stage[2];
+  stage[0] = reinterpret_cast<float2*>(smraw + 128);
+  stage[1] = stage[0] + selems;
+  float2* F = stage[1] + selems;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    s_abort = 0;
+  }
+  __syncthreads();
+  auto issue = [&](int tile, int s) {
+    const int kz = tile / ntx, x0 = (tile - kz * ntx) * a.tx;
+    const int nl = min(a.tx, ng - x0);
+    mbar_expect_tx(&bar[s], (uint32_t)(nl * ng * 8));
+    for (int r = 0; r < nl; r++)
+      bulk_g2s(stage[s] + (size_t)r * ng, a.in + ((size_t)(x0 + r) * ngk + kz) * ng,
+               (uint32_t)(ng * 8), &bar[s]);
+  };
+  if (threadIdx.x == 0 && (int)blockIdx.x < ntile) issue(blockIdx.x, 0);
+  int it = 0;
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x, it++) {
+    const int s = it & 1;
+    if (threadIdx.x == 0 && tile + (int)gridDim.x < ntile) {
+      fence_proxy_async();
+      issue(tile + gridDim.x, s ^ 1);
+    }
+    if (!pipe_wait(bar, it, a.err, &s_abort)) break;
+    const int kz = tile / ntx, x0 = (tile - kz * ntx) * a.tx;
+    const int nl = min(a.tx, ng - x0);
+    const float2* X = fft2_pp_from<false>(stage[s], ng, 0, F, logn, nl, ls, a.tw_full);
+    float2* ob = a.out + (size_t)kz * ng * ng + x0;
+    for (int e = threadIdx.x; e < ng * nl; e += blockDim.x) {
+      const int ky = e / nl, r = e - ky * nl;
+      ob[(size_t)ky * ng + r] = X[r * ls + pidx(ky)];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && s_abort) {
+    mbar_wait(&bar[0], 0);
+    mbar_wait(&bar[1], 0);
   }
 }
 
@@ -110,20 +270,41 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_b(const __grid_constant__ 
 
 int launch_pass_a(const PassAArgs& a, cudaStream_t s) {
   const int M = a.ng / 2;
-  const int ls = ((M + 1) & 1) ? M + 1 : M + 2;
-  const size_t smem = (size_t)a.ty * ls * sizeof(float2);
+  const bool p2 = a.plan_half.logn >= 0;
+  const size_t smem = (size_t)a.ty * line_stride(M + 1, p2) * sizeof(float2);
   const int nty = (a.ng + a.ty - 1) / a.ty;
-  cudaFuncSetAttribute(k_pass_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_pass_a<<<(unsigned)(a.ng * nty), kFftThreads, smem, s>>>(a);
+  const unsigned grid = (unsigned)(a.ng * nty);
+  if (p2 && a.grid && a.pipe_grid > 0) {
+    const size_t sm2 = 128 + 2 * (size_t)a.ty * a.ng * 8 + (size_t)a.ty * line_stride(M + 1, true) * 8;
+    cudaFuncSetAttribute(k_pass_a_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+    k_pass_a_tma<<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
+  } else if (p2) {
+    cudaFuncSetAttribute(k_pass_a<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pass_a<true><<<grid, kFftThreads, smem, s>>>(a);
+  } else {
+    cudaFuncSetAttribute(k_pass_a<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pass_a<false><<<grid, kFftThreads, smem, s>>>(a);
+  }
   return 1;
 }
 
 int launch_pass_b(const PassBArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)a.tx * (a.ng + 1) * sizeof(float2);
+  const bool p2 = a.plan_full.logn >= 0;
+  const size_t smem = (size_t)a.tx * line_stride(a.ng, p2) * sizeof(float2);
   const int ntx = (a.ng + a.tx - 1) / a.tx;
   const int ngk = a.ng / 2 + 1;
-  cudaFuncSetAttribute(k_pass_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_pass_b<<<(unsigned)(ngk * ntx), kFftThreads, smem, s>>>(a);
+  const unsigned grid = (unsigned)(ngk * ntx);
+  if (p2 && a.pipe_grid > 0) {
+    const size_t sm2 = 128 + 3 * ((((size_t)a.tx * line_stride(a.ng, true)) + 1) & ~(size_t)1) * 8;
+    cudaFuncSetAttribute(k_pass_b_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+    k_pass_b_tma<<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
+  } else if (p2) {
+    cudaFuncSetAttribute(k_pass_b<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pass_b<true><<<grid, kFftThreads, smem, s>>>(a);
+  } else {
+    cudaFuncSetAttribute(k_pass_b<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pass_b<false><<<grid, kFftThreads, smem, s>>>(a);
+  }
   return 1;
 }
 

@@ -25,9 +25,12 @@ struct AssignArgs {
   double box[3];
   unsigned long long* mesh0;  // plain grid (lower corner 0)
   unsigned long long* mesh1;  // half-cell shifted grid, or NULL
-  double* wsum;               // [2]: sum w, sum |w| (accumulated)
+  double* wsum;               // [2]: sum w, sum |w|
+  double* wpart;              // [2 * kAssignMaxBlocks] per-block partial sums
   int* err;                   // bit 0: particle outside [0, L)
 };
+
+constexpr int kAssignMaxBlocks = 2048;
 
 // Returns the number of kernel launches issued.
 int launch_assign(const Particles& p, const AssignArgs& a, cudaStream_t s);
@@ -43,6 +46,8 @@ struct PassAArgs {
   const float2* tw_half;        // length ng/2 twiddles
   const float2* tw_full;        // length ng twiddles (r2c split)
   FftPlan plan_half;
+  int pipe_grid;                // > 0: pipelined persistent kernel with this grid
+  int* err;                     // bit 1: pipeline wait timed out
 };
 int launch_pass_a(const PassAArgs& a, cudaStream_t s);
 
@@ -54,6 +59,8 @@ struct PassBArgs {
   float2* out;
   const float2* tw_full;
   FftPlan plan_full;
+  int pipe_grid;
+  int* err;
 };
 int launch_pass_b(const PassBArgs& a, cudaStream_t s);
 
@@ -105,6 +112,6 @@ int launch_geometry(const GeomArgs& a, cudaStream_t s);
 int launch_reduce(const double* part, int grid, int width, double* out, cudaStream_t s);
 
 // Minimum shared memory per CTA the passes need (bytes).
-size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin);
+size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin, bool pow2);
 
 }  // namespace ps

@@ -62,3 +62,11 @@ def perr(got, ref, shot):
     """Max |P_l^got - P_l^ref| relative to the raw monopole P_0 + shot of each bin."""
     scale = np.abs(ref[0]) + shot
     return float((np.abs(np.asarray(got) - np.asarray(ref)) / scale).max())
+
+
+def xerr(got, ref, pl_ref, shot):
+    """Cross-spectrum error relative to sqrt of the two raw auto monopoles
+    (the Cauchy-Schwarz bound on |P_cross|): the cross of independent
+    catalogues is ~0, so its FP32 round-off scales with the autos."""
+    scale = np.sqrt((np.abs(pl_ref[0][0]) + shot[0]) * (np.abs(pl_ref[1][0]) + shot[1]))
+    return float((np.abs(np.asarray(got) - np.asarray(ref)) / scale).max())

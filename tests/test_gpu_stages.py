@@ -1,0 +1,74 @@
+"""Stage-level parity: assignment mesh, FFT and binning, each in isolation."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("assign", [0, 1, 2, 3])
+def test_mesh_matches_reference_fixture(gpu_lib, assign):
+    d = np.load(os.path.join(GOLDEN, "ref_meshes.npz"))
+    with gpu_lib.Estimator(ng=16, assign=assign, interlace=True, dk=0.01) as e:
+        e.assign(0, d["cat"])
+        m0, m1 = e.read_mesh(0, 0), e.read_mesh(0, 1)
+    # FP32 stencil weights, 2^-32 fixed point: ~1e-7 of the largest cell
+    for got, ref in ((m0, d[f"fr_{assign}"]), (m1, d[f"frl_{assign}"])):
+        assert np.abs(got - ref).max() <= 2e-7 * np.abs(ref).max()
+        assert got.sum() == pytest.approx(ref.sum(), rel=1e-9)
+
+
+@pytest.mark.parametrize("assign", [0, 1, 2, 3])
+@pytest.mark.parametrize("interlace", [False, True])
+def test_mesh_matches_oracle_and_is_deterministic(gpu_lib, oracle_mod, assign, interlace):
+    from powspec_gb300 import catalog
+    cat = catalog.lognormal(200000, box=1000.0, seed=8, ngen=64, weights=(0.5, 1.5))
+    ref = oracle_mod.assign("port", cat, 48, 1000.0, assign, interlace)
+    ref = ref if interlace else (ref,)
+    with gpu_lib.Estimator(ng=48, assign=assign, interlace=interlace, dk=0.01) as e:
+        runs = []
+        for _ in range(2):
+            e.assign(0, cat)
+            runs.append([e.read_mesh(0, m) for m in range(2 if interlace else 1)])
+    for m in range(len(ref)):
+        assert np.array_equal(runs[0][m], runs[1][m]), "mesh not bit-reproducible"
+        assert np.abs(runs[0][m] - ref[m]).max() <= 2e-7 * np.abs(ref[m]).max()
+
+
+@pytest.mark.parametrize("ng", [8, 12, 16, 20, 24, 30, 32, 40, 48, 60, 64, 96, 128, 192, 256])
+def test_fft_r2c_matches_numpy(gpu_lib, ng):
+    x = np.random.default_rng(ng).standard_normal((ng, ng, ng)).astype(np.float32)
+    with gpu_lib.Estimator(ng=ng, dk=2 * np.pi / 1000) as e:
+        got = e.fft_r2c(x)
+    ref = np.fft.rfftn(x.astype(np.float64))
+    # FP32 transform: error ~ eps * log2(n) * ||x||_2
+    bound = 6e-8 * np.log2(ng ** 3) * np.sqrt((x.astype(np.float64) ** 2).sum())
+    assert np.abs(got - ref).max() <= bound
+
+
+@pytest.mark.parametrize("assign,interlace", [(1, False), (3, False), (2, True)])
+def test_binning_alone_matches_oracle(gpu_lib, oracle_mod, assign, interlace):
+    import ctypes
+    from powspec_gb300 import catalog
+    ng = 32
+    poles = (0, 1, 2, 3, 4, 5, 6)
+    cat = catalog.lognormal(30000, box=1000.0, seed=5, ngen=32)
+    spec = oracle_mod.Spec(ng=ng, assign=assign, interlace=interlace, dk=0.01, poles=poles)
+    m = oracle_mod.assign("port", cat, ng, 1000.0, assign, False)
+    fk = oracle_mod.r2c(m)
+    alias, cnt, km = oracle_mod.precomp(spec)
+    kedge, _ = oracle_mod.bins(spec)
+    nb = len(kedge) - 1
+    pl = np.zeros((7, nb))
+    lc = np.zeros((7, nb))
+    oracle_mod.port().ps_oracle_count_sim(
+        ng, (ctypes.c_double * 3)(1000., 1000., 1000.), oracle_mod._ptr(alias), oracle_mod._ptr(fk),
+        oracle_mod._ptr(fk), 0, nb, oracle_mod._ptr(kedge), ctypes.c_double(0.01),
+        (ctypes.c_double * 3)(0, 0, 1.), 7, (ctypes.c_int * 7)(*poles), oracle_mod._ptr(pl),
+        oracle_mod._ptr(lc))
+    with gpu_lib.Estimator(ng=ng, assign=assign, interlace=interlace, dk=0.01, poles=poles) as e:
+        got = e.bin_fields(fk.astype(np.complex64))
+    assert (np.abs(got - pl) / np.abs(pl[0])).max() <= 2e-6
