@@ -1,24 +1,28 @@
 """Benchmark of the periodic-box P_l(k) path on GB300.
 
-One step = one evaluation: a catalogue -> {P_0, P_2, P_4}(k) table (particle
-assignment into two interlaced meshes, the r2c FFTs, interlace combine,
-window compensation and Legendre binning, normalisation).
+One step = one evaluation: a catalogue -> {P_0, P_2, P_4}(k) table.
 
-Workload (default): the plain form of the learned-vs-plain comparison: a
-seeded lognormal catalogue of ~4e6 particles (spectrum A k^-1.5
-exp(-(k/0.5)^2), sigma_G^2 = 1, Zel'dovich displacement along z), L = 1000
-Mpc/h, PCS with interlacing at Ng = 1024, l = 0, 2, 4, dk = 0.005 h/Mpc.
-Synthetic data stands in for simulation catalogues (none ship with the
-reference).
+Workloads (synthetic, seeded; no catalogue ships with the reference): a
+lognormal catalogue of ~4e6 particles (spectrum A k^-1.5 exp(-(k/0.5)^2),
+sigma_G^2 = 1, Zel'dovich displacement along z), L = 1000 Mpc/h, dk = 0.005
+h/Mpc, l = 0, 2, 4.
+
+* learned_ng256_vs_plain_ng1024 (default): the learned form -- Ng = 256, PCS,
+  interlaced, 16 |mu| sub-bins, plus the trained correction network -- timed
+  against the plain Ng = 1024 PCS interlaced evaluation of the same
+  catalogue in the same run; the line reports the learned evals/s (value),
+  the plain evals/s, the speed-up and the max error against plain Ng = 1024
+  up to 0.8 k_Nyq(256).  The catalogue's seed is outside the training set.
+* plain_pcs_il_ng1024_n4e6: the plain Ng = 1024 PCS interlaced evaluation.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-Under torchrun (N > 1) every rank evaluates its own catalogues on its GPU
-(replicas: the path has no exchange step); value = all evaluations / max
-time over ranks.
+Under torchrun (N > 1) every rank evaluates its own catalogue on its own GPU
+(replicas: the path has no exchange step); value = all evaluations / the
+max time over ranks.
 
---impl reference times the reference's CPU path: the oracle's FP64 OpenMP C
-restatement of genr_mesh + powspec (the reference sources are not available
-on the GPU machine), on rank 0 only, with all host threads.
+--impl reference times the reference's CPU implementation of the quantity
+both workloads compute (plain Ng = 1024 PCS interlaced): the oracle's FP64
+OpenMP C restatement of genr_mesh + powspec on all host cores, rank 0 only.
 """
 from __future__ import annotations
 
@@ -36,14 +40,18 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOADS = {
-    # name: (ng, assign, interlace, n_particles, box, dk, ngen)
-    "plain_pcs_il_ng1024_n4e6": (1024, 3, True, 4_000_000, 1000.0, 0.005, 256),
-    "plain_pcs_il_ng512_n4e6": (512, 3, True, 4_000_000, 1000.0, 0.005, 256),
-    "plain_cic_ng256_n1e6_uniform": (256, 1, False, 1_000_000, 1000.0, 0.005, 0),
-}
-DEFAULT = "plain_pcs_il_ng1024_n4e6"
+N_PART = 4_000_000
+BOX = 1000.0
+DK = 0.005
+SEED = 1          # held out: the correction was trained on seeds >= 1000
 METRIC = "P_l(k) evals/s on 1 GB300"
+WORKLOADS = {
+    "learned_ng256_vs_plain_ng1024": dict(learned=True, ng=256, assign=3, interlace=True),
+    "plain_pcs_il_ng1024_n4e6": dict(learned=False, ng=1024, assign=3, interlace=True),
+    "plain_pcs_il_ng512_n4e6": dict(learned=False, ng=512, assign=3, interlace=True),
+}
+DEFAULT = "learned_ng256_vs_plain_ng1024"
+PLAIN_REF = dict(ng=1024, assign=3, interlace=True)
 
 
 def peaks():
@@ -55,12 +63,9 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def make_catalogue(wl, seed):
+def make_catalogue(seed):
     from powspec_gb300 import catalog
-    ng, assign, il, n, box, dk, ngen = WORKLOADS[wl]
-    if ngen == 0:
-        return catalog.uniform(n, box=box, seed=seed)
-    return catalog.lognormal(n, box=box, seed=seed, ngen=ngen)
+    return catalog.lognormal(N_PART, box=BOX, seed=seed, ngen=256)
 
 
 class ClockSampler:
@@ -79,7 +84,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -129,203 +134,266 @@ def barrier(world):
         dist.barrier()
 
 
-def allmax(world, v):
+def reduce(world, v, op):
     if world == 1:
         return v
     import torch
     import torch.distributed as dist
     t = torch.tensor([v], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
 
 
-def allsum(world, v):
-    if world == 1:
-        return v
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
-
-
-def algorithmic_bytes(wl, n):
+def algorithmic_bytes(ng, interlace, n):
     """Per-launch algorithmic HBM bytes of each phase (FP32 path).
 
     assignment: N * 32 B (AoS float64 records) + 4 B * Ng^3 per mesh;
     z pass: 4 B * Ng^3 read + 8 B * Ncmplx written; y pass: 8 B * Ncmplx
     read + written; x pass + binning: 8 B * Ncmplx per field read.
     """
-    ng, assign, il, _, box, dk, _ = WORKLOADS[wl]
-    nmesh = 2 if il else 1
+    nmesh = 2 if interlace else 1
     ntot = ng ** 3
     ncx = ng * ng * (ng // 2 + 1)
     return {
-        "assign": n * 32 + 4 * ntot,          # per launch (one mesh)
-        "pass_z": 4 * ntot + 8 * ncx,         # per launch (one field)
-        "pass_y": 16 * ncx,                   # per launch (one field)
-        "pass_x_bin": 8 * ncx * nmesh,        # one launch over all fields
+        "assign": n * 32 + 4 * ntot,
+        "pass_z": 4 * ntot + 8 * ncx,
+        "pass_y": 16 * ncx,
+        "pass_x_bin": 8 * ncx * nmesh,
         "nmesh": nmesh,
         "total": nmesh * (n * 32 + 4 * ntot) + nmesh * (4 * ntot + 8 * ncx) + nmesh * 8 * ncx * 2,
     }
 
 
-def cpu_eval(wl, cat, threads=None):
-    """One evaluation with the oracle's C restatement (FP64, OpenMP)."""
+def roofline(phases_ms, ng, interlace, n, traffic=None):
+    peak, peak_kind = peaks()
+    ab = algorithmic_bytes(ng, interlace, n)
+    kern = {"assign": (phases_ms[0] / ab["nmesh"], ab["assign"]),
+            "pass_z": (phases_ms[1] / ab["nmesh"], ab["pass_z"]),
+            "pass_y": (phases_ms[2] / ab["nmesh"], ab["pass_y"]),
+            "pass_x_bin": (phases_ms[3], ab["pass_x_bin"])}
+    dom = max(kern, key=lambda k: kern[k][0])
+    ms, nbytes = kern[dom]
+    achieved = nbytes / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": (traffic or {}).get(f"ng{ng}", {}).get(dom),
+            "per_kernel_frac": {k: (v[1] / (v[0] * 1e-3) / 1e9) / peak for k, v in kern.items()},
+            "eval_algorithmic_GB": ab["total"] / 1e9,
+            "eval_frac": ab["total"] / (phases_ms[5] * 1e-3) / 1e9 / peak}
+
+
+def cpu_eval(cat, threads=None):
+    """One plain Ng = 1024 PCS interlaced evaluation with the oracle's C
+    restatement (FP64, OpenMP)."""
     import oracle
-    ng, assign, il, n, box, dk, _ = WORKLOADS[wl]
     if threads:
         oracle.set_threads(threads)
-    spec = oracle.Spec(ng=ng, box=box, assign=assign, interlace=il, poles=(0, 2, 4), dk=dk,
+    spec = oracle.Spec(ng=PLAIN_REF["ng"], box=BOX, assign=PLAIN_REF["assign"],
+                       interlace=PLAIN_REF["interlace"], poles=(0, 2, 4), dk=DK,
                        isauto=(True, False), iscross=False)
     t0 = time.perf_counter()
     oracle.run("port", spec, [cat])
     return time.perf_counter() - t0
 
 
+def config_of(wl, n_actual):
+    w = WORKLOADS[wl]
+    c = {"workload": wl, "ng": w["ng"], "assign": ["NGP", "CIC", "TSC", "PCS"][w["assign"]],
+         "interlace": w["interlace"], "n_particles": n_actual, "box": BOX, "dk": DK,
+         "poles": [0, 2, 4], "catalogue": "lognormal", "seed": SEED,
+         "l2": "working set per eval >> 129 MB L2 (int64 meshes, 8 B/cell); no explicit flush"}
+    if w["learned"]:
+        c.update({"nmu": 16, "compared_with": "plain Ng=1024 PCS interlaced, same catalogue",
+                  "kmax": "0.8 k_Nyq(256)"})
+    return c
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
     import oracle
-    wl = args.workload
-    cat = make_catalogue(wl, seed=1)
+    cat = make_catalogue(SEED)
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
-    ng, assign, il, n, box, dk, _ = WORKLOADS[wl]
-    # warm-up: W small evaluations of the same catalogue (Ng = 128)
-    small = oracle.Spec(ng=128, box=box, assign=assign, interlace=il, poles=(0, 2, 4), dk=dk,
+    small = oracle.Spec(ng=128, box=BOX, assign=3, interlace=True, poles=(0, 2, 4), dk=DK,
                         isauto=(True, False), iscross=False)
-    for _ in range(args.warmup):
+    for _ in range(args.warmup):  # warm-up: small evaluations of the same catalogue
         oracle.run("port", small, [cat])
     times = []
-    budget = 180.0
     for _ in range(args.steps):
-        times.append(cpu_eval(wl, cat))
-        if sum(times) > budget:
+        times.append(cpu_eval(cat))
+        if sum(times) > 150.0:  # bounded sample: keep the run within a few minutes
             break
     total = sum(times)
     value = len(times) / total
-    line = {
+    print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
         "n_gpus": args.gpus, "steps": len(times), "steps_requested": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": config_of(wl, n_actual=len(cat)),
+        "data": "synthetic", "config": config_of(args.workload, len(cat)),
+        "reference_computes": "plain Ng=1024 PCS interlaced (genr_mesh + powspec)",
         "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
-                         "sample": f"{len(times)} full evaluation(s) of the workload, "
-                                   f"180 s cap; FFT by the project's FFTW-API shim"},
+                         "sample": f"{len(times)} full evaluation(s), 150 s cap; FFT by the "
+                                   "project's FFTW-API shim, not FFTW"},
         "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line))
+    }))
     return 0
 
 
-def config_of(wl, n_actual):
-    ng, assign, il, n, box, dk, ngen = WORKLOADS[wl]
-    return {"workload": wl, "ng": ng, "assign": ["NGP", "CIC", "TSC", "PCS"][assign],
-            "interlace": il, "n_particles": n_actual, "box": box, "dk": dk, "poles": [0, 2, 4],
-            "catalogue": "lognormal" if ngen else "uniform",
-            "l2": "working set per eval >> 129 MB L2 (int64 meshes 8 B/cell); no explicit flush"}
+def timed(stream, steps, fn):
+    """Device time (CUDA events on the context stream) of `steps` calls."""
+    import torch
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    out = None
+    for _ in range(steps):
+        out = fn()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1), out
 
 
 def run_gpu(args, world, rank, local):
     import torch
 
     import powspec_gb300 as ps
-    wl = args.workload
-    ng, assign, il, n, box, dk, _ = WORKLOADS[wl]
+    from powspec_gb300 import learned
+    wl = WORKLOADS[args.workload]
     torch.cuda.set_device(local)
-    cat = make_catalogue(wl, seed=1 + rank)
+    cat = make_catalogue(SEED + rank)
     nreal = len(cat)
-    est = ps.Estimator(ng=ng, box=box, assign=assign, interlace=il, poles=(0, 2, 4), dk=dk,
-                       device=local)
-    stream = torch.cuda.ExternalStream(est.stream(), device=local)
     d_cat = torch.from_numpy(cat).to(f"cuda:{local}")
-    torch.cuda.synchronize()
-
-    def step_device():
-        est.assign(0, d_cat.data_ptr(), on_device=True, n=nreal)
-        return est.execute()
-
-    for _ in range(args.warmup):
-        step_device()
-    torch.cuda.synchronize()
-
-    # ---- device-resident timed region
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    phases = np.zeros(6)
-    launches = 0
-    with ClockSampler(local) as clk:
-        barrier(world)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            step_device()
-            phases += est.timings()
-            launches += est.launches()
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        barrier(world)
-    dev_ms = ev0.elapsed_time(ev1)
-    clocks = clk.summary()
-    t_max = allmax(world, dev_ms / 1e3)
-    evals = allsum(world, float(args.steps))
-    value = evals / t_max
-
-    # ---- end to end through the public API with host buffers (pinned)
     pinned = torch.from_numpy(cat).pin_memory()
     host_arr = pinned.numpy()
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f)
+
+    # plain fine-mesh context (the reference method; timed for comparison)
+    plain = ps.Estimator(ng=PLAIN_REF["ng"], box=BOX, assign=PLAIN_REF["assign"],
+                         interlace=PLAIN_REF["interlace"], poles=(0, 2, 4), dk=DK, device=local)
+    s_plain = torch.cuda.ExternalStream(plain.stream(), device=local)
+    phases_plain = np.zeros(6)
+
+    def step_plain():
+        plain.assign(0, d_cat.data_ptr(), on_device=True, n=nreal)
+        r = plain.execute()
+        phases_plain[:] += plain.timings()
+        return r
+
+    if wl["learned"]:
+        le = learned.LearnedEstimator(ng=wl["ng"], assign=wl["assign"], interlace=wl["interlace"],
+                                      box=BOX, dk=DK, device=local)
+        stream = torch.cuda.ExternalStream(le.est.stream(), device=local)
+        phases = np.zeros(6)
+        launches = [0]
+
+        def step():
+            out = le.run(device_ptr=d_cat.data_ptr(), n=nreal)
+            phases[:] += le.est.timings()
+            launches[0] += le.est.launches() + 2  # + feature cast and network kernels
+            return out
+
+        def step_e2e():
+            return le.run(host_arr)
+    else:
+        le = None
+        stream, phases, launches = s_plain, phases_plain, [0]
+
+        def step():
+            r = step_plain()
+            launches[0] += plain.launches()
+            return r
+
+        def step_e2e():
+            plain.assign(0, host_arr)
+            return plain.execute()
+
+    for _ in range(args.warmup):
+        step()
+        if le is not None:
+            step_plain()
+    phases[:] = 0
+    phases_plain[:] = 0
+    launches[0] = 0
+
+    with ClockSampler(local) as clk:
+        barrier(world)
+        dev_ms, out = timed(stream, args.steps, step)
+        barrier(world)
+    clocks = clk.summary()
+    ph = phases / args.steps
+    t_max = reduce(world, dev_ms / 1e3, "max")
+    value = reduce(world, float(args.steps), "sum") / t_max
+    nlaunch = launches[0]
+
+    extra = {}
+    if le is not None:
+        # plain Ng = 1024 on the same catalogue: throughput and the error of the learned form
+        phases_plain[:] = 0
+        pl_ms, rp = timed(s_plain, args.steps, step_plain)
+        k, pc, trusted = out
+        ref = rp.pl[0][:, :len(k)]
+        use = trusted & (rp.cnt[:len(k)] > 1) & (ref[0] > 0)
+        err = np.abs(pc - ref)[:, use] / ref[0][use]
+        err_plain = np.abs(le.last_cells.plain - ref)[:, use] / ref[0][use]
+        plain_value = reduce(world, float(args.steps), "sum") / reduce(world, pl_ms / 1e3, "max")
+        extra["learned"] = {
+            "plain_ng1024_evals_per_s": plain_value,
+            "speedup_vs_plain_ng1024": value / plain_value,
+            "max_err_vs_plain_ng1024": float(err.max()),
+            "max_err_by_l": [float(v) for v in err.max(1)],
+            "max_err_uncorrected_ng256": float(err_plain.max()),
+            "bins_compared": int(use.sum()),
+            "bins_not_trusted_below_kmax": int((~trusted[:int(np.sum(k <= 0.8 * np.pi * 256 / BOX))]).sum()),
+            "tolerance": 0.01,
+        }
+        extra["roofline_plain_ng1024"] = roofline(phases_plain / args.steps, 1024, True, nreal, traffic)
+
+    # end to end through the public API with host (pinned) buffers
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        est.assign(0, host_arr)
-        res = est.execute()
+        step_e2e()
     torch.cuda.synchronize()
-    e2e_s = allmax(world, time.perf_counter() - t0)
-    e2e = allsum(world, float(args.steps)) / e2e_s
-    d2h = 8 * 3 * est.nbin + 8 * 4 + 4 * 2  # sums, weight sums, error flags
-    est.close()
+    e2e_s = reduce(world, time.perf_counter() - t0, "max")
+    e2e = reduce(world, float(args.steps), "sum") / e2e_s
+    if le is not None:
+        d2h = 8 * 3 * le.est.nbin * 16 + 8 * 4 + 16 + 4 * le.est.nbin * 16
+    else:
+        d2h = 8 * 3 * plain.nbin + 8 * 4 + 16
 
-    if rank != 0:
-        return 0
-    peak, peak_kind = peaks()
-    ab = algorithmic_bytes(wl, nreal)
-    per = phases / args.steps  # ms per eval: assign, z, y, x+bin, reduce, total
-    kern = {
-        "assign": (per[0] / ab["nmesh"], ab["assign"]),
-        "pass_z": (per[1] / ab["nmesh"], ab["pass_z"]),
-        "pass_y": (per[2] / ab["nmesh"], ab["pass_y"]),
-        "pass_x_bin": (per[3], ab["pass_x_bin"]),
-    }
-    dom = max(kern, key=lambda k: kern[k][0])
-    ms, nbytes = kern[dom]
-    achieved = nbytes / (ms * 1e-3) / 1e9
-    line = {
-        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": config_of(wl, nreal),
-        "phases_ms": {"assign": per[0], "pass_z": per[1], "pass_y": per[2],
-                      "pass_x_bin": per[3], "reduce": per[4], "total": per[5]},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": args.traffic.get(dom) if args.traffic else None,
-                     "eval_algorithmic_GB": ab["total"] / 1e9,
-                     "eval_frac": ab["total"] / (t_max / args.steps * world) / 1e9 / peak},
-        "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": nreal * 32,
-                "d2h_bytes_per_step": d2h},
-        "gpu_launches": launches,
-        "clocks": clocks,
-    }
-    if world == 1 and not args.no_cpu:
-        cpu_s = cpu_eval(wl, cat, threads=os.cpu_count())
-        line["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "evals/s", "cores": os.cpu_count(),
-                                "kind": "port",
-                                "sample": "one full evaluation of the workload (FP64 OpenMP "
-                                          "restatement; FFT by the project's FFTW-API shim)"}
-    print(json.dumps(line))
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_of(args.workload, nreal),
+            "phases_ms": {"assign": ph[0], "pass_z": ph[1], "pass_y": ph[2], "pass_x_bin": ph[3],
+                          "reduce": ph[4], "device_total": ph[5]},
+            "roofline": roofline(ph, wl["ng"], wl["interlace"], nreal, traffic),
+            "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": nreal * 32,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": nlaunch, "clocks": clocks,
+        }
+        line.update(extra)
+        if world == 1 and not args.no_cpu:
+            cpu_s = cpu_eval(cat, threads=os.cpu_count())
+            line["cpu_baseline"] = {
+                "value": 1.0 / cpu_s, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",
+                "sample": "one plain Ng=1024 PCS interlaced evaluation of the same catalogue "
+                          "(FP64 OpenMP restatement of the reference; FFT by the project's "
+                          "FFTW-API shim)"}
+        print(json.dumps(line))
+    if le is not None:
+        le.close()
+    plain.close()
     return 0
 
 
@@ -337,15 +405,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--traffic", type=json.loads, default=None,
-                    help='per-kernel ncu DRAM bytes per launch, e.g. {"pass_z": 1.2e10}')
     args = ap.parse_args()
-    if args.traffic is None:
-        # ncu DRAM read+write bytes per launch, summarised under profiles/
-        tf = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
-        if os.path.exists(tf):
-            with open(tf) as f:
-                args.traffic = json.load(f).get("bytes_per_launch")
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_init()
     if args.impl == "reference":

@@ -136,6 +136,16 @@ int ps_gpu_last_launches(const ps_gpu_ctx *ctx);
  * their own work or record CUDA events around the context's launches. */
 void *ps_gpu_stream(const ps_gpu_ctx *ctx);
 
+/* Splits every k bin of the binning sweep into nmu bins of |mu| in [0, 1]
+ * (1 restores the plain binning; at most 64).  ps_gpu_execute still returns
+ * the usual P_l(k); the raw per-(k, |mu|) sums sum p L_l(mu) of its spectra
+ * (autos, then the cross) are kept for ps_gpu_read_kmu.  Used by the learned
+ * alias correction.  No counterpart in the reference. */
+int ps_gpu_set_mu_bins(ps_gpu_ctx *ctx, int nmu);
+
+/* Copies the last execute's raw sums, [nspec][npole][nbin][nmu]. */
+int ps_gpu_read_kmu(const ps_gpu_ctx *ctx, double *out);
+
 /* ---- Stage-level entry points (checked against the oracle stage by stage) */
 
 /* Copies mesh m (0: Fr, 1: Frl) of catalogue cat to the host as doubles,

@@ -34,6 +34,7 @@ EXPORTED = [
     "ps_gpu_assign_soa", "ps_gpu_execute", "ps_gpu_last_error",
     "ps_gpu_last_timings", "ps_gpu_last_launches", "ps_gpu_read_mesh",
     "ps_gpu_fft_r2c_host", "ps_gpu_bin_fields_host", "ps_gpu_stream",
+    "ps_gpu_set_mu_bins", "ps_gpu_read_kmu",
 ]
 
 
@@ -110,6 +111,8 @@ def lib():
         L.ps_gpu_last_error.restype = ctypes.c_char_p
         L.ps_gpu_last_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.ps_gpu_last_launches.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_set_mu_bins.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ps_gpu_read_kmu.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ps_gpu_stream.argtypes = [ctypes.c_void_p]
         L.ps_gpu_stream.restype = ctypes.c_void_p
         L.ps_gpu_read_mesh.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
@@ -253,6 +256,16 @@ class Estimator:
 
     def launches(self):
         return lib().ps_gpu_last_launches(self._ctx)
+
+    def set_mu_bins(self, nmu):
+        self._check(lib().ps_gpu_set_mu_bins(self._ctx, int(nmu)))
+        self.nmu = int(nmu)
+
+    def read_kmu(self, nspec):
+        """Raw per-(k, |mu|) sums of the last execute: [nspec, npole, nbin, nmu]."""
+        out = np.zeros((nspec, len(self.poles), self.nbin, self.nmu))
+        self._check(lib().ps_gpu_read_kmu(self._ctx, _ptr(out)))
+        return out
 
     def stream(self):
         """The context's cudaStream_t as an integer handle."""

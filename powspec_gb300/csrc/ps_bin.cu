@@ -44,11 +44,11 @@ __device__ __forceinline__ void run_flush(RunAcc<NSPEC>& ra, float* tacc, int np
 
 // Adds one mode with power p[s] (already windowed and weighted) at mu.
 template <int NSPEC>
-__device__ __forceinline__ void run_add(RunAcc<NSPEC>& ra, const ModeGeom& g, int b,
+__device__ __forceinline__ void run_add(RunAcc<NSPEC>& ra, const ModeGeom& g, int b, int nkey,
                                         const float (&p)[NSPEC], float mu, bool skip_odd,
                                         float* tacc, int& lo, int& hi) {
   if (b != ra.bin) {
-    run_flush<NSPEC>(ra, tacc, g.npole, g.nbin, lo, hi);
+    run_flush<NSPEC>(ra, tacc, g.npole, nkey, lo, hi);
     ra.bin = b;
   }
 #pragma unroll
@@ -107,13 +107,14 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
   const int ntile = ngk * nty;
   const ModeGeom& g = a.geom;
   const int nacc = NSPEC * g.npole;
+  const int nkey = g.nbin * g.nmu;  // accumulator key = k bin * nmu + |mu| bin
   const size_t tile_elems = (size_t)a.nfield * a.ty * ls;  // one ping-pong buffer
   float2* sm2 = sm + tile_elems;  // second FFT buffer (ping-pong)
   float* tacc = reinterpret_cast<float*>(sm + 2 * tile_elems);
   __shared__ int srange[2];
-  double* part = STORE ? nullptr : a.partials + (size_t)blockIdx.x * nacc * g.nbin;
+  double* part = STORE ? nullptr : a.partials + (size_t)blockIdx.x * nacc * nkey;
   if (!STORE) {
-    for (int e = threadIdx.x; e < nacc * g.nbin; e += blockDim.x) tacc[e] = 0.f;
+    for (int e = threadIdx.x; e < nacc * nkey; e += blockDim.x) tacc[e] = 0.f;
     if (threadIdx.x == 0) {
       srange[0] = 0x7fffffff;
       srange[1] = -1;
@@ -212,19 +213,20 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
         }
         const float kxf = g.vec[0] * (float)ip;
         const float mu = (kxf * g.los[0] + mu_yz) * rsqrtf(kxf * kxf + k2_yz);
-        run_add<NSPEC>(ra, g, b, p, mu, twice, tacc, lo, hi);
+        const int key = (g.nmu == 1) ? b : b * g.nmu + min(g.nmu - 1, (int)(fabsf(mu) * g.nmu));
+        run_add<NSPEC>(ra, g, key, nkey, p, mu, twice, tacc, lo, hi);
       }
-      run_flush<NSPEC>(ra, tacc, g.npole, g.nbin, lo, hi);
+      run_flush<NSPEC>(ra, tacc, g.npole, nkey, lo, hi);
     }
     note_range(srange, lo, hi);
     if (++ntiles_acc == kMergeEvery) {
-      merge_tile(tacc, srange, part, nacc, g.nbin);
+      merge_tile(tacc, srange, part, nacc, nkey);
       ntiles_acc = 0;
     } else {
       __syncthreads();
     }
   }
-  if (!STORE && ntiles_acc) merge_tile(tacc, srange, part, nacc, g.nbin);
+  if (!STORE && ntiles_acc) merge_tile(tacc, srange, part, nacc, nkey);
 }
 
 // Stand-alone binning of FFTW-layout fields [x][y][kz]: one line per (x, y).
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(kFftThreads) k_bin_fields(const __grid_constan
         const float kzf = g.vec[2] * (float)k;
         const float mu = (kxf * g.los[0] + kyf * g.los[1] + kzf * g.los[2]) *
                          rsqrtf(kxf * kxf + kyf * kyf + kzf * kzf);
-        run_add<1>(ra, g, b, p, mu, twice, tacc, lo, hi);
+        run_add<1>(ra, g, b, g.nbin, p, mu, twice, tacc, lo, hi);
       }
       run_flush<1>(ra, tacc, g.npole, g.nbin, lo, hi);
     }
@@ -383,7 +385,8 @@ void launch_c_p(const PassCArgs& a, cudaStream_t s) {
     launch_c<1, true, P2>(a, (unsigned)ntile, pass_c_smem(a.ng, a.ty, a.nfield, 0, 0, P2), s);
     return;
   }
-  const size_t smem = pass_c_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole, a.geom.nbin, P2);
+  const size_t smem =
+      pass_c_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole, a.geom.nbin * a.geom.nmu, P2);
   switch (a.nspec) {
     case 1: launch_c<1, false, P2>(a, (unsigned)a.grid, smem, s); break;
     case 2: launch_c<2, false, P2>(a, (unsigned)a.grid, smem, s); break;

@@ -122,6 +122,8 @@ struct ps_gpu_ctx {
   int nspec = 0, spec_a[3] = {0, 0, 0}, spec_b[3] = {0, 0, 0}, spec_cat[3] = {0, 0, 0};
   int ty_a = 1, tx_b = 1, ty_c = 1, grid_c = 1;
   int ty_ap = 1, tx_bp = 1;  // tiles of the pipelined passes
+  int nmu = 1;               // |mu| sub-bins of the binning pass
+  std::vector<double> kmu;   // last execute's raw (k, |mu|) sums
   double* d_part = nullptr;
   double* d_sums = nullptr;
   double* d_wsum = nullptr;  // [2 cats][2]
@@ -172,6 +174,22 @@ int ref_bin(const ps_gpu_ctx* c, double km2) {
   if (kmod < c->kedge[0] || kmod >= c->kedge[c->nbin]) return -1;
   const int b = (int)((kmod - c->kedge[0]) / c->p.dk);
   return (b < 0 || b >= c->nbin) ? -1 : b;
+}
+
+// Per-CTA partial sums, reduced sums and the pinned host copy, sized for
+// nspec * npole * nbin * nmu accumulators.
+int alloc_accum(ps_gpu_ctx* c) {
+  const size_t width = (size_t)c->nspec * c->p.npole * c->nbin * c->nmu;
+  if (c->d_part) cudaFree(c->d_part);
+  if (c->d_sums) cudaFree(c->d_sums);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  c->d_part = nullptr;
+  c->d_sums = nullptr;
+  c->h_out = nullptr;
+  CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)c->grid_c * width));
+  CU(cudaMalloc(&c->d_sums, sizeof(double) * width));
+  CU(cudaMallocHost(&c->h_out, sizeof(double) * (width + 8)));
+  return 0;
 }
 
 int validate(ps_gpu_ctx* c, const ps_gpu_params* p) {
@@ -290,6 +308,7 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   ModeGeom& g = c->geom;
   g.ng = ng;
   g.nbin = c->nbin;
+  g.nmu = 1;
   g.npole = p.npole;
   for (int l = 0; l < kMaxPole; l++) g.poles[l] = (l < p.npole) ? p.poles[l] : 0;
   g.logscale = p.logscale;
@@ -332,14 +351,12 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
     CU(cudaMalloc(&c->grid[f], c->ntot * sizeof(unsigned long long)));
     CU(cudaMalloc(&c->cbuf[f], c->ncx * sizeof(float2)));
   }
-  CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)c->grid_c * nacc * c->nbin));
-  CU(cudaMalloc(&c->d_sums, sizeof(double) * (size_t)nacc * c->nbin));
+  if ((rc = alloc_accum(c))) return rc;
   CU(cudaMalloc(&c->d_wsum, sizeof(double) * 4));
   CU(cudaMalloc(&c->d_wpart, sizeof(double) * 2 * kAssignMaxBlocks));
   CU(cudaMalloc(&c->d_err, sizeof(int) * 4));
   CU(cudaMemset(c->d_wsum, 0, sizeof(double) * 4));
   CU(cudaMemset(c->d_err, 0, sizeof(int) * 4));
-  CU(cudaMallocHost(&c->h_out, sizeof(double) * ((size_t)nacc * c->nbin + 8)));
 
   // ---- geometry sweep: counts, mean |k|, multipole mode weights
   {
@@ -504,8 +521,9 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
     if (!c->assigned[k]) return fail(c, PS_GPU_ERR_STATE, "catalogue %d not assigned", k);
   CU(cudaSetDevice(p.device));
   cudaStream_t s = c->stream;
-  const int ng = c->ng, npole = p.npole, nbin = c->nbin;
+  const int ng = c->ng, npole = p.npole, nbin = c->nbin, nmu = c->nmu;
   const int nacc = c->nspec * npole;
+  const int nkey = nbin * nmu;
 
   const bool pipe = c->plan_full.logn >= 0 && !getenv("PS_GPU_NO_PIPELINE");
   CU(cudaMemsetAsync(c->d_err + 2, 0, sizeof(int), s));
@@ -541,7 +559,7 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   }
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[2], s));
-  CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)c->grid_c * nacc * nbin, s));
+  CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)c->grid_c * nacc * nkey, s));
   PassCArgs pc;
   memset(&pc, 0, sizeof pc);
   pc.ng = ng;
@@ -561,13 +579,13 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   c->launches += launch_pass_c(pc, s);
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], s));
-  c->launches += launch_reduce(c->d_part, c->grid_c, nacc * nbin, c->d_sums, s);
+  c->launches += launch_reduce(c->d_part, c->grid_c, nacc * nkey, c->d_sums, s);
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[4], s));
   double* h = c->h_out;
-  CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nbin, cudaMemcpyDeviceToHost, s));
-  CU(cudaMemcpyAsync(h + (size_t)nacc * nbin, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
-  CU(cudaMemcpyAsync(h + (size_t)nacc * nbin + 4, c->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nkey, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h + (size_t)nacc * nkey + 4, c->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   float t = 0;
   if (c->assign_started && cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess) c->timings[0] = t;
@@ -577,9 +595,18 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   c->assign_started = false;
   c->assigned[0] = c->assigned[1] = 0;
 
+  // fold the |mu| sub-bins (kept for ps_gpu_read_kmu)
+  std::vector<double> fold;
   const double* sums = h;
-  const double* wsum = h + (size_t)nacc * nbin;
-  const int* errs = (const int*)(h + (size_t)nacc * nbin + 4);
+  if (nmu > 1) {
+    c->kmu.assign(h, h + (size_t)nacc * nkey);
+    fold.assign((size_t)nacc * nbin, 0.0);
+    for (size_t q = 0; q < (size_t)nacc * nbin; q++)
+      for (int j = 0; j < nmu; j++) fold[q] += h[q * nmu + j];
+    sums = fold.data();
+  }
+  const double* wsum = h + (size_t)nacc * nkey;
+  const int* errs = (const int*)(h + (size_t)nacc * nkey + 4);
   if (errs[2]) return fail(c, PS_GPU_ERR_CUDA, "pipelined pass: bulk-copy wait timed out (flags %d)", errs[2]);
   for (int k = 0; k < p.ncat; k++) {
     // an empty catalogue has no coordinate range (src/genr_mesh.c:518-521)
@@ -636,6 +663,26 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
     }
     if (r->kedge) r->kedge[nbin] = pow(10, c->kedge[nbin]);
   }
+  return 0;
+}
+
+int ps_gpu_set_mu_bins(ps_gpu_ctx* c, int nmu) {
+  if (!c || nmu < 1 || nmu > 64) return fail(c, PS_GPU_ERR_ARG, "number of mu bins must be 1..64");
+  const size_t smem = pass_c_smem(c->ng, c->ty_c, c->nfield, c->nspec * c->p.npole,
+                                  c->nbin * nmu, c->plan_full.logn >= 0);
+  if (smem > 227 * 1024) return fail(c, PS_GPU_ERR_ARG, "too many (k, mu) bins for the binning pass");
+  CU(cudaSetDevice(c->p.device));
+  CU(cudaStreamSynchronize(c->stream));
+  c->nmu = nmu;
+  c->geom.nmu = nmu;
+  c->kmu.clear();
+  return alloc_accum(c);
+}
+
+int ps_gpu_read_kmu(const ps_gpu_ctx* c, double* out) {
+  if (!c || !out) return PS_GPU_ERR_ARG;
+  if (c->nmu < 2 || c->kmu.empty()) return PS_GPU_ERR_STATE;
+  memcpy(out, c->kmu.data(), sizeof(double) * c->kmu.size());
   return 0;
 }
 
@@ -714,6 +761,7 @@ int ps_gpu_bin_fields_host(ps_gpu_ctx* c, const float* f1, const float* f2, doub
   b.f1 = d1;
   b.f2 = d2;
   b.geom = c->geom;
+  b.geom.nmu = 1;
   b.partials = c->d_part;
   b.grid = c->grid_c;
   launch_bin_fields(b, s);

@@ -647,6 +647,7 @@ __device__ __forceinline__ void fft2_lines_from(const float2* src, int sstride, 
 struct ModeGeom {
   int ng;
   int nbin;
+  int nmu;                   // |mu| sub-bins per k bin (1: plain P_l binning)
   int npole;
   int poles[kMaxPole];
   int logscale;

@@ -14,7 +14,7 @@ def declared_symbols():
     syms = set()
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
-        syms |= set(re.findall(r"\b(ps_gpu_\w+)\s*\(", src))
+        syms |= set(re.findall(r"\b(ps_(?:gpu|mlp)_\w+)\s*\(", src))
     return sorted(syms)
 
 

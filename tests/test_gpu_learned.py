@@ -1,0 +1,135 @@
+"""Learned alias correction: the GPU network kernels against the FP64 oracle
+(forward, loss, gradients), training, and what the trained network gains
+over the uncorrected coarse mesh on held-out catalogues."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def synthetic_groups(ngroups, seed=0):
+    rng = np.random.default_rng(seed)
+    x = rng.random((ngroups * 16, 6)).astype(np.float32)
+    a = (rng.random((ngroups * 16, 3)) * [1.0, 0.3, 0.1] / 16).astype(np.float32)
+    g = np.zeros((ngroups, 8), np.float32)
+    g[:, 0:3] = rng.random((ngroups, 3)) * 0.05
+    g[:, 3:6] = rng.standard_normal((ngroups, 3)) * 0.2 + [0.9, 0.1, 0.0]
+    g[:, 6] = 1.0
+    g[:, 7] = 1.0
+    return x, a, g
+
+
+def test_forward_matches_oracle(gpu_lib):
+    from oracle import mlp as om
+    from powspec_gb300 import learned
+    p = om.init_params(3)
+    p[om.ow4:om.ob4] = np.random.default_rng(1).standard_normal(64) * 0.1
+    p[om.ob4] = 0.05
+    m = learned.MLP(params=p)
+    x = np.random.default_rng(2).random((1000, 6)).astype(np.float32)
+    c = m.infer(x)
+    y, _ = om.forward(p, x.astype(np.float64))
+    np.testing.assert_allclose(c, np.exp(y), rtol=2e-3)
+
+
+def test_gradients_match_oracle(gpu_lib):
+    from oracle import mlp as om
+    from powspec_gb300 import learned
+    p = om.init_params(5)
+    rng = np.random.default_rng(6)
+    p[om.ow4:om.ob4] = rng.standard_normal(64) * 0.05
+    x, a, g = synthetic_groups(24, seed=7)
+    m = learned.MLP(params=p)
+    m.set_data(x, a, g)
+    idx = np.arange(24, dtype=np.int32)
+    loss, grad = m.grad(idx)
+    lref, gref = om.loss_and_grad(p, x.astype(np.float64), a, g, idx)
+    assert loss == pytest.approx(lref, rel=2e-3)
+    # BF16 operands: compare each parameter block norm-wise
+    blocks = [(om.oW1, om.ob1), (om.ob1, om.oW2), (om.oW2, om.ob2), (om.ob2, om.oW3),
+              (om.oW3, om.ob3), (om.ob3, om.ow4), (om.ow4, om.ob4), (om.ob4, om.NPARAM)]
+    for lo, hi in blocks:
+        num = np.linalg.norm(grad[lo:hi] - gref[lo:hi])
+        den = np.linalg.norm(gref[lo:hi]) + 1e-30
+        assert num / den < 2e-2, (lo, hi, num / den)
+
+
+def test_training_fits_a_known_correction(gpu_lib):
+    """Targets made with c*(x) = exp(0.1 sin(3 x0) - 0.05 x2): loss must drop."""
+    from oracle import mlp as om
+    from powspec_gb300 import learned
+    x, a, g = synthetic_groups(512, seed=11)
+    cstar = np.exp(0.1 * np.sin(3 * x[:, 0]) - 0.05 * x[:, 2]).reshape(512, 16)
+    f = np.array([1.0, 5.0, 9.0])
+    s = np.einsum("gj,gjl->gl", cstar, a.reshape(512, 16, 3))
+    g[:, 3:6] = f * (s - g[:, 0:3])
+    g[:, 6] = 1.0 / np.maximum(np.abs(g[:, 3]), 0.1) ** 2
+    m = learned.MLP(params=om.init_params(1))
+    m.set_data(x, a, g)
+    l0, _ = m.grad(np.arange(512, dtype=np.int32))
+    learned.train(m, (x, a, g, None), steps=3000, batch=64, lr=3e-3)
+    l1, _ = m.grad(np.arange(512, dtype=np.int32))
+    assert l1 < 0.05 * l0, (l0, l1)
+
+
+def test_checkpoint_round_trip(gpu_lib, tmp_path):
+    from oracle import mlp as om
+    from powspec_gb300 import learned
+    m = learned.MLP(params=om.init_params(2))
+    x, a, g = synthetic_groups(32)
+    learned.train(m, (x, a, g, None), steps=50, batch=32)
+    path = str(tmp_path / "ck.bin")
+    m.save(path)
+    m2 = learned.MLP()
+    m2.load(path)
+    np.testing.assert_array_equal(m.params(), m2.params())
+
+
+def test_cells_reproduce_plain_multipoles(gpu_lib):
+    from powspec_gb300 import Estimator, catalog, learned
+    cat = catalog.lognormal(100000, seed=3, ngen=64)
+    with Estimator(ng=64, assign=2, interlace=True, dk=0.005) as e:
+        plain = e.run([cat]).pl[0]
+        cells = learned.measure_cells(e, cat)
+    # c = 1 reproduces the same evaluation's multipoles exactly (up to FP64 sums)
+    np.testing.assert_allclose(cells.corrected(np.ones(cells.A.shape[:2])), cells.plain,
+                               rtol=1e-9, atol=1e-9 * np.abs(plain).max())
+    # and a separate evaluation up to the FP32 bin-accumulation order
+    np.testing.assert_allclose(cells.plain, plain, rtol=1e-5, atol=1e-5 * np.abs(plain).max())
+
+
+def test_learned_correction_gains_on_held_out(gpu_lib):
+    """Coarse Ng = 64 (CIC without interlacing, and TSC interlaced) corrected
+    towards Ng = 256 PCS interlaced on 12 training catalogues: on 4 held-out
+    catalogues the error against the fine mesh must shrink."""
+    from powspec_gb300 import catalog, learned
+    cats = [catalog.lognormal(1_000_000, seed=100 + s, ngen=128) for s in range(16)]
+    cfgs = [(64, 1, False), (64, 2, True)]
+    pairs = learned.measure_pairs(cats, configs=cfgs, fine_cfg=dict(ng=256, assign=3, interlace=True))
+    assert len(pairs) == 16
+    m = learned.MLP(params=learned.init_params(0))
+    learned.train(m, learned.build_groups(pairs[:12], configs=cfgs), steps=8000, batch=64, lr=1e-3)
+    err = learned.errors(pairs[12:], m, configs=cfgs)
+    e = err[(64, 1, False)]
+    assert e["corrected"].mean() < 0.8 * e["plain"].mean(), (e["corrected"].mean(), e["plain"].mean())
+
+
+def test_committed_weights_meet_tolerance_on_held_out(gpu_lib):
+    """The committed network (trained on seeds >= 1000): on a held-out
+    catalogue, learned Ng = 256 PCS interlaced vs plain Ng = 1024 PCS
+    interlaced is within 1% of P_0 up to 0.8 k_Nyq(256), and closer than the
+    uncorrected Ng = 256 mesh."""
+    from powspec_gb300 import Estimator, catalog, learned
+    cat = catalog.lognormal(4_000_000, seed=7, ngen=256)
+    with learned.LearnedEstimator(ng=256, assign=3, interlace=True) as le:
+        k, pc, trusted = le.run(cat)
+        plain256 = le.last_cells.plain
+    with Estimator(ng=1024, assign=3, interlace=True, dk=0.005) as fine:
+        ref = fine.run([cat])
+    pf = ref.pl[0][:, :len(k)]
+    use = trusted & (ref.cnt[:len(k)] > 1) & (pf[0] > 0)
+    assert use.sum() > 100
+    e_learned = (np.abs(pc - pf)[:, use] / pf[0][use]).max()
+    e_plain = (np.abs(plain256 - pf)[:, use] / pf[0][use]).max()
+    assert e_learned < 0.01, e_learned
+    assert e_learned < e_plain, (e_learned, e_plain)
