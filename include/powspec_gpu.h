@@ -149,7 +149,9 @@ int ps_gpu_read_kmu(const ps_gpu_ctx *ctx, double *out);
 /* ---- Stage-level entry points (checked against the oracle stage by stage) */
 
 /* Copies mesh m (0: Fr, 1: Frl) of catalogue cat to the host as doubles,
- * row-major [ng][ng][ng].  Valid between assign and execute. */
+ * row-major [ng][ng][ng]: the exact fixed-point cell sums (2^-32 units),
+ * re-accumulated from the catalogue's sorted records.  Valid between the
+ * assign of `cat` and the next assign or execute. */
 int ps_gpu_read_mesh(ps_gpu_ctx *ctx, int cat, int m, double *out);
 
 /* Standalone r2c 3-D FFT of a real FP32 cube [ng][ng][ng] (host memory)

@@ -7,6 +7,7 @@
 
 #include <math.h>
 #include <stdarg.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -15,6 +16,7 @@
 #include <vector>
 
 #include "powspec_gpu.h"
+
 #include "ps_internal.h"
 
 using namespace ps;
@@ -123,6 +125,13 @@ struct ps_gpu_ctx {
   int ty_a = 1, tx_b = 1, ty_c = 1, grid_c = 1;
   int ty_ap = 1, tx_bp = 1;  // tiles of the pipelined passes
   int nmu = 1;               // |mu| sub-bins of the binning pass
+  // tile assignment
+  int gT = 0, gnt = 0;
+  size_t nkeys = 0, gcap = 0;
+  unsigned *d_hist = nullptr, *d_bsum = nullptr, *d_rank = nullptr;
+  void* d_rec = nullptr;
+  int last_cat = -1;
+  Particles last_pt{};
   std::vector<double> kmu;   // last execute's raw (k, |mu|) sums
   double* d_part = nullptr;
   double* d_sums = nullptr;
@@ -231,6 +240,11 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
     return fail(c, PS_GPU_ERR_ARG, "GRID_SIZE/2 must be a product of 2, 3 and 5: %d", p.ng);
   if ((size_t)c->nfield * p.ng > (size_t)2 * kPassCElems)
     return fail(c, PS_GPU_ERR_ARG, "GRID_SIZE %d too large for %d fields", p.ng, c->nfield);
+  c->gT = gather_tile(p.ng);
+  if (!c->gT || p.ng > 32767)
+    return fail(c, PS_GPU_ERR_ARG, "GRID_SIZE %d: needs a divisor in [4, 16] with at least 2 tiles", p.ng);
+  c->gnt = p.ng / c->gT;
+  c->nkeys = gather_keys(p.ng);
 
   // spectra: autos, then the cross (src/multipole.c:1221-1226)
   for (int k = 0; k < p.ncat; k++)
@@ -329,7 +343,7 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   c->ty_a = std::min({ng, 16, kCtaElems / (ng / 2)});
   c->tx_b = std::min({ng, 16, kCtaElems / ng});
   // pipelined passes: 64 KB staged per tile (int64 rows for z, complex for y)
-  c->ty_ap = std::max(1, std::min(ng, 8192 / ng));
+  c->ty_ap = std::max(1, std::min(ng, 8192 / (ng / 2)));
   c->tx_bp = std::max(1, std::min(ng, 8192 / ng));
   c->ty_c = std::max(1, std::min(ng, kPassCElems / (c->nfield * ng)));
   const int nacc = c->nspec * p.npole;
@@ -343,14 +357,18 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   // ---- device memory
   size_t freeb = 0, totalb = 0;
   CU(cudaMemGetInfo(&freeb, &totalb));
-  const size_t need = (size_t)c->nfield * (c->ntot * 8 + c->ncx * 8) +
-                      (size_t)c->grid_c * nacc * c->nbin * 8 + (64u << 20);
+  const size_t need = (size_t)c->nfield * (c->ncx * 16) +
+                      (size_t)c->grid_c * nacc * c->nbin * 8 + c->nkeys * 8 + (64u << 20);
   if (need > freeb)
     return fail(c, PS_GPU_ERR_MEMORY, "need %.1f GB of device memory, %.1f GB free", need / 1e9, freeb / 1e9);
+  // per field: the FP32 mesh, later reused for the y-pass output (8 B * Ncmplx
+  // >= 4 B * Ng^3), and the z-pass output
   for (int f = 0; f < c->nfield; f++) {
-    CU(cudaMalloc(&c->grid[f], c->ntot * sizeof(unsigned long long)));
+    CU(cudaMalloc(&c->grid[f], c->ncx * sizeof(float2)));
     CU(cudaMalloc(&c->cbuf[f], c->ncx * sizeof(float2)));
   }
+  CU(cudaMalloc(&c->d_hist, (c->nkeys + 1) * sizeof(unsigned)));
+  CU(cudaMalloc(&c->d_bsum, ((c->nkeys + 4095) / 4096 + 1) * sizeof(unsigned)));
   if ((rc = alloc_accum(c))) return rc;
   CU(cudaMalloc(&c->d_wsum, sizeof(double) * 4));
   CU(cudaMalloc(&c->d_wpart, sizeof(double) * 2 * kAssignMaxBlocks));
@@ -404,7 +422,8 @@ void ps_gpu_destroy(ps_gpu_ctx* c) {
     if (c->cbuf[f]) cudaFree(c->cbuf[f]);
   }
   void* bufs[] = {c->d_bintab, c->d_ksq, c->d_win, c->d_phase, c->d_tw_full, c->d_tw_half,
-                  c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage};
+                  c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage,
+                  c->d_hist, c->d_bsum, c->d_rank, c->d_rec};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -446,31 +465,60 @@ int ensure_stage(ps_gpu_ctx* c, size_t bytes) {
   return 0;
 }
 
+GatherArgs gather_args(ps_gpu_ctx* c, int cat) {
+  GatherArgs g{};
+  g.ng = c->ng;
+  g.assign = c->p.assign;
+  g.interlace = c->p.interlace;
+  g.T = c->gT;
+  g.nt = c->gnt;
+  for (int d = 0; d < 3; d++) {
+    g.box[d] = c->p.box[d];
+    const double s = (double)c->ng / c->p.box[d];
+    g.s_hi[d] = (float)s;
+    g.s_lo[d] = (float)(s - (double)g.s_hi[d]);
+  }
+  g.hist = c->d_hist;
+  g.bsum = c->d_bsum;
+  g.rank = c->d_rank;
+  g.rec = c->d_rec;
+  for (int m = 0; m < c->mpc; m++) g.out[m] = (float*)c->grid[cat * c->mpc + m];
+  g.wsum = c->d_wsum + 2 * cat;
+  g.wpart = c->d_wpart;
+  g.err = c->d_err + cat;
+  return g;
+}
+
 int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
+  // ranks and bucket offsets are 32-bit
+  if (pt.n >= 0xffffffffull)
+    return fail(c, PS_GPU_ERR_RANGE, "%zu particles: at most 2^32 - 2 per catalogue", pt.n);
   CU(cudaSetDevice(c->p.device));
   if (!c->assign_started) {
     CU(cudaEventRecord(c->ev[6], c->stream));
     c->assign_started = true;
     c->launches = 0;
   }
-  for (int m = 0; m < c->mpc; m++)
-    CU(cudaMemsetAsync(c->grid[cat * c->mpc + m], 0, c->ntot * sizeof(unsigned long long), c->stream));
+  if (pt.n > c->gcap) {
+    CU(cudaStreamSynchronize(c->stream));
+    if (c->d_rank) cudaFree(c->d_rank);
+    if (c->d_rec) cudaFree(c->d_rec);
+    c->d_rank = nullptr;
+    c->d_rec = nullptr;
+    c->gcap = 0;
+    CU(cudaMalloc(&c->d_rank, pt.n * sizeof(unsigned)));
+    CU(cudaMalloc(&c->d_rec, pt.n * 48));
+    c->gcap = pt.n;
+  }
   CU(cudaMemsetAsync(c->d_wsum + 2 * cat, 0, sizeof(double) * 2, c->stream));
   CU(cudaMemsetAsync(c->d_err + cat, 0, sizeof(int), c->stream));
-  AssignArgs a;
-  a.ng = c->ng;
-  a.assign = c->p.assign;
-  for (int d = 0; d < 3; d++) a.box[d] = c->p.box[d];
-  a.mesh0 = c->grid[cat * c->mpc];
-  a.mesh1 = c->p.interlace ? c->grid[cat * c->mpc + 1] : nullptr;
-  a.wsum = c->d_wsum + 2 * cat;
-  a.wpart = c->d_wpart;
-  a.err = c->d_err + cat;
-  if (pt.n) c->launches += launch_assign(pt, a, c->stream);
+  if (pt.n) c->launches += launch_gather_assign(pt, gather_args(c, cat), c->stream, false);
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[7], c->stream));
   c->assigned[cat] = 1;
   c->npart[cat] = pt.n;
+  c->last_cat = cat;
+  c->last_pt = pt;
   return 0;
 }
 
@@ -483,6 +531,8 @@ int ps_gpu_assign_aos(ps_gpu_ctx* c, int cat, const double* xyzw, size_t n, int 
   Particles pt{};
   pt.n = n;
   if (on_device) {
+    if ((uintptr_t)xyzw & 31)
+      return fail(c, PS_GPU_ERR_ARG, "device AoS records must be 32-byte aligned");
     pt.aos = xyzw;
   } else {
     int rc = ensure_stage(c, n * 4 * sizeof(double));
@@ -500,6 +550,8 @@ int ps_gpu_assign_soa(ps_gpu_ctx* c, int cat, const float* x, const float* y, co
   Particles pt{};
   pt.n = n;
   if (on_device) {
+    if (((uintptr_t)x | (uintptr_t)y | (uintptr_t)z | (uintptr_t)w) & 3)
+      return fail(c, PS_GPU_ERR_ARG, "device SoA arrays must be 4-byte aligned");
     pt.x = x; pt.y = y; pt.z = z; pt.w = w;
   } else {
     const int na = w ? 4 : 3;
@@ -534,8 +586,8 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
     a.ty = pipe ? c->ty_ap : c->ty_a;
     a.pipe_grid = pipe ? c->nsm : 0;
     a.err = c->d_err + 2;
-    a.grid = (const long long*)c->grid[f];
-    a.fgrid = nullptr;
+    a.grid = nullptr;
+    a.fgrid = (const float*)c->grid[f];
     a.out = c->cbuf[f];
     a.wsum = c->d_wsum + 2 * (f / c->mpc);
     a.tw_half = c->d_tw_half;
@@ -689,10 +741,23 @@ int ps_gpu_read_kmu(const ps_gpu_ctx* c, double* out) {
 int ps_gpu_read_mesh(ps_gpu_ctx* c, int cat, int m, double* out) {
   if (!c || !out || cat < 0 || cat >= c->p.ncat || m < 0 || m >= c->mpc)
     return fail(c, PS_GPU_ERR_ARG, "invalid read_mesh arguments");
+  if (c->last_cat != cat || !c->assigned[cat])
+    return fail(c, PS_GPU_ERR_STATE, "read_mesh: catalogue %d is not the last one assigned", cat);
   CU(cudaSetDevice(c->p.device));
+  long long* tmp = nullptr;
+  CU(cudaMalloc(&tmp, c->ntot * sizeof(long long) * c->mpc));
+  GatherArgs g = gather_args(c, cat);
+  for (int k = 0; k < c->mpc; k++) g.out64[k] = tmp + (size_t)k * c->ntot;
+  launch_gather_assign(c->last_pt, g, c->stream, true);
   std::vector<long long> q(c->ntot);
-  CU(cudaMemcpyAsync(q.data(), c->grid[cat * c->mpc + m], c->ntot * 8, cudaMemcpyDeviceToHost, c->stream));
-  CU(cudaStreamSynchronize(c->stream));
+  cudaError_t e1 = cudaGetLastError();
+  cudaError_t e2 = cudaMemcpyAsync(q.data(), tmp + (size_t)m * c->ntot, c->ntot * 8,
+                                   cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e3 = cudaStreamSynchronize(c->stream);
+  cudaFree(tmp);
+  CU(e1);
+  CU(e2);
+  CU(e3);
   for (size_t i = 0; i < c->ntot; i++) out[i] = (double)q[i] * kFixInv;
   return 0;
 }
@@ -702,7 +767,7 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   CU(cudaSetDevice(c->p.device));
   cudaStream_t s = c->stream;
   const int ng = c->ng;
-  float* d_in = (float*)c->grid[0];  // ntot floats fit in the int64 grid
+  float* d_in = (float*)c->grid[0];  // ntot floats fit in the mesh buffer
   CU(cudaMemcpyAsync(d_in, in, c->ntot * sizeof(float), cudaMemcpyHostToDevice, s));
   PassAArgs a;
   a.ng = ng;

@@ -5,14 +5,14 @@
 // of which reads long contiguous lines, transforms them in shared memory and
 // writes them transposed so that the next pass again reads contiguous lines:
 //
-//   pass A  grid[x][y][z] (int64 fixed point)  ->  A[x][kz][y]   (z, r2c)
+//   pass A  mesh[x][y][z] (FP32)               ->  A[x][kz][y]   (z, r2c)
 //   pass B  A[x][kz][y]                        ->  B[kz][ky][x]  (y)
 //   pass C  B[kz][ky][x] -> x transform, then binned in place (ps_bin.cu)
 //
-// Pass A fuses the fixed-point -> FP32 conversion and subtracts the mean
-// cell value: only the k = 0 mode changes, and the periodic-box estimator
-// never uses it (src/multipole.c:806), while FP32 round-off of every other
-// mode scales with the norm of the input.
+// The meshes arrive as FP32 with the mean cell value already subtracted
+// (ps_gather.cu): only the k = 0 mode changes, which the periodic-box
+// estimator never uses (src/multipole.c:806), while FP32 round-off of every
+// other mode scales with the norm of the input.
 #include "ps_internal.h"
 
 namespace ps {
@@ -143,11 +143,12 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_pass_a_tma(const __grid_cons
   const int ls = line_stride(M + 1, true);
   const int nty = (ng + a.ty - 1) / a.ty;
   const int ntile = ng * nty;
+  const size_t selems = ((size_t)a.ty * ls + 1) & ~(size_t)1;  // 16-byte aligned
   uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
-  long long* stage[2];
-  stage[0] = reinterpret_cast<long long*>(smraw + 128);
-  stage[1] = stage[0] + (size_t)a.ty * ng;
-  float2* F = reinterpret_cast<float2*>(stage[1] + (size_t)a.ty * ng);
+  float2* stage[2];
+  stage[0] = reinterpret_cast<float2*>(smraw + 128);
+  stage[1] = stage[0] + selems;
+  float2* F = stage[1] + selems;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -155,15 +156,14 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_pass_a_tma(const __grid_cons
     s_abort = 0;
   }
   __syncthreads();
-  const double W = *a.wsum;
-  const long long off = __double2ll_rn(W * 4294967296.0 / ((double)ng * ng * ng));
+  // real rows of ng floats, staged as M complex values (x[2m], x[2m+1])
   auto issue = [&](int tile, int s) {
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
-    mbar_expect_tx(&bar[s], (uint32_t)(nl * ng * 8));
-    const long long* src = a.grid + ((size_t)x * ng + y0) * ng;
+    mbar_expect_tx(&bar[s], (uint32_t)(nl * ng * 4));
+    const float* src = a.fgrid + ((size_t)x * ng + y0) * ng;
     for (int r = 0; r < nl; r++)
-      bulk_g2s(stage[s] + (size_t)r * ng, src + (size_t)r * ng, (uint32_t)(ng * 8), &bar[s]);
+      bulk_g2s(stage[s] + (size_t)r * M, src + (size_t)r * ng, (uint32_t)(ng * 4), &bar[s]);
   };
   if (threadIdx.x == 0 && (int)blockIdx.x < ntile) issue(blockIdx.x, 0);
   int it = 0;
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_pass_a_tma(const __grid_cons
     if (!pipe_wait(bar, it, a.err, &s_abort)) break;
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
-    float2* X = fft2_pp_from<true>(stage[s], ng, off, F, logm, nl, ls, a.tw_half);
+    float2* X = fft2_pp_from<false>(stage[s], M, 0, F, logm, nl, ls, a.tw_half);
     const int half = (M >> 1) + 1;
     for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {
       const int r = e / half, k = e - r * half;
@@ -274,8 +274,8 @@ int launch_pass_a(const PassAArgs& a, cudaStream_t s) {
   const size_t smem = (size_t)a.ty * line_stride(M + 1, p2) * sizeof(float2);
   const int nty = (a.ng + a.ty - 1) / a.ty;
   const unsigned grid = (unsigned)(a.ng * nty);
-  if (p2 && a.grid && a.pipe_grid > 0) {
-    const size_t sm2 = 128 + 2 * (size_t)a.ty * a.ng * 8 + (size_t)a.ty * line_stride(M + 1, true) * 8;
+  if (p2 && !a.grid && a.pipe_grid > 0) {
+    const size_t sm2 = 128 + 3 * ((((size_t)a.ty * line_stride(M + 1, true)) + 1) & ~(size_t)1) * 8;
     cudaFuncSetAttribute(k_pass_a_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
     k_pass_a_tma<<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
   } else if (p2) {

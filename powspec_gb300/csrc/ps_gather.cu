@@ -1,0 +1,582 @@
+// ps_gather.cu -- deterministic particle assignment by tiles: every mesh cell
+// is written exactly once, as FP32 (minus the mean cell value), with no
+// global atomics and no zeroing pass.
+//
+// Reference: ngp/cic/tsc/pcs (src/genr_mesh.c:50-412), interlace shift
+// (src/genr_mesh.c:590-602, :815-833), sim-box bound check
+// (src/genr_mesh.c:523-531).
+//
+//  classify  per particle: the stencil base node and fraction on the plain
+//            and the half-cell-shifted grid; its 16^3 tile and which of the
+//            neighbouring tiles its stencils reach (27 classes); histogram
+//            of the (tile, class) keys; weight sums (per-block partials).
+//  scan      exclusive prefix sum of the key counts.
+//  scatter   compact records in key order.
+//  gather    one CTA per tile reads the 125 (neighbour tile, class) buckets
+//            that can reach it, adds every stencil node that falls in the
+//            tile into int64 fixed-point accumulators in shared memory
+//            (integer sums: independent of the order), then writes the tile.
+//
+// Grid coordinates: x = pos * Ng / L is evaluated in double-float FP32
+// arithmetic (error ~1e-7 cell); only when the fraction lies within 4e-6 of
+// a decision point of the reference (0, 1/2, 1) is the reference's exact
+// FP64 sequence (pos - bmin) * Ng / L used instead, so cell indices and
+// branches are the reference's while FP64 work stays rare.
+#include "ps_internal.h"
+
+namespace ps {
+namespace {
+
+constexpr int kGatherThreads = 256;
+constexpr int kMeshPad = 8;  // words between the two meshes' accumulators (bank offset)
+constexpr float kEdge = 4e-6f;
+
+// wsum[0..1] = sums of the per-block partials: lane l adds blocks l, l + 32,
+// ... in order, then a fixed shuffle tree (same order every run).
+__global__ void k_wsum(const double* __restrict__ wpart, int nblocks, double* wsum) {
+  double t0 = 0, t1 = 0;
+  for (int b = threadIdx.x; b < nblocks; b += 32) {
+    t0 += wpart[2 * b];
+    t1 += wpart[2 * b + 1];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+    t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+  }
+  if (threadIdx.x == 0) {
+    wsum[0] = t0;
+    wsum[1] = t1;
+  }
+}
+
+// Stencil base node and parameter of one axis (see node_weights).
+struct Axis {
+  int base;
+  float par;
+};
+
+// Record of one particle in key order (48 bytes).
+struct Rec {
+  short base[2][3];  // [mesh][axis]
+  float par[2][3];
+  float wf;          // weight * 2^32 (FP32, for the node products)
+  long long q;       // llrint(weight * 2^32): the exact NGP node value
+};
+static_assert(sizeof(Rec) == 48, "record layout");
+
+// Offset of the first stencil node from the base and stencil width.
+__host__ __device__ inline int first_off(int assign) { return assign >= 2 ? -1 : 0; }
+__host__ __device__ inline int width(int assign) { return assign + 1; }
+
+// Exact reference grid coordinate (FP64, correctly rounded operations).
+__device__ __forceinline__ void exact_coord(double pos, double L, int ng, bool shift, int& i0,
+                                            double& d) {
+  double bmin = 0.0;
+  if (shift) {
+    bmin = __dsub_rn(0.0, __ddiv_rn(__dmul_rn(0.5, L), (double)ng));
+    if (pos >= __dadd_rn(bmin, L)) pos = __dsub_rn(pos, L);
+  }
+  const double x = __ddiv_rn(__dmul_rn(__dsub_rn(pos, bmin), (double)ng), L);
+  i0 = (int)x;
+  d = __dsub_rn(x, (double)i0);
+  if (i0 >= ng) i0 -= ng;
+}
+
+// Base node and parameter from (cell, fraction).  NGP: nearest node (rounds
+// up at d >= 1/2, src/genr_mesh.c:64-66).  CIC, PCS: the cell, d.  TSC: the
+// nearest node c and the offset u = d or d - 1 from it (src/genr_mesh.c:157-172).
+__device__ __forceinline__ Axis make_axis(int assign, int i0, double d, int ng) {
+  Axis a;
+  if (assign == 0 || assign == 2) {
+    const bool up = d >= 0.5;
+    a.base = up ? ((i0 == ng - 1) ? 0 : i0 + 1) : i0;
+    a.par = up ? (float)__dsub_rn(d, 1.0) : (float)d;
+  } else {
+    a.base = i0;
+    a.par = (float)d;
+  }
+  return a;
+}
+
+__device__ __forceinline__ bool near_edge(float d) {
+  return d < kEdge || d > 1.f - kEdge || fabsf(d - 0.5f) < kEdge;
+}
+
+// Both grids' axis for one coordinate.  pos_hi + pos_lo = pos; s_hi + s_lo = Ng / L.
+__device__ __forceinline__ void axis_pair(int assign, double pos, float pos_hi, float pos_lo,
+                                          float s_hi, float s_lo, double L, int ng, bool il,
+                                          Axis& a0, Axis& a1) {
+  // x = pos * s in double-float: p + t
+  const float p = pos_hi * s_hi;
+  const float e = fmaf(pos_hi, s_hi, -p);
+  const float t = e + fmaf(pos_hi, s_lo, pos_lo * s_hi);
+  int i = (int)floorf(p);
+  float d = (p - (float)i) + t;
+  if (d < 0.f) { i -= 1; d += 1.f; }
+  if (d >= 1.f) { i += 1; d -= 1.f; }
+  if (near_edge(d) || i < 0 || i >= ng) {
+    int i0;
+    double dd;
+    exact_coord(pos, L, ng, false, i0, dd);
+    a0 = make_axis(assign, i0, dd, ng);
+  } else {
+    a0 = make_axis(assign, i, (double)d, ng);
+  }
+  if (!il) {
+    a1 = a0;
+    return;
+  }
+  // shifted grid: x' = x + 1/2, wrapped (the reference moves pos by -L)
+  int i1 = i;
+  float d1 = d + 0.5f;
+  if (d1 >= 1.f) { i1 += 1; d1 -= 1.f; }
+  if (i1 >= ng) i1 -= ng;
+  if (near_edge(d1) || near_edge(d) || i1 < 0 || i1 >= ng) {
+    int i0;
+    double dd;
+    exact_coord(pos, L, ng, true, i0, dd);
+    a1 = make_axis(assign, i0, dd, ng);
+  } else {
+    a1 = make_axis(assign, i1, (double)d1, ng);
+  }
+}
+
+// 1-D weights of the stencil nodes base + first_off + k.  The outermost
+// weight is 1 minus the others, so each axis's weights sum to 1 within one
+// FP32 rounding.
+template <int S>
+__device__ __forceinline__ void node_weights(float par, float (&w)[4]) {
+  if (S == 1) {
+    w[0] = 1.f;
+  } else if (S == 2) {
+    w[0] = 1.f - par;
+    w[1] = par;
+  } else if (S == 3) {
+    const float a = 0.5f - par;
+    w[0] = 0.5f * a * a;
+    w[1] = 0.75f - par * par;
+    w[2] = 1.f - w[0] - w[1];
+  } else {
+    const float f = par, f2 = f * f, f3 = f2 * f, s = 1.f / 6.f;
+    w[3] = f3 * s;
+    w[2] = (1.f + 3.f * (f + f2 - f3)) * s;
+    w[1] = (4.f - 6.f * f2 + 3.f * f3) * s;
+    w[0] = 1.f - w[1] - w[2] - w[3];
+  }
+}
+
+struct Particle {
+  double pos[3];
+  double w;
+};
+
+__device__ __forceinline__ Particle load_particle(const Particles& p, size_t i) {
+  Particle q;
+  if (p.aos) {
+    const double4 r = reinterpret_cast<const double4*>(p.aos)[i];
+    q.pos[0] = r.x; q.pos[1] = r.y; q.pos[2] = r.z; q.w = r.w;
+  } else {
+    q.pos[0] = (double)p.x[i];
+    q.pos[1] = (double)p.y[i];
+    q.pos[2] = (double)p.z[i];
+    q.w = p.w ? (double)p.w[i] : 1.0;
+  }
+  return q;
+}
+
+// Record and key of one particle; returns false if it lies outside the box.
+__device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs& g, Rec& r,
+                                            unsigned& key) {
+  const int ng = g.ng;
+  int tile[3], cls[3];
+  for (int a = 0; a < 3; a++) {
+    const double pos = q.pos[a];
+    if (!(pos >= 0.0 && pos < g.box[a])) return false;
+    const float hi = __double2float_rn(pos);
+    const float lo = __double2float_rn(__dsub_rn(pos, (double)hi));
+    Axis a0, a1;
+    axis_pair(g.assign, pos, hi, lo, g.s_hi[a], g.s_lo[a], g.box[a], ng, g.interlace != 0, a0, a1);
+    r.base[0][a] = (short)a0.base;
+    r.base[1][a] = (short)a1.base;
+    r.par[0][a] = a0.par;
+    r.par[1][a] = a1.par;
+    // reach of both stencils relative to the plain base's tile
+    int diff = a1.base - a0.base;
+    if (diff > ng / 2) diff -= ng;
+    if (diff < -ng / 2) diff += ng;
+    const int t = a0.base / g.T;
+    const int rel = a0.base - t * g.T;
+    const int of = first_off(g.assign), S = width(g.assign);
+    const int lo_r = rel + of + (g.interlace ? min(0, diff) : 0);
+    const int hi_r = rel + of + S - 1 + (g.interlace ? max(0, diff) : 0);
+    tile[a] = t;
+    cls[a] = (lo_r < 0) ? 1 : ((hi_r >= g.T) ? 2 : 0);
+  }
+  r.wf = (float)q.w * kFixScale;
+  r.q = __double2ll_rn(q.w * 4294967296.0);
+  const unsigned t = ((unsigned)tile[0] * g.nt + tile[1]) * g.nt + tile[2];
+  key = t * 27u + (unsigned)(cls[0] + 3 * cls[1] + 9 * cls[2]);
+  return true;
+}
+
+__global__ void __launch_bounds__(256) k_classify(const __grid_constant__ GatherArgs g, Particles p) {
+  double ws = 0.0, wa = 0.0;
+  int bad = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const Particle q = load_particle(p, i);
+    Rec r;
+    unsigned key;
+    if (!make_record(q, g, r, key)) {
+      bad = 1;
+      g.rank[i] = 0xffffffffu;
+      continue;
+    }
+    ws += q.w;
+    wa += fabs(q.w);
+    g.rank[i] = atomicAdd(&g.hist[key], 1u);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ws += __shfl_down_sync(0xffffffffu, ws, o);
+    wa += __shfl_down_sync(0xffffffffu, wa, o);
+  }
+  __shared__ double sws[8], swa[8];
+  if ((threadIdx.x & 31) == 0) {
+    sws[threadIdx.x >> 5] = ws;
+    swa[threadIdx.x >> 5] = wa;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0;
+    for (int k = 0; k < 8; k++) {
+      t0 += sws[k];
+      t1 += swa[k];
+    }
+    g.wpart[2 * blockIdx.x] = t0;
+    g.wpart[2 * blockIdx.x + 1] = t1;
+  }
+  if (bad) atomicOr(g.err, 1);
+}
+
+__global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ GatherArgs g, Particles p) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const unsigned rk = g.rank[i];
+    if (rk == 0xffffffffu) continue;
+    const Particle q = load_particle(p, i);
+    Rec r;
+    unsigned key;
+    make_record(q, g, r, key);
+    reinterpret_cast<Rec*>(g.rec)[g.hist[key] + rk] = r;
+  }
+}
+
+// ---- exclusive scan of nkeys counts in place (hist[nkeys] = total)
+constexpr int kScanPer = 16;  // elements per thread
+constexpr int kScanBlock = 256 * kScanPer;
+
+__device__ __forceinline__ unsigned block_exclusive(unsigned v, unsigned* sh, unsigned& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned s = (lane < 8) ? sh[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < 8) sh[lane] = s;
+  }
+  __syncthreads();
+  const unsigned before = (wid ? sh[wid - 1] : 0) + x - v;
+  total = sh[7];
+  __syncthreads();
+  return before;
+}
+
+__global__ void __launch_bounds__(256) k_scan_reduce(const unsigned* hist, size_t n, unsigned* bsum) {
+  __shared__ unsigned sh[8];
+  const size_t base = (size_t)blockIdx.x * kScanBlock + (size_t)threadIdx.x * kScanPer;
+  unsigned s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++)
+    if (base + k < n) s += hist[base + k];
+  unsigned total;
+  block_exclusive(s, sh, total);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(256) k_scan_blocks(unsigned* bsum, int nb) {
+  __shared__ unsigned sh[8];
+  unsigned carry = 0;
+  for (int c = 0; c < nb; c += 256) {
+    const int i = c + threadIdx.x;
+    const unsigned v = (i < nb) ? bsum[i] : 0;
+    unsigned total;
+    const unsigned ex = block_exclusive(v, sh, total);
+    if (i < nb) bsum[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) bsum[nb] = carry;  // number of classified particles
+}
+
+__global__ void __launch_bounds__(256) k_scan_apply(unsigned* hist, size_t n, const unsigned* bsum,
+                                                    int nb) {
+  __shared__ unsigned sh[8];
+  const size_t base = (size_t)blockIdx.x * kScanBlock + (size_t)threadIdx.x * kScanPer;
+  unsigned v[kScanPer];
+  unsigned s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++) {
+    v[k] = (base + k < n) ? hist[base + k] : 0;
+    s += v[k];
+  }
+  unsigned total;
+  unsigned run = block_exclusive(s, sh, total) + bsum[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++) {
+    if (base + k < n) hist[base + k] = run;
+    run += v[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) hist[n] = bsum[nb];
+}
+
+// ---- gather: one CTA per tile.  TT: compile-time tile edge (0: g.T).
+template <int S, bool INT64, int TT>
+__global__ void __launch_bounds__(kGatherThreads) k_gather(const __grid_constant__ GatherArgs g) {
+  extern __shared__ __align__(16) unsigned long long acc[];  // [nmesh][T^3 + kMeshPad]
+  __shared__ unsigned bstart[128];
+  __shared__ unsigned boff[125];
+  const int T = TT ? TT : g.T;
+  const int nt = g.nt, ng = g.ng;
+  const int T3 = T * T * T;
+  const int nmesh = g.interlace ? 2 : 1;
+  const int tile = blockIdx.x;
+  const int tx = tile / (nt * nt), ty = (tile / nt) % nt, tz = tile % nt;
+  const int org[3] = {tx * T, ty * T, tz * T};
+  // the 125 buckets that can reach this tile (loads issued before the
+  // accumulators are zeroed, so their latency overlaps the stores)
+  unsigned h0 = 0, hc = 0;
+  if (threadIdx.x < 125) {
+    int k = threadIdx.x;
+    int off[3], c[3];
+    // 5 choices per axis: neighbour -1 (class 2), own (classes 0, 1, 2), +1 (class 1)
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const int ch = k % 5;
+      k /= 5;
+      off[a] = (ch == 0) ? -1 : ((ch == 4) ? 1 : 0);
+      c[a] = (ch == 0) ? 2 : ((ch == 4) ? 1 : ch - 1);
+    }
+    const int nx = (tx + off[0] + nt) % nt, ny = (ty + off[1] + nt) % nt, nz = (tz + off[2] + nt) % nt;
+    const unsigned key =
+        ((unsigned)((nx * nt + ny) * nt + nz)) * 27u + (unsigned)(c[0] + 3 * c[1] + 9 * c[2]);
+    h0 = g.hist[key];
+    hc = g.hist[key + 1];
+  }
+  const int nacc = nmesh * (T3 + kMeshPad);
+  if (TT % 4 == 0 && TT) {
+    ulonglong2* a2 = reinterpret_cast<ulonglong2*>(acc);
+    for (int e = threadIdx.x; e < nacc / 2; e += blockDim.x) a2[e] = make_ulonglong2(0ull, 0ull);
+  } else {
+    for (int e = threadIdx.x; e < nacc; e += blockDim.x) acc[e] = 0ull;
+  }
+  if (threadIdx.x < 128) {
+    if (threadIdx.x < 125) boff[threadIdx.x] = h0;
+    bstart[threadIdx.x] = hc - h0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    // exclusive scan of 128 entries, 4 per lane
+    const int l = threadIdx.x;
+    const unsigned v0 = bstart[4 * l], v1 = bstart[4 * l + 1], v2 = bstart[4 * l + 2],
+                   v3 = bstart[4 * l + 3];
+    const unsigned s = v0 + v1 + v2 + v3;
+    unsigned x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (l >= o) x += y;
+    }
+    const unsigned ex = x - s;
+    __syncwarp();
+    bstart[4 * l] = ex;
+    bstart[4 * l + 1] = ex + v0;
+    bstart[4 * l + 2] = ex + v0 + v1;
+    bstart[4 * l + 3] = ex + v0 + v1 + v2;
+  }
+  __syncthreads();
+  const unsigned total = bstart[125];
+  const Rec* rec = reinterpret_cast<const Rec*>(g.rec);
+  const int of = first_off(g.assign);
+  // Work item = (record, mesh, z node): P lanes per mesh (P = S rounded up
+  // to a power of two), G = nmesh * P lanes per record, aligned within the
+  // warp.  Lanes of one record hit consecutive words along z (no bank
+  // conflicts); the meshes are kMeshPad words apart.
+  constexpr int P = (S == 3) ? 4 : S;
+  const int G = nmesh * P;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane % G, m = sub / P, kz = sub % P;
+  const unsigned nwork = total * (unsigned)G;
+  for (unsigned u = threadIdx.x; u < nwork; u += blockDim.x) {
+    const unsigned i = u / (unsigned)G;
+    // largest b with bstart[b] <= i (bstart[0] = 0, bstart[125] = total > i)
+    int b = 0;
+#pragma unroll
+    for (int step = 64; step > 0; step >>= 1)
+      if (b + step < 126 && bstart[b + step] <= i) b += step;
+    if (kz >= S) continue;
+    const Rec r = rec[boff[b] + (i - bstart[b])];
+    float w[3][4];
+    int loc[3][4];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      node_weights<S>(r.par[m][a], w[a]);
+#pragma unroll
+      for (int k = 0; k < S; k++) {
+        int node = r.base[m][a] + of + k;
+        node += (node < 0) ? ng : 0;
+        node -= (node >= ng) ? ng : 0;
+        int l = node - org[a];
+        l += (l < 0) ? ng : 0;
+        loc[a][k] = (l < T) ? l : -1;
+      }
+    }
+    // this lane's z node
+    float wz = w[2][0];
+    int lz = loc[2][0];
+#pragma unroll
+    for (int k = 1; k < S; k++)
+      if (kz == k) {
+        wz = w[2][k];
+        lz = loc[2][k];
+      }
+    if (lz < 0) continue;
+    unsigned long long* A = acc + m * (T3 + kMeshPad) + lz;
+    const float wzf = wz * r.wf;
+#pragma unroll
+    for (int x = 0; x < S; x++) {
+      if (loc[0][x] < 0) continue;
+      const float wxz = w[0][x] * wzf;
+      const int row = loc[0][x] * T;
+#pragma unroll
+      for (int y = 0; y < S; y++) {
+        if (loc[1][y] < 0) continue;
+        const long long q = (S == 1) ? r.q : __float2ll_rn(wxz * w[1][y]);
+        atomicAdd(&A[(row + loc[1][y]) * T], (unsigned long long)q);
+      }
+    }
+  }
+  __syncthreads();
+  // write the tile: rows of T cells along z
+  const long long off = INT64 ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
+  for (int m = 0; m < nmesh; m++) {
+    const unsigned long long* A = acc + m * (T3 + kMeshPad);
+    if (TT % 4 == 0 && TT) {
+      // 4 consecutive z cells per thread; ng and the tile origin are multiples of 4
+      for (int e = threadIdx.x; e < T3 / 4; e += blockDim.x) {
+        const int lz = (e % (TT / 4)) * 4, ly = (e / (TT / 4)) % TT, lx = e / (TT * TT / 4);
+        const size_t cell = ((size_t)(org[0] + lx) * ng + org[1] + ly) * ng + org[2] + lz;
+        const ulonglong2 u0 = reinterpret_cast<const ulonglong2*>(A)[2 * e];
+        const ulonglong2 u1 = reinterpret_cast<const ulonglong2*>(A)[2 * e + 1];
+        if (INT64) {
+          longlong2* o = reinterpret_cast<longlong2*>(g.out64[m] + cell);
+          o[0] = make_longlong2((long long)u0.x, (long long)u0.y);
+          o[1] = make_longlong2((long long)u1.x, (long long)u1.y);
+        } else {
+          *reinterpret_cast<float4*>(g.out[m] + cell) =
+              make_float4(fix_to_float((long long)u0.x - off), fix_to_float((long long)u0.y - off),
+                          fix_to_float((long long)u1.x - off), fix_to_float((long long)u1.y - off));
+        }
+      }
+    } else {
+      for (int e = threadIdx.x; e < T3; e += blockDim.x) {
+        const int lx = e / (T * T), ly = (e / T) % T, lz = e % T;
+        const size_t cell = ((size_t)(org[0] + lx) * ng + org[1] + ly) * ng + org[2] + lz;
+        const long long v = (long long)A[e];
+        if (INT64)
+          g.out64[m][cell] = v;
+        else
+          g.out[m][cell] = fix_to_float(v - off);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+int gather_tile(int ng) {
+  int best = 0;
+  for (int t = 4; t <= 16; t++)
+    if (ng % t == 0 && ng / t >= 2) best = t;
+  return best;
+}
+
+size_t gather_keys(int ng) {
+  const int T = gather_tile(ng);
+  if (!T) return 0;
+  const size_t nt = (size_t)(ng / T);
+  return nt * nt * nt * 27;
+}
+
+int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool int64_out) {
+  int n = 0;
+  const size_t nkeys = gather_keys(g.ng);
+  if (!int64_out) {
+    cudaMemsetAsync(g.hist, 0, (nkeys + 1) * sizeof(unsigned), s);
+    size_t blocks = (p.n + 255) / 256;
+    if (blocks > (size_t)kAssignMaxBlocks) blocks = kAssignMaxBlocks;
+    if (blocks < 1) blocks = 1;
+    k_classify<<<(unsigned)blocks, 256, 0, s>>>(g, p);
+    n++;
+    k_wsum<<<1, 32, 0, s>>>(g.wpart, (int)blocks, g.wsum);
+    n++;
+    const int nb = (int)((nkeys + kScanBlock - 1) / kScanBlock);
+    k_scan_reduce<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum);
+    k_scan_blocks<<<1, 256, 0, s>>>(g.bsum, nb);
+    k_scan_apply<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum, nb);
+    n += 3;
+    k_scatter<<<(unsigned)blocks, 256, 0, s>>>(g, p);
+    n++;
+  }
+  const int T = g.T;
+  const size_t smem = (size_t)(g.interlace ? 2 : 1) * (T * T * T + kMeshPad) * sizeof(unsigned long long);
+  const unsigned ntile = (unsigned)(g.nt * g.nt * g.nt);
+#define PS_GATHER_T(SS, TV)                                                                    \
+  if (int64_out) {                                                                             \
+    cudaFuncSetAttribute(k_gather<SS, true, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                         (int)smem);                                                           \
+    k_gather<SS, true, TV><<<ntile, kGatherThreads, smem, s>>>(g);                             \
+  } else {                                                                                     \
+    cudaFuncSetAttribute(k_gather<SS, false, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                         (int)smem);                                                           \
+    k_gather<SS, false, TV><<<ntile, kGatherThreads, smem, s>>>(g);                            \
+  }
+#define PS_GATHER(SS)          \
+  if (T == 16) {               \
+    PS_GATHER_T(SS, 16)        \
+  } else {                     \
+    PS_GATHER_T(SS, 0)         \
+  }
+  switch (g.assign) {
+    case 0: PS_GATHER(1); break;
+    case 1: PS_GATHER(2); break;
+    case 2: PS_GATHER(3); break;
+    default: PS_GATHER(4); break;
+  }
+#undef PS_GATHER_T
+#undef PS_GATHER
+  n++;
+  return n;
+}
+
+}  // namespace ps

@@ -19,21 +19,28 @@ struct Particles {
   size_t n;
 };
 
-struct AssignArgs {
-  int ng;
-  int assign;
+constexpr int kAssignMaxBlocks = 2048;  // per-block weight partials
+
+// Tile assignment (ps_gather.cu).
+struct GatherArgs {
+  int ng, assign, interlace;
+  int T, nt;               // tile edge (cells) and tiles per axis
   double box[3];
-  unsigned long long* mesh0;  // plain grid (lower corner 0)
-  unsigned long long* mesh1;  // half-cell shifted grid, or NULL
-  double* wsum;               // [2]: sum w, sum |w|
-  double* wpart;              // [2 * kAssignMaxBlocks] per-block partial sums
-  int* err;                   // bit 0: particle outside [0, L)
+  float s_hi[3], s_lo[3];  // Ng / L as a double-float pair per axis
+  unsigned* hist;          // [nkeys + 1] counts, then offsets
+  unsigned* bsum;          // [ceil(nkeys / 4096) + 1]
+  unsigned* rank;          // [n]
+  void* rec;               // [n] 48-byte records
+  float* out[2];           // FP32 meshes minus the mean cell value
+  long long* out64[2];     // or exact fixed-point meshes (diagnostics)
+  double* wsum;            // [2]
+  double* wpart;           // [2 * kAssignMaxBlocks]
+  int* err;                // bit 0: particle outside [0, L)
 };
-
-constexpr int kAssignMaxBlocks = 2048;
-
-// Returns the number of kernel launches issued.
-int launch_assign(const Particles& p, const AssignArgs& a, cudaStream_t s);
+int gather_tile(int ng);    // tile edge for this mesh size, 0 if unsupported
+size_t gather_keys(int ng);  // number of (tile, class) keys
+// int64_out: only the gather step, into out64 (records must be in place).
+int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool int64_out);
 
 // z transform: fixed-point grid [x][y][z] -> A[x][kz][y] (complex).
 struct PassAArgs {

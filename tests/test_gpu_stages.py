@@ -8,6 +8,8 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
+MESH_RTOL = 2e-7  # of the largest cell (FP32 node products)
+
 
 @pytest.mark.parametrize("assign", [0, 1, 2, 3])
 def test_mesh_matches_reference_fixture(gpu_lib, assign):
@@ -15,10 +17,12 @@ def test_mesh_matches_reference_fixture(gpu_lib, assign):
     with gpu_lib.Estimator(ng=16, assign=assign, interlace=True, dk=0.01) as e:
         e.assign(0, d["cat"])
         m0, m1 = e.read_mesh(0, 0), e.read_mesh(0, 1)
-    # FP32 stencil weights, 2^-32 fixed point: ~1e-7 of the largest cell
+    # Each node value is an FP32 product of the 1-D weights (~4 roundings,
+    # ~2.4e-7 relative) rounded to 2^-32 units; the mesh total then matches
+    # sum(w) to that relative rounding (only the unused k = 0 mode sees it).
     for got, ref in ((m0, d[f"fr_{assign}"]), (m1, d[f"frl_{assign}"])):
-        assert np.abs(got - ref).max() <= 2e-7 * np.abs(ref).max()
-        assert got.sum() == pytest.approx(ref.sum(), rel=1e-9)
+        assert np.abs(got - ref).max() <= MESH_RTOL * np.abs(ref).max()
+        assert got.sum() == pytest.approx(ref.sum(), rel=1e-7)
 
 
 @pytest.mark.parametrize("assign", [0, 1, 2, 3])
@@ -35,7 +39,7 @@ def test_mesh_matches_oracle_and_is_deterministic(gpu_lib, oracle_mod, assign, i
             runs.append([e.read_mesh(0, m) for m in range(2 if interlace else 1)])
     for m in range(len(ref)):
         assert np.array_equal(runs[0][m], runs[1][m]), "mesh not bit-reproducible"
-        assert np.abs(runs[0][m] - ref[m]).max() <= 2e-7 * np.abs(ref[m]).max()
+        assert np.abs(runs[0][m] - ref[m]).max() <= MESH_RTOL * np.abs(ref[m]).max()
 
 
 @pytest.mark.parametrize("ng", [8, 12, 16, 20, 24, 30, 32, 40, 48, 60, 64, 96, 128, 192, 256])
