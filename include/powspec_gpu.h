@@ -167,6 +167,21 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx *ctx, const float *in, float *out);
 int ps_gpu_bin_fields_host(ps_gpu_ctx *ctx, const float *f1, const float *f2,
                            double *pl);
 
+/* The same binning over DEVICE fields, allocating nothing: no counterpart in
+ * the reference.  For callers that hold the device memory in their own pool
+ * (in-situ measurement inside a simulation step), where cudaMalloc would
+ * synchronise the device or fail.  f1, f2: device half-complex FP32 fields
+ * [ng][ng][ng/2+1] (re, im); pl: device output [npole][nbin] doubles, written
+ * asynchronously on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * The per-CTA partial sums live in one static device array per GPU (4,096,000
+ * bytes): npole * nbin must be <= 3200, else PS_GPU_ERR_RANGE.  The first call
+ * on a device looks that array up (cudaGetSymbolAddress); make it before any
+ * stream capture.  All calls on one device share the array: calls whose
+ * stream work can overlap race and corrupt each other's sums, so order them
+ * on one stream. */
+int ps_gpu_bin_fields_noalloc(ps_gpu_ctx *ctx, const float *f1, const float *f2,
+                              double *pl, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

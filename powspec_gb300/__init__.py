@@ -34,7 +34,7 @@ EXPORTED = [
     "ps_gpu_assign_soa", "ps_gpu_execute", "ps_gpu_last_error",
     "ps_gpu_last_timings", "ps_gpu_last_launches", "ps_gpu_read_mesh",
     "ps_gpu_fft_r2c_host", "ps_gpu_bin_fields_host", "ps_gpu_stream",
-    "ps_gpu_set_mu_bins", "ps_gpu_read_kmu",
+    "ps_gpu_set_mu_bins", "ps_gpu_read_kmu", "ps_gpu_bin_fields_noalloc",
 ]
 
 
@@ -118,6 +118,7 @@ def lib():
         L.ps_gpu_read_mesh.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.ps_gpu_fft_r2c_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ps_gpu_bin_fields_host.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
+        L.ps_gpu_bin_fields_noalloc.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 4
         _lib = L
     return _lib
 

@@ -524,6 +524,28 @@ int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
 
 }  // namespace
 
+namespace ps {
+
+int ctx_view(const ps_gpu_ctx* c, CtxView* v) {
+  if (!c || !v) return 1;
+  v->ng = c->ng;
+  v->device = c->p.device;
+  v->geom = c->geom;
+  return 0;
+}
+
+int ctx_fail(ps_gpu_ctx* c, int code, const char* fmt, ...) {
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof c->err, fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+}  // namespace ps
+
 extern "C" {
 
 int ps_gpu_assign_aos(ps_gpu_ctx* c, int cat, const double* xyzw, size_t n, int on_device) {

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include "powspec_gpu.h"
 #include "ps_common.cuh"
 
 namespace ps {
@@ -120,5 +121,14 @@ int launch_reduce(const double* part, int grid, int width, double* out, cudaStre
 
 // Minimum shared memory per CTA the passes need (bytes).
 size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin, bool pow2);
+
+// Read-only view of a context for entry points outside ps_capi.cu.
+struct CtxView {
+  int ng, device;
+  ModeGeom geom;  // device tables owned by the context
+};
+int ctx_view(const ps_gpu_ctx* c, CtxView* v);  // nonzero if c is NULL
+// Records the message as the context's last error; returns code.
+int ctx_fail(ps_gpu_ctx* c, int code, const char* fmt, ...);
 
 }  // namespace ps

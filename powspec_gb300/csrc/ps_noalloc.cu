@@ -1,0 +1,105 @@
+// ps_noalloc.cu -- binning of given half-complex fields without any device
+// allocation on the call path.
+//
+// Who needs it: a code that measures P_l(k) in situ, between the kernels of
+// its own time step (an N-body or hydro solver, a mock pipeline), usually
+// owns the device memory through its own pool.  A cudaMalloc there
+// synchronises the whole device, breaking the solver's stream overlap, and
+// fails outright once the pool has taken the free memory.  Such a caller
+// creates the estimator context once at start-up (that allocates its
+// geometry tables) and then needs a per-step call that allocates nothing.
+//
+// The call runs the same kernels as ps_gpu_bin_fields_host (k_bin_fields,
+// then the ordered reduce of the per-CTA partial sums).  The partials live in
+// the file-scope array below instead of the context's cudaMalloc'd buffer.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "powspec_gpu.h"
+#include "ps_internal.h"
+
+namespace ps {
+namespace {
+
+constexpr int kNoAllocMaxCtas = 160;     // partial-sum rows (one per CTA)
+constexpr int kNoAllocMaxWidth = 3200;   // npole * nbin
+constexpr size_t kNoAllocScratchBytes =  // 4,096,000 bytes
+    (size_t)kNoAllocMaxCtas * kNoAllocMaxWidth * sizeof(double);
+constexpr int kMaxDevices = 64;
+
+// Per-CTA partial sums [grid][npole * nbin] of every call on this device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_setup_mutex;
+void* g_scratch_ptr[kMaxDevices] = {};
+int g_nsm[kMaxDevices] = {};
+
+// Once per device, with that device current: the scratch array's device
+// address and the SM count.
+cudaError_t setup_device(int dev, void** ptr, int* nsm) {
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    int n = 0;
+    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    g_nsm[dev] = n;
+    g_scratch_ptr[dev] = p;
+  }
+  *ptr = g_scratch_ptr[dev];
+  *nsm = g_nsm[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace ps
+
+using namespace ps;
+
+extern "C" int ps_gpu_bin_fields_noalloc(ps_gpu_ctx* c, const float* f1, const float* f2,
+                                         double* pl, void* stream) {
+  CtxView v;
+  if (ctx_view(c, &v)) return PS_GPU_ERR_ARG;
+  if (!f1 || !f2 || !pl)
+    return ctx_fail(c, PS_GPU_ERR_ARG, "bin_fields_noalloc: null field or output pointer");
+  if (((uintptr_t)f1 | (uintptr_t)f2 | (uintptr_t)pl) & 7)
+    return ctx_fail(c, PS_GPU_ERR_ARG, "bin_fields_noalloc: pointers must be 8-byte aligned");
+  const int width = v.geom.npole * v.geom.nbin;
+  if (width > kNoAllocMaxWidth)
+    return ctx_fail(c, PS_GPU_ERR_RANGE,
+                    "bin_fields_noalloc: npole * nbin = %d exceeds the scratch limit %d", width,
+                    kNoAllocMaxWidth);
+  if (v.device < 0 || v.device >= kMaxDevices)
+    return ctx_fail(c, PS_GPU_ERR_ARG, "bin_fields_noalloc: device %d out of range", v.device);
+  cudaError_t e = cudaSetDevice(v.device);
+  void* scratch = nullptr;
+  int nsm = 0;
+  if (e == cudaSuccess) e = setup_device(v.device, &scratch, &nsm);
+  if (e != cudaSuccess)
+    return ctx_fail(c, PS_GPU_ERR_CUDA, "bin_fields_noalloc set-up: %s", cudaGetErrorString(e));
+  const int grid = nsm < kNoAllocMaxCtas ? nsm : kNoAllocMaxCtas;
+  cudaStream_t s = (cudaStream_t)stream;
+  double* part = (double*)scratch;
+  // the kernel adds its tile sums into the partials: they start at zero
+  e = cudaMemsetAsync(part, 0, (size_t)grid * width * sizeof(double), s);
+  if (e != cudaSuccess)
+    return ctx_fail(c, PS_GPU_ERR_CUDA, "bin_fields_noalloc memset: %s", cudaGetErrorString(e));
+  BinFieldArgs b;
+  b.ng = v.ng;
+  b.f1 = (const float2*)f1;
+  b.f2 = (const float2*)f2;
+  b.geom = v.geom;
+  b.geom.nmu = 1;
+  b.partials = part;
+  b.grid = grid;
+  launch_bin_fields(b, s);
+  launch_reduce(part, grid, width, pl, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return ctx_fail(c, PS_GPU_ERR_CUDA, "bin_fields_noalloc launch: %s", cudaGetErrorString(e));
+  return 0;
+}
