@@ -507,7 +507,7 @@ int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
     c->d_rec = nullptr;
     c->gcap = 0;
     CU(cudaMalloc(&c->d_rank, pt.n * sizeof(unsigned)));
-    CU(cudaMalloc(&c->d_rec, pt.n * 48));
+    CU(cudaMalloc(&c->d_rec, pt.n * gather_record_bytes()));
     c->gcap = pt.n;
   }
   CU(cudaMemsetAsync(c->d_wsum + 2 * cat, 0, sizeof(double) * 2, c->stream));

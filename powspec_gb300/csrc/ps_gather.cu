@@ -27,8 +27,9 @@
 namespace ps {
 namespace {
 
-constexpr int kGatherThreads = 256;
+constexpr int kGatherThreads = 512;  // 16 warps; 3 CTAs per SM fit (registers, shared memory)
 constexpr int kMeshPad = 8;  // words between the two meshes' accumulators (bank offset)
+constexpr unsigned kSparseRecords = 64;  // at most: one pass over all records, rows flagged
 constexpr float kEdge = 4e-6f;
 
 // wsum[0..1] = sums of the per-block partials: lane l adds blocks l, l + 32,
@@ -64,6 +65,29 @@ struct Rec {
   long long q;       // llrint(weight * 2^32): the exact NGP node value
 };
 static_assert(sizeof(Rec) == 48, "record layout");
+
+// Record of a TSC/PCS particle for the gather (112 bytes): the 1-D node
+// weights per mesh and axis, with weight * 2^32 folded into the x weights.
+struct __align__(16) WRec {
+  float w[2][3][4];   // [mesh][axis][node]
+  short base[2][4];   // [mesh][axis]; [mesh][3] = 1: every node value |v| < 2^31
+};
+static_assert(sizeof(WRec) == 112, "weighted record layout");
+constexpr size_t kRecBytes = 112;  // room for either record kind
+
+// round-to-nearest-even of v as int64 from 32-bit conversions only (the
+// direct FP32 -> int64 conversion runs several times slower): v = hi * 2^32
+// + r with hi = trunc(v / 2^32) and r exact (an FMA of multiples of ulp(v)),
+// |r| < 2^32.  Valid for |v| < 2^63.
+__device__ __forceinline__ long long round_fix(float v) {
+  const int hi = __float2int_rz(v * 2.3283064365386963e-10f);
+  const float r = fmaf((float)(-hi), 4294967296.f, v);
+  const long long lo = (long long)__float2uint_rn(fabsf(r));
+  const long long h = (long long)hi * 4294967296ll;
+  return (r < 0.f) ? h - lo : h + lo;
+}
+// |v| < 2^31: one 32-bit conversion
+__device__ __forceinline__ long long round_small(float v) { return (long long)__float2int_rn(v); }
 
 // Offset of the first stencil node from the base and stencil width.
 __host__ __device__ inline int first_off(int assign) { return assign >= 2 ? -1 : 0; }
@@ -174,7 +198,7 @@ struct Particle {
 __device__ __forceinline__ Particle load_particle(const Particles& p, size_t i) {
   Particle q;
   if (p.aos) {
-    const double4 r = reinterpret_cast<const double4*>(p.aos)[i];
+    const double4_32a r = reinterpret_cast<const double4_32a*>(p.aos)[i];  // 32-byte aligned (checked)
     q.pos[0] = r.x; q.pos[1] = r.y; q.pos[2] = r.z; q.w = r.w;
   } else {
     q.pos[0] = (double)p.x[i];
@@ -235,7 +259,14 @@ __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ Gather
     }
     ws += q.w;
     wa += fabs(q.w);
-    g.rank[i] = atomicAdd(&g.hist[key], 1u);
+    // Rank within the key, aggregated over the lanes of this warp that share
+    // it (catalogues are often spatially ordered: whole warps hit one key).
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(&g.hist[key], (unsigned)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    g.rank[i] = base + __popc(peers & ((1u << lane) - 1u));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -269,7 +300,36 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ GatherA
     Rec r;
     unsigned key;
     make_record(q, g, r, key);
-    reinterpret_cast<Rec*>(g.rec)[g.hist[key] + rk] = r;
+    const unsigned slot = g.hist[key] + rk;
+    if (g.assign >= 2) {
+      WRec v;
+#pragma unroll
+      for (int m = 0; m < 2; m++) {
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          float w[4];
+          if (g.assign == 2) {
+            node_weights<3>(r.par[m][a], w);
+            w[3] = 0.f;
+          } else {
+            node_weights<4>(r.par[m][a], w);
+          }
+#pragma unroll
+          for (int k = 0; k < 4; k++) v.w[m][a][k] = (a == 0) ? w[k] * r.wf : w[k];
+          v.base[m][a] = r.base[m][a];
+        }
+        // bound of every node value of this mesh: product of the axis maxima
+        float bound = 1.f;
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+          bound *= fmaxf(fmaxf(fabsf(v.w[m][a][0]), fabsf(v.w[m][a][1])),
+                         fmaxf(fabsf(v.w[m][a][2]), fabsf(v.w[m][a][3])));
+        v.base[m][3] = bound < 0.999f * 2147483648.f ? 1 : 0;
+      }
+      reinterpret_cast<WRec*>(g.rec)[slot] = v;
+    } else {
+      reinterpret_cast<Rec*>(g.rec)[slot] = r;
+    }
   }
 }
 
@@ -352,16 +412,16 @@ __global__ void __launch_bounds__(256) k_scan_apply(unsigned* hist, size_t n, co
 
 // ---- gather: one CTA per tile.  TT: compile-time tile edge (0: g.T).
 template <int S, bool INT64, int TT>
-__global__ void __launch_bounds__(kGatherThreads) k_gather(const __grid_constant__ GatherArgs g) {
+__global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_constant__ GatherArgs g) {
   extern __shared__ __align__(16) unsigned long long acc[];  // [nmesh][T^3 + kMeshPad]
   __shared__ unsigned bstart[128];
   __shared__ unsigned boff[125];
+  __shared__ unsigned rowmask[2][8];  // T = 16: touched (x, y) rows per mesh
   const int T = TT ? TT : g.T;
   const int nt = g.nt, ng = g.ng;
   const int T3 = T * T * T;
   const int nmesh = g.interlace ? 2 : 1;
-  const int tile = blockIdx.x;
-  const int tx = tile / (nt * nt), ty = (tile / nt) % nt, tz = tile % nt;
+  const int tx = blockIdx.z, ty = blockIdx.y, tz = blockIdx.x;  // grid (nt, nt, nt)
   const int org[3] = {tx * T, ty * T, tz * T};
   // the 125 buckets that can reach this tile (loads issued before the
   // accumulators are zeroed, so their latency overlaps the stores)
@@ -377,18 +437,22 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(const __grid_constant
       off[a] = (ch == 0) ? -1 : ((ch == 4) ? 1 : 0);
       c[a] = (ch == 0) ? 2 : ((ch == 4) ? 1 : ch - 1);
     }
-    const int nx = (tx + off[0] + nt) % nt, ny = (ty + off[1] + nt) % nt, nz = (tz + off[2] + nt) % nt;
+    auto wrap = [nt](int v) { return v < 0 ? v + nt : (v >= nt ? v - nt : v); };
+    const int nx = wrap(tx + off[0]), ny = wrap(ty + off[1]), nz = wrap(tz + off[2]);
     const unsigned key =
         ((unsigned)((nx * nt + ny) * nt + nz)) * 27u + (unsigned)(c[0] + 3 * c[1] + 9 * c[2]);
     h0 = g.hist[key];
     hc = g.hist[key + 1];
   }
-  const int nacc = nmesh * (T3 + kMeshPad);
-  if (TT % 4 == 0 && TT) {
-    ulonglong2* a2 = reinterpret_cast<ulonglong2*>(acc);
-    for (int e = threadIdx.x; e < nacc / 2; e += blockDim.x) a2[e] = make_ulonglong2(0ull, 0ull);
-  } else {
-    for (int e = threadIdx.x; e < nacc; e += blockDim.x) acc[e] = 0ull;
+  {
+    // zeroed while the bucket loads are in flight
+    const int nacc = nmesh * (T3 + kMeshPad);
+    if constexpr (TT % 4 == 0 && TT != 0) {
+      ulonglong2* a2 = reinterpret_cast<ulonglong2*>(acc);
+      for (int e = threadIdx.x; e < nacc / 2; e += blockDim.x) a2[e] = make_ulonglong2(0ull, 0ull);
+    } else {
+      for (int e = threadIdx.x; e < nacc; e += blockDim.x) acc[e] = 0ull;
+    }
   }
   if (threadIdx.x < 128) {
     if (threadIdx.x < 125) boff[threadIdx.x] = h0;
@@ -418,87 +482,222 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(const __grid_constant
   const unsigned total = bstart[125];
   const Rec* rec = reinterpret_cast<const Rec*>(g.rec);
   const int of = first_off(g.assign);
-  // Work item = (record, mesh, z node): P lanes per mesh (P = S rounded up
-  // to a power of two), G = nmesh * P lanes per record, aligned within the
-  // warp.  Lanes of one record hit consecutive words along z (no bank
-  // conflicts); the meshes are kMeshPad words apart.
-  constexpr int P = (S == 3) ? 4 : S;
-  const int G = nmesh * P;
-  const int lane = threadIdx.x & 31;
-  const int sub = lane % G, m = sub / P, kz = sub % P;
-  const unsigned nwork = total * (unsigned)G;
-  for (unsigned u = threadIdx.x; u < nwork; u += blockDim.x) {
-    const unsigned i = u / (unsigned)G;
-    // largest b with bstart[b] <= i (bstart[0] = 0, bstart[125] = total > i)
-    int b = 0;
+  constexpr bool kSwz = (S >= 3 && TT == 16);
+  // Local index of the first stencil node, s = base + of - org taken in
+  // [-(S-1), ng-(S-1)): then s + k lies in [0, T) exactly for the nodes
+  // inside the tile (T <= ng/2 < ng - S + 1).
+  auto rel = [&](int base, int a) {
+    int s = base + of - org[a];
+    s += (s < 0) ? ng : 0;
+    s -= (s >= ng - (S - 1)) ? ng : 0;
+    return s;
+  };
+  // Sparse tiles: one pass over all records (below), which also flags the
+  // (x, y) rows of 16 z cells that it touches; the write-out converts only
+  // those and writes -mean elsewhere.  Dense tiles: every row is flagged.
+  const bool sparse = (S >= 3) && total <= kSparseRecords;
+  if (threadIdx.x < 16) rowmask[threadIdx.x >> 3][threadIdx.x & 7] = (sparse && TT == 16) ? 0u : ~0u;
+  __syncthreads();
+  if constexpr (S >= 3) {
+   if (sparse) {
+    // Lane = (record, mesh, z node), 4 lanes per record and mesh: all the
+    // records of the tile in one step.  The z = 0 lane flags the rows.
+    const WRec* recs = reinterpret_cast<const WRec*>(g.rec);
+    const int G = nmesh * 4;
+    for (unsigned u = threadIdx.x; u < total * (unsigned)G; u += blockDim.x) {
+      const unsigned i = u / (unsigned)G;
+      const int sub = (int)(u - i * (unsigned)G), m = sub >> 2, kz = sub & 3;
+      int b = 0;
 #pragma unroll
-    for (int step = 64; step > 0; step >>= 1)
-      if (b + step < 126 && bstart[b + step] <= i) b += step;
-    if (kz >= S) continue;
-    const Rec r = rec[boff[b] + (i - bstart[b])];
-    float w[3][4];
-    int loc[3][4];
+      for (int step = 64; step > 0; step >>= 1)
+        if (b + step < 126 && bstart[b + step] <= i) b += step;
+      const WRec* rp = recs + boff[b] + (i - bstart[b]);
+      const short4 bs = *reinterpret_cast<const short4*>(&rp->base[m][0]);
+      const float4 wx4 = *reinterpret_cast<const float4*>(&rp->w[m][0][0]);
+      const float4 wy4 = *reinterpret_cast<const float4*>(&rp->w[m][1][0]);
+      const float wz = rp->w[m][2][kz];
+      const float wxs[4] = {wx4.x, wx4.y, wx4.z, wx4.w}, wys[4] = {wy4.x, wy4.y, wy4.z, wy4.w};
+      const int sx = rel(bs.x, 0), sy = rel(bs.y, 1), lz = rel(bs.z, 2) + kz;
+      if constexpr (TT == 16) {
+        if (kz == 0) {
+          const int lo = max(sy, 0), hi = min(sy + S, 16);
+          if (lo < hi) {
+            const unsigned ybits = ((1u << (hi - lo)) - 1u) << lo;
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      node_weights<S>(r.par[m][a], w[a]);
+            for (int x = 0; x < S; x++) {
+              const int lx = sx + x;
+              if ((unsigned)lx < 16u) atomicOr(&rowmask[m][lx >> 1], ybits << ((lx & 1) * 16));
+            }
+          }
+        }
+      }
+      if (kz >= S || (unsigned)lz >= (unsigned)T) continue;
+      unsigned long long* A = acc + m * (T3 + kMeshPad);
 #pragma unroll
-      for (int k = 0; k < S; k++) {
-        int node = r.base[m][a] + of + k;
-        node += (node < 0) ? ng : 0;
-        node -= (node >= ng) ? ng : 0;
-        int l = node - org[a];
-        l += (l < 0) ? ng : 0;
-        loc[a][k] = (l < T) ? l : -1;
+      for (int x = 0; x < S; x++) {
+        const int lx = sx + x;
+        if ((unsigned)lx >= (unsigned)T) continue;
+        const float wxz = wxs[x] * wz;
+#pragma unroll
+        for (int y = 0; y < S; y++) {
+          const int ly = sy + y;
+          if ((unsigned)ly >= (unsigned)T) continue;
+          const int col = kSwz ? (lz ^ ((ly & 3) << 2)) : lz;
+          const float v = wxz * wys[y];
+          const long long q = bs.w ? round_small(v) : round_fix(v);
+          atomicAdd(&A[(lx * T + ly) * T + col], (unsigned long long)q);
+        }
       }
     }
-    // this lane's z node
-    float wz = w[2][0];
-    int lz = loc[2][0];
+   } else {
+    // One record per warp.  Lane = (mesh, or x parity with one mesh; y node;
+    // z node); each lane loops over the x nodes.  With the swizzle, the 16
+    // (y, z) cells of one mesh and x plane sit in 16 distinct bank pairs.
+    // The next record's loads are issued before this one's atomics.
+    const WRec* recs = reinterpret_cast<const WRec*>(g.rec);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int half = lane >> 4, yy = (lane >> 2) & 3, zz = lane & 3;
+    const int m = (nmesh == 2) ? half : 0;
+    const bool act = yy < S && zz < S;
+    struct Ld {
+      float4 wx;
+      float wy, wz;
+      int b0, b1, b2, small;
+    };
+    auto load = [&](unsigned i, int& b) {
+      while (bstart[b + 1] <= i) b++;  // warp-uniform; i only grows
+      const WRec* rp = recs + boff[b] + (i - bstart[b]);
+      Ld L;
+      L.wx = *reinterpret_cast<const float4*>(&rp->w[m][0][0]);
+      L.wy = rp->w[m][1][yy];
+      L.wz = rp->w[m][2][zz];
+      const short4 bs = *reinterpret_cast<const short4*>(&rp->base[m][0]);
+      L.b0 = bs.x;
+      L.b1 = bs.y;
+      L.b2 = bs.z;
+      L.small = bs.w;
+      return L;
+    };
+    int b = 0;
+    unsigned i = warp;
+    Ld nxt{};
+    if (i < total) nxt = load(i, b);
+    for (; i < total; i += nw) {
+      const Ld cur = nxt;
+      if (i + nw < total) nxt = load(i + nw, b);
+      if (!act) continue;
+      const int ly = rel(cur.b1, 1) + yy, lz = rel(cur.b2, 2) + zz;
+      if ((unsigned)ly >= (unsigned)T || (unsigned)lz >= (unsigned)T) continue;
+      const float wyz = cur.wy * cur.wz;
+      const int col = kSwz ? (lz ^ ((ly & 3) << 2)) : lz;
+      unsigned long long* A = acc + m * (T3 + kMeshPad) + ly * T + col;
+      const int dx = rel(cur.b0, 0);
+      const float wxs[4] = {cur.wx.x, cur.wx.y, cur.wx.z, cur.wx.w};
 #pragma unroll
-    for (int k = 1; k < S; k++)
-      if (kz == k) {
-        wz = w[2][k];
-        lz = loc[2][k];
+      for (int x = 0; x < S; x++) {
+        if (nmesh == 1 && (x & 1) != half) continue;  // one mesh: the halves split x
+        const int lx = dx + x;
+        if ((unsigned)lx >= (unsigned)T) continue;
+        const float v = wxs[x] * wyz;
+        const long long q = cur.small ? round_small(v) : round_fix(v);  // warp-uniform
+        atomicAdd(&A[lx * T * T], (unsigned long long)q);
       }
-    if (lz < 0) continue;
-    unsigned long long* A = acc + m * (T3 + kMeshPad) + lz;
-    const float wzf = wz * r.wf;
-#pragma unroll
-    for (int x = 0; x < S; x++) {
-      if (loc[0][x] < 0) continue;
-      const float wxz = w[0][x] * wzf;
-      const int row = loc[0][x] * T;
-#pragma unroll
-      for (int y = 0; y < S; y++) {
-        if (loc[1][y] < 0) continue;
-        const long long q = (S == 1) ? r.q : __float2ll_rn(wxz * w[1][y]);
-        atomicAdd(&A[(row + loc[1][y]) * T], (unsigned long long)q);
+    }
+   }
+  } else {
+    // Work item = (record, mesh, z node): P lanes per mesh (P = S rounded up
+    // to a power of two), G = nmesh * P lanes per record, aligned within the
+    // warp.  Lanes of one record hit consecutive words along z (no bank
+    // conflicts); the meshes are kMeshPad words apart.
+    constexpr int P = (S == 3) ? 4 : S;
+    const int G = nmesh * P;
+    const int lane = threadIdx.x & 31;
+    const int sub = lane % G, m = sub / P, kz = sub % P;
+    const unsigned nwork = total * (unsigned)G;
+    for (unsigned u = threadIdx.x; u < nwork; u += blockDim.x) {
+      const unsigned i = u / (unsigned)G;
+      // largest b with bstart[b] <= i (bstart[0] = 0, bstart[125] = total > i)
+      int b = 0;
+  #pragma unroll
+      for (int step = 64; step > 0; step >>= 1)
+        if (b + step < 126 && bstart[b + step] <= i) b += step;
+      if (kz >= S) continue;
+      const Rec r = rec[boff[b] + (i - bstart[b])];
+      float w[3][4];
+      int loc[3][4];
+  #pragma unroll
+      for (int a = 0; a < 3; a++) {
+        node_weights<S>(m ? r.par[1][a] : r.par[0][a], w[a]);
+  #pragma unroll
+        for (int k = 0; k < S; k++) {
+          int node = (m ? r.base[1][a] : r.base[0][a]) + of + k;
+          node += (node < 0) ? ng : 0;
+          node -= (node >= ng) ? ng : 0;
+          int l = node - org[a];
+          l += (l < 0) ? ng : 0;
+          loc[a][k] = (l < T) ? l : -1;
+        }
+      }
+      // this lane's z node
+      float wz = w[2][0];
+      int lz = loc[2][0];
+  #pragma unroll
+      for (int k = 1; k < S; k++)
+        if (kz == k) {
+          wz = w[2][k];
+          lz = loc[2][k];
+        }
+      if (lz < 0) continue;
+      unsigned long long* A = acc + m * (T3 + kMeshPad) + lz;
+      const float wzf = wz * r.wf;
+  #pragma unroll
+      for (int x = 0; x < S; x++) {
+        if (loc[0][x] < 0) continue;
+        const float wxz = w[0][x] * wzf;
+        const int row = loc[0][x] * T;
+  #pragma unroll
+        for (int y = 0; y < S; y++) {
+          if (loc[1][y] < 0) continue;
+          const long long q = (S == 1) ? r.q : round_fix(wxz * w[1][y]);
+          atomicAdd(&A[(row + loc[1][y]) * T], (unsigned long long)q);
+        }
       }
     }
   }
   __syncthreads();
   // write the tile: rows of T cells along z
   const long long off = INT64 ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
-  for (int m = 0; m < nmesh; m++) {
-    const unsigned long long* A = acc + m * (T3 + kMeshPad);
-    if (TT % 4 == 0 && TT) {
-      // 4 consecutive z cells per thread; ng and the tile origin are multiples of 4
-      for (int e = threadIdx.x; e < T3 / 4; e += blockDim.x) {
-        const int lz = (e % (TT / 4)) * 4, ly = (e / (TT / 4)) % TT, lx = e / (TT * TT / 4);
-        const size_t cell = ((size_t)(org[0] + lx) * ng + org[1] + ly) * ng + org[2] + lz;
-        const ulonglong2 u0 = reinterpret_cast<const ulonglong2*>(A)[2 * e];
-        const ulonglong2 u1 = reinterpret_cast<const ulonglong2*>(A)[2 * e + 1];
-        if (INT64) {
-          longlong2* o = reinterpret_cast<longlong2*>(g.out64[m] + cell);
-          o[0] = make_longlong2((long long)u0.x, (long long)u0.y);
-          o[1] = make_longlong2((long long)u1.x, (long long)u1.y);
-        } else {
-          *reinterpret_cast<float4*>(g.out[m] + cell) =
-              make_float4(fix_to_float((long long)u0.x - off), fix_to_float((long long)u0.y - off),
-                          fix_to_float((long long)u1.x - off), fix_to_float((long long)u1.y - off));
-        }
+  if constexpr (TT == 16) {
+    // 4 consecutive z cells per thread and step; untouched rows are -mean
+    const float cst = fix_to_float(-off);
+    for (int e = threadIdx.x; e < nmesh * 256 * 4; e += blockDim.x) {
+      const int q = e & 3, row = (e >> 2) & 255, m = e >> 10;
+      const int lx = row >> 4, ly = row & 15;
+      const size_t cell = ((size_t)(org[0] + lx) * ng + org[1] + ly) * ng + org[2] + 4 * q;
+      const bool touched = (rowmask[m][row >> 5] >> (row & 31)) & 1u;
+      ulonglong2 u0 = make_ulonglong2(0ull, 0ull), u1 = u0;
+      if (touched) {
+        const ulonglong2* Ar =
+            reinterpret_cast<const ulonglong2*>(acc + m * (T3 + kMeshPad) + row * 16);
+        const int pq = kSwz ? (q ^ (ly & 3)) : q;  // stored block of z cells [4q, 4q + 4)
+        u0 = Ar[2 * pq];
+        u1 = Ar[2 * pq + 1];
       }
-    } else {
+      if (INT64) {
+        longlong2* o = reinterpret_cast<longlong2*>(g.out64[m] + cell);
+        o[0] = make_longlong2((long long)u0.x, (long long)u0.y);
+        o[1] = make_longlong2((long long)u1.x, (long long)u1.y);
+      } else {
+        float4 v = make_float4(cst, cst, cst, cst);
+        if (touched)
+          v = make_float4(fix_to_float((long long)u0.x - off), fix_to_float((long long)u0.y - off),
+                          fix_to_float((long long)u1.x - off), fix_to_float((long long)u1.y - off));
+        *reinterpret_cast<float4*>(g.out[m] + cell) = v;
+      }
+    }
+  } else {
+    for (int m = 0; m < nmesh; m++) {
+      const unsigned long long* A = acc + m * (T3 + kMeshPad);
       for (int e = threadIdx.x; e < T3; e += blockDim.x) {
         const int lx = e / (T * T), ly = (e / T) % T, lz = e % T;
         const size_t cell = ((size_t)(org[0] + lx) * ng + org[1] + ly) * ng + org[2] + lz;
@@ -520,6 +719,8 @@ int gather_tile(int ng) {
     if (ng % t == 0 && ng / t >= 2) best = t;
   return best;
 }
+
+size_t gather_record_bytes() { return kRecBytes; }
 
 size_t gather_keys(int ng) {
   const int T = gather_tile(ng);
@@ -550,16 +751,19 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
   }
   const int T = g.T;
   const size_t smem = (size_t)(g.interlace ? 2 : 1) * (T * T * T + kMeshPad) * sizeof(unsigned long long);
-  const unsigned ntile = (unsigned)(g.nt * g.nt * g.nt);
+  const dim3 ntile((unsigned)g.nt, (unsigned)g.nt, (unsigned)g.nt);
+  // Few particles per tile: 8 warps per CTA (a CTA's accumulators are held
+  // until its last warp ends); many: 16 warps to hide the record latency.
+  const unsigned nthr = ((double)p.n >= 64.0 * g.nt * g.nt * g.nt) ? kGatherThreads : kGatherThreads / 2;
 #define PS_GATHER_T(SS, TV)                                                                    \
   if (int64_out) {                                                                             \
     cudaFuncSetAttribute(k_gather<SS, true, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                          (int)smem);                                                           \
-    k_gather<SS, true, TV><<<ntile, kGatherThreads, smem, s>>>(g);                             \
+    k_gather<SS, true, TV><<<ntile, nthr, smem, s>>>(g);                             \
   } else {                                                                                     \
     cudaFuncSetAttribute(k_gather<SS, false, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                          (int)smem);                                                           \
-    k_gather<SS, false, TV><<<ntile, kGatherThreads, smem, s>>>(g);                            \
+    k_gather<SS, false, TV><<<ntile, nthr, smem, s>>>(g);                            \
   }
 #define PS_GATHER(SS)          \
   if (T == 16) {               \

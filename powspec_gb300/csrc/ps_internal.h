@@ -31,7 +31,7 @@ struct GatherArgs {
   unsigned* hist;          // [nkeys + 1] counts, then offsets
   unsigned* bsum;          // [ceil(nkeys / 4096) + 1]
   unsigned* rank;          // [n]
-  void* rec;               // [n] 48-byte records
+  void* rec;               // [n] records, gather_record_bytes() each
   float* out[2];           // FP32 meshes minus the mean cell value
   long long* out64[2];     // or exact fixed-point meshes (diagnostics)
   double* wsum;            // [2]
@@ -40,6 +40,7 @@ struct GatherArgs {
 };
 int gather_tile(int ng);    // tile edge for this mesh size, 0 if unsupported
 size_t gather_keys(int ng);  // number of (tile, class) keys
+size_t gather_record_bytes();  // bytes per particle record
 // int64_out: only the gather step, into out64 (records must be in place).
 int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool int64_out);
 
