@@ -13,7 +13,8 @@ h/Mpc, l = 0, 2, 4.
   catalogue in the same run; the line reports the learned evals/s (value),
   the plain evals/s, the speed-up and the max error against plain Ng = 1024
   up to 0.8 k_Nyq(256).  The catalogue's seed is outside the training set.
-* plain_pcs_il_ng1024_n4e6: the plain Ng = 1024 PCS interlaced evaluation.
+* plain_pcs_il_ng{1024,512,256}_n4e6: the plain PCS interlaced evaluation at
+  that mesh size (the Ng = 256 one is the small case the ncu captures use).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun (N > 1) every rank evaluates its own catalogue on its own GPU
@@ -49,6 +50,7 @@ WORKLOADS = {
     "learned_ng256_vs_plain_ng1024": dict(learned=True, ng=256, assign=3, interlace=True),
     "plain_pcs_il_ng1024_n4e6": dict(learned=False, ng=1024, assign=3, interlace=True),
     "plain_pcs_il_ng512_n4e6": dict(learned=False, ng=512, assign=3, interlace=True),
+    "plain_pcs_il_ng256_n4e6": dict(learned=False, ng=256, assign=3, interlace=True),
 }
 DEFAULT = "learned_ng256_vs_plain_ng1024"
 PLAIN_REF = dict(ng=1024, assign=3, interlace=True)
@@ -147,7 +149,8 @@ def reduce(world, v, op):
 def algorithmic_bytes(ng, interlace, n):
     """Per-launch algorithmic HBM bytes of each phase (FP32 path).
 
-    assignment: N * 32 B (AoS float64 records) + 4 B * Ng^3 per mesh;
+    assignment: N * 32 B (AoS float64 records) + 4 B * Ng^3 per mesh (the
+    roofline counts both meshes against the whole assignment phase);
     z pass: 4 B * Ng^3 read + 8 B * Ncmplx written; y pass: 8 B * Ncmplx
     read + written; x pass + binning: 8 B * Ncmplx per field read.
     """
@@ -164,17 +167,23 @@ def algorithmic_bytes(ng, interlace, n):
     }
 
 
-def roofline(phases_ms, ng, interlace, n, traffic=None):
+def roofline(phases_ms, ng, interlace, n, traffic=None, assign=3):
     peak, peak_kind = peaks()
     ab = algorithmic_bytes(ng, interlace, n)
-    kern = {"assign": (phases_ms[0] / ab["nmesh"], ab["assign"]),
+    # assignment: the whole phase (both meshes in one pass over the particles);
+    # FFT passes: per launch (one launch per mesh); x pass + binning: one launch
+    kern = {"assign": (phases_ms[0], ab["nmesh"] * ab["assign"]),
             "pass_z": (phases_ms[1] / ab["nmesh"], ab["pass_z"]),
             "pass_y": (phases_ms[2] / ab["nmesh"], ab["pass_y"]),
             "pass_x_bin": (phases_ms[3], ab["pass_x_bin"])}
     dom = max(kern, key=lambda k: kern[k][0])
     ms, nbytes = kern[dom]
     achieved = nbytes / (ms * 1e-3) / 1e9
+    # the assignment's real limit is shared-memory atomics: stencil node updates/s
+    nodes = n * (assign + 1) ** 3 * ab["nmesh"]
+    atom = {"node_updates_per_s": nodes / (phases_ms[0] * 1e-3), "per_eval": nodes}
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+            "assign_atomics": atom,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
             "traffic": (traffic or {}).get(f"ng{ng}", {}).get(dom),
             "per_kernel_frac": {k: (v[1] / (v[0] * 1e-3) / 1e9) / peak for k, v in kern.items()},
@@ -201,7 +210,8 @@ def config_of(wl, n_actual):
     c = {"workload": wl, "ng": w["ng"], "assign": ["NGP", "CIC", "TSC", "PCS"][w["assign"]],
          "interlace": w["interlace"], "n_particles": n_actual, "box": BOX, "dk": DK,
          "poles": [0, 2, 4], "catalogue": "lognormal", "seed": SEED,
-         "l2": "working set per eval >> 129 MB L2 (int64 meshes, 8 B/cell); no explicit flush"}
+         "l2": "working set per eval >> 129 MB L2 (FP32 meshes 4 B/cell + 8 B/mode "
+               "complex passes + 112 B/particle records); no explicit flush"}
     if w["learned"]:
         c.update({"nmu": 16, "compared_with": "plain Ng=1024 PCS interlaced, same catalogue",
                   "kmax": "0.8 k_Nyq(256)"})
@@ -275,8 +285,10 @@ def run_gpu(args, world, rank, local):
             traffic = json.load(f)
 
     # plain fine-mesh context (the reference method; timed for comparison)
-    plain = ps.Estimator(ng=PLAIN_REF["ng"], box=BOX, assign=PLAIN_REF["assign"],
-                         interlace=PLAIN_REF["interlace"], poles=(0, 2, 4), dk=DK, device=local)
+    pref = PLAIN_REF if wl["learned"] else dict(ng=wl["ng"], assign=wl["assign"],
+                                                 interlace=wl["interlace"])
+    plain = ps.Estimator(ng=pref["ng"], box=BOX, assign=pref["assign"],
+                         interlace=pref["interlace"], poles=(0, 2, 4), dk=DK, device=local)
     s_plain = torch.cuda.ExternalStream(plain.stream(), device=local)
     phases_plain = np.zeros(6)
 
