@@ -98,6 +98,82 @@ __device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int
   __syncthreads();
 }
 
+// Binning of one transformed tile: lines f * nl + r of X (field f, row ky0 + r
+// of plane kz), each mode windowed, combined and added to the tile sums.
+template <int NSPEC, bool P2>
+__device__ __forceinline__ void bin_lines(const PassCArgs& a, const float2* X, int ls, int kz,
+                                          int ky0, int nl, float* tacc, int& lo, int& hi) {
+  const int ng = a.ng;
+  const ModeGeom& g = a.geom;
+  const int nkey = g.nbin * g.nmu;
+  const int mpc = a.interlace ? 2 : 1;
+  const bool interlace = a.interlace != 0, two_cat = a.ncat > 1;
+  int spec_a[NSPEC], spec_b[NSPEC];
+#pragma unroll
+  for (int s = 0; s < NSPEC; s++) {
+    spec_a[s] = a.spec_a[s];
+    spec_b[s] = a.spec_b[s];
+  }
+  const bool twice = !(kz == 0 || 2 * kz == ng);
+  const float wk = twice ? 2.f : 1.f;
+  const float kzf = g.vec[2] * (float)kz;
+  const int chunks = (ng + kRun - 1) / kRun;
+  for (int e = threadIdx.x; e < nl * chunks; e += blockDim.x) {
+    const int r = e / chunks;
+    const int i0 = (e - r * chunks) * kRun;
+    const int ky = ky0 + r;
+    const int jp = dsigned(ky, ng), ja = abs(jp);
+    const float wjk = __ldg(&g.win[ng + ky]) * __ldg(&g.win[2 * ng + kz]) * wk;
+    const float kyf = g.vec[1] * (float)jp;
+    const float mu_yz = kyf * g.los[1] + kzf * g.los[2];
+    const float k2_yz = kyf * kyf + kzf * kzf;
+    const int n_yz = ja * ja + kz * kz;
+    RunAcc<NSPEC> ra;
+    ra.bin = -1;
+#pragma unroll
+    for (int s = 0; s < NSPEC; s++)
+#pragma unroll
+      for (int l = 0; l < kMaxPole; l++) ra.v[s][l] = 0.f;
+    const int iend = min(i0 + kRun, ng);
+    for (int i = i0; i < iend; i++) {
+      const int ip = dsigned(i, ng), ia = abs(ip);
+      const int n = ia * ia + n_yz;
+      if (n == 0) continue;  // DC (src/multipole.c:806)
+      const int b = mode_bin_fast(g, ia, ja, kz, n);
+      if (b < 0) continue;
+      // combined field of each catalogue: (F0 + exp(i theta) F1) / 2
+      const int li = lidx<P2>(i);
+      float2 G0 = X[r * ls + li], G1 = G0;
+      if (interlace) {
+        const float2 ph = __ldg(&g.phase[ip + jp + kz + ng]);
+        const float2 t = cmul(ph, X[(nl + r) * ls + li]);
+        G0 = make_float2(0.5f * (G0.x + t.x), 0.5f * (G0.y + t.y));
+      }
+      if (two_cat) {
+        G1 = X[(mpc * nl + r) * ls + li];
+        if (interlace) {
+          const float2 ph = __ldg(&g.phase[ip + jp + kz + ng]);
+          const float2 t = cmul(ph, X[((mpc + 1) * nl + r) * ls + li]);
+          G1 = make_float2(0.5f * (G1.x + t.x), 0.5f * (G1.y + t.y));
+        }
+      }
+      const float wwin = __ldg(&g.win[i]) * wjk;
+      float p[NSPEC];
+#pragma unroll
+      for (int s = 0; s < NSPEC; s++) {
+        const float2 A = spec_a[s] ? G1 : G0;
+        const float2 B = spec_b[s] ? G1 : G0;
+        p[s] = (A.x * B.x + A.y * B.y) * wwin;
+      }
+      const float kxf = g.vec[0] * (float)ip;
+      const float mu = (kxf * g.los[0] + mu_yz) * rsqrtf(kxf * kxf + k2_yz);
+      const int key = (g.nmu == 1) ? b : b * g.nmu + min(g.nmu - 1, (int)(fabsf(mu) * g.nmu));
+      run_add<NSPEC>(ra, g, key, nkey, p, mu, twice, tacc, lo, hi);
+    }
+    run_flush<NSPEC>(ra, tacc, g.npole, nkey, lo, hi);
+  }
+}
+
 // Pass C.  Lines of tile: field f, row r -> smem line f * nl + r.
 template <int NSPEC, bool STORE, bool P2>
 __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ PassCArgs a) {
@@ -121,15 +197,6 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
     }
     __syncthreads();
   }
-  const int mpc = a.interlace ? 2 : 1;  // meshes per catalogue
-  const bool interlace = a.interlace != 0, two_cat = a.ncat > 1;
-  int spec_a[NSPEC], spec_b[NSPEC];
-#pragma unroll
-  for (int s = 0; s < NSPEC; s++) {
-    spec_a[s] = a.spec_a[s];
-    spec_b[s] = a.spec_b[s];
-  }
-
   int ntiles_acc = 0;
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const int kz = tile / nty;
@@ -159,65 +226,8 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
       continue;
     }
 
-    const bool twice = !(kz == 0 || 2 * kz == ng);
-    const float wk = twice ? 2.f : 1.f;
-    const float kzf = g.vec[2] * (float)kz;
-    const int chunks = (ng + kRun - 1) / kRun;
     int lo = 0x7fffffff, hi = -1;
-    for (int e = threadIdx.x; e < nl * chunks; e += blockDim.x) {
-      const int r = e / chunks;
-      const int i0 = (e - r * chunks) * kRun;
-      const int ky = ky0 + r;
-      const int jp = dsigned(ky, ng), ja = abs(jp);
-      const float wjk = __ldg(&g.win[ng + ky]) * __ldg(&g.win[2 * ng + kz]) * wk;
-      const float kyf = g.vec[1] * (float)jp;
-      const float mu_yz = kyf * g.los[1] + kzf * g.los[2];
-      const float k2_yz = kyf * kyf + kzf * kzf;
-      const int n_yz = ja * ja + kz * kz;
-      RunAcc<NSPEC> ra;
-      ra.bin = -1;
-#pragma unroll
-      for (int s = 0; s < NSPEC; s++)
-#pragma unroll
-        for (int l = 0; l < kMaxPole; l++) ra.v[s][l] = 0.f;
-      const int iend = min(i0 + kRun, ng);
-      for (int i = i0; i < iend; i++) {
-        const int ip = dsigned(i, ng), ia = abs(ip);
-        const int n = ia * ia + n_yz;
-        if (n == 0) continue;  // DC (src/multipole.c:806)
-        const int b = mode_bin(g, ia, ja, kz, n);
-        if (b < 0) continue;
-        // combined field of each catalogue: (F0 + exp(i theta) F1) / 2
-        const int li = lidx<P2>(i);
-        float2 G0 = X[r * ls + li], G1 = G0;
-        if (interlace) {
-          const float2 ph = __ldg(&g.phase[ip + jp + kz + ng]);
-          const float2 t = cmul(ph, X[(nl + r) * ls + li]);
-          G0 = make_float2(0.5f * (G0.x + t.x), 0.5f * (G0.y + t.y));
-        }
-        if (two_cat) {
-          G1 = X[(mpc * nl + r) * ls + li];
-          if (interlace) {
-            const float2 ph = __ldg(&g.phase[ip + jp + kz + ng]);
-            const float2 t = cmul(ph, X[((mpc + 1) * nl + r) * ls + li]);
-            G1 = make_float2(0.5f * (G1.x + t.x), 0.5f * (G1.y + t.y));
-          }
-        }
-        const float wwin = __ldg(&g.win[i]) * wjk;
-        float p[NSPEC];
-#pragma unroll
-        for (int s = 0; s < NSPEC; s++) {
-          const float2 A = spec_a[s] ? G1 : G0;
-          const float2 B = spec_b[s] ? G1 : G0;
-          p[s] = (A.x * B.x + A.y * B.y) * wwin;
-        }
-        const float kxf = g.vec[0] * (float)ip;
-        const float mu = (kxf * g.los[0] + mu_yz) * rsqrtf(kxf * kxf + k2_yz);
-        const int key = (g.nmu == 1) ? b : b * g.nmu + min(g.nmu - 1, (int)(fabsf(mu) * g.nmu));
-        run_add<NSPEC>(ra, g, key, nkey, p, mu, twice, tacc, lo, hi);
-      }
-      run_flush<NSPEC>(ra, tacc, g.npole, nkey, lo, hi);
-    }
+    bin_lines<NSPEC, P2>(a, X, ls, kz, ky0, nl, tacc, lo, hi);
     note_range(srange, lo, hi);
     if (++ntiles_acc == kMergeEvery) {
       merge_tile(tacc, srange, part, nacc, nkey);
@@ -227,6 +237,80 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
     }
   }
   if (!STORE && ntiles_acc) merge_tile(tacc, srange, part, nacc, nkey);
+}
+
+// Pass C, pipelined (power-of-two Ng): persistent CTAs, the lines of the next
+// tile copied by cp.async.bulk into one stage buffer while the current one is
+// transformed (ping-pong between its stage buffer and F) and binned.  Every
+// mbarrier wait is bounded; on a timeout the kernel flags a.err, drains its
+// copies and stops.
+template <int NSPEC>
+__global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_constant__ PassCArgs a) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ int s_abort;
+  __shared__ int srange[2];
+  const int ng = a.ng, ngk = (ng >> 1) + 1, ls = line_stride(ng, true);
+  const int nty = (ng + a.ty - 1) / a.ty;
+  const int ntile = ngk * nty;
+  const ModeGeom& g = a.geom;
+  const int nacc = NSPEC * g.npole;
+  const int nkey = g.nbin * g.nmu;
+  const size_t selems = pass_c_tma_elems(ng, a.ty, a.nfield);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
+  float2* stage[2];
+  stage[0] = reinterpret_cast<float2*>(smraw + 128);
+  stage[1] = stage[0] + selems;
+  float2* F = stage[1] + selems;
+  float* tacc = reinterpret_cast<float*>(F + selems);
+  double* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
+  for (int e = threadIdx.x; e < nacc * nkey; e += blockDim.x) tacc[e] = 0.f;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    s_abort = 0;
+    srange[0] = 0x7fffffff;
+    srange[1] = -1;
+  }
+  __syncthreads();
+  auto issue = [&](int tile, int s) {
+    const int kz = tile / nty, ky0 = (tile - kz * nty) * a.ty;
+    const int nl = min(a.ty, ng - ky0);
+    mbar_expect_tx(&bar[s], (uint32_t)(a.nfield * nl * ng * 8));
+    for (int f = 0; f < a.nfield; f++)
+      for (int r = 0; r < nl; r++)
+        bulk_g2s(stage[s] + (size_t)(f * nl + r) * ng, a.in[f] + ((size_t)kz * ng + ky0 + r) * ng,
+                 (uint32_t)(ng * 8), &bar[s]);
+  };
+  if (threadIdx.x == 0 && (int)blockIdx.x < ntile) issue(blockIdx.x, 0);
+  int it = 0, ntiles_acc = 0;
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x, it++) {
+    const int s = it & 1;
+    if (threadIdx.x == 0 && tile + (int)gridDim.x < ntile) {
+      fence_proxy_async();
+      issue(tile + gridDim.x, s ^ 1);
+    }
+    if (!pipe_wait(bar, it, a.err, &s_abort)) break;
+    const int kz = tile / nty, ky0 = (tile - kz * nty) * a.ty;
+    const int nl = min(a.ty, ng - ky0);
+    const float2* X = fft2_pp_from<false, 4>(stage[s], ng, 0, F, a.plan_full.logn, a.nfield * nl,
+                                             ls, a.tw_full);
+    int lo = 0x7fffffff, hi = -1;
+    bin_lines<NSPEC, true>(a, X, ls, kz, ky0, nl, tacc, lo, hi);
+    note_range(srange, lo, hi);
+    if (++ntiles_acc == kMergeEvery) {
+      merge_tile(tacc, srange, part, nacc, nkey);
+      ntiles_acc = 0;
+    } else {
+      __syncthreads();
+    }
+  }
+  if (ntiles_acc && !s_abort) merge_tile(tacc, srange, part, nacc, nkey);
+  // never exit with a bulk copy in flight into this CTA's memory
+  if (threadIdx.x == 0 && s_abort) {
+    mbar_wait(&bar[0], 0);
+    mbar_wait(&bar[1], 0);
+  }
 }
 
 // Stand-alone binning of FFTW-layout fields [x][y][kz]: one line per (x, y).
@@ -369,6 +453,10 @@ size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin, bool pow2) {
          (size_t)nacc * nbin * sizeof(float);
 }
 
+size_t pass_c_tma_smem(int ng, int ty, int nfield, int nacc, int nkey) {
+  return 128 + 3 * pass_c_tma_elems(ng, ty, nfield) * sizeof(float2) + (size_t)nacc * nkey * sizeof(float);
+}
+
 namespace {
 template <int NSPEC, bool STORE, bool P2>
 void launch_c(const PassCArgs& a, unsigned grid, size_t smem, cudaStream_t s) {
@@ -387,6 +475,20 @@ void launch_c_p(const PassCArgs& a, cudaStream_t s) {
   }
   const size_t smem =
       pass_c_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole, a.geom.nbin * a.geom.nmu, P2);
+  if (P2 && a.pipe) {
+    const size_t sm2 = pass_c_tma_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole,
+                                       a.geom.nbin * a.geom.nmu);
+#define PS_C_TMA(NS)                                                                        \
+  cudaFuncSetAttribute(k_pass_c_tma<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2); \
+  k_pass_c_tma<NS><<<(unsigned)a.grid, kFftThreads, sm2, s>>>(a);
+    switch (a.nspec) {
+      case 1: PS_C_TMA(1); break;
+      case 2: PS_C_TMA(2); break;
+      default: PS_C_TMA(3); break;
+    }
+#undef PS_C_TMA
+    return;
+  }
   switch (a.nspec) {
     case 1: launch_c<1, false, P2>(a, (unsigned)a.grid, smem, s); break;
     case 2: launch_c<2, false, P2>(a, (unsigned)a.grid, smem, s); break;

@@ -124,6 +124,8 @@ struct ps_gpu_ctx {
   int nspec = 0, spec_a[3] = {0, 0, 0}, spec_b[3] = {0, 0, 0}, spec_cat[3] = {0, 0, 0};
   int ty_a = 1, tx_b = 1, ty_c = 1, grid_c = 1;
   int ty_ap = 1, tx_bp = 1;  // tiles of the pipelined passes
+  bool radix32_b = false;
+  int ty_ct = 1, grid_ct = 0;  // pipelined pass C (grid 0: not available)
   int nmu = 1;               // |mu| sub-bins of the binning pass
   // tile assignment
   int gT = 0, gnt = 0;
@@ -185,6 +187,35 @@ int ref_bin(const ps_gpu_ctx* c, double km2) {
   return (b < 0 || b >= c->nbin) ? -1 : b;
 }
 
+// Tiles and persistent grids of both pass-C kernels for the current number
+// of (k, mu) accumulators.  Plain kernel: kPassCElems complex per tile, as
+// many CTAs per SM as fit.  Pipelined kernel (power-of-two Ng): the largest
+// tile (rows per field) that lets two CTAs share an SM, else one CTA.
+int plan_pass_c(ps_gpu_ctx* c) {
+  const int ng = c->ng;
+  const int nacc = c->nspec * c->p.npole, nkey = c->nbin * c->nmu;
+  c->ty_c = std::max(1, std::min(ng, kPassCElems / (c->nfield * ng)));
+  const size_t smem_c = pass_c_smem(ng, c->ty_c, c->nfield, nacc, nkey, c->plan_full.logn >= 0);
+  if (smem_c > 227 * 1024)
+    return fail(c, PS_GPU_ERR_ARG, "too many (k, mu) bins (%d) for the binning pass", nkey);
+  const int per_sm = std::max(1, std::min(4, (int)((228 * 1024) / (smem_c + 2048))));
+  const int ntile_c = c->ngk * ((ng + c->ty_c - 1) / c->ty_c);
+  c->grid_c = std::min(ntile_c, c->nsm * per_sm);
+  c->grid_ct = 0;
+  if (c->plan_full.logn >= 0) {
+    const size_t half = 113 * 1024, full = 227 * 1024;
+    int ty = std::max(1, std::min(ng, kPassCElems / (c->nfield * ng)));
+    while (ty > 1 && pass_c_tma_smem(ng, ty, c->nfield, nacc, nkey) > half) ty >>= 1;
+    const size_t sm = pass_c_tma_smem(ng, ty, c->nfield, nacc, nkey);
+    if (sm <= full) {
+      const int per = sm <= half ? 2 : 1;
+      c->ty_ct = ty;
+      c->grid_ct = std::min(c->ngk * ((ng + ty - 1) / ty), c->nsm * per);
+    }
+  }
+  return 0;
+}
+
 // Per-CTA partial sums, reduced sums and the pinned host copy, sized for
 // nspec * npole * nbin * nmu accumulators.
 int alloc_accum(ps_gpu_ctx* c) {
@@ -195,7 +226,7 @@ int alloc_accum(ps_gpu_ctx* c) {
   c->d_part = nullptr;
   c->d_sums = nullptr;
   c->h_out = nullptr;
-  CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)c->grid_c * width));
+  CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)std::max(c->grid_c, c->grid_ct) * width));
   CU(cudaMalloc(&c->d_sums, sizeof(double) * width));
   CU(cudaMallocHost(&c->h_out, sizeof(double) * (width + 8)));
   return 0;
@@ -328,6 +359,17 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   g.logscale = p.logscale;
   g.nmax = nmax;
   g.bintab = c->d_bintab;
+  // FP32 bin estimate: |error of t| <= ~4 ulp of (|k| + |k0|) / dk; trusted
+  // beyond twice that from an edge, and only where the table also applies
+  {
+    const double span = (fabs(c->kedge[0]) + fabs(c->kedge[c->nbin])) / p.dk + 2.0;
+    const double eps = 8.0 * 1.1920928955078125e-7 * span;
+    g.fastbin = (c->d_bintab && !p.logscale && eps < 0.05) ? 1 : 0;
+    g.v2f = (float)(vec[0] * vec[0]);
+    g.k0f = (float)c->kedge[0];
+    g.inv_dkf = (float)(1.0 / p.dk);
+    g.eps_t = (float)eps;
+  }
   g.ksq = c->d_ksq;
   g.win = c->d_win;
   g.phase = c->d_phase;
@@ -342,23 +384,24 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   // ---- tiles and persistent grid of the binning pass
   c->ty_a = std::min({ng, 16, kCtaElems / (ng / 2)});
   c->tx_b = std::min({ng, 16, kCtaElems / ng});
-  // pipelined passes: 64 KB staged per tile (int64 rows for z, complex for y)
-  c->ty_ap = std::max(1, std::min(ng, 8192 / (ng / 2)));
-  c->tx_bp = std::max(1, std::min(ng, 8192 / ng));
-  c->ty_c = std::max(1, std::min(ng, kPassCElems / (c->nfield * ng)));
+  // pipelined passes: kPipeElems complex values per tile, two CTAs per SM
+  c->ty_ap = std::max(1, std::min(ng, kPipeElems / (ng / 2)));
+  // y pass: long lines (Ng >= 512) take radix-32 passes on 8192-value tiles,
+  // one CTA per SM (fewer shared-memory passes); shorter ones two CTAs per SM
+  c->radix32_b = ng >= 512;
+  c->tx_bp = std::max(1, std::min(ng, (c->radix32_b ? 2 * kPipeElems : kPipeElems) / ng));
   const int nacc = c->nspec * p.npole;
-  const size_t smem_c = pass_c_smem(ng, c->ty_c, c->nfield, nacc, c->nbin, c->plan_full.logn >= 0);
-  if (smem_c > 227 * 1024)
-    return fail(c, PS_GPU_ERR_ARG, "too many bins (%d) for the binning pass", c->nbin);
-  const int per_sm = std::max(1, std::min(4, (int)((228 * 1024) / (smem_c + 2048))));
-  const int ntile_c = c->ngk * ((ng + c->ty_c - 1) / c->ty_c);
-  c->grid_c = std::min(ntile_c, c->nsm * per_sm);
+  {
+    const int rc = plan_pass_c(c);
+    if (rc) return rc;
+  }
 
   // ---- device memory
   size_t freeb = 0, totalb = 0;
   CU(cudaMemGetInfo(&freeb, &totalb));
   const size_t need = (size_t)c->nfield * (c->ncx * 16) +
-                      (size_t)c->grid_c * nacc * c->nbin * 8 + c->nkeys * 8 + (64u << 20);
+                      (size_t)std::max(c->grid_c, c->grid_ct) * nacc * c->nbin * 8 + c->nkeys * 8 +
+                      (64u << 20);
   if (need > freeb)
     return fail(c, PS_GPU_ERR_MEMORY, "need %.1f GB of device memory, %.1f GB free", need / 1e9, freeb / 1e9);
   // per field: the FP32 mesh, later reused for the y-pass output (8 B * Ncmplx
@@ -606,7 +649,7 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
     PassAArgs a;
     a.ng = ng;
     a.ty = pipe ? c->ty_ap : c->ty_a;
-    a.pipe_grid = pipe ? c->nsm : 0;
+    a.pipe_grid = pipe ? 2 * c->nsm : 0;  // two CTAs per SM
     a.err = c->d_err + 2;
     a.grid = nullptr;
     a.fgrid = (const float*)c->grid[f];
@@ -623,7 +666,8 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
     PassBArgs b;
     b.ng = ng;
     b.tx = pipe ? c->tx_bp : c->tx_b;
-    b.pipe_grid = pipe ? c->nsm : 0;
+    b.pipe_grid = pipe ? (c->radix32_b ? 1 : 2) * c->nsm : 0;
+    b.radix32 = c->radix32_b ? 1 : 0;
     b.err = c->d_err + 2;
     b.in = c->cbuf[f];
     b.out = (float2*)c->grid[f];
@@ -633,11 +677,15 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   }
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[2], s));
-  CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)c->grid_c * nacc * nkey, s));
+  const bool pipe_c = pipe && c->grid_ct > 0;
+  const int grid_c = pipe_c ? c->grid_ct : c->grid_c;
+  CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)grid_c * nacc * nkey, s));
   PassCArgs pc;
   memset(&pc, 0, sizeof pc);
   pc.ng = ng;
-  pc.ty = c->ty_c;
+  pc.ty = pipe_c ? c->ty_ct : c->ty_c;
+  pc.pipe = pipe_c ? 1 : 0;
+  pc.err = c->d_err + 2;
   pc.nfield = c->nfield;
   pc.interlace = p.interlace;
   pc.ncat = p.ncat;
@@ -649,11 +697,11 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   pc.plan_full = c->plan_full;
   pc.geom = c->geom;
   pc.partials = c->d_part;
-  pc.grid = c->grid_c;
+  pc.grid = grid_c;
   c->launches += launch_pass_c(pc, s);
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], s));
-  c->launches += launch_reduce(c->d_part, c->grid_c, nacc * nkey, c->d_sums, s);
+  c->launches += launch_reduce(c->d_part, grid_c, nacc * nkey, c->d_sums, s);
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[4], s));
   double* h = c->h_out;
@@ -742,12 +790,16 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
 
 int ps_gpu_set_mu_bins(ps_gpu_ctx* c, int nmu) {
   if (!c || nmu < 1 || nmu > 64) return fail(c, PS_GPU_ERR_ARG, "number of mu bins must be 1..64");
-  const size_t smem = pass_c_smem(c->ng, c->ty_c, c->nfield, c->nspec * c->p.npole,
-                                  c->nbin * nmu, c->plan_full.logn >= 0);
-  if (smem > 227 * 1024) return fail(c, PS_GPU_ERR_ARG, "too many (k, mu) bins for the binning pass");
   CU(cudaSetDevice(c->p.device));
   CU(cudaStreamSynchronize(c->stream));
+  const int old_nmu = c->nmu;
   c->nmu = nmu;
+  const int rc = plan_pass_c(c);
+  if (rc) {
+    c->nmu = old_nmu;
+    plan_pass_c(c);
+    return rc;
+  }
   c->geom.nmu = nmu;
   c->kmu.clear();
   return alloc_accum(c);
@@ -812,6 +864,7 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   b.tw_full = c->d_tw_full;
   b.plan_full = c->plan_full;
   b.pipe_grid = 0;
+  b.radix32 = 0;
   b.err = c->d_err + 2;
   launch_pass_b(b, s);
   PassCArgs pc;

@@ -16,6 +16,7 @@ constexpr int kMaxPlan = 24;       // radix passes per transform length
 constexpr int kFftThreads = 256;   // threads of every FFT-pass CTA
 constexpr int kElemsPerThread = 32;  // complex values a thread stages per pass
 constexpr int kCtaElems = kFftThreads * kElemsPerThread;  // 8192 complex = 64 KB
+constexpr int kPipeElems = 4096;  // complex values per tile of the pipelined z/y passes
 constexpr int kPassCElems = 4096;  // complex per ping-pong buffer of the binning pass
 
 // Fixed-point mesh: every stencil node adds llrint(w_node * 2^32) to an int64
@@ -493,6 +494,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+// Wait for stage it & 1 of a two-stage pipeline (all threads).  On timeout:
+// sets bit 1 of *err and the block's abort flag; returns false once aborted.
+__device__ __forceinline__ bool pipe_wait(uint64_t* bar, int it, int* err, int* s_abort) {
+  if (!mbar_wait(&bar[it & 1], (uint32_t)((it >> 1) & 1))) {
+    atomicOr(err, 2);
+    *s_abort = 1;
+  }
+  __syncthreads();
+  return *s_abort == 0;
+}
+
 // First radix pass of a pipelined transform: reads lines of n = 2^logn
 // from an unpadded staging buffer (line stride sstride), writes the padded
 // FFT buffer (line stride ls).
@@ -562,21 +574,22 @@ __device__ __forceinline__ void fft2_rest(float2* buf, int logn, int first, int 
 // free once the first pass has read it; it must hold nlines * ls complex).
 // Returns the buffer holding the padded result.  `fix` != NULL: the staged
 // lines are int64 fixed-point cells minus `off` (the first pass converts).
-template <bool FIX>
+template <bool FIX, int MAXLOG = 5>
 __device__ __forceinline__ float2* fft2_pp_from(void* stage, int sstride, long long off,
                                                 float2* F, int logn, int nlines, int ls,
                                                 const float2* __restrict__ tw) {
+  static_assert(MAXLOG == 4 || MAXLOG == 5, "radix 16 or 32");
   int first;
-  if (logn >= 5) {
+  if (MAXLOG == 5 && logn >= 5) {
     if (FIX) fft2_first_pass_fix<32, 5>((const long long*)stage, sstride, off, F, logn, nlines, ls);
     else fft2_first_pass<32, 5>((const float2*)stage, sstride, F, logn, nlines, ls);
     first = 5;
+  } else if (logn >= 4) {
+    if (FIX) fft2_first_pass_fix<16, 4>((const long long*)stage, sstride, off, F, logn, nlines, ls);
+    else fft2_first_pass<16, 4>((const float2*)stage, sstride, F, logn, nlines, ls);
+    first = 4;
   } else {
     switch (logn) {
-      case 4:
-        if (FIX) fft2_first_pass_fix<16, 4>((const long long*)stage, sstride, off, F, logn, nlines, ls);
-        else fft2_first_pass<16, 4>((const float2*)stage, sstride, F, logn, nlines, ls);
-        break;
       case 3:
         if (FIX) fft2_first_pass_fix<8, 3>((const long long*)stage, sstride, off, F, logn, nlines, ls);
         else fft2_first_pass<8, 3>((const float2*)stage, sstride, F, logn, nlines, ls);
@@ -595,8 +608,9 @@ __device__ __forceinline__ float2* fft2_pp_from(void* stage, int sstride, long l
   float2* a = F;
   float2* b = (float2*)stage;
   int logNs = first;
-  for (; logn - logNs >= 5; logNs += 5) {
-    fft2_pass_pp<32, 5>(a, b, logn, nlines, ls, logNs, tw);
+  for (; logn - logNs >= MAXLOG; logNs += MAXLOG) {
+    if (MAXLOG == 5) fft2_pass_pp<32, 5>(a, b, logn, nlines, ls, logNs, tw);
+    else fft2_pass_pp<16, 4>(a, b, logn, nlines, ls, logNs, tw);
     float2* t = a; a = b; b = t;
   }
   const int rem = logn - logNs;
@@ -659,6 +673,10 @@ struct ModeGeom {
   double kedge0, kedgeN, dk;
   float vec[3];              // 2 pi / L per axis (FP32, for mu only)
   float los[3];
+  // FP32 bin estimate (linear bins, cubic box): t = (sqrt(n v2) - k0) / dk;
+  // trusted when farther than eps_t from a bin edge, else the exact path
+  int fastbin;
+  float v2f, k0f, inv_dkf, eps_t;
 };
 
 // Bin of a mode with |i'| = ia, |j'| = ja, k = ka, n = ia^2+ja^2+ka^2.
@@ -677,6 +695,22 @@ __device__ __forceinline__ int mode_bin(const ModeGeom& g, int ia, int ja, int k
   if (kmod < g.kedge0 || kmod >= g.kedgeN) return -1;
   const int b = (int)__ddiv_rn(__dsub_rn(kmod, g.kedge0), g.dk);
   return (b < 0 || b >= g.nbin) ? -1 : b;
+}
+
+// The same bin, from the FP32 estimate where it is unambiguous (no memory
+// access); modes within eps_t of an edge, or outside the fast setting, take
+// mode_bin (the table, then the exact FP64 sequence).
+__device__ __forceinline__ int mode_bin_fast(const ModeGeom& g, int ia, int ja, int ka, int n) {
+  if (g.fastbin) {
+    const float t = (__fsqrt_rn((float)n * g.v2f) - g.k0f) * g.inv_dkf;
+    const float fl = floorf(t);
+    const float fr = t - fl;
+    if (fr > g.eps_t && fr < 1.f - g.eps_t) {
+      const int b = (int)fl;
+      return (b < 0 || b >= g.nbin) ? -1 : b;
+    }
+  }
+  return mode_bin(g, ia, ja, ka, n);
 }
 
 // Legendre polynomial P_ell(x) (math/legpoly.h:47-62), FP32.

@@ -126,16 +126,7 @@ struct Pipe {
   int it;
 };
 
-__device__ __forceinline__ bool pipe_wait(uint64_t* bar, int it, int* err, int* s_abort) {
-  if (!mbar_wait(&bar[it & 1], (uint32_t)((it >> 1) & 1))) {
-    atomicOr(err, 2);
-    *s_abort = 1;
-  }
-  __syncthreads();
-  return *s_abort == 0;
-}
-
-__global__ void __launch_bounds__(kFftThreads, 1) k_pass_a_tma(const __grid_constant__ PassAArgs a) {
+__global__ void __launch_bounds__(kFftThreads, 2) k_pass_a_tma(const __grid_constant__ PassAArgs a) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int s_abort;
   const int ng = a.ng, M = ng >> 1, ngk = M + 1;
@@ -176,7 +167,7 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_pass_a_tma(const __grid_cons
     if (!pipe_wait(bar, it, a.err, &s_abort)) break;
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
-    float2* X = fft2_pp_from<false>(stage[s], M, 0, F, logm, nl, ls, a.tw_half);
+    float2* X = fft2_pp_from<false, 4>(stage[s], M, 0, F, logm, nl, ls, a.tw_half);
     const int half = (M >> 1) + 1;
     for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {
       const int r = e / half, k = e - r * half;
@@ -212,7 +203,10 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_pass_a_tma(const __grid_cons
   }
 }
 
-__global__ void __launch_bounds__(kFftThreads, 1) k_pass_b_tma(const __grid_constant__ PassBArgs a) {
+// MAXLOG 5: radix-32 passes, 8192-value tiles, one CTA per SM (long lines);
+// MAXLOG 4: radix-16 passes, 4096-value tiles, two CTAs per SM.
+template <int MAXLOG>
+__global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma(const __grid_constant__ PassBArgs a) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int s_abort;
   const int ng = a.ng, ngk = (ng >> 1) + 1;
@@ -252,7 +246,7 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_pass_b_tma(const __grid_cons
     if (!pipe_wait(bar, it, a.err, &s_abort)) break;
     const int kz = tile / ntx, x0 = (tile - kz * ntx) * a.tx;
     const int nl = min(a.tx, ng - x0);
-    const float2* X = fft2_pp_from<false>(stage[s], ng, 0, F, logn, nl, ls, a.tw_full);
+    const float2* X = fft2_pp_from<false, MAXLOG>(stage[s], ng, 0, F, logn, nl, ls, a.tw_full);
     float2* ob = a.out + (size_t)kz * ng * ng + x0;
     for (int e = threadIdx.x; e < ng * nl; e += blockDim.x) {
       const int ky = e / nl, r = e - ky * nl;
@@ -296,8 +290,13 @@ int launch_pass_b(const PassBArgs& a, cudaStream_t s) {
   const unsigned grid = (unsigned)(ngk * ntx);
   if (p2 && a.pipe_grid > 0) {
     const size_t sm2 = 128 + 3 * ((((size_t)a.tx * line_stride(a.ng, true)) + 1) & ~(size_t)1) * 8;
-    cudaFuncSetAttribute(k_pass_b_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-    k_pass_b_tma<<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
+    if (a.radix32) {
+      cudaFuncSetAttribute(k_pass_b_tma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+      k_pass_b_tma<5><<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
+    } else {
+      cudaFuncSetAttribute(k_pass_b_tma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+      k_pass_b_tma<4><<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
+    }
   } else if (p2) {
     cudaFuncSetAttribute(k_pass_b<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_pass_b<true><<<grid, kFftThreads, smem, s>>>(a);

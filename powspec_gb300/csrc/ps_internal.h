@@ -69,6 +69,7 @@ struct PassBArgs {
   const float2* tw_full;
   FftPlan plan_full;
   int pipe_grid;
+  int radix32;  // pipelined kernel: radix-32 passes on 8192-value tiles
   int* err;
 };
 int launch_pass_b(const PassBArgs& a, cudaStream_t s);
@@ -90,8 +91,16 @@ struct PassCArgs {
   ModeGeom geom;
   double* partials;             // [grid][nspec*npole*nbin] FP64
   int grid;                     // persistent CTAs (bin mode)
+  int pipe;                     // power-of-two Ng: the cp.async.bulk-pipelined kernel
+  int* err;                     // bit 1: a pipeline wait timed out
 };
 int launch_pass_c(const PassCArgs& a, cudaStream_t s);
+// Dynamic shared memory of the pipelined pass C (barriers, 2 stages + FFT
+// buffer, tile sums); complex elements of one of its buffers.
+size_t pass_c_tma_smem(int ng, int ty, int nfield, int nacc, int nkey);
+__host__ __device__ inline size_t pass_c_tma_elems(int ng, int ty, int nfield) {
+  return ((size_t)nfield * ty * line_stride(ng, true) + 1) & ~(size_t)1;  // 16-byte multiple
+}
 
 // Binning of standard-layout half-complex fields [x][y][kz].
 struct BinFieldArgs {
