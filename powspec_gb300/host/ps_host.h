@@ -1,0 +1,78 @@
+/*
+ * ps_host.h -- the command-line program of the GB300 periodic-box path.
+ *
+ * Keeps powspec's interface for the simulation-box case: the configuration
+ * file keywords and command-line options (src/load_conf.c:366-417), the ASCII
+ * catalogue reader's formatter / column / expression semantics
+ * (io/read_ascii.c), and the output file format (src/save_res.c:35-229).
+ * The estimator itself runs through the C ABI of include/powspec_gpu.h.
+ */
+#ifndef PS_HOST_H
+#define PS_HOST_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+/* Exit codes: the reference's POWSPEC_ERR_* (src/define.h:112-124). */
+#define PSH_ERR_MEMORY (-1)
+#define PSH_ERR_ARG (-2)
+#define PSH_ERR_FILE (-3)
+#define PSH_ERR_CFG (-4)
+#define PSH_ERR_AST (-5)
+#define PSH_ERR_ASCII (-6)
+#define PSH_ERR_CONF (-10)
+#define PSH_ERR_CATA (-11)
+
+/* ---- configuration: raw string values per keyword, typed on access ---- */
+enum { PSH_SRC_NONE = 0, PSH_SRC_FILE = 1, PSH_SRC_CMD = 5 };
+
+typedef struct {
+  char sopt;          /* short option, 0 if none */
+  const char *lopt;   /* long option */
+  const char *key;    /* configuration keyword */
+  int array;          /* accepts several values */
+  /* value */
+  int src;            /* PSH_SRC_*: command line has priority over the file */
+  int n;
+  char **val;
+} psh_opt;
+
+typedef struct {
+  psh_opt *opt;
+  int nopt;
+} psh_cfg;
+
+int psh_cfg_init(psh_cfg *c);
+void psh_cfg_free(psh_cfg *c);
+/* Command line: -h / --help and -t / --template print and return 1. */
+int psh_cfg_cmdline(psh_cfg *c, int argc, char **argv);
+int psh_cfg_file(psh_cfg *c, const char *fname);
+psh_opt *psh_cfg_get(psh_cfg *c, const char *key);
+int psh_size(psh_cfg *c, const char *key);
+const char *psh_str(psh_cfg *c, const char *key, int i);
+int psh_int(psh_cfg *c, const char *key, int i, long *out);
+int psh_dbl(psh_cfg *c, const char *key, int i, double *out);
+int psh_bool(psh_cfg *c, const char *key, int i, bool *out);
+
+/* ---- expressions over catalogue columns ($n, ${n}) ---- */
+typedef struct psh_expr psh_expr;
+/* Compiles src; *maxcol receives the largest column referenced. */
+psh_expr *psh_expr_compile(const char *src, int *maxcol, char *err, size_t errlen);
+double psh_expr_eval(const psh_expr *e, const double *col);
+void psh_expr_free(psh_expr *e);
+
+/* ---- ASCII catalogues ---- */
+typedef struct {
+  const char *fname;
+  long skip;
+  char comment;       /* '\0': no comment lines */
+  const char *fmtr;   /* scanf-style formatter */
+  const char *pos[3];
+  const char *wcomp;  /* NULL: unit weights */
+  const char *sel;    /* NULL: no selection */
+} psh_ascii;
+
+/* Reads the catalogue into *xyzw ({x, y, z, w} records), sets *n and *wsum. */
+int psh_read_ascii(const psh_ascii *in, double **xyzw, size_t *n, double *wsum, bool verbose);
+
+#endif

@@ -1,0 +1,108 @@
+"""The C host program: powspec.conf keywords, command-line options, the ASCII
+reader's formatter / expression / selection semantics (CPU, everything before
+the GPU is needed) and the output file format against the reference's own
+output on the same catalogue (GPU)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+
+@pytest.fixture(scope="session")
+def cli():
+    from powspec_gb300 import buildlib
+    if not os.path.exists(buildlib.LIB):
+        buildlib.build_lib()
+    exe = buildlib.build_cli()
+    assert exe and os.path.exists(exe)
+    return exe
+
+
+def run(exe, args, cwd):
+    return subprocess.run([exe] + args, cwd=cwd, capture_output=True, text=True, timeout=300)
+
+
+@pytest.fixture
+def workdir(tmp_path):
+    for f in ("data.txt", "powspec.conf"):
+        shutil.copy(os.path.join(GOLDEN, "cli", f), tmp_path / f)
+    return tmp_path
+
+
+def test_help_and_template(cli, tmp_path):
+    r = run(cli, ["-h"], tmp_path)
+    assert r.returncode == 0
+    for key in ("DATA_CATALOG", "GRID_SIZE", "PARTICLE_ASSIGN", "GRID_INTERLACE", "MULTIPOLE",
+                "OUTPUT_AUTO", "--box-size", "-G"):
+        assert key in r.stdout
+    r = run(cli, ["--template"], tmp_path)
+    assert r.returncode == 0 and "BIN_SIZE" in r.stdout and "LINE_OF_SIGHT" in r.stdout
+
+
+def test_survey_geometry_is_refused(cli, workdir):
+    r = run(cli, ["-c", "powspec.conf", "--sim", "F"], workdir)
+    assert r.returncode != 0
+    assert "CUBIC_SIM" in r.stderr
+
+
+def test_existing_output_without_overwrite(cli, workdir):
+    (workdir / "exists.txt").write_text("x\n")
+    r = run(cli, ["-c", "powspec.conf", "-a", "exists.txt", "-w", "0"], workdir)
+    assert r.returncode != 0 and "exists" in r.stderr
+
+
+@pytest.mark.parametrize("args,msg", [
+    (["-p", "[$1, $2]"], "DATA_POSITION"),
+    (["-p", "[$1, $2, $9]"], "column 9"),
+    (["-p", "[$1, $2, sqrt($3]"], "invalid expression"),
+    (["--grid-size", "1"], "GRID_SIZE"),
+    (["-n", "7"], "PARTICLE_ASSIGN"),
+    (["--pole", "[0, 8]"], "MULTIPOLE"),
+    (["--line-of-sight", "[1, 1, 0]"], "unit vector"),
+    (["-b", "0"], "BIN_SIZE"),
+])
+def test_configuration_errors(cli, workdir, args, msg):
+    r = run(cli, ["-c", "powspec.conf", "-a", "o.txt"] + args, workdir)
+    assert r.returncode != 0
+    assert msg in r.stderr
+
+
+def test_reader_formatter_expressions_selection(cli, workdir):
+    # 2 header lines skipped, comment and blank lines ignored, a suppressed
+    # string column, arithmetic in the positions, weights from a column and a
+    # selection on them: 2 of 3 objects kept.
+    (workdir / "d.txt").write_text(
+        "# header\nsecond header line\n1.0 x 2.0 3.0 0.5\n4 y 5 6 1.5\n# c\n\n7 z 8 9 2.5\n")
+    r = run(cli, ["-c", "powspec.conf", "-d", "d.txt", "--data-skip=2", "--data-comment=#",
+                  "--data-formatter=%lf %*s %lf %lf %lf", "-p", "[$1*10, ${2}+1, $3]",
+                  "--data-wt-comp=$4", "--data-select=$4 < 2", "-a", "o.txt", "-v", "T"], workdir)
+    assert "2 objects read from `d.txt'" in r.stdout, r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_output_matches_reference_file(cli, workdir):
+    """Same catalogue and powspec.conf as the reference's run: header lines,
+    k columns and mode counts identical; P_l within the FP32 tolerance."""
+    os.remove(workdir / "powspec.conf")
+    shutil.copy(os.path.join(GOLDEN, "cli", "powspec.conf"), workdir / "powspec.conf")
+    r = run(cli, ["-c", "powspec.conf", "-a", "gpu_auto.txt"], workdir)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = (workdir / "gpu_auto.txt").read_text().splitlines()
+    ref = open(os.path.join(GOLDEN, "cli", "ref_auto.txt")).read().splitlines()
+    assert len(got) == len(ref)
+    head = [i for i, l in enumerate(ref) if l.startswith("#")]
+    for i in head:
+        assert got[i] == ref[i]
+    shot = float(ref[4].split("Shot noise:")[1].split(",")[0])
+    g = np.array([[float(x) for x in l.split()] for l in got if not l.startswith("#")])
+    f = np.array([[float(x) for x in l.split()] for l in ref if not l.startswith("#")])
+    rows = [l for l in got if not l.startswith("#")]
+    rrows = [l for l in ref if not l.startswith("#")]
+    for a, b in zip(rows, rrows):  # kcen kmin kmax kavg nmod: same text
+        assert a.split()[:5] == b.split()[:5]
+    scale = np.abs(f[:, 5]) + shot
+    assert (np.abs(g[:, 5:] - f[:, 5:]) / scale[:, None]).max() <= 1e-5
