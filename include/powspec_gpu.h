@@ -182,6 +182,35 @@ int ps_gpu_bin_fields_host(ps_gpu_ctx *ctx, const float *f1, const float *f2,
 int ps_gpu_bin_fields_noalloc(ps_gpu_ctx *ctx, const float *f1, const float *f2,
                               double *pl, void *stream);
 
+/* ---- Ensembles of catalogues (mock ensembles for covariances).  No
+ * counterpart in the reference, which evaluates one catalogue per run. ---- */
+typedef struct ps_gpu_batch ps_gpu_batch;
+
+/* Records, once, every launch of ncat single-catalogue evaluations through
+ * ctx (assignment, FFT passes, binning, reduction into a result slot per
+ * catalogue, one copy of all slots to pinned host memory) as one CUDA graph.
+ * ctx must hold one catalogue (ncat == 1); xyzw[i] are device AoS records
+ * {x, y, z, w} (32-byte aligned) of n[i] objects, which must stay in place
+ * while the batch exists.  Catalogues with different meshes or schemes go to
+ * different contexts (and batches, which may run concurrently). */
+int ps_gpu_batch_create(ps_gpu_ctx *ctx, int ncat, const double *const *xyzw,
+                        const size_t *n, ps_gpu_batch **batch);
+/* One graph launch on the context's stream; wait != 0 blocks until done. */
+int ps_gpu_batch_launch(ps_gpu_batch *batch, int wait);
+int ps_gpu_batch_wait(ps_gpu_batch *batch);
+/* Result of catalogue i of the last completed launch (as ps_gpu_execute). */
+int ps_gpu_batch_result(ps_gpu_batch *batch, int i, ps_gpu_result *r);
+/* Kernel launches recorded in the graph. */
+int ps_gpu_batch_launches(const ps_gpu_batch *batch);
+void ps_gpu_batch_destroy(ps_gpu_batch *batch);
+
+/* Autotuner (no counterpart in the reference): times the alternative launch
+ * configurations on one catalogue -- gather CTA size, radix-16 / radix-32
+ * z and y passes, pipelined or plain last pass -- with `reps` evaluations
+ * each, and keeps the fastest for the context.  choice[4] (if not NULL):
+ * gather threads, z radix-32, y radix-32, pipelined pass C. */
+int ps_gpu_autotune(ps_gpu_ctx *ctx, const double *xyzw, size_t n, int reps, int *choice);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,7 +35,48 @@ EXPORTED = [
     "ps_gpu_last_timings", "ps_gpu_last_launches", "ps_gpu_read_mesh",
     "ps_gpu_fft_r2c_host", "ps_gpu_bin_fields_host", "ps_gpu_stream",
     "ps_gpu_set_mu_bins", "ps_gpu_read_kmu", "ps_gpu_bin_fields_noalloc",
+    "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
+    "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune",
 ]
+
+
+class Batch:
+    """Many catalogues through one Estimator (ncat = 1): every launch of all
+    their evaluations recorded once as a CUDA graph, replayed by launch().
+    The device catalogues (AoS float64, 32-byte aligned) must stay alive."""
+
+    def __init__(self, est, device_ptrs, ns):
+        self.est = est
+        self.ncat = len(ns)
+        ptrs = (ctypes.c_void_p * self.ncat)(*[ctypes.c_void_p(int(p)) for p in device_ptrs])
+        nn = (ctypes.c_size_t * self.ncat)(*[int(v) for v in ns])
+        self._b = ctypes.c_void_p()
+        est._check(lib().ps_gpu_batch_create(est._ctx, self.ncat, ptrs, nn, ctypes.byref(self._b)))
+
+    def launch(self, wait=True):
+        self.est._check(lib().ps_gpu_batch_launch(self._b, 1 if wait else 0))
+
+    def wait(self):
+        self.est._check(lib().ps_gpu_batch_wait(self._b))
+
+    def result(self, i) -> "Spectrum":
+        r, out = self.est._result()
+        self.est._check(lib().ps_gpu_batch_result(self._b, int(i), ctypes.byref(r)))
+        return self.est._spectrum(r, out)
+
+    def launches(self):
+        return lib().ps_gpu_batch_launches(self._b)
+
+    def close(self):
+        if self._b:
+            lib().ps_gpu_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PowspecError(RuntimeError):
@@ -119,6 +160,16 @@ def lib():
         L.ps_gpu_fft_r2c_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ps_gpu_bin_fields_host.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
         L.ps_gpu_bin_fields_noalloc.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 4
+        L.ps_gpu_batch_create.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+        L.ps_gpu_batch_launch.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ps_gpu_batch_wait.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Result)]
+        L.ps_gpu_batch_launches.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_batch_destroy.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_batch_destroy.restype = None
+        L.ps_gpu_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                      ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -228,7 +279,7 @@ class Estimator:
                 self._check(L.ps_gpu_assign_soa(self._ctx, cat, _ptr(arrs[0]), _ptr(arrs[1]),
                                                 _ptr(arrs[2]), _ptr(wa), len(arrs[0]), 0))
 
-    def execute(self) -> Spectrum:
+    def _result(self):
         nb, npole = self.nbin, len(self.poles)
         out = dict(k=np.zeros(nb), kedge=np.zeros(nb + 1), km=np.zeros(nb),
                    cnt=np.zeros(nb, np.uint64), lcnt=np.zeros((npole, nb)),
@@ -241,9 +292,30 @@ class Estimator:
         r.lcnt = out["lcnt"].ctypes.data_as(_dp)
         r.pl = out["pl"].ctypes.data_as(_dp)
         r.xpl = out["xpl"].ctypes.data_as(_dp)
-        self._check(lib().ps_gpu_execute(self._ctx, ctypes.byref(r)))
+        return r, out
+
+    @staticmethod
+    def _spectrum(r, out):
         return Spectrum(nbin=r.nbin, shot=np.array(r.shot[:]), norm=np.array(r.norm[:]),
                         wdata=np.array(r.wdata[:]), **out)
+
+    def execute(self) -> Spectrum:
+        r, out = self._result()
+        self._check(lib().ps_gpu_execute(self._ctx, ctypes.byref(r)))
+        return self._spectrum(r, out)
+
+    def autotune(self, device_ptr, n, reps=2):
+        """Time the alternative launch configurations on one catalogue (device
+        AoS float64 records) and keep the fastest; returns the choices."""
+        ch = np.zeros(4, np.int32)
+        self._check(lib().ps_gpu_autotune(self._ctx, ctypes.c_void_p(device_ptr), int(n), int(reps),
+                                          _ptr(ch)))
+        return dict(gather_threads=int(ch[0]), z_radix32=bool(ch[1]), y_radix32=bool(ch[2]),
+                    pipelined_pass_c=bool(ch[3]))
+
+    def batch(self, device_ptrs, ns):
+        """A CUDA-graph batch of single-catalogue evaluations (see Batch)."""
+        return Batch(self, device_ptrs, ns)
 
     def run(self, cats):
         for i, c in enumerate(cats):

@@ -125,6 +125,11 @@ struct ps_gpu_ctx {
   int ty_a = 1, tx_b = 1, ty_c = 1, grid_c = 1;
   int ty_ap = 1, tx_bp = 1;  // tiles of the pipelined passes
   bool radix32_b = false;
+  // tuning knobs (ps_gpu_autotune): z-pass variant, gather CTA size (0: by
+  // density), pipelined pass C on / off
+  bool radix32_a = false;
+  int gather_threads = 0;
+  bool pipe_c_on = true;
   int ty_ct = 1, grid_ct = 0;  // pipelined pass C (grid 0: not available)
   int nmu = 1;               // |mu| sub-bins of the binning pass
   // tile assignment
@@ -185,6 +190,15 @@ int ref_bin(const ps_gpu_ctx* c, double km2) {
   if (kmod < c->kedge[0] || kmod >= c->kedge[c->nbin]) return -1;
   const int b = (int)((kmod - c->kedge[0]) / c->p.dk);
   return (b < 0 || b >= c->nbin) ? -1 : b;
+}
+
+// Tiles of the pipelined z and y passes for their current variants:
+// kPipeElems complex values per tile (radix 16, two CTAs per SM) or twice
+// that (radix 32, one CTA per SM).
+void plan_pipes(ps_gpu_ctx* c) {
+  const int ng = c->ng;
+  c->ty_ap = std::max(1, std::min(ng, (c->radix32_a ? 2 * kPipeElems : kPipeElems) / (ng / 2)));
+  c->tx_bp = std::max(1, std::min(ng, (c->radix32_b ? 2 * kPipeElems : kPipeElems) / ng));
 }
 
 // Tiles and persistent grids of both pass-C kernels for the current number
@@ -384,12 +398,11 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   // ---- tiles and persistent grid of the binning pass
   c->ty_a = std::min({ng, 16, kCtaElems / (ng / 2)});
   c->tx_b = std::min({ng, 16, kCtaElems / ng});
-  // pipelined passes: kPipeElems complex values per tile, two CTAs per SM
-  c->ty_ap = std::max(1, std::min(ng, kPipeElems / (ng / 2)));
   // y pass: long lines (Ng >= 512) take radix-32 passes on 8192-value tiles,
-  // one CTA per SM (fewer shared-memory passes); shorter ones two CTAs per SM
+  // one CTA per SM (fewer shared-memory passes); shorter ones two CTAs per SM.
+  // The z pass takes radix-16 passes; both can be retuned (ps_gpu_autotune).
   c->radix32_b = ng >= 512;
-  c->tx_bp = std::max(1, std::min(ng, (c->radix32_b ? 2 * kPipeElems : kPipeElems) / ng));
+  plan_pipes(c);
   const int nacc = c->nspec * p.npole;
   {
     const int rc = plan_pass_c(c);
@@ -529,7 +542,23 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat) {
   g.wsum = c->d_wsum + 2 * cat;
   g.wpart = c->d_wpart;
   g.err = c->d_err + cat;
+  g.threads = c->gather_threads;
   return g;
+}
+
+// Rank and record buffers for n particles (reallocated only to grow).
+int ensure_gather_capacity(ps_gpu_ctx* c, size_t n) {
+  if (n <= c->gcap) return 0;
+  CU(cudaStreamSynchronize(c->stream));
+  if (c->d_rank) cudaFree(c->d_rank);
+  if (c->d_rec) cudaFree(c->d_rec);
+  c->d_rank = nullptr;
+  c->d_rec = nullptr;
+  c->gcap = 0;
+  CU(cudaMalloc(&c->d_rank, n * sizeof(unsigned)));
+  CU(cudaMalloc(&c->d_rec, n * gather_record_bytes()));
+  c->gcap = n;
+  return 0;
 }
 
 int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
@@ -542,16 +571,9 @@ int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
     c->assign_started = true;
     c->launches = 0;
   }
-  if (pt.n > c->gcap) {
-    CU(cudaStreamSynchronize(c->stream));
-    if (c->d_rank) cudaFree(c->d_rank);
-    if (c->d_rec) cudaFree(c->d_rec);
-    c->d_rank = nullptr;
-    c->d_rec = nullptr;
-    c->gcap = 0;
-    CU(cudaMalloc(&c->d_rank, pt.n * sizeof(unsigned)));
-    CU(cudaMalloc(&c->d_rec, pt.n * gather_record_bytes()));
-    c->gcap = pt.n;
+  {
+    const int rc = ensure_gather_capacity(c, pt.n);
+    if (rc) return rc;
   }
   CU(cudaMemsetAsync(c->d_wsum + 2 * cat, 0, sizeof(double) * 2, c->stream));
   CU(cudaMemsetAsync(c->d_err + cat, 0, sizeof(int), c->stream));
@@ -562,6 +584,163 @@ int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
   c->npart[cat] = pt.n;
   c->last_cat = cat;
   c->last_pt = pt;
+  return 0;
+}
+
+}  // namespace
+
+namespace {
+
+// Every launch of one evaluation after the assignment (passes A, B, C and
+// the reduction into sums_dst, device [nspec*npole][nbin*nmu]), on the
+// context stream, without synchronising: usable inside a stream capture.
+int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
+  const ps_gpu_params& p = c->p;
+  cudaStream_t s = c->stream;
+  const int ng = c->ng, npole = p.npole, nbin = c->nbin, nmu = c->nmu;
+  const int nacc = c->nspec * npole;
+  const int nkey = nbin * nmu;
+  const bool pipe = c->plan_full.logn >= 0 && !getenv("PS_GPU_NO_PIPELINE");
+  CU(cudaMemsetAsync(c->d_err + 2, 0, sizeof(int), s));
+  if (events) CU(cudaEventRecord(c->ev[0], s));
+  for (int f = 0; f < c->nfield; f++) {
+    PassAArgs a;
+    a.ng = ng;
+    a.ty = pipe ? c->ty_ap : c->ty_a;
+    a.pipe_grid = pipe ? (c->radix32_a ? 1 : 2) * c->nsm : 0;
+    a.radix32 = c->radix32_a ? 1 : 0;
+    a.err = c->d_err + 2;
+    a.grid = nullptr;
+    a.fgrid = (const float*)c->grid[f];
+    a.out = c->cbuf[f];
+    a.wsum = c->d_wsum + 2 * (f / c->mpc);
+    a.tw_half = c->d_tw_half;
+    a.tw_full = c->d_tw_full;
+    a.plan_half = c->plan_half;
+    c->launches += launch_pass_a(a, s);
+  }
+  CU(cudaGetLastError());
+  if (events) CU(cudaEventRecord(c->ev[1], s));
+  for (int f = 0; f < c->nfield; f++) {
+    PassBArgs b;
+    b.ng = ng;
+    b.tx = pipe ? c->tx_bp : c->tx_b;
+    b.pipe_grid = pipe ? (c->radix32_b ? 1 : 2) * c->nsm : 0;
+    b.radix32 = c->radix32_b ? 1 : 0;
+    b.err = c->d_err + 2;
+    b.in = c->cbuf[f];
+    b.out = (float2*)c->grid[f];
+    b.tw_full = c->d_tw_full;
+    b.plan_full = c->plan_full;
+    c->launches += launch_pass_b(b, s);
+  }
+  CU(cudaGetLastError());
+  if (events) CU(cudaEventRecord(c->ev[2], s));
+  const bool pipe_c = pipe && c->pipe_c_on && c->grid_ct > 0;
+  const int grid_c = pipe_c ? c->grid_ct : c->grid_c;
+  CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)grid_c * nacc * nkey, s));
+  PassCArgs pc;
+  memset(&pc, 0, sizeof pc);
+  pc.ng = ng;
+  pc.ty = pipe_c ? c->ty_ct : c->ty_c;
+  pc.pipe = pipe_c ? 1 : 0;
+  pc.err = c->d_err + 2;
+  pc.nfield = c->nfield;
+  pc.interlace = p.interlace;
+  pc.ncat = p.ncat;
+  pc.nspec = c->nspec;
+  for (int k = 0; k < 3; k++) { pc.spec_a[k] = c->spec_a[k]; pc.spec_b[k] = c->spec_b[k]; }
+  for (int f = 0; f < c->nfield; f++) pc.in[f] = (const float2*)c->grid[f];
+  pc.store = nullptr;
+  pc.tw_full = c->d_tw_full;
+  pc.plan_full = c->plan_full;
+  pc.geom = c->geom;
+  pc.partials = c->d_part;
+  pc.grid = grid_c;
+  c->launches += launch_pass_c(pc, s);
+  CU(cudaGetLastError());
+  if (events) CU(cudaEventRecord(c->ev[3], s));
+  c->launches += launch_reduce(c->d_part, grid_c, nacc * nkey, sums_dst, s);
+  CU(cudaGetLastError());
+  if (events) CU(cudaEventRecord(c->ev[4], s));
+  return 0;
+}
+
+// Host epilogue of one evaluation from its raw results: h = sums
+// [nacc][nbin*nmu] followed by wsum[4] and the error flags (4 ints).
+int finish(ps_gpu_ctx* c, const double* h, const size_t* npart, ps_gpu_result* r, bool keep_kmu) {
+  const ps_gpu_params& p = c->p;
+  const int npole = p.npole, nbin = c->nbin, nmu = c->nmu;
+  const int nacc = c->nspec * npole;
+  const int nkey = nbin * nmu;
+  // fold the |mu| sub-bins (kept for ps_gpu_read_kmu)
+  std::vector<double> fold;
+  const double* sums = h;
+  if (nmu > 1) {
+    if (keep_kmu) c->kmu.assign(h, h + (size_t)nacc * nkey);
+    fold.assign((size_t)nacc * nbin, 0.0);
+    for (size_t q = 0; q < (size_t)nacc * nbin; q++)
+      for (int j = 0; j < nmu; j++) fold[q] += h[q * nmu + j];
+    sums = fold.data();
+  }
+  const double* wsum = h + (size_t)nacc * nkey;
+  const int* errs = (const int*)(h + (size_t)nacc * nkey + 4);
+  if (errs[2]) return fail(c, PS_GPU_ERR_CUDA, "pipelined pass: bulk-copy wait timed out (flags %d)", errs[2]);
+  for (int k = 0; k < p.ncat; k++) {
+    // an empty catalogue has no coordinate range (src/genr_mesh.c:518-521)
+    if (!npart[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: no objects", k);
+    if (errs[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: coordinate outside [0, BOX_SIZE)", k);
+    if (!(wsum[2 * k + 1] < kFixMaxWeight))
+      return fail(c, PS_GPU_ERR_RANGE, "catalogue %d: total |weight| %g exceeds the fixed-point range", k, wsum[2 * k + 1]);
+  }
+
+  // epilogue (src/genr_mesh.c:904-910, src/multipole.c:1047-1087)
+  const double vol = p.box[0] * p.box[1] * p.box[2];
+  for (int k = 0; k < 2; k++) {
+    r->wdata[k] = (k < p.ncat) ? wsum[2 * k] : 0;
+    r->shot[k] = (k < p.ncat) ? vol / r->wdata[k] : 0;
+    r->norm[k] = (k < p.ncat) ? r->wdata[k] * r->wdata[k] / vol : 0;
+  }
+  r->nbin = nbin;
+  for (int s2 = 0; s2 < c->nspec; s2++) {
+    const int cat = c->spec_cat[s2];
+    double* dst = (cat >= 0) ? (r->pl ? r->pl + (size_t)cat * npole * nbin : nullptr) : r->xpl;
+    if (!dst) continue;
+    for (int l = 0; l < npole; l++) {
+      for (int i = 0; i < nbin; i++) {
+        double v = sums[((size_t)s2 * npole + l) * nbin + i];
+        const double cn = (double)c->cnt[i];
+        if (cat >= 0) {
+          if (c->cnt[i]) {
+            v /= r->norm[cat] * cn;
+            v -= r->shot[cat] * c->lcnt[(size_t)l * nbin + i] / cn;
+          }
+        } else if (c->cnt[i]) {
+          v /= sqrt(r->norm[0] * r->norm[1]) * cn;
+        }
+        v *= 2 * p.poles[l] + 1;
+        dst[(size_t)l * nbin + i] = v;
+      }
+    }
+  }
+  for (int i = 0; i < nbin; i++) {
+    if (r->k) r->k[i] = c->kcen[i];
+    if (r->km) r->km[i] = c->km[i];
+    if (r->kedge) r->kedge[i] = c->kedge[i];
+    if (r->cnt) r->cnt[i] = c->cnt[i];
+  }
+  if (r->kedge) r->kedge[nbin] = c->kedge[nbin];
+  if (r->lcnt) memcpy(r->lcnt, c->lcnt.data(), sizeof(double) * (size_t)npole * nbin);
+  // log bins: src/multipole.c:1267-1274, including its reuse of the rescaled k
+  if (p.logscale) {
+    for (int i = 0; i < nbin; i++) {
+      const double kc = pow(10, c->kcen[i]);
+      if (r->k) r->k[i] = kc;
+      if (r->km) r->km[i] = pow(10, kc);
+      if (r->kedge) r->kedge[i] = pow(10, kc);
+    }
+    if (r->kedge) r->kedge[nbin] = pow(10, c->kedge[nbin]);
+  }
   return 0;
 }
 
@@ -638,72 +817,10 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
     if (!c->assigned[k]) return fail(c, PS_GPU_ERR_STATE, "catalogue %d not assigned", k);
   CU(cudaSetDevice(p.device));
   cudaStream_t s = c->stream;
-  const int ng = c->ng, npole = p.npole, nbin = c->nbin, nmu = c->nmu;
-  const int nacc = c->nspec * npole;
-  const int nkey = nbin * nmu;
-
-  const bool pipe = c->plan_full.logn >= 0 && !getenv("PS_GPU_NO_PIPELINE");
-  CU(cudaMemsetAsync(c->d_err + 2, 0, sizeof(int), s));
-  CU(cudaEventRecord(c->ev[0], s));
-  for (int f = 0; f < c->nfield; f++) {
-    PassAArgs a;
-    a.ng = ng;
-    a.ty = pipe ? c->ty_ap : c->ty_a;
-    a.pipe_grid = pipe ? 2 * c->nsm : 0;  // two CTAs per SM
-    a.err = c->d_err + 2;
-    a.grid = nullptr;
-    a.fgrid = (const float*)c->grid[f];
-    a.out = c->cbuf[f];
-    a.wsum = c->d_wsum + 2 * (f / c->mpc);
-    a.tw_half = c->d_tw_half;
-    a.tw_full = c->d_tw_full;
-    a.plan_half = c->plan_half;
-    c->launches += launch_pass_a(a, s);
-  }
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(c->ev[1], s));
-  for (int f = 0; f < c->nfield; f++) {
-    PassBArgs b;
-    b.ng = ng;
-    b.tx = pipe ? c->tx_bp : c->tx_b;
-    b.pipe_grid = pipe ? (c->radix32_b ? 1 : 2) * c->nsm : 0;
-    b.radix32 = c->radix32_b ? 1 : 0;
-    b.err = c->d_err + 2;
-    b.in = c->cbuf[f];
-    b.out = (float2*)c->grid[f];
-    b.tw_full = c->d_tw_full;
-    b.plan_full = c->plan_full;
-    c->launches += launch_pass_b(b, s);
-  }
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(c->ev[2], s));
-  const bool pipe_c = pipe && c->grid_ct > 0;
-  const int grid_c = pipe_c ? c->grid_ct : c->grid_c;
-  CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)grid_c * nacc * nkey, s));
-  PassCArgs pc;
-  memset(&pc, 0, sizeof pc);
-  pc.ng = ng;
-  pc.ty = pipe_c ? c->ty_ct : c->ty_c;
-  pc.pipe = pipe_c ? 1 : 0;
-  pc.err = c->d_err + 2;
-  pc.nfield = c->nfield;
-  pc.interlace = p.interlace;
-  pc.ncat = p.ncat;
-  pc.nspec = c->nspec;
-  for (int k = 0; k < 3; k++) { pc.spec_a[k] = c->spec_a[k]; pc.spec_b[k] = c->spec_b[k]; }
-  for (int f = 0; f < c->nfield; f++) pc.in[f] = (const float2*)c->grid[f];
-  pc.store = nullptr;
-  pc.tw_full = c->d_tw_full;
-  pc.plan_full = c->plan_full;
-  pc.geom = c->geom;
-  pc.partials = c->d_part;
-  pc.grid = grid_c;
-  c->launches += launch_pass_c(pc, s);
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(c->ev[3], s));
-  c->launches += launch_reduce(c->d_part, grid_c, nacc * nkey, c->d_sums, s);
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(c->ev[4], s));
+  const int nacc = c->nspec * p.npole;
+  const int nkey = c->nbin * c->nmu;
+  int rc = enqueue_passes(c, c->d_sums, true);
+  if (rc) return rc;
   double* h = c->h_out;
   CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nkey, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
@@ -716,76 +833,7 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   if (cudaEventElapsedTime(&t, c->ev[0], c->ev[4]) == cudaSuccess) c->timings[5] = t + c->timings[0];
   c->assign_started = false;
   c->assigned[0] = c->assigned[1] = 0;
-
-  // fold the |mu| sub-bins (kept for ps_gpu_read_kmu)
-  std::vector<double> fold;
-  const double* sums = h;
-  if (nmu > 1) {
-    c->kmu.assign(h, h + (size_t)nacc * nkey);
-    fold.assign((size_t)nacc * nbin, 0.0);
-    for (size_t q = 0; q < (size_t)nacc * nbin; q++)
-      for (int j = 0; j < nmu; j++) fold[q] += h[q * nmu + j];
-    sums = fold.data();
-  }
-  const double* wsum = h + (size_t)nacc * nkey;
-  const int* errs = (const int*)(h + (size_t)nacc * nkey + 4);
-  if (errs[2]) return fail(c, PS_GPU_ERR_CUDA, "pipelined pass: bulk-copy wait timed out (flags %d)", errs[2]);
-  for (int k = 0; k < p.ncat; k++) {
-    // an empty catalogue has no coordinate range (src/genr_mesh.c:518-521)
-    if (!c->npart[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: no objects", k);
-    if (errs[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: coordinate outside [0, BOX_SIZE)", k);
-    if (!(wsum[2 * k + 1] < kFixMaxWeight))
-      return fail(c, PS_GPU_ERR_RANGE, "catalogue %d: total |weight| %g exceeds the fixed-point range", k, wsum[2 * k + 1]);
-  }
-
-  // epilogue (src/genr_mesh.c:904-910, src/multipole.c:1047-1087)
-  const double vol = p.box[0] * p.box[1] * p.box[2];
-  for (int k = 0; k < 2; k++) {
-    r->wdata[k] = (k < p.ncat) ? wsum[2 * k] : 0;
-    r->shot[k] = (k < p.ncat) ? vol / r->wdata[k] : 0;
-    r->norm[k] = (k < p.ncat) ? r->wdata[k] * r->wdata[k] / vol : 0;
-  }
-  r->nbin = nbin;
-  for (int s2 = 0; s2 < c->nspec; s2++) {
-    const int cat = c->spec_cat[s2];
-    double* dst = (cat >= 0) ? (r->pl ? r->pl + (size_t)cat * npole * nbin : nullptr) : r->xpl;
-    if (!dst) continue;
-    for (int l = 0; l < npole; l++) {
-      for (int i = 0; i < nbin; i++) {
-        double v = sums[((size_t)s2 * npole + l) * nbin + i];
-        const double cn = (double)c->cnt[i];
-        if (cat >= 0) {
-          if (c->cnt[i]) {
-            v /= r->norm[cat] * cn;
-            v -= r->shot[cat] * c->lcnt[(size_t)l * nbin + i] / cn;
-          }
-        } else if (c->cnt[i]) {
-          v /= sqrt(r->norm[0] * r->norm[1]) * cn;
-        }
-        v *= 2 * p.poles[l] + 1;
-        dst[(size_t)l * nbin + i] = v;
-      }
-    }
-  }
-  for (int i = 0; i < nbin; i++) {
-    if (r->k) r->k[i] = c->kcen[i];
-    if (r->km) r->km[i] = c->km[i];
-    if (r->kedge) r->kedge[i] = c->kedge[i];
-    if (r->cnt) r->cnt[i] = c->cnt[i];
-  }
-  if (r->kedge) r->kedge[nbin] = c->kedge[nbin];
-  if (r->lcnt) memcpy(r->lcnt, c->lcnt.data(), sizeof(double) * (size_t)npole * nbin);
-  // log bins: src/multipole.c:1267-1274, including its reuse of the rescaled k
-  if (p.logscale) {
-    for (int i = 0; i < nbin; i++) {
-      const double kc = pow(10, c->kcen[i]);
-      if (r->k) r->k[i] = kc;
-      if (r->km) r->km[i] = pow(10, kc);
-      if (r->kedge) r->kedge[i] = pow(10, kc);
-    }
-    if (r->kedge) r->kedge[nbin] = pow(10, c->kedge[nbin]);
-  }
-  return 0;
+  return finish(c, h, c->npart, r, true);
 }
 
 int ps_gpu_set_mu_bins(ps_gpu_ctx* c, int nmu) {
@@ -854,6 +902,7 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   a.tw_full = c->d_tw_full;
   a.plan_half = c->plan_half;
   a.pipe_grid = 0;
+  a.radix32 = 0;
   a.err = c->d_err + 2;
   launch_pass_a(a, s);
   PassBArgs b;
@@ -909,6 +958,211 @@ int ps_gpu_bin_fields_host(ps_gpu_ctx* c, const float* f1, const float* f2, doub
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(pl, c->d_sums, sizeof(double) * (size_t)npole * nbin, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+
+// ---- ensembles: one CUDA graph per batch of catalogues -----------------
+
+}  // extern "C"
+
+struct ps_gpu_batch {
+  ps_gpu_ctx* c = nullptr;
+  int ncat = 0;
+  std::vector<size_t> n;
+  size_t stride = 0;          // doubles per catalogue: sums, wsum[4], 4 error ints
+  double* d_res = nullptr;    // [ncat][stride]
+  double* h_res = nullptr;    // pinned copy
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int launches = 0;
+};
+
+namespace {
+
+void batch_free(ps_gpu_batch* b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->d_res) cudaFree(b->d_res);
+  if (b->h_res) cudaFreeHost(b->h_res);
+  delete b;
+}
+
+// Enqueues catalogue i of the batch (assignment, passes, reduction, result
+// slot); returns a status like the entry points.
+int batch_enqueue(ps_gpu_ctx* c, ps_gpu_batch* b, int i, const double* xyzw) {
+  cudaStream_t s = c->stream;
+  const int nacc = c->nspec * c->p.npole, nkey = c->nbin * c->nmu;
+  double* slot = b->d_res + (size_t)i * b->stride;
+  CU(cudaMemsetAsync(c->d_wsum, 0, sizeof(double) * 4, s));
+  CU(cudaMemsetAsync(c->d_err, 0, sizeof(int) * 4, s));
+  if (b->n[i]) {
+    Particles pt{};
+    pt.aos = xyzw;
+    pt.n = b->n[i];
+    b->launches += launch_gather_assign(pt, gather_args(c, 0), s, false);
+  }
+  CU(cudaGetLastError());
+  const int launches0 = c->launches;
+  const int rc = enqueue_passes(c, slot, false);
+  b->launches += c->launches - launches0;
+  if (rc) return rc;
+  CU(cudaMemcpyAsync(slot + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4,
+                     cudaMemcpyDeviceToDevice, s));
+  CU(cudaMemcpyAsync(slot + (size_t)nacc * nkey + 4, c->d_err, sizeof(int) * 4,
+                     cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ps_gpu_batch_create(ps_gpu_ctx* c, int ncat, const double* const* xyzw, const size_t* n,
+                        ps_gpu_batch** out) {
+  if (!c || !out || ncat < 1 || !xyzw || !n) return fail(c, PS_GPU_ERR_ARG, "invalid batch arguments");
+  *out = nullptr;
+  if (c->p.ncat != 1) return fail(c, PS_GPU_ERR_ARG, "batches need a single-catalogue context");
+  size_t nmax = 0;
+  for (int i = 0; i < ncat; i++) {
+    if (n[i] && (!xyzw[i] || ((uintptr_t)xyzw[i] & 31)))
+      return fail(c, PS_GPU_ERR_ARG, "batch catalogue %d: device records must be 32-byte aligned", i);
+    if (n[i] >= 0xffffffffull) return fail(c, PS_GPU_ERR_RANGE, "batch catalogue %d: too many particles", i);
+    nmax = std::max(nmax, n[i]);
+  }
+  CU(cudaSetDevice(c->p.device));
+  int rc = ensure_gather_capacity(c, nmax);
+  if (rc) return rc;
+  ps_gpu_batch* b = new ps_gpu_batch;
+  b->c = c;
+  b->ncat = ncat;
+  b->n.assign(n, n + ncat);
+  const int nacc = c->nspec * c->p.npole, nkey = c->nbin * c->nmu;
+  b->stride = (size_t)nacc * nkey + 6;
+  cudaError_t e = cudaMalloc(&b->d_res, sizeof(double) * b->stride * ncat);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_res, sizeof(double) * b->stride * ncat);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    batch_free(b);
+    return fail(c, PS_GPU_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e));
+  }
+  // Record every launch; the capture is always ended, also on an error.
+  e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    batch_free(b);
+    return fail(c, PS_GPU_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
+  }
+  for (int i = 0; i < ncat && !rc; i++) rc = batch_enqueue(c, b, i, xyzw[i]);
+  if (!rc) {
+    e = cudaMemcpyAsync(b->h_res, b->d_res, sizeof(double) * b->stride * ncat, cudaMemcpyDeviceToHost,
+                        c->stream);
+    if (e != cudaSuccess) rc = fail(c, PS_GPU_ERR_CUDA, "batch copy: %s", cudaGetErrorString(e));
+  }
+  const cudaError_t ee = cudaStreamEndCapture(c->stream, &b->graph);
+  if (!rc && ee != cudaSuccess) rc = fail(c, PS_GPU_ERR_CUDA, "stream capture: %s", cudaGetErrorString(ee));
+  if (!rc) {
+    e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (e != cudaSuccess) rc = fail(c, PS_GPU_ERR_CUDA, "graph instantiation: %s", cudaGetErrorString(e));
+  }
+  if (rc) {
+    cudaGetLastError();
+    batch_free(b);
+    return rc;
+  }
+  *out = b;
+  return 0;
+}
+
+int ps_gpu_batch_launch(ps_gpu_batch* b, int wait) {
+  if (!b) return PS_GPU_ERR_ARG;
+  ps_gpu_ctx* c = b->c;
+  CU(cudaSetDevice(c->p.device));
+  CU(cudaGraphLaunch(b->exec, c->stream));
+  c->launches = b->launches;
+  if (wait) CU(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int ps_gpu_batch_wait(ps_gpu_batch* b) {
+  if (!b) return PS_GPU_ERR_ARG;
+  ps_gpu_ctx* c = b->c;
+  CU(cudaSetDevice(c->p.device));
+  CU(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int ps_gpu_batch_result(ps_gpu_batch* b, int i, ps_gpu_result* r) {
+  if (!b || !r || i < 0 || i >= b->ncat) return b ? fail(b->c, PS_GPU_ERR_ARG, "invalid batch result index") : PS_GPU_ERR_ARG;
+  return finish(b->c, b->h_res + (size_t)i * b->stride, &b->n[i], r, false);
+}
+
+int ps_gpu_batch_launches(const ps_gpu_batch* b) { return b ? b->launches : PS_GPU_ERR_ARG; }
+
+void ps_gpu_batch_destroy(ps_gpu_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->c->p.device);
+  cudaStreamSynchronize(b->c->stream);
+  batch_free(b);
+}
+
+// ---- autotuner ----------------------------------------------------------
+
+int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* choice) {
+  if (!c || !xyzw || !n || reps < 1) return fail(c, PS_GPU_ERR_ARG, "invalid autotune arguments");
+  if (c->p.ncat != 1) return fail(c, PS_GPU_ERR_ARG, "autotune needs a single-catalogue context");
+  ps_gpu_result r;
+  memset(&r, 0, sizeof r);
+  // mean phase times of `reps` evaluations (after one untimed)
+  auto measure = [&](float* t) -> int {
+    for (int k = 0; k < 6; k++) t[k] = 0.f;
+    for (int it = 0; it <= reps; it++) {
+      int rc = ps_gpu_assign_aos(c, 0, xyzw, n, 1);
+      if (!rc) rc = ps_gpu_execute(c, &r);
+      if (rc) return rc;
+      if (it)
+        for (int k = 0; k < 6; k++) t[k] += c->timings[k] / reps;
+    }
+    return 0;
+  };
+  float t[6];
+  int rc;
+  // gather CTA size (phase 0)
+  {
+    const int cand[2] = {256, 512};
+    float best = 1e30f;
+    int arg = c->gather_threads;
+    for (int k = 0; k < 2; k++) {
+      c->gather_threads = cand[k];
+      if ((rc = measure(t))) return rc;
+      if (t[0] < best) { best = t[0]; arg = cand[k]; }
+    }
+    c->gather_threads = arg;
+  }
+  const bool pipe = c->plan_full.logn >= 0 && !getenv("PS_GPU_NO_PIPELINE");
+  if (pipe) {
+    // z-pass variant (phase 1), y-pass variant (phase 2), pass C (phase 3)
+    for (int knob = 0; knob < 3; knob++) {
+      if (knob == 2 && c->grid_ct <= 0) break;
+      bool* v = knob == 0 ? &c->radix32_a : knob == 1 ? &c->radix32_b : &c->pipe_c_on;
+      float best = 1e30f;
+      bool arg = *v;
+      for (int k = 0; k < 2; k++) {
+        *v = (k == 1);
+        plan_pipes(c);
+        if ((rc = measure(t))) return rc;
+        if (t[1 + knob] < best) { best = t[1 + knob]; arg = *v; }
+      }
+      *v = arg;
+      plan_pipes(c);
+    }
+  }
+  if (choice) {
+    choice[0] = c->gather_threads;
+    choice[1] = c->radix32_a;
+    choice[2] = c->radix32_b;
+    choice[3] = c->pipe_c_on;
+  }
   return 0;
 }
 

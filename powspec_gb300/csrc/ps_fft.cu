@@ -126,7 +126,10 @@ struct Pipe {
   int it;
 };
 
-__global__ void __launch_bounds__(kFftThreads, 2) k_pass_a_tma(const __grid_constant__ PassAArgs a) {
+// MAXLOG 4: radix-16 passes on 4096-value tiles, two CTAs per SM; MAXLOG 5:
+// radix-32 passes on 8192-value tiles, one CTA per SM.
+template <int MAXLOG>
+__global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_a_tma(const __grid_constant__ PassAArgs a) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int s_abort;
   const int ng = a.ng, M = ng >> 1, ngk = M + 1;
@@ -167,7 +170,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_a_tma(const __grid_cons
     if (!pipe_wait(bar, it, a.err, &s_abort)) break;
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
-    float2* X = fft2_pp_from<false, 4>(stage[s], M, 0, F, logm, nl, ls, a.tw_half);
+    float2* X = fft2_pp_from<false, MAXLOG>(stage[s], M, 0, F, logm, nl, ls, a.tw_half);
     const int half = (M >> 1) + 1;
     for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {
       const int r = e / half, k = e - r * half;
@@ -270,8 +273,13 @@ int launch_pass_a(const PassAArgs& a, cudaStream_t s) {
   const unsigned grid = (unsigned)(a.ng * nty);
   if (p2 && !a.grid && a.pipe_grid > 0) {
     const size_t sm2 = 128 + 3 * ((((size_t)a.ty * line_stride(M + 1, true)) + 1) & ~(size_t)1) * 8;
-    cudaFuncSetAttribute(k_pass_a_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-    k_pass_a_tma<<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
+    if (a.radix32) {
+      cudaFuncSetAttribute(k_pass_a_tma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+      k_pass_a_tma<5><<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
+    } else {
+      cudaFuncSetAttribute(k_pass_a_tma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+      k_pass_a_tma<4><<<(unsigned)a.pipe_grid, kFftThreads, sm2, s>>>(a);
+    }
   } else if (p2) {
     cudaFuncSetAttribute(k_pass_a<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_pass_a<true><<<grid, kFftThreads, smem, s>>>(a);

@@ -754,7 +754,9 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
   const dim3 ntile((unsigned)g.nt, (unsigned)g.nt, (unsigned)g.nt);
   // Few particles per tile: 8 warps per CTA (a CTA's accumulators are held
   // until its last warp ends); many: 16 warps to hide the record latency.
-  const unsigned nthr = ((double)p.n >= 64.0 * g.nt * g.nt * g.nt) ? kGatherThreads : kGatherThreads / 2;
+  const unsigned nthr = g.threads ? (unsigned)g.threads
+                                   : ((double)p.n >= 64.0 * g.nt * g.nt * g.nt) ? kGatherThreads
+                                                                                : kGatherThreads / 2;
 #define PS_GATHER_T(SS, TV)                                                                    \
   if (int64_out) {                                                                             \
     cudaFuncSetAttribute(k_gather<SS, true, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \

@@ -37,6 +37,7 @@ struct GatherArgs {
   double* wsum;            // [2]
   double* wpart;           // [2 * kAssignMaxBlocks]
   int* err;                // bit 0: particle outside [0, L)
+  int threads;             // CTA size of the gather: 256, 512 or 0 (by density)
 };
 int gather_tile(int ng);    // tile edge for this mesh size, 0 if unsupported
 size_t gather_keys(int ng);  // number of (tile, class) keys
@@ -55,7 +56,8 @@ struct PassAArgs {
   const float2* tw_half;        // length ng/2 twiddles
   const float2* tw_full;        // length ng twiddles (r2c split)
   FftPlan plan_half;
-  int pipe_grid;                // > 0: pipelined persistent kernel with this grid
+  int pipe_grid;
+  int radix32;  // pipelined kernel: radix-32 passes on 8192-value tiles                // > 0: pipelined persistent kernel with this grid
   int* err;                     // bit 1: pipeline wait timed out
 };
 int launch_pass_a(const PassAArgs& a, cudaStream_t s);
