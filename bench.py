@@ -15,6 +15,11 @@ h/Mpc, l = 0, 2, 4.
   up to 0.8 k_Nyq(256).  The catalogue's seed is outside the training set.
 * plain_pcs_il_ng{1024,512,256}_n4e6: the plain PCS interlaced evaluation at
   that mesh size (the Ng = 256 one is the small case the ncu captures use).
+* ensemble_256_mixed: a mock ensemble of 256 lognormal catalogues with N
+  log-uniform in [1e5, 5e6], Ng from {128, 192, 256, 384} and CIC or TSC,
+  interlaced; grouped by configuration, autotuned, each group's evaluations
+  recorded as one CUDA graph; reported against the same evaluations one
+  catalogue at a time.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun (N > 1) every rank evaluates its own catalogue on its own GPU
@@ -51,7 +56,12 @@ WORKLOADS = {
     "plain_pcs_il_ng1024_n4e6": dict(learned=False, ng=1024, assign=3, interlace=True),
     "plain_pcs_il_ng512_n4e6": dict(learned=False, ng=512, assign=3, interlace=True),
     "plain_pcs_il_ng256_n4e6": dict(learned=False, ng=256, assign=3, interlace=True),
+    "ensemble_256_mixed": dict(learned=False, ensemble=True, ng=0, assign=1, interlace=True),
 }
+# mock ensemble: 256 catalogues, N log-uniform in [1e5, 5e6], Ng from
+# {128, 192, 256, 384}, CIC or TSC, interlaced (seeded draws)
+ENS_NCAT, ENS_NMIN, ENS_NMAX = 256, 1e5, 5e6
+ENS_NG, ENS_ASSIGN = (128, 192, 256, 384), (1, 2)
 DEFAULT = "learned_ng256_vs_plain_ng1024"
 PLAIN_REF = dict(ng=1024, assign=3, interlace=True)
 
@@ -205,8 +215,39 @@ def cpu_eval(cat, threads=None):
     return time.perf_counter() - t0
 
 
+def ensemble_plan(seed):
+    """Seeded (n, ng, assign) of each ensemble catalogue."""
+    rng = np.random.default_rng(seed + 4242)
+    n = np.exp(rng.uniform(np.log(ENS_NMIN), np.log(ENS_NMAX), ENS_NCAT)).astype(np.int64)
+    ng = rng.choice(ENS_NG, ENS_NCAT)
+    asg = rng.choice(ENS_ASSIGN, ENS_NCAT)
+    return [(int(a), int(b_), int(c)) for a, b_, c in zip(n, ng, asg)]
+
+
+def _ens_cat(args):
+    from powspec_gb300 import catalog
+    n, seed = args
+    return catalog.lognormal(n, box=BOX, seed=seed, ngen=128)
+
+
+def make_ensemble(seed):
+    """The ensemble's catalogues (spawn pool: the caller has not touched the GPU)."""
+    import multiprocessing as mp
+    plan = ensemble_plan(seed)
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        cats = pool.map(_ens_cat, [(n, seed * 100000 + i) for i, (n, _, _) in enumerate(plan)],
+                        chunksize=4)
+    return plan, cats
+
+
 def config_of(wl, n_actual):
     w = WORKLOADS[wl]
+    if w.get("ensemble"):
+        return {"workload": wl, "catalogues": ENS_NCAT, "n_particles_total": n_actual,
+                "n_range": [ENS_NMIN, ENS_NMAX], "ng_choices": list(ENS_NG),
+                "assign_choices": ["CIC", "TSC"], "interlace": True, "box": BOX, "dk": DK,
+                "poles": [0, 2, 4], "catalogue": "lognormal (ngen 128)", "seed": SEED,
+                "l2": "working set per group >> 129 MB L2; no explicit flush"}
     c = {"workload": wl, "ng": w["ng"], "assign": ["NGP", "CIC", "TSC", "PCS"][w["assign"]],
          "interlace": w["interlace"], "n_particles": n_actual, "box": BOX, "dk": DK,
          "poles": [0, 2, 4], "catalogue": "lognormal", "seed": SEED,
@@ -218,9 +259,46 @@ def config_of(wl, n_actual):
     return c
 
 
+def run_reference_ensemble(args):
+    """The oracle port over the ensemble's catalogues, in order, until the
+    time cap: the same per-catalogue evaluations the GPU arm batches."""
+    import oracle
+    plan, cats = make_ensemble(SEED)
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    small = oracle.Spec(ng=64, box=BOX, assign=1, interlace=True, poles=(0, 2, 4), dk=DK,
+                        isauto=(True, False), iscross=False)
+    for _ in range(args.warmup):
+        oracle.run("port", small, [cats[0]])
+    t0 = time.perf_counter()
+    done = 0
+    for (n, ng, a), cat in zip(plan, cats):
+        spec = oracle.Spec(ng=ng, box=BOX, assign=a, interlace=True, poles=(0, 2, 4), dk=DK,
+                           isauto=(True, False), iscross=False)
+        oracle.run("port", spec, [cat])
+        done += 1
+        if time.perf_counter() - t0 > 150.0:
+            break
+    total = time.perf_counter() - t0
+    value = done / total
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
+        "n_gpus": args.gpus, "steps": 1, "warmup": args.warmup, "ms_per_step": 1e3 * total / done,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_of(args.workload, int(sum(len(c) for c in cats))),
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": f"the first {done} of {len(cats)} ensemble catalogues, "
+                                   "150 s cap; FFT by the project's FFTW-API shim"},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+    return 0
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
+    if WORKLOADS[args.workload].get("ensemble"):
+        return run_reference_ensemble(args)
     import oracle
     cat = make_catalogue(SEED)
     threads = os.cpu_count() or 1
@@ -409,6 +487,93 @@ def run_gpu(args, world, rank, local):
     return 0
 
 
+def run_ensemble(args, world, rank, local):
+    plan, cats = make_ensemble(SEED + rank)  # before any GPU call (spawn pool)
+    import torch
+
+    from powspec_gb300.ensemble import Ensemble
+    torch.cuda.set_device(local)
+    dev = [torch.from_numpy(c).to(f"cuda:{local}") for c in cats]
+    pinned = [torch.from_numpy(c).pin_memory() for c in cats]
+    configs = [(ng, a, True) for _, ng, a in plan]
+    ntot = int(sum(len(c) for c in cats))
+    t0 = time.perf_counter()
+    ens = Ensemble(dev, configs, box=BOX, dk=DK, device=local)
+    setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        ens.run()
+    with ClockSampler(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ens.launch()
+            ens.wait()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        barrier(world)
+    out = ens.results()
+    t_max = reduce(world, el, "max")
+    value = reduce(world, float(args.steps * len(cats)), "sum") / t_max
+    # the same evaluations one catalogue at a time (host round trip each)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = ens.run_plain()
+    torch.cuda.synchronize()
+    plain_s = reduce(world, time.perf_counter() - t0, "max")
+    plain_value = reduce(world, float(len(cats)), "sum") / plain_s
+    err = 0.0
+    for g, r in zip(out, ref):
+        use = r.cnt > 0
+        scale = np.abs(r.pl[0][0][use]) + r.shot[0]
+        err = max(err, float((np.abs(g.pl[0][:, use] - r.pl[0][:, use]) / scale).max()))
+    # end to end: host catalogues copied in (pinned), graphs, results out
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for d, h in zip(dev, pinned):
+            d.copy_(h, non_blocking=True)
+        torch.cuda.synchronize()
+        ens.launch()
+        ens.wait()
+        ens.results()
+    e2e_s = reduce(world, time.perf_counter() - t0, "max")
+    e2e = reduce(world, float(args.steps * len(cats)), "sum") / e2e_s
+    nlaunch = ens.launches() * args.steps
+    # algorithmic bytes of all evaluations (assignment, 3 FFT passes, binning)
+    tot = 0
+    for (n, ng, a), c in zip(plan, cats):
+        tot += algorithmic_bytes(ng, True, len(c))["total"]
+    peak, peak_kind = peaks()
+    achieved = tot * args.steps / el / 1e9
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_of(args.workload, ntot),
+            "step": "one step = all 256 catalogues (one CUDA-graph launch per configuration group)",
+            "groups": {f"ng{k[0]}_{['NGP', 'CIC', 'TSC', 'PCS'][k[1]]}": len(v)
+                       for k, v in ens.groups.items()},
+            "autotune": {f"ng{k[0]}_{['NGP', 'CIC', 'TSC', 'PCS'][k[1]]}": v
+                         for k, v in ens.tuning.items()},
+            "setup_s": setup_s,
+            "plain_per_catalogue_evals_per_s": plain_value,
+            "speedup_vs_per_catalogue": value / plain_value,
+            "max_err_vs_per_catalogue": err,
+            "roofline": {"bound": "hbm", "kernel": "whole ensemble (all kernels)",
+                         "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None},
+            "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": ntot * 32,
+                    "d2h_bytes_per_step": int(sum(len(idx) * (3 * ens.est[cf].nbin + 6) * 8
+                                                  for cf, idx in ens.groups.items()))},
+            "gpu_launches": nlaunch, "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    ens.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -422,6 +587,8 @@ def main():
     world, rank, local = dist_init()
     if args.impl == "reference":
         rc = run_reference(args, world, rank)
+    elif WORKLOADS[args.workload].get("ensemble"):
+        rc = run_ensemble(args, world, rank, local)
     else:
         rc = run_gpu(args, world, rank, local)
     if world > 1:
