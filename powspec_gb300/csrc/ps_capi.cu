@@ -533,6 +533,11 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat) {
     const double s = (double)c->ng / c->p.box[d];
     g.s_hi[d] = (float)s;
     g.s_lo[d] = (float)(s - (double)g.s_hi[d]);
+    double L = c->p.box[d];
+    memcpy(&g.box_bits[d], &L, sizeof L);
+    float bf = (float)L;
+    if ((double)bf < L) bf = nextafterf(bf, INFINITY);
+    g.box_f[d] = bf;
   }
   g.hist = c->d_hist;
   g.bsum = c->d_bsum;

@@ -190,21 +190,72 @@ __device__ __forceinline__ void node_weights(float par, float (&w)[4]) {
   }
 }
 
+// 2^k as a float (0 below the normal range).
+__device__ __forceinline__ float exp2i(int k) {
+  return k < -126 ? 0.f : __int_as_float((k + 127) << 23);
+}
+
+// Non-negative double (bit pattern b) as hi + lo floats with integer
+// operations only (FP64 arithmetic is slow on this GPU): hi = the top 24
+// significand bits (rounded), lo = the rest rounded to float.  The error of
+// hi + lo is below 2^-48 relative for values above 2^-74 (smaller ones lose
+// lo, an absolute error below 2^-98), far inside the tolerance that sends a
+// coordinate to the exact FP64 path.
+__device__ __forceinline__ void split_pos(long long b, float& hi, float& lo) {
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0) {  // zero (subnormals count as 0)
+    hi = lo = 0.f;
+    return;
+  }
+  const long long m = (b & 0xfffffffffffffLL) | 0x10000000000000LL;  // 53 bits
+  const int hm = (int)((m + (1LL << 28)) >> 29);                     // <= 2^24
+  const int lm = (int)(m - ((long long)hm << 29));                   // |lm| <= 2^28
+  hi = __int2float_rn(hm) * exp2i(e - 1046);
+  lo = __int2float_rn(lm) * exp2i(e - 1075);
+}
+
 struct Particle {
-  double pos[3];
+  double pos[3];     // AoS input: the coordinates as given (exact path only)
+  float hi[3], lo[3];
   double w;
+  float wf;          // weight as float
+  bool ok;           // inside [0, L) on every axis
+  bool aos;          // FP64 input (pos holds the coordinates)
 };
 
-__device__ __forceinline__ Particle load_particle(const Particles& p, size_t i) {
+__device__ __forceinline__ Particle load_particle(const Particles& p, const GatherArgs& g, size_t i) {
   Particle q;
+  q.ok = true;
+  q.aos = p.aos != nullptr;
   if (p.aos) {
     const double4_32a r = reinterpret_cast<const double4_32a*>(p.aos)[i];  // 32-byte aligned (checked)
-    q.pos[0] = r.x; q.pos[1] = r.y; q.pos[2] = r.z; q.w = r.w;
+    const double v[3] = {r.x, r.y, r.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      q.pos[a] = v[a];
+      long long b = __double_as_longlong(v[a]);
+      if (b == (long long)0x8000000000000000ull) b = 0;  // -0.0 >= 0 holds
+      // 0 <= pos < L on the bit patterns (ordered as the values for pos >= 0;
+      // negatives have the sign bit, NaN sorts above any finite L)
+      if (b < 0 || b >= g.box_bits[a]) q.ok = false;
+      split_pos(b, q.hi[a], q.lo[a]);
+    }
+    q.w = r.w;
+    const long long wb = __double_as_longlong(r.w);
+    float wh, wl;
+    split_pos(wb & 0x7fffffffffffffffLL, wh, wl);
+    q.wf = (wb < 0) ? -(wh + wl) : (wh + wl);
   } else {
-    q.pos[0] = (double)p.x[i];
-    q.pos[1] = (double)p.y[i];
-    q.pos[2] = (double)p.z[i];
-    q.w = p.w ? (double)p.w[i] : 1.0;
+    const float v[3] = {p.x[i], p.y[i], p.z[i]};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      q.hi[a] = v[a];
+      q.lo[a] = 0.f;
+      q.pos[a] = 0.0;  // not used: the exact path converts hi
+      if (!(v[a] >= 0.f && v[a] < g.box_f[a])) q.ok = false;  // box_f: smallest float >= L
+    }
+    q.wf = p.w ? p.w[i] : 1.f;
+    q.w = (double)q.wf;
   }
   return q;
 }
@@ -214,13 +265,11 @@ __device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs&
                                             unsigned& key) {
   const int ng = g.ng;
   int tile[3], cls[3];
+  if (!q.ok) return false;
   for (int a = 0; a < 3; a++) {
-    const double pos = q.pos[a];
-    if (!(pos >= 0.0 && pos < g.box[a])) return false;
-    const float hi = __double2float_rn(pos);
-    const float lo = __double2float_rn(__dsub_rn(pos, (double)hi));
     Axis a0, a1;
-    axis_pair(g.assign, pos, hi, lo, g.s_hi[a], g.s_lo[a], g.box[a], ng, g.interlace != 0, a0, a1);
+    axis_pair(g.assign, q.aos ? q.pos[a] : (double)q.hi[a], q.hi[a], q.lo[a], g.s_hi[a], g.s_lo[a],
+              g.box[a], ng, g.interlace != 0, a0, a1);
     r.base[0][a] = (short)a0.base;
     r.base[1][a] = (short)a1.base;
     r.par[0][a] = a0.par;
@@ -237,8 +286,8 @@ __device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs&
     tile[a] = t;
     cls[a] = (lo_r < 0) ? 1 : ((hi_r >= g.T) ? 2 : 0);
   }
-  r.wf = (float)q.w * kFixScale;
-  r.q = __double2ll_rn(q.w * 4294967296.0);
+  r.wf = q.wf * kFixScale;
+  r.q = (g.assign == 0) ? __double2ll_rn(q.w * 4294967296.0) : 0;  // NGP node value only
   const unsigned t = ((unsigned)tile[0] * g.nt + tile[1]) * g.nt + tile[2];
   key = t * 27u + (unsigned)(cls[0] + 3 * cls[1] + 9 * cls[2]);
   return true;
@@ -249,7 +298,7 @@ __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ Gather
   int bad = 0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const Particle q = load_particle(p, i);
+    const Particle q = load_particle(p, g, i);
     Rec r;
     unsigned key;
     if (!make_record(q, g, r, key)) {
@@ -296,7 +345,7 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ GatherA
        i += (size_t)gridDim.x * blockDim.x) {
     const unsigned rk = g.rank[i];
     if (rk == 0xffffffffu) continue;
-    const Particle q = load_particle(p, i);
+    const Particle q = load_particle(p, g, i);
     Rec r;
     unsigned key;
     make_record(q, g, r, key);

@@ -28,6 +28,8 @@ struct GatherArgs {
   int T, nt;               // tile edge (cells) and tiles per axis
   double box[3];
   float s_hi[3], s_lo[3];  // Ng / L as a double-float pair per axis
+  long long box_bits[3];   // bit pattern of L (AoS FP64 bound check)
+  float box_f[3];          // smallest float >= L (SoA FP32 bound check)
   unsigned* hist;          // [nkeys + 1] counts, then offsets
   unsigned* bsum;          // [ceil(nkeys / 4096) + 1]
   unsigned* rank;          // [n]
