@@ -51,12 +51,14 @@ __device__ __forceinline__ void run_add(RunAcc<NSPEC>& ra, const ModeGeom& g, in
     run_flush<NSPEC>(ra, tacc, g.npole, nkey, lo, hi);
     ra.bin = b;
   }
+  const float m2 = mu * mu;
 #pragma unroll
   for (int l = 0; l < kMaxPole; l++) {
     if (l < g.npole) {
-      const int ell = g.poles[l];
-      if (skip_odd && (ell & 1)) continue;  // cancels between half-spaces (src/multipole.c:844)
-      const float L = legendre(ell, mu);
+      const bool odd = (g.lodd >> l) & 1;
+      if (skip_odd && odd) continue;  // cancels between half-spaces (src/multipole.c:844)
+      float L = fmaf(fmaf(fmaf(g.lc[l][3], m2, g.lc[l][2]), m2, g.lc[l][1]), m2, g.lc[l][0]);
+      if (odd) L *= mu;
 #pragma unroll
       for (int s = 0; s < NSPEC; s++) ra.v[s][l] = fmaf(p[s], L, ra.v[s][l]);
     }

@@ -384,6 +384,20 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
     g.inv_dkf = (float)(1.0 / p.dk);
     g.eps_t = (float)eps;
   }
+  // Legendre polynomials (math/legpoly.h:47-62) as Horner coefficients in mu^2
+  {
+    static const float lc[7][4] = {{1.f, 0, 0, 0},           {1.f, 0, 0, 0},
+                                   {-0.5f, 1.5f, 0, 0},      {-1.5f, 2.5f, 0, 0},
+                                   {0.375f, -3.75f, 4.375f, 0}, {1.875f, -8.75f, 7.875f, 0},
+                                   {-0.3125f, 6.5625f, -19.6875f, 14.4375f}};
+    g.lodd = 0;
+    for (int l = 0; l < kMaxPole; l++)
+      for (int q = 0; q < 4; q++) g.lc[l][q] = 0.f;
+    for (int l = 0; l < p.npole; l++) {
+      for (int q = 0; q < 4; q++) g.lc[l][q] = lc[p.poles[l]][q];
+      if (p.poles[l] & 1) g.lodd |= 1 << l;
+    }
+  }
   g.ksq = c->d_ksq;
   g.win = c->d_win;
   g.phase = c->d_phase;

@@ -677,6 +677,9 @@ struct ModeGeom {
   // trusted when farther than eps_t from a bin edge, else the exact path
   int fastbin;
   float v2f, k0f, inv_dkf, eps_t;
+  // L_ell(mu) = [mu if ell odd] * (c0 + c1 mu^2 + c2 mu^4 + c3 mu^6) per pole
+  float lc[kMaxPole][4];
+  int lodd;                  // bit l: pole l is odd
 };
 
 // Bin of a mode with |i'| = ia, |j'| = ja, k = ka, n = ia^2+ja^2+ka^2.
