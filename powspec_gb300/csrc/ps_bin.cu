@@ -141,7 +141,18 @@ __device__ __forceinline__ void bin_lines(const PassCArgs& a, const float2* X, i
       const int ip = dsigned(i, ng), ia = abs(ip);
       const int n = ia * ia + n_yz;
       if (n == 0) continue;  // DC (src/multipole.c:806)
-      const int b = mode_bin_fast(g, ia, ja, kz, n);
+      // one reciprocal square root gives both |k| (bin estimate) and mu
+      const float kxf = g.vec[0] * (float)ip;
+      const float rq = rsqrtf(kxf * kxf + k2_yz);
+      int b;
+      if (g.fastbin) {
+        const float t = (fmaf(kxf, kxf, k2_yz) * rq - g.k0f) * g.inv_dkf;
+        const float fl = floorf(t), fr = t - fl;
+        b = (fr > g.eps_t && fr < 1.f - g.eps_t) ? ((fl < 0.f || fl >= (float)g.nbin) ? -1 : (int)fl)
+                                                 : mode_bin(g, ia, ja, kz, n);
+      } else {
+        b = mode_bin(g, ia, ja, kz, n);
+      }
       if (b < 0) continue;
       // combined field of each catalogue: (F0 + exp(i theta) F1) / 2
       const int li = lidx<P2>(i);
@@ -167,8 +178,7 @@ __device__ __forceinline__ void bin_lines(const PassCArgs& a, const float2* X, i
         const float2 B = spec_b[s] ? G1 : G0;
         p[s] = (A.x * B.x + A.y * B.y) * wwin;
       }
-      const float kxf = g.vec[0] * (float)ip;
-      const float mu = (kxf * g.los[0] + mu_yz) * rsqrtf(kxf * kxf + k2_yz);
+      const float mu = (kxf * g.los[0] + mu_yz) * rq;
       const int key = (g.nmu == 1) ? b : b * g.nmu + min(g.nmu - 1, (int)(fabsf(mu) * g.nmu));
       run_add<NSPEC>(ra, g, key, nkey, p, mu, twice, tacc, lo, hi);
     }

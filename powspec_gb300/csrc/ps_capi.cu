@@ -373,13 +373,14 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   g.logscale = p.logscale;
   g.nmax = nmax;
   g.bintab = c->d_bintab;
-  // FP32 bin estimate: |error of t| <= ~4 ulp of (|k| + |k0|) / dk; trusted
-  // beyond twice that from an edge, and only where the table also applies
+  // FP32 bin estimate from the FP32 components of k (vec * index, squares,
+  // sums, a reciprocal square root): |error of t| <= ~8 ulp of
+  // (|k| + |k0|) / dk; trusted beyond twice that from an edge, and only
+  // where the table also applies
   {
     const double span = (fabs(c->kedge[0]) + fabs(c->kedge[c->nbin])) / p.dk + 2.0;
-    const double eps = 8.0 * 1.1920928955078125e-7 * span;
+    const double eps = 16.0 * 1.1920928955078125e-7 * span;
     g.fastbin = (c->d_bintab && !p.logscale && eps < 0.05) ? 1 : 0;
-    g.v2f = (float)(vec[0] * vec[0]);
     g.k0f = (float)c->kedge[0];
     g.inv_dkf = (float)(1.0 / p.dk);
     g.eps_t = (float)eps;

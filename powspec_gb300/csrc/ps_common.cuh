@@ -673,10 +673,11 @@ struct ModeGeom {
   double kedge0, kedgeN, dk;
   float vec[3];              // 2 pi / L per axis (FP32, for mu only)
   float los[3];
-  // FP32 bin estimate (linear bins, cubic box): t = (sqrt(n v2) - k0) / dk;
-  // trusted when farther than eps_t from a bin edge, else the exact path
+  // FP32 bin estimate (linear bins, cubic box): t = (|k| - k0) / dk from the
+  // FP32 wave vector; trusted when farther than eps_t from a bin edge, else
+  // the table and the exact path
   int fastbin;
-  float v2f, k0f, inv_dkf, eps_t;
+  float k0f, inv_dkf, eps_t;
   // L_ell(mu) = [mu if ell odd] * (c0 + c1 mu^2 + c2 mu^4 + c3 mu^6) per pole
   float lc[kMaxPole][4];
   int lodd;                  // bit l: pole l is odd
@@ -698,36 +699,6 @@ __device__ __forceinline__ int mode_bin(const ModeGeom& g, int ia, int ja, int k
   if (kmod < g.kedge0 || kmod >= g.kedgeN) return -1;
   const int b = (int)__ddiv_rn(__dsub_rn(kmod, g.kedge0), g.dk);
   return (b < 0 || b >= g.nbin) ? -1 : b;
-}
-
-// The same bin, from the FP32 estimate where it is unambiguous (no memory
-// access); modes within eps_t of an edge, or outside the fast setting, take
-// mode_bin (the table, then the exact FP64 sequence).
-__device__ __forceinline__ int mode_bin_fast(const ModeGeom& g, int ia, int ja, int ka, int n) {
-  if (g.fastbin) {
-    const float t = (__fsqrt_rn((float)n * g.v2f) - g.k0f) * g.inv_dkf;
-    const float fl = floorf(t);
-    const float fr = t - fl;
-    if (fr > g.eps_t && fr < 1.f - g.eps_t) {
-      const int b = (int)fl;
-      return (b < 0 || b >= g.nbin) ? -1 : b;
-    }
-  }
-  return mode_bin(g, ia, ja, ka, n);
-}
-
-// Legendre polynomial P_ell(x) (math/legpoly.h:47-62), FP32.
-__device__ __forceinline__ float legendre(int ell, float x) {
-  const float x2 = x * x;
-  switch (ell) {
-    case 0: return 1.f;
-    case 1: return x;
-    case 2: return 1.5f * x2 - 0.5f;
-    case 3: return 2.5f * x * (x2 - 0.6f);
-    case 4: return (4.375f * x2 - 3.75f) * x2 + 0.375f;
-    case 5: return 8.75f * x * ((0.9f * x2 - 1.f) * x2 + 0.21428571428571428f);
-    default: return ((14.4375f * x2 - 19.6875f) * x2 + 6.5625f) * x2 - 0.3125f;
-  }
 }
 
 inline int signed_index(int i, int ng) { return (i <= (ng >> 1)) ? i : i - ng; }
