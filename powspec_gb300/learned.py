@@ -392,6 +392,7 @@ class LearnedEstimator:
             key = f"ng{ng}_{['NGP', 'CIC', 'TSC', 'PCS'][assign]}_{'il' if interlace else 'noil'}"
             self.disabled = set(r.get(key, {}).get("disabled_bins", []))
         self.last_cells = None
+        self._x = None
 
     def close(self):
         self.est.close()
@@ -411,7 +412,13 @@ class LearnedEstimator:
         else:
             cells = measure_cells(self.est, cat)
         self.last_cells = cells
-        pc = correct(self.mlp, cells, self.cfg[1], self.cfg[2])
+        # feature rows: all columns but the shot-noise ratio depend on the
+        # context only, so they are built once
+        if self._x is None or len(self._x) != len(cells.kcen) * NMU:
+            self._x = features(cells.kcen, cells.kny, self.cfg[1], self.cfg[2],
+                               np.zeros(len(cells.kcen)))
+        self._x[:, 5] = np.repeat(cells.shot_ratio(), NMU)
+        pc = cells.corrected(self.mlp.infer(self._x))
         trusted = kmax_frac(cells, self.frac)
         for b in self.disabled:
             if b < len(trusted):
