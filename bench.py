@@ -57,7 +57,12 @@ WORKLOADS = {
     "plain_pcs_il_ng512_n4e6": dict(learned=False, ng=512, assign=3, interlace=True),
     "plain_pcs_il_ng256_n4e6": dict(learned=False, ng=256, assign=3, interlace=True),
     "ensemble_256_mixed": dict(learned=False, ensemble=True, ng=0, assign=1, interlace=True),
+    # large single mesh: N = 1.5e8 lognormal, FP32 SoA positions, FP32 weights
+    # uniform in [0.5, 1.5], L = 2000 Mpc/h, dk = 0.002
+    "large_pcs_il_ng1024_n1.5e8_f32": dict(learned=False, large=True, ng=1024, assign=3, interlace=True),
+    "large_pcs_il_ng2048_n1.5e8_f32": dict(learned=False, large=True, ng=2048, assign=3, interlace=True),
 }
+LARGE_N, LARGE_BOX, LARGE_DK = 150_000_000, 2000.0, 0.002
 # mock ensemble: 256 catalogues, N log-uniform in [1e5, 5e6], Ng from
 # {128, 192, 256, 384}, CIC or TSC, interlaced (seeded draws)
 ENS_NCAT, ENS_NMIN, ENS_NMAX = 256, 1e5, 5e6
@@ -156,7 +161,7 @@ def reduce(world, v, op):
     return float(t.item())
 
 
-def algorithmic_bytes(ng, interlace, n):
+def algorithmic_bytes(ng, interlace, n, bp=32):
     """Per-launch algorithmic HBM bytes of each phase (FP32 path).
 
     assignment: N * 32 B (AoS float64 records) + 4 B * Ng^3 per mesh (the
@@ -168,18 +173,18 @@ def algorithmic_bytes(ng, interlace, n):
     ntot = ng ** 3
     ncx = ng * ng * (ng // 2 + 1)
     return {
-        "assign": n * 32 + 4 * ntot,
+        "assign": n * bp + 4 * ntot,
         "pass_z": 4 * ntot + 8 * ncx,
         "pass_y": 16 * ncx,
         "pass_x_bin": 8 * ncx * nmesh,
         "nmesh": nmesh,
-        "total": nmesh * (n * 32 + 4 * ntot) + nmesh * (4 * ntot + 8 * ncx) + nmesh * 8 * ncx * 2,
+        "total": nmesh * (n * bp + 4 * ntot) + nmesh * (4 * ntot + 8 * ncx) + nmesh * 8 * ncx * 2,
     }
 
 
-def roofline(phases_ms, ng, interlace, n, traffic=None, assign=3):
+def roofline(phases_ms, ng, interlace, n, traffic=None, assign=3, bp=32):
     peak, peak_kind = peaks()
-    ab = algorithmic_bytes(ng, interlace, n)
+    ab = algorithmic_bytes(ng, interlace, n, bp)
     # assignment: the whole phase (both meshes in one pass over the particles);
     # FFT passes: per launch (one launch per mesh); x pass + binning: one launch
     kern = {"assign": (phases_ms[0], ab["nmesh"] * ab["assign"]),
@@ -242,6 +247,11 @@ def make_ensemble(seed):
 
 def config_of(wl, n_actual):
     w = WORKLOADS[wl]
+    if w.get("large"):
+        return {"workload": wl, "ng": w["ng"], "assign": "PCS", "interlace": True,
+                "n_particles": n_actual, "positions": "float32 SoA", "weights": "float32 U[0.5, 1.5]",
+                "box": LARGE_BOX, "dk": LARGE_DK, "poles": [0, 2, 4], "catalogue": "lognormal (ngen 256)",
+                "seed": SEED, "l2": "working set per eval >> 129 MB L2; no explicit flush"}
     if w.get("ensemble"):
         return {"workload": wl, "catalogues": ENS_NCAT, "n_particles_total": n_actual,
                 "n_range": [ENS_NMIN, ENS_NMAX], "ng_choices": list(ENS_NG),
@@ -294,11 +304,48 @@ def run_reference_ensemble(args):
     return 0
 
 
+def run_reference_large(args):
+    """The oracle port on the large single-mesh workload: one bounded
+    evaluation at Ng = 1024; Ng = 2048 does not fit the FP64 meshes in host
+    memory."""
+    wl = WORKLOADS[args.workload]
+    if wl["ng"] > 1024:
+        print(json.dumps({"impl": "reference", "unavailable": "the FP64 reference at Ng=2048 "
+                          "needs about 0.3 TB of host memory for its meshes"}))
+        return 0
+    import oracle
+    from powspec_gb300 import catalog
+    x, y, z, w = catalog.lognormal(LARGE_N, box=LARGE_BOX, seed=SEED, ngen=256,
+                                   weights=(0.5, 1.5), soa=True)
+    cat = np.stack([x, y, z, w], axis=1).astype(np.float64)
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    spec = oracle.Spec(ng=wl["ng"], box=LARGE_BOX, assign=wl["assign"], interlace=wl["interlace"],
+                       poles=(0, 2, 4), dk=LARGE_DK, isauto=(True, False), iscross=False)
+    t0 = time.perf_counter()
+    oracle.run("port", spec, [cat])
+    total = time.perf_counter() - t0
+    value = 1.0 / total
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
+        "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * total,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_of(args.workload, len(cat)),
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": "one evaluation of the workload's catalogue; FFT by the "
+                                   "project's FFTW-API shim"},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+    return 0
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
     if WORKLOADS[args.workload].get("ensemble"):
         return run_reference_ensemble(args)
+    if WORKLOADS[args.workload].get("large"):
+        return run_reference_large(args)
     import oracle
     cat = make_catalogue(SEED)
     threads = os.cpu_count() or 1
@@ -574,6 +621,72 @@ def run_ensemble(args, world, rank, local):
     return 0
 
 
+def run_large(args, world, rank, local):
+    import torch
+
+    import powspec_gb300 as ps
+    from powspec_gb300 import catalog
+    wl = WORKLOADS[args.workload]
+    x, y, z, w = catalog.lognormal(LARGE_N, box=LARGE_BOX, seed=SEED + rank, ngen=256,
+                                   weights=(0.5, 1.5), soa=True)
+    n = len(x)
+    torch.cuda.set_device(local)
+    dev = [torch.from_numpy(v).to(f"cuda:{local}") for v in (x, y, z, w)]
+    host = [torch.from_numpy(v).pin_memory().numpy() for v in (x, y, z, w)]
+    est = ps.Estimator(ng=wl["ng"], box=LARGE_BOX, assign=wl["assign"], interlace=wl["interlace"],
+                       poles=(0, 2, 4), dk=LARGE_DK, device=local)
+    stream = torch.cuda.ExternalStream(est.stream(), device=local)
+    phases = np.zeros(6)
+    launches = [0]
+
+    def step():
+        est.assign(0, x=dev[0].data_ptr(), y=dev[1].data_ptr(), z=dev[2].data_ptr(),
+                   w=dev[3].data_ptr(), on_device=True, n=n)
+        r = est.execute()
+        phases[:] += est.timings()
+        launches[0] += est.launches()
+        return r
+
+    for _ in range(args.warmup):
+        step()
+    phases[:] = 0
+    launches[0] = 0
+    with ClockSampler(local) as clk:
+        barrier(world)
+        dev_ms, _ = timed(stream, args.steps, step)
+        barrier(world)
+    ph = phases / args.steps
+    t_max = reduce(world, dev_ms / 1e3, "max")
+    value = reduce(world, float(args.steps), "sum") / t_max
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        est.assign(0, x=host[0], y=host[1], z=host[2], w=host[3])
+        est.execute()
+    e2e_s = reduce(world, time.perf_counter() - t0, "max")
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_of(args.workload, n),
+            "phases_ms": {"assign": ph[0], "pass_z": ph[1], "pass_y": ph[2], "pass_x_bin": ph[3],
+                          "reduce": ph[4], "device_total": ph[5]},
+            "roofline": roofline(ph, wl["ng"], wl["interlace"], n, None, wl["assign"], bp=16),
+            "e2e": {"value": args.steps / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": n * 16,
+                    "d2h_bytes_per_step": 8 * 3 * est.nbin + 8 * 4 + 16},
+            "gpu_launches": launches[0], "clocks": clk.summary(),
+            "cpu_baseline": None,
+            "cpu_baseline_note": ("the FP64 reference at Ng=2048 needs about 0.3 TB of host memory"
+                                  if wl["ng"] > 1024 else
+                                  "one FP64 evaluation of 1.5e8 particles exceeds the few-minute "
+                                  "sample budget of this run: bench.py --impl reference times it"),
+        }
+        print(json.dumps(line))
+    est.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -589,6 +702,8 @@ def main():
         rc = run_reference(args, world, rank)
     elif WORKLOADS[args.workload].get("ensemble"):
         rc = run_ensemble(args, world, rank, local)
+    elif WORKLOADS[args.workload].get("large"):
+        rc = run_large(args, world, rank, local)
     else:
         rc = run_gpu(args, world, rank, local)
     if world > 1:

@@ -81,8 +81,10 @@ def lognormal(nbar_total, box=1000.0, seed=1, ngen=128, zeldovich=4.0, weights=N
     else:
         w = rng.uniform(weights[0], weights[1], n)
     if soa:
-        return (pos[:, 0].astype(np.float32), pos[:, 1].astype(np.float32),
-                pos[:, 2].astype(np.float32), w.astype(np.float32))
+        # FP32 rounding may reach L itself: keep every coordinate below it
+        top = np.nextafter(np.float32(box), np.float32(0))
+        xyz = [np.minimum(pos[:, a].astype(np.float32), top) for a in range(3)]
+        return xyz[0], xyz[1], xyz[2], w.astype(np.float32)
     out = np.empty((n, 4), dtype=dtype)
     out[:, :3] = pos
     out[:, 3] = w
