@@ -416,6 +416,7 @@ def run_gpu(args, world, rank, local):
                          interlace=pref["interlace"], poles=(0, 2, 4), dk=DK, device=local)
     s_plain = torch.cuda.ExternalStream(plain.stream(), device=local)
     phases_plain = np.zeros(6)
+    tuning = {"plain": plain.autotune(d_cat.data_ptr(), nreal)}  # set-up, not timed
 
     def step_plain():
         plain.assign(0, d_cat.data_ptr(), on_device=True, n=nreal)
@@ -426,6 +427,7 @@ def run_gpu(args, world, rank, local):
     if wl["learned"]:
         le = learned.LearnedEstimator(ng=wl["ng"], assign=wl["assign"], interlace=wl["interlace"],
                                       box=BOX, dk=DK, device=local)
+        tuning["learned"] = le.est.autotune(d_cat.data_ptr(), nreal)
         stream = torch.cuda.ExternalStream(le.est.stream(), device=local)
         phases = np.zeros(6)
         launches = [0]
@@ -517,7 +519,7 @@ def run_gpu(args, world, rank, local):
             "roofline": roofline(ph, wl["ng"], wl["interlace"], nreal, traffic),
             "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": nreal * 32,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": nlaunch, "clocks": clocks,
+            "gpu_launches": nlaunch, "clocks": clocks, "autotune": tuning,
         }
         line.update(extra)
         if world == 1 and not args.no_cpu:

@@ -205,10 +205,11 @@ int ps_gpu_batch_launches(const ps_gpu_batch *batch);
 void ps_gpu_batch_destroy(ps_gpu_batch *batch);
 
 /* Autotuner (no counterpart in the reference): times the alternative launch
- * configurations on one catalogue -- gather CTA size, radix-16 / radix-32
+ * configurations on one catalogue -- gather CTA size and dense-tile mapping, radix-16 / radix-32
  * z and y passes, pipelined or plain last pass -- with `reps` evaluations
- * each, and keeps the fastest for the context.  choice[4] (if not NULL):
- * gather threads, z radix-32, y radix-32, pipelined pass C. */
+ * each, and keeps the fastest for the context.  choice[5] (if not NULL):
+ * gather threads, z radix-32, y radix-32, pipelined pass C, lane groups on
+ * dense tiles. */
 int ps_gpu_autotune(ps_gpu_ctx *ctx, const double *xyzw, size_t n, int reps, int *choice);
 
 #ifdef __cplusplus

@@ -307,11 +307,11 @@ class Estimator:
     def autotune(self, device_ptr, n, reps=2):
         """Time the alternative launch configurations on one catalogue (device
         AoS float64 records) and keep the fastest; returns the choices."""
-        ch = np.zeros(4, np.int32)
+        ch = np.zeros(5, np.int32)
         self._check(lib().ps_gpu_autotune(self._ctx, ctypes.c_void_p(device_ptr), int(n), int(reps),
                                           _ptr(ch)))
         return dict(gather_threads=int(ch[0]), z_radix32=bool(ch[1]), y_radix32=bool(ch[2]),
-                    pipelined_pass_c=bool(ch[3]))
+                    pipelined_pass_c=bool(ch[3]), dense_lane_groups=bool(ch[4]))
 
     def batch(self, device_ptrs, ns):
         """A CUDA-graph batch of single-catalogue evaluations (see Batch)."""

@@ -129,6 +129,7 @@ struct ps_gpu_ctx {
   // density), pipelined pass C on / off
   bool radix32_a = false;
   int gather_threads = 0;
+  unsigned gather_sparse_max = 512;  // records per tile up to which lane groups are used
   bool pipe_c_on = true;
   int ty_ct = 1, grid_ct = 0;  // pipelined pass C (grid 0: not available)
   int nmu = 1;               // |mu| sub-bins of the binning pass
@@ -563,6 +564,7 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat) {
   g.wpart = c->d_wpart;
   g.err = c->d_err + cat;
   g.threads = c->gather_threads;
+  g.sparse_max = c->gather_sparse_max;
   return g;
 }
 
@@ -1159,6 +1161,18 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
     }
     c->gather_threads = arg;
   }
+  // dense tiles: one record per warp or lane groups (phase 0)
+  {
+    const unsigned cand[2] = {512u, 0xffffffffu};
+    float best = 1e30f;
+    unsigned arg = c->gather_sparse_max;
+    for (int k = 0; k < 2; k++) {
+      c->gather_sparse_max = cand[k];
+      if ((rc = measure(t))) return rc;
+      if (t[0] < best) { best = t[0]; arg = cand[k]; }
+    }
+    c->gather_sparse_max = arg;
+  }
   const bool pipe = c->plan_full.logn >= 0 && !getenv("PS_GPU_NO_PIPELINE");
   if (pipe) {
     // z-pass variant (phase 1), y-pass variant (phase 2), pass C (phase 3)
@@ -1178,6 +1192,7 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
     }
   }
   if (choice) {
+    choice[4] = c->gather_sparse_max == 0xffffffffu ? 1 : 0;
     choice[0] = c->gather_threads;
     choice[1] = c->radix32_a;
     choice[2] = c->radix32_b;

@@ -29,7 +29,6 @@ namespace {
 
 constexpr int kGatherThreads = 512;  // 16 warps; 3 CTAs per SM fit (registers, shared memory)
 constexpr int kMeshPad = 8;  // words between the two meshes' accumulators (bank offset)
-constexpr unsigned kSparseRecords = 64;  // at most: one pass over all records, rows flagged
 constexpr float kEdge = 4e-6f;
 
 // wsum[0..1] = sums of the per-block partials: lane l adds blocks l, l + 32,
@@ -544,7 +543,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
   // Sparse tiles: one pass over all records (below), which also flags the
   // (x, y) rows of 16 z cells that it touches; the write-out converts only
   // those and writes -mean elsewhere.  Dense tiles: every row is flagged.
-  const bool sparse = (S >= 3) && total <= kSparseRecords;
+  const bool sparse = (S >= 3) && total <= g.sparse_max;
   if (threadIdx.x < 16) rowmask[threadIdx.x >> 3][threadIdx.x & 7] = (sparse && TT == 16) ? 0u : ~0u;
   __syncthreads();
   if constexpr (S >= 3) {

@@ -40,6 +40,8 @@ struct GatherArgs {
   double* wpart;           // [2 * kAssignMaxBlocks]
   int* err;                // bit 0: particle outside [0, L)
   int threads;             // CTA size of the gather: 256, 512 or 0 (by density)
+  unsigned sparse_max;     // tiles with at most this many records: lane groups, rows flagged;
+                           // more: one record per warp (TSC/PCS)
 };
 int gather_tile(int ng);    // tile edge for this mesh size, 0 if unsupported
 size_t gather_keys(int ng);  // number of (tile, class) keys
