@@ -86,7 +86,7 @@ def build_cli():
     if _stale(CLI, deps):
         cmd = ["gcc", "-std=c99", "-O2", "-Wall", "-o", CLI] + srcs + [
             "-I" + os.path.join(ROOT, "include"), "-I" + HOST,
-            "-L" + HERE, "-lpowspec_gpu", "-Wl,-rpath,$ORIGIN", "-lm"]
+            "-L" + HERE, "-lpowspec_gpu", "-Wl,-rpath,$ORIGIN", "-lm", "-pthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             raise RuntimeError(f"host CLI build failed:\n{r.stderr}")

@@ -324,6 +324,10 @@ double psh_expr_eval(const psh_expr *e, const double *col) {
   return r;
 }
 
+int psh_expr_column(const psh_expr *e) {
+  return (e && e->n == 1 && e->ins[0].op == OP_COL) ? e->ins[0].col : -1;
+}
+
 void psh_expr_free(psh_expr *e) {
   if (!e) return;
   free(e->ins);

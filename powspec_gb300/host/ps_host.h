@@ -4,7 +4,8 @@
  * Keeps powspec's interface for the simulation-box case: the configuration
  * file keywords and command-line options (src/load_conf.c:366-417), the ASCII
  * catalogue reader's formatter / column / expression semantics
- * (io/read_ascii.c), and the output file format (src/save_res.c:35-229).
+ * (io/read_ascii.c) -- plus NumPy .npy catalogues -- and the output file
+ * format (src/save_res.c:35-229).
  * The estimator itself runs through the C ABI of include/powspec_gpu.h.
  */
 #ifndef PS_HOST_H
@@ -60,19 +61,29 @@ typedef struct psh_expr psh_expr;
 psh_expr *psh_expr_compile(const char *src, int *maxcol, char *err, size_t errlen);
 double psh_expr_eval(const psh_expr *e, const double *col);
 void psh_expr_free(psh_expr *e);
+/* The 0-based column an expression is made of alone ($n), else -1. */
+int psh_expr_column(const psh_expr *e);
 
-/* ---- ASCII catalogues ---- */
+/* ---- catalogues ---- */
 typedef struct {
   const char *fname;
-  long skip;
-  char comment;       /* '\0': no comment lines */
-  const char *fmtr;   /* scanf-style formatter */
+  long skip;          /* ASCII: header lines dropped */
+  char comment;       /* ASCII: '\0': no comment lines */
+  const char *fmtr;   /* ASCII: scanf-style formatter */
   const char *pos[3];
   const char *wcomp;  /* NULL: unit weights */
   const char *sel;    /* NULL: no selection */
-} psh_ascii;
+  int nthread;        /* host threads; 0: OMP_NUM_THREADS, else the online cores */
+} psh_catalog;
 
-/* Reads the catalogue into *xyzw ({x, y, z, w} records), sets *n and *wsum. */
-int psh_read_ascii(const psh_ascii *in, double **xyzw, size_t *n, double *wsum, bool verbose);
+/* Reads an ASCII catalogue (DATA_FORMAT = 0) into *xyzw ({x, y, z, w}
+ * records in file order), sets *n and *wsum. */
+int psh_read_ascii(const psh_catalog *in, double **xyzw, size_t *n, double *wsum, bool verbose);
+/* Reads a NumPy .npy array (DATA_FORMAT = 2): 1-D or 2-D, f4 / f8 / i4 / i8
+ * of either byte order, C or Fortran order; the columns of a row are $1,
+ * $2, ... of the expressions.  skip, comment and fmtr are not used. */
+int psh_read_npy(const psh_catalog *in, double **xyzw, size_t *n, double *wsum, bool verbose);
+/* Decimal string to double with strtod's syntax and correct rounding. */
+double psh_strtod(const char *s, char **end);
 
 #endif

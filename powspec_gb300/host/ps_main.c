@@ -7,7 +7,9 @@
  * meshes and evaluate the power spectrum multipoles, save the results
  * (src/save_res.c:35-229, same header lines, columns and number formats).
  * Survey geometries (CUBIC_SIM = F: randoms, coordinate conversion) and FITS
- * catalogues are outside this program and rejected with an error.
+ * catalogues are outside this program and rejected with an error.  Besides
+ * ASCII (DATA_FORMAT = 0), DATA_FORMAT = 2 reads NumPy .npy arrays, whose
+ * columns take the same position / weight / selection expressions.
  */
 #define _POSIX_C_SOURCE 200809L
 #include <math.h>
@@ -24,6 +26,7 @@
 typedef struct {
   bool issim, intlace, logscale, oheader, verbose, isauto[2], iscross;
   int ndata, gsize, assign, npole, poles[7];
+  int dfmt[2];  /* DATA_FORMAT: 0 ASCII, 2 NumPy .npy */
   long ovwrite;
   double bsize[3], los[3], kmin, kmax, kbin;
   const char *oauto[2], *ocross;
@@ -129,16 +132,21 @@ static int verify(psh_cfg *cfg, Conf *c) {
   for (int i = 0; i < c->ndata; i++) {
     long t = 0;
     if (psh_int(cfg, "DATA_FORMAT", i, &t) < 0) return PSH_ERR_CFG;
-    if (t != 0) {
-      fprintf(stderr, "Error: only ASCII catalogues (DATA_FORMAT = 0) are supported\n");
+    if (t == 1) {
+      fprintf(stderr, "Error: FITS format is not enabled\n");
       return PSH_ERR_CFG;
     }
+    if (t != 0 && t != 2) {
+      fprintf(stderr, "Error: invalid `DATA_FORMAT': %ld (0: ASCII, 2: NumPy .npy)\n", t);
+      return PSH_ERR_CFG;
+    }
+    c->dfmt[i] = (int)t;
     const char *fn = psh_str(cfg, "DATA_CATALOG", i);
     if (access(fn, R_OK)) {
       fprintf(stderr, "Error: cannot access `DATA_CATALOG': `%s'\n", fn);
       return PSH_ERR_FILE;
     }
-    if (psh_size(cfg, "DATA_FORMATTER") <= i) {
+    if (t == 0 && psh_size(cfg, "DATA_FORMATTER") <= i) {
       fprintf(stderr, "Error: %s of `DATA_FORMATTER'\n",
               psh_size(cfg, "DATA_FORMATTER") ? "too few elements" : "not set");
       return PSH_ERR_CFG;
@@ -378,7 +386,7 @@ int main(int argc, char **argv) {
   size_t ndata[2] = {0, 0};
   double wsum[2] = {0, 0};
   for (int i = 0; i < c.ndata && !rc; i++) {
-    psh_ascii in;
+    psh_catalog in;
     memset(&in, 0, sizeof in);
     in.fname = psh_str(&cfg, "DATA_CATALOG", i);
     long skip = 0;
@@ -395,7 +403,8 @@ int main(int argc, char **argv) {
     in.sel = psh_str(&cfg, "DATA_SELECTION", i);
     if (in.sel && !*in.sel) in.sel = NULL;
     if (in.wcomp && !*in.wcomp) in.wcomp = NULL;
-    rc = psh_read_ascii(&in, &xyzw[i], &ndata[i], &wsum[i], c.verbose);
+    rc = c.dfmt[i] == 2 ? psh_read_npy(&in, &xyzw[i], &ndata[i], &wsum[i], c.verbose)
+                        : psh_read_ascii(&in, &xyzw[i], &ndata[i], &wsum[i], c.verbose);
     if (!rc && ndata[i] == 0) {
       fprintf(stderr, "Error: no object read from `%s'\n", in.fname);
       rc = PSH_ERR_CATA;

@@ -83,6 +83,54 @@ def test_reader_formatter_expressions_selection(cli, workdir):
     assert "2 objects read from `d.txt'" in r.stdout, r.stdout + r.stderr
 
 
+@pytest.mark.parametrize("fmt,msg", [("1", "FITS format is not enabled"),
+                                     ("3", "invalid `DATA_FORMAT'")])
+def test_unsupported_formats(cli, workdir, fmt, msg):
+    r = run(cli, ["-c", "powspec.conf", "-a", "o.txt", "-f", fmt], workdir)
+    assert r.returncode != 0 and msg in r.stderr
+
+
+def _npy_catalogue(workdir):
+    a = np.loadtxt(workdir / "data.txt")
+    # Fortran order: one contiguous array per column; columns permuted so
+    # that the expressions differ from the ASCII run's
+    np.save(workdir / "data.npy", np.asfortranarray(a[:, [3, 0, 1, 2]]))
+    return a.shape[0]
+
+
+def test_npy_catalogue_is_read(cli, workdir):
+    n = _npy_catalogue(workdir)
+    r = run(cli, ["-c", "powspec.conf", "-d", "data.npy", "-f", "2", "-p", "[$2, $3, $4]",
+                  "--data-wt-comp=$1", "-a", "o.txt", "-v", "T"], workdir)
+    assert "%d objects read from `data.npy'" % n in r.stdout, r.stdout + r.stderr
+    r = run(cli, ["-c", "powspec.conf", "-d", "data.npy", "-f", "2", "-p", "[$2, $3, $5]",
+                  "-a", "o.txt"], workdir)
+    assert r.returncode != 0 and "column 5" in r.stderr
+
+
+@pytest.mark.gpu
+def test_npy_catalogue_gives_the_ascii_result(cli, workdir):
+    """The same values as .npy and as ASCII: the same output file."""
+    _npy_catalogue(workdir)
+    r = run(cli, ["-c", "powspec.conf", "-a", "a.txt"], workdir)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = run(cli, ["-c", "powspec.conf", "-d", "data.npy", "-f", "2", "-p", "[$2, $3, $4]",
+                  "--data-wt-comp=$1", "-a", "b.txt"], workdir)
+    assert r.returncode == 0, r.stdout + r.stderr
+    a = (workdir / "a.txt").read_text().splitlines()
+    b = (workdir / "b.txt").read_text().splitlines()
+    assert len(a) == len(b)
+    assert [l for l in a if l.startswith("#")] == [l for l in b if l.startswith("#")]
+    ra = [l.split() for l in a if not l.startswith("#")]
+    rb = [l.split() for l in b if not l.startswith("#")]
+    assert [x[:5] for x in ra] == [x[:5] for x in rb]  # k columns and mode counts
+    # P_l: the same mesh; FP32 binning sums may add in another order
+    pa = np.array([[float(v) for v in x[5:]] for x in ra])
+    pb = np.array([[float(v) for v in x[5:]] for x in rb])
+    shot = float(a[4].split("Shot noise:")[1].split(",")[0])
+    assert (np.abs(pa - pb) / (np.abs(pa[:, :1]) + shot)).max() <= 1e-6
+
+
 @pytest.mark.gpu
 def test_cli_output_matches_reference_file(cli, workdir):
     """Same catalogue and powspec.conf as the reference's run: header lines,
