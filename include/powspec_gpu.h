@@ -205,12 +205,17 @@ int ps_gpu_batch_launches(const ps_gpu_batch *batch);
 void ps_gpu_batch_destroy(ps_gpu_batch *batch);
 
 /* Autotuner (no counterpart in the reference): times the alternative launch
- * configurations on one catalogue -- gather CTA size and dense-tile mapping, radix-16 / radix-32
- * z and y passes, pipelined or plain last pass -- with `reps` evaluations
- * each, and keeps the fastest for the context.  choice[5] (if not NULL):
- * gather threads, z radix-32, y radix-32, pipelined pass C, lane groups on
- * dense tiles. */
+ * configurations on one catalogue -- region or tile gather, gather CTA size
+ * and dense-tile mapping, radix-16 / radix-32 z and y passes, pipelined or
+ * plain last pass -- with `reps` evaluations each, and keeps the fastest for
+ * the context.  choice[6] (if not NULL): gather threads, z radix-32,
+ * y radix-32, pipelined pass C, lane groups on dense tiles, region gather. */
 int ps_gpu_autotune(ps_gpu_ctx *ctx, const double *xyzw, size_t n, int reps, int *choice);
+/* Sets the configurations ps_gpu_autotune chooses (no counterpart in the
+ * reference), in its choice[6] order; -1 keeps an entry.  choice[5] = 2
+ * returns the region gather to its default: on when there is a particle
+ * for every 32 cells or more. */
+int ps_gpu_set_tuning(ps_gpu_ctx *ctx, const int *choice);
 
 #ifdef __cplusplus
 }

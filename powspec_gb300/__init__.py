@@ -36,7 +36,7 @@ EXPORTED = [
     "ps_gpu_fft_r2c_host", "ps_gpu_bin_fields_host", "ps_gpu_stream",
     "ps_gpu_set_mu_bins", "ps_gpu_read_kmu", "ps_gpu_bin_fields_noalloc",
     "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
-    "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune",
+    "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune", "ps_gpu_set_tuning",
 ]
 
 
@@ -170,6 +170,7 @@ def lib():
         L.ps_gpu_batch_destroy.restype = None
         L.ps_gpu_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                       ctypes.c_void_p]
+        L.ps_gpu_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -307,11 +308,23 @@ class Estimator:
     def autotune(self, device_ptr, n, reps=2):
         """Time the alternative launch configurations on one catalogue (device
         AoS float64 records) and keep the fastest; returns the choices."""
-        ch = np.zeros(5, np.int32)
+        ch = np.zeros(6, np.int32)
         self._check(lib().ps_gpu_autotune(self._ctx, ctypes.c_void_p(device_ptr), int(n), int(reps),
                                           _ptr(ch)))
         return dict(gather_threads=int(ch[0]), z_radix32=bool(ch[1]), y_radix32=bool(ch[2]),
-                    pipelined_pass_c=bool(ch[3]), dense_lane_groups=bool(ch[4]))
+                    pipelined_pass_c=bool(ch[3]), dense_lane_groups=bool(ch[4]),
+                    region_gather=bool(ch[5]))
+
+    def set_tuning(self, gather_threads=None, z_radix32=None, y_radix32=None,
+                   pipelined_pass_c=None, dense_lane_groups=None, region_gather=None):
+        """Sets launch configurations (the autotuner's choices; None keeps one).
+        region_gather: True, False, or "auto" (by particles per cell)."""
+        def v(x):
+            return -1 if x is None else int(x)
+        rg = -1 if region_gather is None else (2 if region_gather == "auto" else int(bool(region_gather)))
+        ch = np.array([v(gather_threads), v(z_radix32), v(y_radix32), v(pipelined_pass_c),
+                       v(dense_lane_groups), rg], np.int32)
+        self._check(lib().ps_gpu_set_tuning(self._ctx, _ptr(ch)))
 
     def batch(self, device_ptrs, ns):
         """A CUDA-graph batch of single-catalogue evaluations (see Batch)."""

@@ -130,6 +130,7 @@ struct ps_gpu_ctx {
   bool radix32_a = false;
   int gather_threads = 0;
   unsigned gather_sparse_max = 512;  // records per tile up to which lane groups are used
+  int gather_region = -1;  // region gather: 1 on, 0 off, -1 by density (TSC/PCS, 16^3 tiles)
   bool pipe_c_on = true;
   int ty_ct = 1, grid_ct = 0;  // pipelined pass C (grid 0: not available)
   int nmu = 1;               // |mu| sub-bins of the binning pass
@@ -138,6 +139,8 @@ struct ps_gpu_ctx {
   size_t nkeys = 0, gcap = 0;
   unsigned *d_hist = nullptr, *d_bsum = nullptr, *d_rank = nullptr;
   void* d_rec = nullptr;
+  unsigned long long* d_region = nullptr;  // region sums of the region gather
+  size_t region_bytes = 0;
   int last_cat = -1;
   Particles last_pt{};
   std::vector<double> kmu;   // last execute's raw (k, |mu|) sums
@@ -495,7 +498,7 @@ void ps_gpu_destroy(ps_gpu_ctx* c) {
   }
   void* bufs[] = {c->d_bintab, c->d_ksq, c->d_win, c->d_phase, c->d_tw_full, c->d_tw_half,
                   c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage,
-                  c->d_hist, c->d_bsum, c->d_rank, c->d_rec};
+                  c->d_hist, c->d_bsum, c->d_rank, c->d_rec, c->d_region};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -537,7 +540,37 @@ int ensure_stage(ps_gpu_ctx* c, size_t bytes) {
   return 0;
 }
 
-GatherArgs gather_args(ps_gpu_ctx* c, int cat) {
+// Region buffer of the region gather: every tile's regions.
+size_t region_words(const ps_gpu_ctx* c) {
+  return (size_t)c->gnt * c->gnt * c->gnt * (size_t)c->mpc * gather_region_words(c->p.assign);
+}
+size_t region_need(const ps_gpu_ctx* c) {  // region words, then a flag byte per tile
+  return region_words(c) * sizeof(unsigned long long) + (size_t)c->gnt * c->gnt * c->gnt;
+}
+
+// The region gather for a catalogue of n particles: forced on or off by the
+// tuning knob, else when there is a particle for every 32 cells or more (its
+// cost is the region traffic, 2.3x the mesh in int64, whatever the count;
+// the tile gather's grows with the particles and their halo replays).
+bool use_region(const ps_gpu_ctx* c, size_t n) {
+  if (!gather_region_ok(c->ng, c->gT, c->p.assign)) return false;
+  if (c->gather_region >= 0) return c->gather_region == 1;
+  return (double)n * 32.0 >= (double)c->ntot && region_need(c) <= ((size_t)64 << 30);
+}
+
+int ensure_region(ps_gpu_ctx* c) {
+  const size_t need = region_need(c);
+  if (need <= c->region_bytes) return 0;
+  CU(cudaStreamSynchronize(c->stream));
+  if (c->d_region) cudaFree(c->d_region);
+  c->d_region = nullptr;
+  c->region_bytes = 0;
+  CU(cudaMalloc(&c->d_region, need));
+  c->region_bytes = need;
+  return 0;
+}
+
+GatherArgs gather_args(ps_gpu_ctx* c, int cat, size_t n) {
   GatherArgs g{};
   g.ng = c->ng;
   g.assign = c->p.assign;
@@ -565,6 +598,9 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat) {
   g.err = c->d_err + cat;
   g.threads = c->gather_threads;
   g.sparse_max = c->gather_sparse_max;
+  g.region = use_region(c, n) ? 1 : 0;
+  g.regbuf = c->d_region;
+  g.regflag = c->d_region ? reinterpret_cast<unsigned char*>(c->d_region + region_words(c)) : nullptr;
   return g;
 }
 
@@ -594,12 +630,13 @@ int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
     c->launches = 0;
   }
   {
-    const int rc = ensure_gather_capacity(c, pt.n);
+    int rc = ensure_gather_capacity(c, pt.n);
+    if (!rc && use_region(c, pt.n)) rc = ensure_region(c);
     if (rc) return rc;
   }
   CU(cudaMemsetAsync(c->d_wsum + 2 * cat, 0, sizeof(double) * 2, c->stream));
   CU(cudaMemsetAsync(c->d_err + cat, 0, sizeof(int), c->stream));
-  if (pt.n) c->launches += launch_gather_assign(pt, gather_args(c, cat), c->stream, false);
+  if (pt.n) c->launches += launch_gather_assign(pt, gather_args(c, cat, pt.n), c->stream, false);
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[7], c->stream));
   c->assigned[cat] = 1;
@@ -711,6 +748,7 @@ int finish(ps_gpu_ctx* c, const double* h, const size_t* npart, ps_gpu_result* r
   for (int k = 0; k < p.ncat; k++) {
     // an empty catalogue has no coordinate range (src/genr_mesh.c:518-521)
     if (!npart[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: no objects", k);
+    if (errs[k] & 2) return fail(c, PS_GPU_ERR_CUDA, "catalogue %d: region index out of range", k);
     if (errs[k]) return fail(c, PS_GPU_ERR_CATA, "catalogue %d: coordinate outside [0, BOX_SIZE)", k);
     if (!(wsum[2 * k + 1] < kFixMaxWeight))
       return fail(c, PS_GPU_ERR_RANGE, "catalogue %d: total |weight| %g exceeds the fixed-point range", k, wsum[2 * k + 1]);
@@ -890,7 +928,7 @@ int ps_gpu_read_mesh(ps_gpu_ctx* c, int cat, int m, double* out) {
   CU(cudaSetDevice(c->p.device));
   long long* tmp = nullptr;
   CU(cudaMalloc(&tmp, c->ntot * sizeof(long long) * c->mpc));
-  GatherArgs g = gather_args(c, cat);
+  GatherArgs g = gather_args(c, cat, c->last_pt.n);
   for (int k = 0; k < c->mpc; k++) g.out64[k] = tmp + (size_t)k * c->ntot;
   launch_gather_assign(c->last_pt, g, c->stream, true);
   std::vector<long long> q(c->ntot);
@@ -1023,7 +1061,7 @@ int batch_enqueue(ps_gpu_ctx* c, ps_gpu_batch* b, int i, const double* xyzw) {
     Particles pt{};
     pt.aos = xyzw;
     pt.n = b->n[i];
-    b->launches += launch_gather_assign(pt, gather_args(c, 0), s, false);
+    b->launches += launch_gather_assign(pt, gather_args(c, 0, pt.n), s, false);
   }
   CU(cudaGetLastError());
   const int launches0 = c->launches;
@@ -1055,6 +1093,8 @@ int ps_gpu_batch_create(ps_gpu_ctx* c, int ncat, const double* const* xyzw, cons
   }
   CU(cudaSetDevice(c->p.device));
   int rc = ensure_gather_capacity(c, nmax);
+  for (int i = 0; i < ncat && !rc; i++)
+    if (n[i] && use_region(c, n[i])) rc = ensure_region(c);
   if (rc) return rc;
   ps_gpu_batch* b = new ps_gpu_batch;
   b->c = c;
@@ -1130,6 +1170,22 @@ void ps_gpu_batch_destroy(ps_gpu_batch* b) {
 
 // ---- autotuner ----------------------------------------------------------
 
+int ps_gpu_set_tuning(ps_gpu_ctx* c, const int* choice) {
+  if (!c || !choice) return fail(c, PS_GPU_ERR_ARG, "invalid set_tuning arguments");
+  if (choice[0] != -1 && choice[0] != 0 && choice[0] != 256 && choice[0] != 512)
+    return fail(c, PS_GPU_ERR_ARG, "gather threads: 0 (by density), 256 or 512");
+  CU(cudaSetDevice(c->p.device));
+  CU(cudaStreamSynchronize(c->stream));
+  if (choice[0] >= 0) c->gather_threads = choice[0];
+  if (choice[1] >= 0) c->radix32_a = choice[1] != 0;
+  if (choice[2] >= 0) c->radix32_b = choice[2] != 0;
+  if (choice[3] >= 0) c->pipe_c_on = choice[3] != 0;
+  if (choice[4] >= 0) c->gather_sparse_max = choice[4] ? 0xffffffffu : 512u;
+  if (choice[5] >= 0) c->gather_region = choice[5] >= 2 ? -1 : choice[5];
+  plan_pipes(c);
+  return 0;
+}
+
 int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* choice) {
   if (!c || !xyzw || !n || reps < 1) return fail(c, PS_GPU_ERR_ARG, "invalid autotune arguments");
   if (c->p.ncat != 1) return fail(c, PS_GPU_ERR_ARG, "autotune needs a single-catalogue context");
@@ -1160,6 +1216,18 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
       if (t[0] < best) { best = t[0]; arg = cand[k]; }
     }
     c->gather_threads = arg;
+  }
+  // region gather or tile gather (phase 0), where the region buffer is
+  // at most 16 GB
+  if (gather_region_ok(c->ng, c->gT, c->p.assign) && region_need(c) <= ((size_t)16 << 30)) {
+    float best = 1e30f;
+    int arg = c->gather_region;
+    for (int k = 0; k < 2; k++) {
+      c->gather_region = k;
+      if ((rc = measure(t))) return rc;
+      if (t[0] < best) { best = t[0]; arg = k; }
+    }
+    c->gather_region = arg;
   }
   // dense tiles: one record per warp or lane groups (phase 0)
   {
@@ -1197,6 +1265,7 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
     choice[1] = c->radix32_a;
     choice[2] = c->radix32_b;
     choice[3] = c->pipe_c_on;
+    choice[5] = use_region(c, n) ? 1 : 0;
   }
   return 0;
 }

@@ -69,7 +69,7 @@ static_assert(sizeof(Rec) == 48, "record layout");
 // weights per mesh and axis, with weight * 2^32 folded into the x weights.
 struct __align__(16) WRec {
   float w[2][3][4];   // [mesh][axis][node]
-  short base[2][4];   // [mesh][axis]; [mesh][3] = 1: every node value |v| < 2^31
+  short base[2][4];   // [mesh][axis]; [mesh][3]: node value bound (k_scatter)
 };
 static_assert(sizeof(WRec) == 112, "weighted record layout");
 constexpr size_t kRecBytes = 112;  // room for either record kind
@@ -339,6 +339,22 @@ __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ Gather
   if (bad) atomicOr(g.err, 1);
 }
 
+// Region geometry of the region gather (kernels below): R cells per axis
+// cover every node a home tile's records reach, local cells [of - 1, T + of
+// + S - 1]; shared-memory z rows are padded to RZ words.
+constexpr int kRegT = 16;
+constexpr int kRegDepth = 8;  // records in flight per warp (shared-memory ring)
+constexpr int reg_row(int r) { return (r % 16 == 4 || r % 16 == 12) ? r : reg_row(r + 1); }
+template <int S>
+struct RegGeom {
+  static constexpr int R = kRegT + S + 1;  // region edge (cells)
+  static constexpr int RP = (R * R * R + 1) & ~1;  // words per mesh in memory, even (16-byte rows)
+  // Shared-memory z rows padded to RZ = 4 or 12 (mod 16) words: the 4 x 4
+  // (y, z) nodes of a mesh then fall in 16 distinct 8-byte bank pairs.
+  static constexpr int RZ = reg_row(R);
+  static constexpr int SM = (R * R * RZ + 1) & ~1;  // shared words per mesh
+};
+
 __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ GatherArgs g, Particles p) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -366,13 +382,37 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ GatherA
           for (int k = 0; k < 4; k++) v.w[m][a][k] = (a == 0) ? w[k] * r.wf : w[k];
           v.base[m][a] = r.base[m][a];
         }
+        if (g.region) {
+          // Region word offset of the first node: region index = base -
+          // home tile origin + 1 per axis, wrapped into [0, T + 1] (the
+          // shifted grid's base may sit one cell outside the home tile,
+          // across the periodic edge).
+          int l[3];
+#pragma unroll
+          for (int a = 0; a < 3; a++) {
+            l[a] = (int)r.base[m][a] - ((int)r.base[0][a] / g.T) * g.T + 1;
+            l[a] += (l[a] < 0) ? g.ng : 0;
+            l[a] -= (l[a] > g.T + 1) ? g.ng : 0;
+            if (l[a] < 0 || l[a] > g.T + 1) {  // the grids' bases differ by at most a cell
+              atomicOr(g.err, 2);
+              l[a] = 0;
+            }
+          }
+          const int R = (g.assign == 2) ? RegGeom<3>::R : RegGeom<4>::R;
+          const int RZ = (g.assign == 2) ? RegGeom<3>::RZ : RegGeom<4>::RZ;
+          v.base[m][0] = (short)((l[0] * R + l[1]) * RZ + l[2]);
+          v.base[m][1] = v.base[m][2] = 0;
+        }
         // bound of every node value of this mesh: product of the axis maxima
         float bound = 1.f;
 #pragma unroll
         for (int a = 0; a < 3; a++)
           bound *= fmaxf(fmaxf(fabsf(v.w[m][a][0]), fabsf(v.w[m][a][1])),
                          fmaxf(fabsf(v.w[m][a][2]), fabsf(v.w[m][a][3])));
-        v.base[m][3] = bound < 0.999f * 2147483648.f ? 1 : 0;
+        // [mesh][3]: bit 8 set when every node value is below 2^31 (one
+        // 32-bit conversion); bits 0-7 the least e >= 0 with bound < 2^e
+        const int e = max(0, ((__float_as_int(bound) >> 23) & 0xff) - 126);
+        v.base[m][3] = (short)((bound < 0.999f * 2147483648.f ? 0x100 : 0) | min(e, 255));
       }
       reinterpret_cast<WRec*>(g.rec)[slot] = v;
     } else {
@@ -581,18 +621,20 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
       }
       if (kz >= S || (unsigned)lz >= (unsigned)T) continue;
       unsigned long long* A = acc + m * (T3 + kMeshPad);
+      // node value wx * (wy * wz), in the order of the other mappings, so
+      // that the mesh does not depend on which one runs
+      const float wyz[4] = {wys[0] * wz, wys[1] * wz, wys[2] * wz, wys[3] * wz};
 #pragma unroll
       for (int x = 0; x < S; x++) {
         const int lx = sx + x;
         if ((unsigned)lx >= (unsigned)T) continue;
-        const float wxz = wxs[x] * wz;
 #pragma unroll
         for (int y = 0; y < S; y++) {
           const int ly = sy + y;
           if ((unsigned)ly >= (unsigned)T) continue;
           const int col = kSwz ? (lz ^ ((ly & 3) << 2)) : lz;
-          const float v = wxz * wys[y];
-          const long long q = bs.w ? round_small(v) : round_fix(v);
+          const float v = wxs[x] * wyz[y];
+          const long long q = (bs.w & 0x100) ? round_small(v) : round_fix(v);
           atomicAdd(&A[(lx * T + ly) * T + col], (unsigned long long)q);
         }
       }
@@ -623,7 +665,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
       L.b0 = bs.x;
       L.b1 = bs.y;
       L.b2 = bs.z;
-      L.small = bs.w;
+      L.small = bs.w & 0x100;
       return L;
     };
     int b = 0;
@@ -759,7 +801,295 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
   }
 }
 
+// 16-byte asynchronous copy global -> shared (one group per commit).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// ---- region gather.  One CTA per home tile (the tile of the plain grid's
+// base node): each record is added once, into shared-memory accumulators
+// that cover every node its stencils reach, local cells [of - 1, T + of +
+// S - 1] per axis.  The regions are written out and k_region_sum adds, for
+// each cell, the up to 8 regions that cover it.  The integer sums are the
+// tile gather's, so the mesh is the same to the bit.
+template <int S, int NM>
+__global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const __grid_constant__ GatherArgs g) {
+  constexpr int R = RegGeom<S>::R, RP = RegGeom<S>::RP, RZ = RegGeom<S>::RZ, SM = RegGeom<S>::SM;
+  // 64-bit path: acc[NM][SM].  Split path, the same bytes as 32-bit words:
+  // the node values q mod 2^32 summed at [c * NM + m], q >> 16 summed at
+  // HW + [c * NM + m] (meshes interleaved: with two meshes the half-warps
+  // use even and odd banks).
+  extern __shared__ __align__(16) unsigned long long acc[];
+  constexpr int HW = NM * R * R * RZ;
+  unsigned* const w32 = reinterpret_cast<unsigned*>(acc);
+  __shared__ float bound_sum[2];
+  const int nt = g.nt;
+  const unsigned tile = ((unsigned)blockIdx.z * nt + blockIdx.y) * nt + blockIdx.x;
+  const unsigned beg = g.hist[tile * 27u], end = g.hist[tile * 27u + 27u];
+  if (beg == end) {  // k_region_sum skips tiles without records
+    if (threadIdx.x == 0) g.regflag[tile] = 0;
+    return;
+  }
+  // Lane = (mesh, y node, z node) with two meshes, (record of a pair, y
+  // node, z node) with one; each lane loops over the x nodes.
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int half = lane >> 4, yy = (lane >> 2) & 3, zz = lane & 3;
+  const int m = (NM == 2) ? half : 0;
+  const bool act = yy < S && zz < S;
+  struct Ld {
+    float4 wx;
+    float wy, wz;
+    short4 bs;
+  };
+  // This warp's records, kRegDepth steps in flight.  A step is P records
+  // (one with two meshes; with one mesh the half-warps take one each), each
+  // copied as 7 x 16 bytes with cp.async into the warp's ring slot, one
+  // group per step; step k is read once the groups up to k have landed.
+  constexpr int P = (NM == 2) ? 1 : 2;
+  unsigned char* const ring =
+      reinterpret_cast<unsigned char*>(acc + NM * SM) + warp * (kRegDepth * P * sizeof(WRec));
+  auto records = [&](auto&& proc) {
+    const unsigned w0 = beg + (unsigned)(warp * P), step = (unsigned)(nw * P);
+    const unsigned K = (w0 < end) ? (end - w0 + step - 1) / step : 0u;
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(g.rec);
+    auto issue = [&](unsigned k) {
+      if (k < K && lane < 7 * P) {
+        const int sub = lane / 7, part = lane - 7 * sub;
+        const unsigned i = w0 + k * step + (unsigned)sub;
+        if (i < end)
+          cp_async16(ring + ((k % kRegDepth) * P + sub) * sizeof(WRec) + part * 16,
+                     src + (size_t)i * sizeof(WRec) + part * 16);
+      }
+      cp_async_commit();
+    };
+    for (unsigned k = 0; k + 1 < (unsigned)kRegDepth; k++) issue(k);
+    for (unsigned k = 0; k < K; k++) {
+      __syncwarp();  // the slot refilled next was read in step k - 1
+      issue(k + kRegDepth - 1);
+      cp_async_wait<kRegDepth - 1>();
+      __syncwarp();  // every lane's part of step k has landed
+      const int sub = (P == 2) ? half : 0;
+      if (w0 + k * step + (unsigned)sub < end) {
+        const unsigned char* rp = ring + ((k % kRegDepth) * P + sub) * sizeof(WRec);
+        Ld L;
+        L.wx = *reinterpret_cast<const float4*>(rp + m * 48);
+        L.wy = *reinterpret_cast<const float*>(rp + m * 48 + 16 + yy * 4);
+        L.wz = *reinterpret_cast<const float*>(rp + m * 48 + 32 + zz * 4);
+        L.bs = *reinterpret_cast<const short4*>(rp + 96 + m * 8);
+        proc(L);
+      }
+    }
+    cp_async_wait<0>();
+    __syncwarp();
+  };
+  auto zero = [&]() {
+    ulonglong2* a2 = reinterpret_cast<ulonglong2*>(acc);
+    for (int e = threadIdx.x; e < NM * SM / 2; e += blockDim.x) a2[e] = make_ulonglong2(0ull, 0ull);
+  };
+  // Split path.  With q = 2^16 h + l (0 <= l < 2^16), H = sum h and
+  // L = sum l: at most 65535 records put at most 65535 terms in a cell, so
+  // 0 <= L < 2^32 and L = (sum q - 2^16 H) mod 2^32; with the records'
+  // bounds summing below 2^46, H fits in int32.  The cell value is then
+  // 2^16 H + L exactly.  A tile past the bound sum is redone below.
+  bool split = end - beg <= 65535u;
+  if (split) {
+    zero();
+    if (threadIdx.x < 2) bound_sum[threadIdx.x] = 0.f;
+    __syncthreads();
+    float bsum = 0.f;
+    const int lbase = (yy * RZ + zz) * NM + m;
+    auto proc = [&](const Ld& cur) {
+      if (!act) return;
+      bsum += __int_as_float((min(cur.bs.w & 0xff, 127) + 127) << 23);
+      unsigned* A = w32 + lbase + cur.bs.x * NM;
+      const float wyz = cur.wy * cur.wz;
+      const float wxs[4] = {cur.wx.x, cur.wx.y, cur.wx.z, cur.wx.w};
+      if (cur.bs.w & 0x100) {
+#pragma unroll
+        for (int x = 0; x < S; x++) {
+          const int q = __float2int_rn(wxs[x] * wyz);
+          atomicAdd(A + x * R * RZ * NM, (unsigned)q);
+          atomicAdd(reinterpret_cast<int*>(A + HW) + x * R * RZ * NM, q >> 16);
+        }
+      } else {
+#pragma unroll
+        for (int x = 0; x < S; x++) {
+          const long long q = round_fix(wxs[x] * wyz);
+          atomicAdd(A + x * R * RZ * NM, (unsigned)q);
+          atomicAdd(reinterpret_cast<int*>(A + HW) + x * R * RZ * NM, (int)(q >> 16));
+        }
+      }
+    };
+    records(proc);
+    if (lane == 0 || lane == 16) atomicAdd(&bound_sum[(NM == 2) ? half : 0], bsum);
+    __syncthreads();
+    split = bound_sum[0] < 70368744177664.f && bound_sum[1] < 70368744177664.f;  // 2^46
+    if (split) {
+      // one z row per warp and step, out without the padding: [NM][R][R][R]
+      unsigned long long* o = g.regbuf + (size_t)tile * NM * RP;
+      for (int rw = warp; rw < NM * R * R; rw += nw) {
+        const int mm = rw / (R * R), row = rw - mm * (R * R);
+        if (lane < R) {
+          const int w = (row * RZ + lane) * NM + mm;
+          const int h = (int)w32[HW + w];
+          const unsigned l = w32[w] - ((unsigned)h << 16);
+          o[(size_t)mm * RP + row * R + lane] = (unsigned long long)(((long long)h << 16) + (long long)l);
+        }
+      }
+      if (threadIdx.x == 0) g.regflag[tile] = 1;
+      return;
+    }
+    __syncthreads();  // every thread has read the bound sums
+  }
+  // 64-bit path
+  zero();
+  __syncthreads();
+  {
+    const int lofs = m * SM + yy * RZ + zz;
+    auto proc = [&](const Ld& cur) {
+      if (!act) return;
+      unsigned long long* A = acc + lofs + cur.bs.x;
+      const float wyz = cur.wy * cur.wz;
+      const float wxs[4] = {cur.wx.x, cur.wx.y, cur.wx.z, cur.wx.w};
+      if (cur.bs.w & 0x100) {
+#pragma unroll
+        for (int x = 0; x < S; x++)
+          atomicAdd(A + x * R * RZ, (unsigned long long)round_small(wxs[x] * wyz));
+      } else {
+#pragma unroll
+        for (int x = 0; x < S; x++)
+          atomicAdd(A + x * R * RZ, (unsigned long long)round_fix(wxs[x] * wyz));
+      }
+    };
+    records(proc);
+  }
+  __syncthreads();
+  // out without the row padding: [NM][R][R][R] (+1 word to keep RP even)
+  unsigned long long* o = g.regbuf + (size_t)tile * NM * RP;
+  for (int rw = warp; rw < NM * R * R; rw += nw) {
+    const int mm = rw / (R * R), row = rw - mm * (R * R);
+    if (lane < R) o[(size_t)mm * RP + row * R + lane] = acc[mm * SM + row * RZ + lane];
+  }
+  if (threadIdx.x == 0) g.regflag[tile] = 1;
+}
+
+// Regions covering cell c along one axis: the home tile t0 = c / T at
+// region index u - of + 1 (u = c - t0 T), the tile before for u < S + of,
+// the tile after for u >= T + of - 1 (never both: S < T).
+template <int S>
+__device__ __forceinline__ int region_sources(int c, int nt, int* t, int* idx) {
+  constexpr int T = kRegT, of = (S >= 3) ? -1 : 0;
+  const int t0 = c / T, u = c - t0 * T;
+  t[0] = t0;
+  idx[0] = u - of + 1;
+  if (u < S + of) {
+    t[1] = (t0 == 0) ? nt - 1 : t0 - 1;
+    idx[1] = u + T - of + 1;
+    return 2;
+  }
+  if (u >= T + of - 1) {
+    t[1] = (t0 == nt - 1) ? 0 : t0 + 1;
+    idx[1] = u - T - of + 1;
+    return 2;
+  }
+  return 1;
+}
+
+// Mesh from the regions: 4 consecutive z cells per thread, the FP32 value
+// minus the mean cell value (or the exact fixed-point sum).
+template <int S, bool INT64>
+__global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ GatherArgs g) {
+  constexpr int T = kRegT, R = RegGeom<S>::R, RP = RegGeom<S>::RP, of = (S >= 3) ? -1 : 0;
+  const int ng = g.ng, nt = g.nt, nm = g.interlace ? 2 : 1, nq = ng >> 2;
+  const size_t per = (size_t)ng * ng * nq;
+  const long long off = INT64 ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < (size_t)nm * per;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int m = (int)(e / per);
+    size_t r = e - (size_t)m * per;
+    const int zq = (int)(r % (size_t)nq);
+    r /= (size_t)nq;
+    const int y = (int)(r % (size_t)ng), x = (int)(r / (size_t)ng);
+    int tx[2], ix[2], ty[2], iy[2];
+    const int nx = region_sources<S>(x, nt, tx, ix), ny = region_sources<S>(y, nt, ty, iy);
+    const int z0 = 4 * zq, tz0 = z0 / T, uz = z0 - tz0 * T;
+    const int tzp = (tz0 == 0) ? nt - 1 : tz0 - 1, tzn = (tz0 == nt - 1) ? 0 : tz0 + 1;
+    long long s[4] = {0, 0, 0, 0};
+    // a tile without records wrote neither its region nor a flag of 1: its
+    // words are read (in flight with the flag) and dropped
+    for (int a = 0; a < nx; a++)
+      for (int b = 0; b < ny; b++) {
+        const unsigned tb = ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt;
+        const int row = (ix[a] * R + iy[b]) * R;
+        auto at = [&](unsigned t, int iz) {
+          return (long long)g.regbuf[((size_t)t * nm + m) * RP + row + iz];
+        };
+        {
+          const unsigned t = tb + tz0;
+          const bool f = g.regflag[t] != 0;
+          long long v[4];
+#pragma unroll
+          for (int k = 0; k < 4; k++) v[k] = at(t, uz + k - of + 1);
+#pragma unroll
+          for (int k = 0; k < 4; k++) s[k] += f ? v[k] : 0;
+        }
+        if (uz < S + of) {
+          const unsigned t = tb + tzp;
+          const bool f = g.regflag[t] != 0;
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if (uz + k < S + of) {
+              const long long v = at(t, uz + k + T - of + 1);
+              s[k] += f ? v : 0;
+            }
+        }
+        if (uz + 3 >= T + of - 1) {
+          const unsigned t = tb + tzn;
+          const bool f = g.regflag[t] != 0;
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if (uz + k >= T + of - 1) {
+              const long long v = at(t, uz + k - T - of + 1);
+              s[k] += f ? v : 0;
+            }
+        }
+      }
+    const size_t cell = ((size_t)x * ng + y) * ng + z0;
+    if (INT64) {
+      longlong2* o = reinterpret_cast<longlong2*>(g.out64[m] + cell);
+      o[0] = make_longlong2(s[0], s[1]);
+      o[1] = make_longlong2(s[2], s[3]);
+    } else {
+      *reinterpret_cast<float4*>(g.out[m] + cell) =
+          make_float4(fix_to_float(s[0] - off), fix_to_float(s[1] - off),
+                      fix_to_float(s[2] - off), fix_to_float(s[3] - off));
+    }
+  }
+}
+
 }  // namespace
+
+bool gather_region_ok(int ng, int T, int assign) {
+  return assign >= 2 && T == kRegT && ng >= kRegT + width(assign) + 1;
+}
+
+size_t gather_region_words(int assign) {
+  return assign == 2 ? (size_t)RegGeom<3>::RP : (size_t)RegGeom<4>::RP;
+}
+
+size_t gather_region_smem(int assign, int interlace) {
+  // accumulators + one record ring per warp (1024 threads with two meshes,
+  // 512 with one; P records per ring slot)
+  const size_t acc = (size_t)(interlace ? 2 : 1) * (assign == 2 ? RegGeom<3>::SM : RegGeom<4>::SM) *
+                     sizeof(unsigned long long);
+  return acc + (size_t)(interlace ? 32 : 16) * kRegDepth * (interlace ? 1 : 2) * sizeof(WRec);
+}
 
 int gather_tile(int ng) {
   int best = 0;
@@ -796,6 +1126,34 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
     n += 3;
     k_scatter<<<(unsigned)blocks, 256, 0, s>>>(g, p);
     n++;
+  }
+  if (g.region) {
+    const dim3 ntile((unsigned)g.nt, (unsigned)g.nt, (unsigned)g.nt);
+    const int nm = g.interlace ? 2 : 1;
+    const size_t smem = gather_region_smem(g.assign, g.interlace);
+    const size_t work = (size_t)nm * g.ng * g.ng * (g.ng / 4);
+    const unsigned sblocks = (unsigned)((work + 255) / 256 < 152 * 16 ? (work + 255) / 256 : 152 * 16);
+#define PS_REGION(SS)                                                                          \
+  if (nm == 2) {                                                                               \
+    cudaFuncSetAttribute(k_gather_region<SS, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                         (int)smem);                                                           \
+    k_gather_region<SS, 2><<<ntile, 1024, smem, s>>>(g);                                       \
+  } else {                                                                                     \
+    cudaFuncSetAttribute(k_gather_region<SS, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                         (int)smem);                                                           \
+    k_gather_region<SS, 1><<<ntile, 512, smem, s>>>(g);                                        \
+  }                                                                                            \
+  if (int64_out)                                                                               \
+    k_region_sum<SS, true><<<sblocks, 256, 0, s>>>(g);                                         \
+  else                                                                                         \
+    k_region_sum<SS, false><<<sblocks, 256, 0, s>>>(g);
+    if (g.assign == 2) {
+      PS_REGION(3)
+    } else {
+      PS_REGION(4)
+    }
+#undef PS_REGION
+    return n + 2;
   }
   const int T = g.T;
   const size_t smem = (size_t)(g.interlace ? 2 : 1) * (T * T * T + kMeshPad) * sizeof(unsigned long long);

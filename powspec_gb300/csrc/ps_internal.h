@@ -38,12 +38,19 @@ struct GatherArgs {
   long long* out64[2];     // or exact fixed-point meshes (diagnostics)
   double* wsum;            // [2]
   double* wpart;           // [2 * kAssignMaxBlocks]
-  int* err;                // bit 0: particle outside [0, L)
+  int* err;                // bit 0: particle outside [0, L); bit 1: region index out of range
   int threads;             // CTA size of the gather: 256, 512 or 0 (by density)
   unsigned sparse_max;     // tiles with at most this many records: lane groups, rows flagged;
                            // more: one record per warp (TSC/PCS)
+  int region;              // 1: each record once, into its home tile's region (TSC/PCS, T = 16)
+  unsigned long long* regbuf;  // [tiles][meshes][gather_region_words()] region sums
+  unsigned char* regflag;      // [tiles] 1: the tile wrote its region (it has records)
 };
 int gather_tile(int ng);    // tile edge for this mesh size, 0 if unsupported
+// Region path: possible for this mesh and scheme; words per tile and mesh.
+bool gather_region_ok(int ng, int T, int assign);
+size_t gather_region_words(int assign);
+size_t gather_region_smem(int assign, int interlace);  // shared bytes of a region CTA
 size_t gather_keys(int ng);  // number of (tile, class) keys
 size_t gather_record_bytes();  // bytes per particle record
 // int64_out: only the gather step, into out64 (records must be in place).
