@@ -348,7 +348,8 @@ constexpr int reg_row(int r) { return (r % 16 == 4 || r % 16 == 12) ? r : reg_ro
 template <int S>
 struct RegGeom {
   static constexpr int R = kRegT + S + 1;  // region edge (cells)
-  static constexpr int RP = (R * R * R + 1) & ~1;  // words per mesh in memory, even (16-byte rows)
+  static constexpr int RG = (R + 1) & ~1;  // z row of a region in memory (even: 16-byte pairs)
+  static constexpr int RP = R * R * RG;    // words per mesh in memory
   // Shared-memory z rows padded to RZ = 4 or 12 (mod 16) words: the 4 x 4
   // (y, z) nodes of a mesh then fall in 16 distinct 8-byte bank pairs.
   static constexpr int RZ = reg_row(R);
@@ -821,6 +822,7 @@ __device__ __forceinline__ void cp_async_wait() {
 template <int S, int NM>
 __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const __grid_constant__ GatherArgs g) {
   constexpr int R = RegGeom<S>::R, RP = RegGeom<S>::RP, RZ = RegGeom<S>::RZ, SM = RegGeom<S>::SM;
+  constexpr int RG = RegGeom<S>::RG;
   // 64-bit path: acc[NM][SM].  Split path, the same bytes as 32-bit words:
   // the node values q mod 2^32 summed at [c * NM + m], q >> 16 summed at
   // HW + [c * NM + m] (meshes interleaved: with two meshes the half-warps
@@ -931,7 +933,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     __syncthreads();
     split = bound_sum[0] < 70368744177664.f && bound_sum[1] < 70368744177664.f;  // 2^46
     if (split) {
-      // one z row per warp and step, out without the padding: [NM][R][R][R]
+      // one z row per warp and step, out as [NM][R][R][RG]
       unsigned long long* o = g.regbuf + (size_t)tile * NM * RP;
       for (int rw = warp; rw < NM * R * R; rw += nw) {
         const int mm = rw / (R * R), row = rw - mm * (R * R);
@@ -939,7 +941,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
           const int w = (row * RZ + lane) * NM + mm;
           const int h = (int)w32[HW + w];
           const unsigned l = w32[w] - ((unsigned)h << 16);
-          o[(size_t)mm * RP + row * R + lane] = (unsigned long long)(((long long)h << 16) + (long long)l);
+          o[(size_t)mm * RP + row * RG + lane] = (unsigned long long)(((long long)h << 16) + (long long)l);
         }
       }
       if (threadIdx.x == 0) g.regflag[tile] = 1;
@@ -970,11 +972,11 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     records(proc);
   }
   __syncthreads();
-  // out without the row padding: [NM][R][R][R] (+1 word to keep RP even)
+  // out with z rows of RG words: [NM][R][R][RG]
   unsigned long long* o = g.regbuf + (size_t)tile * NM * RP;
   for (int rw = warp; rw < NM * R * R; rw += nw) {
     const int mm = rw / (R * R), row = rw - mm * (R * R);
-    if (lane < R) o[(size_t)mm * RP + row * R + lane] = acc[mm * SM + row * RZ + lane];
+    if (lane < R) o[(size_t)mm * RP + row * RG + lane] = acc[mm * SM + row * RZ + lane];
   }
   if (threadIdx.x == 0) g.regflag[tile] = 1;
 }
@@ -1001,12 +1003,17 @@ __device__ __forceinline__ int region_sources(int c, int nt, int* t, int* idx) {
   return 1;
 }
 
-// Mesh from the regions: 4 consecutive z cells per thread, the FP32 value
-// minus the mean cell value (or the exact fixed-point sum).
+// Mesh from the regions: 8 consecutive z cells per thread, the FP32 value
+// minus the mean cell value (or the exact fixed-point sum).  The home
+// tile's 8 words are four 16-byte loads; a tile without records wrote
+// neither its region nor a flag of 1, and its words (loaded alongside the
+// flag) are dropped.
 template <int S, bool INT64>
-__global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ GatherArgs g) {
-  constexpr int T = kRegT, R = RegGeom<S>::R, RP = RegGeom<S>::RP, of = (S >= 3) ? -1 : 0;
-  const int ng = g.ng, nt = g.nt, nm = g.interlace ? 2 : 1, nq = ng >> 2;
+__global__ void __launch_bounds__(256, 4) k_region_sum(const __grid_constant__ GatherArgs g) {
+  constexpr int T = kRegT, R = RegGeom<S>::R, RG = RegGeom<S>::RG, RP = RegGeom<S>::RP;
+  constexpr int of = (S >= 3) ? -1 : 0;
+  static_assert((1 - of) % 2 == 0, "home block of z words starts on a 16-byte boundary");
+  const int ng = g.ng, nt = g.nt, nm = g.interlace ? 2 : 1, nq = ng >> 3;
   const size_t per = (size_t)ng * ng * nq;
   const long long off = INT64 ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < (size_t)nm * per;
@@ -1018,57 +1025,66 @@ __global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ Gath
     const int y = (int)(r % (size_t)ng), x = (int)(r / (size_t)ng);
     int tx[2], ix[2], ty[2], iy[2];
     const int nx = region_sources<S>(x, nt, tx, ix), ny = region_sources<S>(y, nt, ty, iy);
-    const int z0 = 4 * zq, tz0 = z0 / T, uz = z0 - tz0 * T;
+    const int z0 = 8 * zq, tz0 = z0 / T, uz = z0 - tz0 * T;  // uz = 0 or 8
     const int tzp = (tz0 == 0) ? nt - 1 : tz0 - 1, tzn = (tz0 == nt - 1) ? 0 : tz0 + 1;
-    long long s[4] = {0, 0, 0, 0};
-    // a tile without records wrote neither its region nor a flag of 1: its
-    // words are read (in flight with the flag) and dropped
+    long long s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int a = 0; a < nx; a++)
       for (int b = 0; b < ny; b++) {
         const unsigned tb = ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt;
-        const int row = (ix[a] * R + iy[b]) * R;
-        auto at = [&](unsigned t, int iz) {
-          return (long long)g.regbuf[((size_t)t * nm + m) * RP + row + iz];
-        };
+        const int row = (ix[a] * R + iy[b]) * RG;
         {
           const unsigned t = tb + tz0;
           const bool f = g.regflag[t] != 0;
-          long long v[4];
-#pragma unroll
-          for (int k = 0; k < 4; k++) v[k] = at(t, uz + k - of + 1);
-#pragma unroll
-          for (int k = 0; k < 4; k++) s[k] += f ? v[k] : 0;
+          const longlong2* p = reinterpret_cast<const longlong2*>(
+              g.regbuf + ((size_t)t * nm + m) * RP + row + uz - of + 1);
+          const longlong2 v0 = p[0], v1 = p[1], v2 = p[2], v3 = p[3];
+          if (f) {
+            s[0] += v0.x;
+            s[1] += v0.y;
+            s[2] += v1.x;
+            s[3] += v1.y;
+            s[4] += v2.x;
+            s[5] += v2.y;
+            s[6] += v3.x;
+            s[7] += v3.y;
+          }
         }
-        if (uz < S + of) {
+        if (uz == 0) {  // cells u < S + of: the tile before, words u + T - of + 1
           const unsigned t = tb + tzp;
           const bool f = g.regflag[t] != 0;
+          const unsigned long long* p = g.regbuf + ((size_t)t * nm + m) * RP + row + T - of + 1;
+          long long v[S + of];
 #pragma unroll
-          for (int k = 0; k < 4; k++)
-            if (uz + k < S + of) {
-              const long long v = at(t, uz + k + T - of + 1);
-              s[k] += f ? v : 0;
-            }
-        }
-        if (uz + 3 >= T + of - 1) {
+          for (int k = 0; k < S + of; k++) v[k] = (long long)p[k];
+          if (f) {
+#pragma unroll
+            for (int k = 0; k < S + of; k++) s[k] += v[k];
+          }
+        } else {  // cells u >= T + of - 1: the tile after, words u - T - of + 1
           const unsigned t = tb + tzn;
           const bool f = g.regflag[t] != 0;
+          constexpr int k0 = T + of - 1 - 8;
+          const unsigned long long* p = g.regbuf + ((size_t)t * nm + m) * RP + row;
+          long long v[8 - k0];
 #pragma unroll
-          for (int k = 0; k < 4; k++)
-            if (uz + k >= T + of - 1) {
-              const long long v = at(t, uz + k - T - of + 1);
-              s[k] += f ? v : 0;
-            }
+          for (int k = k0; k < 8; k++) v[k - k0] = (long long)p[8 + k - T - of + 1];
+          if (f) {
+#pragma unroll
+            for (int k = k0; k < 8; k++) s[k] += v[k - k0];
+          }
         }
       }
     const size_t cell = ((size_t)x * ng + y) * ng + z0;
     if (INT64) {
       longlong2* o = reinterpret_cast<longlong2*>(g.out64[m] + cell);
-      o[0] = make_longlong2(s[0], s[1]);
-      o[1] = make_longlong2(s[2], s[3]);
+#pragma unroll
+      for (int k = 0; k < 4; k++) o[k] = make_longlong2(s[2 * k], s[2 * k + 1]);
     } else {
-      *reinterpret_cast<float4*>(g.out[m] + cell) =
-          make_float4(fix_to_float(s[0] - off), fix_to_float(s[1] - off),
-                      fix_to_float(s[2] - off), fix_to_float(s[3] - off));
+      float4* o = reinterpret_cast<float4*>(g.out[m] + cell);
+      o[0] = make_float4(fix_to_float(s[0] - off), fix_to_float(s[1] - off),
+                         fix_to_float(s[2] - off), fix_to_float(s[3] - off));
+      o[1] = make_float4(fix_to_float(s[4] - off), fix_to_float(s[5] - off),
+                         fix_to_float(s[6] - off), fix_to_float(s[7] - off));
     }
   }
 }
@@ -1131,7 +1147,7 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
     const dim3 ntile((unsigned)g.nt, (unsigned)g.nt, (unsigned)g.nt);
     const int nm = g.interlace ? 2 : 1;
     const size_t smem = gather_region_smem(g.assign, g.interlace);
-    const size_t work = (size_t)nm * g.ng * g.ng * (g.ng / 4);
+    const size_t work = (size_t)nm * g.ng * g.ng * (g.ng / 8);
     const unsigned sblocks = (unsigned)((work + 255) / 256 < 152 * 16 ? (work + 255) / 256 : 152 * 16);
 #define PS_REGION(SS)                                                                          \
   if (nm == 2) {                                                                               \
