@@ -343,7 +343,6 @@ __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ Gather
 // cover every node a home tile's records reach, local cells [of - 1, T + of
 // + S - 1]; shared-memory z rows are padded to RZ words.
 constexpr int kRegT = 16;
-constexpr int kRegDepth = 8;  // records in flight per warp (shared-memory ring)
 constexpr int reg_row(int r) { return (r % 16 == 4 || r % 16 == 12) ? r : reg_row(r + 1); }
 template <int S>
 struct RegGeom {
@@ -849,42 +848,43 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     float wy, wz;
     short4 bs;
   };
-  // This warp's records, kRegDepth steps in flight.  A step is P records
-  // (one with two meshes; with one mesh the half-warps take one each), each
-  // copied as 7 x 16 bytes with cp.async into the warp's ring slot, one
-  // group per step; step k is read once the groups up to k have landed.
-  constexpr int P = (NM == 2) ? 1 : 2;
+  // This warp's records, in stages of 4 consecutive ones (with one mesh
+  // the half-warps take alternate records), two stages in flight: a stage
+  // is copied as 28 x 16 bytes with cp.async into the warp's ring, one
+  // group per stage, and read once its group has landed.
+  constexpr int Q = 4;
   unsigned char* const ring =
-      reinterpret_cast<unsigned char*>(acc + NM * SM) + warp * (kRegDepth * P * sizeof(WRec));
+      reinterpret_cast<unsigned char*>(acc + NM * SM) + warp * (2 * Q * sizeof(WRec));
   auto records = [&](auto&& proc) {
-    const unsigned w0 = beg + (unsigned)(warp * P), step = (unsigned)(nw * P);
+    const unsigned w0 = beg + (unsigned)(warp * Q), step = (unsigned)(nw * Q);
     const unsigned K = (w0 < end) ? (end - w0 + step - 1) / step : 0u;
-    const unsigned char* src = reinterpret_cast<const unsigned char*>(g.rec);
+    const int cj = lane / 7, part = lane - 7 * cj;  // copy lanes 0-27: record cj, 16-byte part
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(g.rec) + part * 16;
     auto issue = [&](unsigned k) {
-      if (k < K && lane < 7 * P) {
-        const int sub = lane / 7, part = lane - 7 * sub;
-        const unsigned i = w0 + k * step + (unsigned)sub;
-        if (i < end)
-          cp_async16(ring + ((k % kRegDepth) * P + sub) * sizeof(WRec) + part * 16,
-                     src + (size_t)i * sizeof(WRec) + part * 16);
-      }
+      const unsigned i = w0 + k * step + (unsigned)cj;
+      if (k < K && lane < 7 * Q && i < end)
+        cp_async16(ring + ((k & 1) * Q + cj) * sizeof(WRec) + part * 16, src + (size_t)i * sizeof(WRec));
       cp_async_commit();
     };
-    for (unsigned k = 0; k + 1 < (unsigned)kRegDepth; k++) issue(k);
+    issue(0);
     for (unsigned k = 0; k < K; k++) {
-      __syncwarp();  // the slot refilled next was read in step k - 1
-      issue(k + kRegDepth - 1);
-      cp_async_wait<kRegDepth - 1>();
-      __syncwarp();  // every lane's part of step k has landed
-      const int sub = (P == 2) ? half : 0;
-      if (w0 + k * step + (unsigned)sub < end) {
-        const unsigned char* rp = ring + ((k % kRegDepth) * P + sub) * sizeof(WRec);
-        Ld L;
-        L.wx = *reinterpret_cast<const float4*>(rp + m * 48);
-        L.wy = *reinterpret_cast<const float*>(rp + m * 48 + 16 + yy * 4);
-        L.wz = *reinterpret_cast<const float*>(rp + m * 48 + 32 + zz * 4);
-        L.bs = *reinterpret_cast<const short4*>(rp + 96 + m * 8);
-        proc(L);
+      __syncwarp();  // the stage refilled next was read in step k - 1
+      issue(k + 1);
+      cp_async_wait<1>();
+      __syncwarp();  // every lane's part of stage k has landed
+      const unsigned i0 = w0 + k * step;
+#pragma unroll
+      for (int jj = 0; jj < ((NM == 2) ? Q : Q / 2); jj++) {
+        const int j = (NM == 2) ? jj : 2 * jj + half;
+        if (i0 + (unsigned)j < end) {
+          const unsigned char* rp = ring + ((k & 1) * Q + j) * sizeof(WRec);
+          Ld L;
+          L.wx = *reinterpret_cast<const float4*>(rp + m * 48);
+          L.wy = *reinterpret_cast<const float*>(rp + m * 48 + 16 + yy * 4);
+          L.wz = *reinterpret_cast<const float*>(rp + m * 48 + 32 + zz * 4);
+          L.bs = *reinterpret_cast<const short4*>(rp + 96 + m * 8);
+          proc(L);
+        }
       }
     }
     cp_async_wait<0>();
@@ -935,13 +935,18 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     if (split) {
       // one z row per warp and step, out as [NM][R][R][RG]
       unsigned long long* o = g.regbuf + (size_t)tile * NM * RP;
+      int mm = 0, row = warp;  // this warp's row, advanced by nw rows a step
       for (int rw = warp; rw < NM * R * R; rw += nw) {
-        const int mm = rw / (R * R), row = rw - mm * (R * R);
         if (lane < R) {
           const int w = (row * RZ + lane) * NM + mm;
           const int h = (int)w32[HW + w];
           const unsigned l = w32[w] - ((unsigned)h << 16);
-          o[(size_t)mm * RP + row * RG + lane] = (unsigned long long)(((long long)h << 16) + (long long)l);
+          o[mm * RP + row * RG + lane] = (unsigned long long)(((long long)h << 16) + (long long)l);
+        }
+        row += nw;
+        if (row >= R * R) {
+          row -= R * R;
+          mm++;
         }
       }
       if (threadIdx.x == 0) g.regflag[tile] = 1;
@@ -974,9 +979,14 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
   __syncthreads();
   // out with z rows of RG words: [NM][R][R][RG]
   unsigned long long* o = g.regbuf + (size_t)tile * NM * RP;
+  int mm = 0, row = warp;
   for (int rw = warp; rw < NM * R * R; rw += nw) {
-    const int mm = rw / (R * R), row = rw - mm * (R * R);
-    if (lane < R) o[(size_t)mm * RP + row * RG + lane] = acc[mm * SM + row * RZ + lane];
+    if (lane < R) o[mm * RP + row * RG + lane] = acc[mm * SM + row * RZ + lane];
+    row += nw;
+    if (row >= R * R) {
+      row -= R * R;
+      mm++;
+    }
   }
   if (threadIdx.x == 0) g.regflag[tile] = 1;
 }
@@ -1100,11 +1110,11 @@ size_t gather_region_words(int assign) {
 }
 
 size_t gather_region_smem(int assign, int interlace) {
-  // accumulators + one record ring per warp (1024 threads with two meshes,
-  // 512 with one; P records per ring slot)
+  // accumulators + a ring of 2 stages x 4 records per warp (1024 threads
+  // with two meshes, 512 with one)
   const size_t acc = (size_t)(interlace ? 2 : 1) * (assign == 2 ? RegGeom<3>::SM : RegGeom<4>::SM) *
                      sizeof(unsigned long long);
-  return acc + (size_t)(interlace ? 32 : 16) * kRegDepth * (interlace ? 1 : 2) * sizeof(WRec);
+  return acc + (size_t)(interlace ? 32 : 16) * 2 * 4 * sizeof(WRec);
 }
 
 int gather_tile(int ng) {
