@@ -1217,9 +1217,13 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
     }
     c->gather_threads = arg;
   }
-  // region gather or tile gather (phase 0), where the region buffer is
-  // at most 16 GB
-  if (gather_region_ok(c->ng, c->gT, c->p.assign) && region_need(c) <= ((size_t)16 << 30)) {
+  // region gather or tile gather (phase 0), timed where neither clearly
+  // wins: between 1/256 and 1/8 particles per cell, with a region buffer of
+  // at most 16 GB; elsewhere the density rule of use_region decides
+  c->gather_region = -1;
+  const double density = (double)n / (double)c->ntot;
+  if (gather_region_ok(c->ng, c->gT, c->p.assign) && region_need(c) <= ((size_t)16 << 30) &&
+      density >= 1.0 / 256 && density < 1.0 / 8) {
     float best = 1e30f;
     int arg = c->gather_region;
     for (int k = 0; k < 2; k++) {
