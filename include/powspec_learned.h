@@ -20,6 +20,8 @@
 #ifndef POWSPEC_LEARNED_H
 #define POWSPEC_LEARNED_H
 
+#include "powspec_gpu.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -55,6 +57,16 @@ int ps_mlp_train(ps_mlp *m, const int *idx, int nsteps, int batch, float lr,
 
 /* c[i] = exp(y(x[i])) for n feature rows x[n][6] (host memory). */
 int ps_mlp_infer(ps_mlp *m, const float *x, int n, float *c);
+
+/* One learned evaluation, all on the GPU: the context's passes (one
+ * catalogue assigned; poles 0, 2, 4; linear bins; |mu| sub-bins set with
+ * ps_gpu_set_mu_bins to the network's 16), then on the context's stream the
+ * cell features, the network's c = exp(y) per (k, |mu|) cell and
+ * Pc_l = (2l+1) (sum_j c_j A_jl - B_l), with one copy back.  res is filled
+ * as by ps_gpu_execute (the uncorrected multipoles); pl_corr receives the
+ * corrected ones, [3][nbin].  The network's weights are only read: do not
+ * train it meanwhile. */
+int ps_gpu_execute_learned(ps_gpu_ctx *ctx, ps_mlp *m, ps_gpu_result *res, double *pl_corr);
 
 /* Checkpoint with parameters, Adam moments and step count; load resumes. */
 int ps_mlp_save(ps_mlp *m, const char *path);

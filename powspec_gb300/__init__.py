@@ -37,6 +37,7 @@ EXPORTED = [
     "ps_gpu_set_mu_bins", "ps_gpu_read_kmu", "ps_gpu_bin_fields_noalloc",
     "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
     "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune", "ps_gpu_set_tuning",
+    "ps_gpu_execute_learned",
 ]
 
 

@@ -141,6 +141,15 @@ struct ps_gpu_ctx {
   void* d_rec = nullptr;
   unsigned long long* d_region = nullptr;  // region sums of the region gather
   size_t region_bytes = 0;
+  // learned correction (ps_gpu_execute_learned): kcen, cnt, lcnt on the
+  // device, cell features / BF16 copy / corrections, corrected P_l
+  double* d_lgeo = nullptr;
+  float* d_lx = nullptr;
+  void* d_lxb = nullptr;
+  float* d_lc = nullptr;
+  double* d_lout = nullptr;
+  double* h_lout = nullptr;
+  int lcells = 0;
   int last_cat = -1;
   Particles last_pt{};
   std::vector<double> kmu;   // last execute's raw (k, |mu|) sums
@@ -498,10 +507,12 @@ void ps_gpu_destroy(ps_gpu_ctx* c) {
   }
   void* bufs[] = {c->d_bintab, c->d_ksq, c->d_win, c->d_phase, c->d_tw_full, c->d_tw_half,
                   c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage,
-                  c->d_hist, c->d_bsum, c->d_rank, c->d_rec, c->d_region};
+                  c->d_hist, c->d_bsum, c->d_rank, c->d_rec, c->d_region, c->d_lgeo,
+                  c->d_lx, c->d_lxb, c->d_lc, c->d_lout};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->h_lout) cudaFreeHost(c->h_lout);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -894,6 +905,83 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   c->assign_started = false;
   c->assigned[0] = c->assigned[1] = 0;
   return finish(c, h, c->npart, r, true);
+}
+
+int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* pl_corr) {
+  if (!c || !m || !r || !pl_corr) return fail(c, PS_GPU_ERR_ARG, "null argument");
+  const ps_gpu_params& p = c->p;
+  if (p.ncat != 1 || p.npole != 3 || p.poles[0] != 0 || p.poles[1] != 2 || p.poles[2] != 4 ||
+      p.logscale)
+    return fail(c, PS_GPU_ERR_ARG,
+                "the learned correction needs one catalogue, poles (0, 2, 4) and linear bins");
+  if (!c->assigned[0]) return fail(c, PS_GPU_ERR_STATE, "catalogue 0 not assigned");
+  CU(cudaSetDevice(p.device));
+  cudaStream_t s = c->stream;
+  const int nbin = c->nbin, nmu = c->nmu, nkey = nbin * nmu, nacc = p.npole;
+  if (c->lcells != nkey) {  // per-context buffers and constants
+    CU(cudaStreamSynchronize(s));
+    void* old[] = {c->d_lgeo, c->d_lx, c->d_lxb, c->d_lc, c->d_lout};
+    for (void* b : old)
+      if (b) cudaFree(b);
+    if (c->h_lout) cudaFreeHost(c->h_lout);
+    c->d_lgeo = c->d_lout = c->h_lout = nullptr;
+    c->d_lx = c->d_lc = nullptr;
+    c->d_lxb = nullptr;
+    c->lcells = 0;
+    const int fw = learned_feature_width();
+    std::vector<double> geo((size_t)(2 + nacc) * nbin);
+    for (int b = 0; b < nbin; b++) {
+      geo[b] = c->kcen[b];
+      geo[nbin + b] = (double)c->cnt[b];
+    }
+    memcpy(geo.data() + 2 * nbin, c->lcnt.data(), sizeof(double) * (size_t)nacc * nbin);
+    CU(cudaMalloc(&c->d_lgeo, sizeof(double) * geo.size()));
+    CU(cudaMemcpy(c->d_lgeo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice));
+    CU(cudaMalloc(&c->d_lx, sizeof(float) * (size_t)nkey * fw));
+    CU(cudaMalloc(&c->d_lxb, 2 * (size_t)nkey * fw));
+    CU(cudaMalloc(&c->d_lc, sizeof(float) * (size_t)nkey));
+    CU(cudaMalloc(&c->d_lout, sizeof(double) * (size_t)nacc * nbin));
+    CU(cudaMallocHost(&c->h_lout, sizeof(double) * (size_t)nacc * nbin));
+    c->lcells = nkey;
+  }
+  int rc = enqueue_passes(c, c->d_sums, true);
+  if (rc) return rc;
+  LearnedArgs a{};
+  a.sums = c->d_sums;
+  a.wsum = c->d_wsum;
+  a.kcen = c->d_lgeo;
+  a.cnt = c->d_lgeo + nbin;
+  a.lcnt = c->d_lgeo + 2 * nbin;
+  a.volume = p.box[0] * p.box[1] * p.box[2];
+  a.kny = M_PI * c->ng / std::max(p.box[0], std::max(p.box[1], p.box[2]));
+  a.assign3 = (float)(p.assign / 3.0);
+  a.interlace = p.interlace ? 1.f : 0.f;
+  a.nbin = nbin;
+  a.nmu = nmu;
+  a.npole = nacc;
+  a.x = c->d_lx;
+  a.xb = c->d_lxb;
+  a.c = c->d_lc;
+  a.out = c->d_lout;
+  if ((rc = learned_enqueue(m, a, s))) return fail(c, rc, "learned correction launch failed");
+  c->launches += 4;
+  double* h = c->h_out;
+  CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nkey, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h + (size_t)nacc * nkey + 4, c->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(c->h_lout, c->d_lout, sizeof(double) * (size_t)nacc * nbin, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  float t = 0;
+  if (c->assign_started && cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess) c->timings[0] = t;
+  for (int i = 0; i < 4; i++)
+    if (cudaEventElapsedTime(&t, c->ev[i], c->ev[i + 1]) == cudaSuccess) c->timings[1 + i] = t;
+  if (cudaEventElapsedTime(&t, c->ev[0], c->ev[4]) == cudaSuccess) c->timings[5] = t + c->timings[0];
+  c->assign_started = false;
+  c->assigned[0] = c->assigned[1] = 0;
+  rc = finish(c, h, c->npart, r, true);
+  if (rc) return rc;
+  memcpy(pl_corr, c->h_lout, sizeof(double) * (size_t)nacc * nbin);
+  return 0;
 }
 
 int ps_gpu_set_mu_bins(ps_gpu_ctx* c, int nmu) {

@@ -6,6 +6,7 @@
 #include <stddef.h>
 
 #include "powspec_gpu.h"
+#include "powspec_learned.h"
 #include "ps_common.cuh"
 
 namespace ps {
@@ -46,6 +47,25 @@ struct GatherArgs {
   unsigned long long* regbuf;  // [tiles][meshes][gather_region_words()] region sums
   unsigned char* regflag;      // [tiles] 1: the tile wrote its region (it has records)
 };
+// Learned correction on the device (ps_mlp.cu), after a binning pass with
+// |mu| sub-bins: cell features, network, corrected multipoles.
+struct LearnedArgs {
+  const double* sums;  // [npole][nbin * nmu] raw sums of p L_l (one auto spectrum)
+  const double* wsum;  // W at [0]
+  const double* kcen;  // [nbin] bin centres
+  const double* cnt;   // [nbin] mode counts
+  const double* lcnt;  // [npole][nbin] sums of w L_l
+  double volume, kny;
+  float assign3, interlace;  // features: scheme / 3, 0 or 1
+  int nbin, nmu, npole;      // npole 3: l = 0, 2, 4
+  float* x;                  // [nbin * nmu][16] feature rows
+  void* xb;                  // [nbin * nmu][16] BF16 copy
+  float* c;                  // [nbin * nmu] corrections exp(y)
+  double* out;               // [npole][nbin] corrected P_l
+};
+int learned_enqueue(::ps_mlp* m, const LearnedArgs& a, cudaStream_t s);
+int learned_feature_width();
+
 int gather_tile(int ng);    // tile edge for this mesh size, 0 if unsupported
 // Region path: possible for this mesh and scheme; words per tile and mesh.
 bool gather_region_ok(int ng, int T, int assign);

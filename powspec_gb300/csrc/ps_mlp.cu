@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "powspec_gpu.h"
+#include "ps_internal.h"
 
 namespace {
 
@@ -463,7 +464,89 @@ int launch_mlp(ps_mlp* m, TrainArgs& a, int grid) {
   return 0;
 }
 
+// Learned correction of one measurement (one CTA per k bin).  Features
+// (k/k_Nyq, (k/k_Nyq)^2, mu^2, scheme/3, interlace, shot ratio) of the
+// (k, |mu|) cells from the raw sums: A_jl = sums_l / (norm cnt), shot ratio
+// = clip(shot / sum_j A_j0, 0, 1), with norm = W^2 / V, shot = V / W
+// (src/genr_mesh.c:904-910); the FP64 values are rounded to FP32 as the
+// host feature builder does.
+__global__ void k_learned_features(const ps::LearnedArgs a) {
+  const int b = blockIdx.x;
+  __shared__ double s_a0[64];
+  __shared__ double s_ratio;
+  const double W = a.wsum[0], norm = W * W / a.volume, shot = a.volume / W;
+  const double cb = a.cnt[b], safe = fmax(cb, 1.0);
+  for (int j = threadIdx.x; j < a.nmu; j += blockDim.x)
+    s_a0[j] = (cb > 0) ? a.sums[(size_t)b * a.nmu + j] / (norm * safe) : 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double raw0 = 0.0;  // in j order
+    for (int j = 0; j < a.nmu; j++) raw0 += s_a0[j];
+    s_ratio = fmin(fmax(shot / fmax(raw0, 1e-30), 0.0), 1.0);
+  }
+  __syncthreads();
+  const double q = a.kcen[b] / a.kny;
+  for (int j = threadIdx.x; j < a.nmu; j += blockDim.x) {
+    const double mu = (j + 0.5) / a.nmu;
+    float* xr = a.x + ((size_t)b * a.nmu + j) * kK1;
+    xr[0] = (float)q;
+    xr[1] = (float)(q * q);
+    xr[2] = (float)(mu * mu);
+    xr[3] = a.assign3;
+    xr[4] = a.interlace;
+    xr[5] = (float)s_ratio;
+#pragma unroll
+    for (int k = kIn; k < kK1; k++) xr[k] = 0.f;
+  }
+}
+
+// P_l = (2l + 1) (sum_j c_j A_jl - shot lcnt_l / cnt), l = 0, 2, 4, the
+// cells summed in j order.
+__global__ void k_learned_combine(const ps::LearnedArgs a) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nbin) return;
+  const double W = a.wsum[0], norm = W * W / a.volume, shot = a.volume / W;
+  const double cb = a.cnt[b], safe = fmax(cb, 1.0);
+  const int nkey = a.nbin * a.nmu;
+  for (int l = 0; l < a.npole; l++) {
+    double s = 0.0;
+    if (cb > 0)
+      for (int j = 0; j < a.nmu; j++)
+        s += (double)a.c[(size_t)b * a.nmu + j] * (a.sums[(size_t)l * nkey + (size_t)b * a.nmu + j] / (norm * safe));
+    const double B = (cb > 0) ? shot * a.lcnt[(size_t)l * a.nbin + b] / safe : 0.0;
+    a.out[(size_t)l * a.nbin + b] = (4.0 * l + 1.0) * (s - B);
+  }
+}
+
 }  // namespace
+
+namespace ps {
+
+int learned_feature_width() { return kK1; }
+
+// Features, network and combination on stream s (the caller's context
+// stream); the network's weights are only read.
+int learned_enqueue(::ps_mlp* m, const LearnedArgs& a, cudaStream_t s) {
+  if (!m || a.nmu < 1 || a.nmu > 64 || a.npole != 3) return PS_GPU_ERR_ARG;
+  const int n = a.nbin * a.nmu;
+  k_learned_features<<<a.nbin, 64, 0, s>>>(a);
+  k_to_bf16<<<(unsigned)(((size_t)n * kK1 + 255) / 256), 256, 0, s>>>(a.x, (bf16*)a.xb, (size_t)n * kK1);
+  TrainArgs t{};
+  t.x = (bf16*)a.xb;
+  t.params = m->d_params;
+  t.bw = m->d_bw;
+  t.train = 0;
+  t.out = a.c;
+  t.nrows = n;
+  const size_t smem = sizeof(Smem);
+  cudaError_t e = cudaFuncSetAttribute(k_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return PS_GPU_ERR_CUDA;
+  k_mlp<<<(n + kRows - 1) / kRows, 256, smem, s>>>(t);
+  k_learned_combine<<<(a.nbin + 127) / 128, 128, 0, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : PS_GPU_ERR_CUDA;
+}
+
+}  // namespace ps
 
 extern "C" {
 

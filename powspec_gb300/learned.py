@@ -51,6 +51,7 @@ def _mlp_lib():
         L.ps_mlp_infer.argtypes = [vp, vp, ctypes.c_int, vp]
         L.ps_mlp_save.argtypes = [vp, ctypes.c_char_p]
         L.ps_mlp_load.argtypes = [vp, ctypes.c_char_p]
+        L.ps_gpu_execute_learned.argtypes = [vp, vp, vp, vp]
         L._mlp_ready = True
     return L
 
@@ -391,8 +392,9 @@ class LearnedEstimator:
                 r = json.load(f)
             key = f"ng{ng}_{['NGP', 'CIC', 'TSC', 'PCS'][assign]}_{'il' if interlace else 'noil'}"
             self.disabled = set(r.get(key, {}).get("disabled_bins", []))
-        self.last_cells = None
+        self._last = None
         self._x = None
+        self._trusted = None
 
     def close(self):
         self.est.close()
@@ -405,15 +407,44 @@ class LearnedEstimator:
         self.close()
 
     def run(self, cat=None, *, device_ptr=None, n=None):
+        """One learned evaluation (ps_gpu_execute_learned: the passes, the
+        cell features, the network and the corrected multipoles all on the
+        GPU, one copy back).  cat: host AoS float64 [N, 4]; or a device
+        pointer with n."""
+        if device_ptr is not None:
+            self.est.assign(0, device_ptr, on_device=True, n=n)
+        else:
+            self.est.assign(0, cat)
+        r, out = self.est._result()
+        pc = np.zeros((len(POLES), self.est.nbin))
+        rc = _mlp_lib().ps_gpu_execute_learned(self.est._ctx, self.mlp._m, ctypes.byref(r), _ptr(pc))
+        if rc:
+            raise PowspecError(rc, lib().ps_gpu_last_error(self.est._ctx).decode())
+        spec = Estimator._spectrum(r, out)
+        self._last = spec
+        if self._trusted is None:
+            kny = np.pi * self.est.params.ng / max(self.est.params.box)
+            trusted = spec.k <= self.frac * kny
+            for b in self.disabled:
+                if b < len(trusted):
+                    trusted[b] = False
+            self._trusted = trusted
+        return spec.k, pc, self._trusted.copy()
+
+    @property
+    def last_cells(self):
+        """The (k, |mu|) cells of the last run (read back on request)."""
+        return None if self._last is None else _cells_from_result(self.est, self._last)
+
+    def run_host_correction(self, cat=None, *, device_ptr=None, n=None):
+        """The same evaluation with the cells, features and correction formed
+        on the host (numpy) around the network's inference kernel."""
         if device_ptr is not None:
             self.est.assign(0, device_ptr, on_device=True, n=n)
             r = self.est.execute()
             cells = _cells_from_result(self.est, r)
         else:
             cells = measure_cells(self.est, cat)
-        self.last_cells = cells
-        # feature rows: all columns but the shot-noise ratio depend on the
-        # context only, so they are built once
         if self._x is None or len(self._x) != len(cells.kcen) * NMU:
             self._x = features(cells.kcen, cells.kny, self.cfg[1], self.cfg[2],
                                np.zeros(len(cells.kcen)))

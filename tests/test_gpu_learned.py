@@ -133,3 +133,26 @@ def test_committed_weights_meet_tolerance_on_held_out(gpu_lib):
     e_plain = (np.abs(plain256 - pf)[:, use] / pf[0][use]).max()
     assert e_learned < 0.01, e_learned
     assert e_learned < e_plain, (e_learned, e_plain)
+
+
+@pytest.mark.parametrize("ng,assign,interlace", [(128, 3, True), (256, 2, False)])
+def test_device_correction_matches_host_correction(gpu_lib, ng, assign, interlace):
+    """ps_gpu_execute_learned (features, network and corrected multipoles on
+    the GPU) against the host correction of the same evaluation's cells:
+    features in numpy (FP64, then FP32 as the device kernel rounds them)
+    through the same inference kernel.  A second evaluation through the host
+    path agrees to the binning's run-to-run FP32 summation error."""
+    from powspec_gb300 import catalog, learned
+    cat = catalog.lognormal(600_000, seed=23, ngen=128)
+    with learned.LearnedEstimator(ng=ng, assign=assign, interlace=interlace) as le:
+        k1, p1, t1 = le.run(cat)
+        cells = le.last_cells
+        x = learned.features(cells.kcen, cells.kny, assign, interlace, cells.shot_ratio())
+        p2 = cells.corrected(le.mlp.infer(x))
+        k3, p3, t3 = le.run_host_correction(cat)
+    scale = np.abs(cells.plain[0]) + cells.shot
+    d = np.abs(p1 - p2) / scale
+    assert np.median(d) <= 1e-12
+    assert d.max() <= 1e-6
+    assert np.array_equal(k1, k3) and np.array_equal(t1, t3)
+    assert (np.abs(p1 - p3) / scale).max() <= 5e-6
