@@ -33,6 +33,7 @@ OpenMP C restatement of genr_mesh + powspec on all host cores, rank 0 only.
 from __future__ import annotations
 
 import argparse
+import itertools
 import json
 import os
 import statistics
@@ -438,8 +439,8 @@ def run_gpu(args, world, rank, local):
             launches[0] += le.est.launches() + 2  # + feature cast and network kernels
             return out
 
-        def step_e2e():
-            return le.run(host_arr)
+        def e2e_stream(k):
+            return le.run_stream(itertools.repeat(host_arr, k))
     else:
         le = None
         stream, phases, launches = s_plain, phases_plain, [0]
@@ -449,9 +450,8 @@ def run_gpu(args, world, rank, local):
             launches[0] += plain.launches()
             return r
 
-        def step_e2e():
-            plain.assign(0, host_arr)
-            return plain.execute()
+        def e2e_stream(k):
+            return plain.run_stream(itertools.repeat(host_arr, k))
 
     for _ in range(args.warmup):
         step()
@@ -494,12 +494,16 @@ def run_gpu(args, world, rank, local):
         }
         extra["roofline_plain_ng1024"] = roofline(phases_plain / args.steps, 1024, True, nreal, traffic)
 
-    # end to end through the public API with host (pinned) buffers
+    # End to end through the public API with host (pinned) buffers: every
+    # step copies its catalogue in (staged, overlapping the step before) and
+    # reads its result back.  Staging slots allocated untimed first.
+    for _ in e2e_stream(2):
+        pass
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step_e2e()
+    for _ in e2e_stream(args.steps):
+        pass
     torch.cuda.synchronize()
     e2e_s = reduce(world, time.perf_counter() - t0, "max")
     e2e = reduce(world, float(args.steps), "sum") / e2e_s

@@ -115,6 +115,17 @@ int ps_gpu_assign_soa(ps_gpu_ctx *ctx, int cat, const float *x,
                       const float *y, const float *z, const float *w,
                       size_t n, int on_device);
 
+/* Staged input (no counterpart in the reference): ps_gpu_stage_aos starts
+ * copying n AoS records from pinned host memory into device slot `slot`
+ * (0 or 1) on the context's copy stream and returns at once;
+ * ps_gpu_assign_staged(ctx, cat, slot) then assigns them, its kernels
+ * waiting for that copy.  With two slots the copy of the next catalogue
+ * overlaps the evaluation of this one.  The host records must stay
+ * unchanged until the catalogue's execute returns; a slot is refilled only
+ * after the kernels that read its previous catalogue. */
+int ps_gpu_stage_aos(ps_gpu_ctx *ctx, int slot, const double *xyzw, size_t n);
+int ps_gpu_assign_staged(ps_gpu_ctx *ctx, int cat, int slot);
+
 /* FFTs, interlace combine, window compensation, binning and normalisation
  * (src/multipole.c:435-505, :778-1087, :1267-1274).  Blocks until the
  * results are on the host. */

@@ -37,7 +37,7 @@ EXPORTED = [
     "ps_gpu_set_mu_bins", "ps_gpu_read_kmu", "ps_gpu_bin_fields_noalloc",
     "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
     "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune", "ps_gpu_set_tuning",
-    "ps_gpu_execute_learned",
+    "ps_gpu_execute_learned", "ps_gpu_stage_aos", "ps_gpu_assign_staged",
 ]
 
 
@@ -172,6 +172,8 @@ def lib():
         L.ps_gpu_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                       ctypes.c_void_p]
         L.ps_gpu_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.ps_gpu_stage_aos.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
+        L.ps_gpu_assign_staged.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -230,6 +232,7 @@ class Estimator:
             self.close()
             raise PowspecError(rc, msg)
         self.nbin = L.ps_gpu_nbin(self._ctx)
+        self._staged = [None, None]
 
     def last_error(self):
         if not self._ctx:
@@ -326,6 +329,36 @@ class Estimator:
         ch = np.array([v(gather_threads), v(z_radix32), v(y_radix32), v(pipelined_pass_c),
                        v(dense_lane_groups), rg], np.int32)
         self._check(lib().ps_gpu_set_tuning(self._ctx, _ptr(ch)))
+
+    def stage(self, slot, particles):
+        """Starts copying host AoS float64 [N, 4] records (pinned memory for
+        an asynchronous copy) into staging slot 0 or 1; returns at once."""
+        a = np.ascontiguousarray(particles, dtype=np.float64)
+        self._staged[slot] = a  # kept alive until the slot is reused
+        self._check(lib().ps_gpu_stage_aos(self._ctx, slot, a.ctypes.data_as(ctypes.c_void_p), len(a)))
+
+    def assign_staged(self, cat, slot):
+        """Assigns the catalogue in a staging slot (after its copy)."""
+        self._check(lib().ps_gpu_assign_staged(self._ctx, cat, slot))
+
+    def run_stream(self, cats, execute=None):
+        """Evaluates host catalogues one after another (one catalogue per
+        context), the copy of each overlapping the evaluation of the one
+        before through the two staging slots; yields the results."""
+        execute = execute or self.execute
+        it = iter(cats)
+        cur = next(it, None)
+        slot = 0
+        if cur is None:
+            return
+        self.stage(slot, cur)
+        while cur is not None:
+            nxt = next(it, None)
+            if nxt is not None:
+                self.stage(1 - slot, nxt)
+            self.assign_staged(0, slot)
+            yield execute()
+            cur, slot = nxt, 1 - slot
 
     def batch(self, device_ptrs, ns):
         """A CUDA-graph batch of single-catalogue evaluations (see Batch)."""

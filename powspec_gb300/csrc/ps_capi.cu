@@ -150,6 +150,14 @@ struct ps_gpu_ctx {
   double* d_lout = nullptr;
   double* h_lout = nullptr;
   int lcells = 0;
+  // staged input (ps_gpu_stage_aos): two device slots filled on a copy
+  // stream; copied[s] marks a slot's copy done, used[s] the end of the
+  // assignment kernels that read it
+  cudaStream_t copy_stream = nullptr;
+  void* d_slot[2] = {nullptr, nullptr};
+  size_t slot_bytes[2] = {0, 0}, slot_n[2] = {0, 0};
+  cudaEvent_t copied[2] = {nullptr, nullptr}, used[2] = {nullptr, nullptr};
+  bool slot_full[2] = {false, false};
   int last_cat = -1;
   Particles last_pt{};
   std::vector<double> kmu;   // last execute's raw (k, |mu|) sums
@@ -501,6 +509,7 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
 void ps_gpu_destroy(ps_gpu_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   for (int f = 0; f < 4; f++) {
     if (c->grid[f]) cudaFree(c->grid[f]);
     if (c->cbuf[f]) cudaFree(c->cbuf[f]);
@@ -508,11 +517,16 @@ void ps_gpu_destroy(ps_gpu_ctx* c) {
   void* bufs[] = {c->d_bintab, c->d_ksq, c->d_win, c->d_phase, c->d_tw_full, c->d_tw_half,
                   c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage,
                   c->d_hist, c->d_bsum, c->d_rank, c->d_rec, c->d_region, c->d_lgeo,
-                  c->d_lx, c->d_lxb, c->d_lc, c->d_lout};
+                  c->d_lx, c->d_lxb, c->d_lc, c->d_lout, c->d_slot[0], c->d_slot[1]};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_out) cudaFreeHost(c->h_out);
   if (c->h_lout) cudaFreeHost(c->h_lout);
+  for (int k = 0; k < 2; k++) {
+    if (c->copied[k]) cudaEventDestroy(c->copied[k]);
+    if (c->used[k]) cudaEventDestroy(c->used[k]);
+  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -856,6 +870,53 @@ int ps_gpu_assign_aos(ps_gpu_ctx* c, int cat, const double* xyzw, size_t n, int 
     pt.aos = (const double*)c->d_stage;
   }
   return assign_common(c, cat, pt);
+}
+
+int ps_gpu_stage_aos(ps_gpu_ctx* c, int slot, const double* xyzw, size_t n) {
+  if (!c || slot < 0 || slot > 1 || (!xyzw && n)) return fail(c, PS_GPU_ERR_ARG, "invalid stage arguments");
+  CU(cudaSetDevice(c->p.device));
+  if (!c->copy_stream) {
+    CU(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; k++) {
+      CU(cudaEventCreateWithFlags(&c->copied[k], cudaEventDisableTiming));
+      CU(cudaEventCreateWithFlags(&c->used[k], cudaEventDisableTiming));
+      CU(cudaEventRecord(c->used[k], c->stream));
+    }
+  }
+  const size_t bytes = n * 4 * sizeof(double);
+  if (bytes > c->slot_bytes[slot]) {
+    // the slot may still be read by earlier assignment kernels
+    CU(cudaEventSynchronize(c->used[slot]));
+    CU(cudaStreamSynchronize(c->copy_stream));
+    if (c->d_slot[slot]) cudaFree(c->d_slot[slot]);
+    c->d_slot[slot] = nullptr;
+    c->slot_bytes[slot] = 0;
+    CU(cudaMalloc(&c->d_slot[slot], bytes));
+    c->slot_bytes[slot] = bytes;
+  }
+  // the copy waits for the kernels that read this slot's previous catalogue
+  CU(cudaStreamWaitEvent(c->copy_stream, c->used[slot], 0));
+  if (n) CU(cudaMemcpyAsync(c->d_slot[slot], xyzw, bytes, cudaMemcpyHostToDevice, c->copy_stream));
+  CU(cudaEventRecord(c->copied[slot], c->copy_stream));
+  c->slot_n[slot] = n;
+  c->slot_full[slot] = true;
+  return 0;
+}
+
+int ps_gpu_assign_staged(ps_gpu_ctx* c, int cat, int slot) {
+  if (!c || cat < 0 || cat >= c->p.ncat || slot < 0 || slot > 1)
+    return fail(c, PS_GPU_ERR_ARG, "invalid assign arguments");
+  if (!c->slot_full[slot]) return fail(c, PS_GPU_ERR_STATE, "staging slot %d holds no catalogue", slot);
+  CU(cudaSetDevice(c->p.device));
+  CU(cudaStreamWaitEvent(c->stream, c->copied[slot], 0));
+  Particles pt{};
+  pt.n = c->slot_n[slot];
+  pt.aos = (const double*)c->d_slot[slot];
+  const int rc = assign_common(c, cat, pt);
+  // the slot is free again once the classify and scatter kernels are done
+  CU(cudaEventRecord(c->used[slot], c->stream));
+  c->slot_full[slot] = false;
+  return rc;
 }
 
 int ps_gpu_assign_soa(ps_gpu_ctx* c, int cat, const float* x, const float* y, const float* z,

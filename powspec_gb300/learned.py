@@ -415,6 +415,14 @@ class LearnedEstimator:
             self.est.assign(0, device_ptr, on_device=True, n=n)
         else:
             self.est.assign(0, cat)
+        return self._execute()
+
+    def run_stream(self, cats):
+        """run() over host catalogues, the copy of each overlapping the
+        evaluation of the one before (two staging slots)."""
+        return self.est.run_stream(cats, execute=self._execute)
+
+    def _execute(self):
         r, out = self.est._result()
         pc = np.zeros((len(POLES), self.est.nbin))
         rc = _mlp_lib().ps_gpu_execute_learned(self.est._ctx, self.mlp._m, ctypes.byref(r), _ptr(pc))
