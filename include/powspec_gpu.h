@@ -115,6 +115,17 @@ int ps_gpu_assign_soa(ps_gpu_ctx *ctx, int cat, const float *x,
                       const float *y, const float *z, const float *w,
                       size_t n, int on_device);
 
+/* Survey catalogue `cat` (CUBIC_SIM = F; monopole only): the context's
+ * catalogue holds the data with weights w and the randoms with weights
+ * -alpha w, positions minus the box's lower corner (src/genr_mesh.c:797-809,
+ * :541-566).  P_0 = (sum / cnt - shot) / norm with the given shot noise and
+ * normalisation (src/read_cata.c:173-183, src/multipole.c:1108-1116); the
+ * k = 0 mode is summed when it lies in the first bin (src/multipole.c:593).
+ * The result reports shot / norm as its shot noise (src/save_res.c:89).
+ * Multipoles l > 0 of surveys (the Yamamoto estimator, src/mp_template.c)
+ * are not provided: the context must have poles {0}. */
+int ps_gpu_set_survey(ps_gpu_ctx *ctx, int cat, double shot, double norm);
+
 /* Staged input (no counterpart in the reference): ps_gpu_stage_aos starts
  * copying n AoS records from pinned host memory into device slot `slot`
  * (0 or 1) on the context's copy stream and returns at once;

@@ -37,7 +37,7 @@ EXPORTED = [
     "ps_gpu_set_mu_bins", "ps_gpu_read_kmu", "ps_gpu_bin_fields_noalloc",
     "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
     "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune", "ps_gpu_set_tuning",
-    "ps_gpu_execute_learned", "ps_gpu_stage_aos", "ps_gpu_assign_staged",
+    "ps_gpu_execute_learned", "ps_gpu_stage_aos", "ps_gpu_assign_staged", "ps_gpu_set_survey",
 ]
 
 
@@ -174,6 +174,7 @@ def lib():
         L.ps_gpu_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ps_gpu_stage_aos.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
         L.ps_gpu_assign_staged.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.ps_gpu_set_survey.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double]
         _lib = L
     return _lib
 
@@ -329,6 +330,12 @@ class Estimator:
         ch = np.array([v(gather_threads), v(z_radix32), v(y_radix32), v(pipelined_pass_c),
                        v(dense_lane_groups), rg], np.int32)
         self._check(lib().ps_gpu_set_tuning(self._ctx, _ptr(ch)))
+
+    def set_survey(self, cat, shot, norm):
+        """Survey normalisation of catalogue `cat` (monopole contexts): P_0 =
+        (sum / cnt - shot) / norm; the catalogue holds the data (weights w)
+        and the randoms (weights -alpha w), relative to the box corner."""
+        self._check(lib().ps_gpu_set_survey(self._ctx, cat, float(shot), float(norm)))
 
     def stage(self, slot, particles):
         """Starts copying host AoS float64 [N, 4] records (pinned memory for

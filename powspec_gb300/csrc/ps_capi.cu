@@ -158,6 +158,9 @@ struct ps_gpu_ctx {
   size_t slot_bytes[2] = {0, 0}, slot_n[2] = {0, 0};
   cudaEvent_t copied[2] = {nullptr, nullptr}, used[2] = {nullptr, nullptr};
   bool slot_full[2] = {false, false};
+  // survey normalisation per catalogue (ps_gpu_set_survey)
+  bool survey[2] = {false, false};
+  double survey_shot[2] = {0, 0}, survey_norm[2] = {0, 0};
   int last_cat = -1;
   Particles last_pt{};
   std::vector<double> kmu;   // last execute's raw (k, |mu|) sums
@@ -779,13 +782,23 @@ int finish(ps_gpu_ctx* c, const double* h, const size_t* npart, ps_gpu_result* r
       return fail(c, PS_GPU_ERR_RANGE, "catalogue %d: total |weight| %g exceeds the fixed-point range", k, wsum[2 * k + 1]);
   }
 
-  // epilogue (src/genr_mesh.c:904-910, src/multipole.c:1047-1087)
+  // epilogue (src/genr_mesh.c:904-910, src/multipole.c:1047-1087); surveys:
+  // the shot noise and normalisation given (src/read_cata.c:173-183), the
+  // shot noise reported as shot / norm (src/save_res.c:89)
   const double vol = p.box[0] * p.box[1] * p.box[2];
   for (int k = 0; k < 2; k++) {
     r->wdata[k] = (k < p.ncat) ? wsum[2 * k] : 0;
     r->shot[k] = (k < p.ncat) ? vol / r->wdata[k] : 0;
     r->norm[k] = (k < p.ncat) ? r->wdata[k] * r->wdata[k] / vol : 0;
+    if (k < p.ncat && c->survey[k]) {
+      r->shot[k] = c->survey_shot[k] / c->survey_norm[k];
+      r->norm[k] = c->survey_norm[k];
+    }
   }
+  // Surveys sum the k = 0 mode when it lies in a bin (src/multipole.c:593-606;
+  // simulation boxes skip it, :806).  Its value is F_a(0) F_b(0) = W_a W_b,
+  // the fields' weight sums (the mesh holds mean-free values).
+  const bool dc_bin = !p.logscale && c->kedge[0] <= 0.0 && nbin > 0;
   r->nbin = nbin;
   for (int s2 = 0; s2 < c->nspec; s2++) {
     const int cat = c->spec_cat[s2];
@@ -795,10 +808,14 @@ int finish(ps_gpu_ctx* c, const double* h, const size_t* npart, ps_gpu_result* r
       for (int i = 0; i < nbin; i++) {
         double v = sums[((size_t)s2 * npole + l) * nbin + i];
         const double cn = (double)c->cnt[i];
+        const bool sv = cat >= 0 ? c->survey[cat] : (c->survey[0] && c->survey[1]);
+        if (sv && dc_bin && i == 0 && p.poles[l] == 0)
+          v += wsum[2 * c->spec_a[s2]] * wsum[2 * c->spec_b[s2]];
         if (cat >= 0) {
           if (c->cnt[i]) {
             v /= r->norm[cat] * cn;
-            v -= r->shot[cat] * c->lcnt[(size_t)l * nbin + i] / cn;
+            // surveys subtract the shot noise whole (src/multipole.c:1113)
+            v -= sv ? r->shot[cat] : r->shot[cat] * c->lcnt[(size_t)l * nbin + i] / cn;
           }
         } else if (c->cnt[i]) {
           v /= sqrt(r->norm[0] * r->norm[1]) * cn;
@@ -966,6 +983,19 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   c->assign_started = false;
   c->assigned[0] = c->assigned[1] = 0;
   return finish(c, h, c->npart, r, true);
+}
+
+int ps_gpu_set_survey(ps_gpu_ctx* c, int cat, double shot, double norm) {
+  if (!c || cat < 0 || cat >= c->p.ncat) return fail(c, PS_GPU_ERR_ARG, "invalid survey arguments");
+  if (c->p.npole != 1 || c->p.poles[0] != 0)
+    return fail(c, PS_GPU_ERR_ARG,
+                "survey catalogues: only the monopole (multipoles l > 0 need the Yamamoto "
+                "estimator, which this library does not provide)");
+  if (!(norm > 0) || !(shot >= 0)) return fail(c, PS_GPU_ERR_ARG, "survey normalisation must be > 0");
+  c->survey[cat] = true;
+  c->survey_shot[cat] = shot;
+  c->survey_norm[cat] = norm;
+  return 0;
 }
 
 int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* pl_corr) {

@@ -74,10 +74,18 @@ typedef struct {
   const char *wcomp;  /* NULL: unit weights */
   const char *sel;    /* NULL: no selection */
   int nthread;        /* host threads; 0: OMP_NUM_THREADS, else the online cores */
+  /* survey catalogues (CUBIC_SIM = F): record weight = completeness x FKP
+   * weight; sums as io/read_ascii.c:880-895 */
+  int survey;
+  const char *wfkp;   /* NULL: 1 */
+  const char *nz;     /* NULL: 0 */
+  double *sumw2;      /* out: sum of (wc wfkp)^2 (surveys) */
+  double *sumw2n;     /* out: sum of wc wfkp^2 nz (surveys) */
 } psh_catalog;
 
 /* Reads an ASCII catalogue (DATA_FORMAT = 0) into *xyzw ({x, y, z, w}
- * records in file order), sets *n and *wsum. */
+ * records in file order), sets *n and *wsum (the sum of the completeness
+ * weights, in file order). */
 int psh_read_ascii(const psh_catalog *in, double **xyzw, size_t *n, double *wsum, bool verbose);
 /* Reads a NumPy .npy array (DATA_FORMAT = 2): 1-D or 2-D, f4 / f8 / i4 / i8
  * of either byte order, C or Fortran order; the columns of a row are $1,

@@ -6,12 +6,16 @@
  * configuration (src/load_conf.c:876-1130), read the catalogues, build the
  * meshes and evaluate the power spectrum multipoles, save the results
  * (src/save_res.c:35-229, same header lines, columns and number formats).
- * Survey geometries (CUBIC_SIM = F: randoms, coordinate conversion) and FITS
+ * Survey catalogues (CUBIC_SIM = F) are evaluated for the monopole: data
+ * minus alpha x randoms with FKP weights in a box fitted to the catalogues
+ * (src/read_cata.c:95-185, src/genr_mesh.c:427-566, :797-809).  Multipoles
+ * l > 0 of surveys (the Yamamoto estimator), coordinate conversion and FITS
  * catalogues are outside this program and rejected with an error.  Besides
  * ASCII (DATA_FORMAT = 0), DATA_FORMAT = 2 reads NumPy .npy arrays, whose
  * columns take the same position / weight / selection expressions.
  */
 #define _POSIX_C_SOURCE 200809L
+#include <float.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -26,7 +30,10 @@
 typedef struct {
   bool issim, intlace, logscale, oheader, verbose, isauto[2], iscross;
   int ndata, gsize, assign, npole, poles[7];
-  int dfmt[2];  /* DATA_FORMAT: 0 ASCII, 2 NumPy .npy */
+  int dfmt[2], rfmt[2];  /* DATA_FORMAT, RAND_FORMAT: 0 ASCII, 2 NumPy .npy */
+  double bmin[3];        /* lower box corner: 0 for simulation boxes */
+  double bpad[3];        /* BOX_PAD (surveys without BOX_SIZE) */
+  bool bset;             /* BOX_SIZE given */
   long ovwrite;
   double bsize[3], los[3], kmin, kmax, kbin;
   const char *oauto[2], *ocross;
@@ -75,15 +82,93 @@ static int check_output(const char *fname, const char *key, long ovwrite) {
   return 0;
 }
 
+/* Reads catalogue i of `which` (DATA or RAND) with its keywords.  Surveys
+ * take FKP weights and n(z) too (io/read_ascii.c:880-895). */
+static int read_cat(psh_cfg *cfg, const Conf *c, const char *which, int i, int fmt,
+                    double **xyzw, size_t *n, double *wsum, double *sumw2, double *sumw2n) {
+  char key[32];
+  psh_catalog in;
+  memset(&in, 0, sizeof in);
+#define K(name) (snprintf(key, sizeof key, "%s_" name, which), key)
+  in.fname = psh_str(cfg, K("CATALOG"), i);
+  long skip = 0;
+  if (psh_int(cfg, K("SKIP"), i, &skip) < 0 || skip < 0) return PSH_ERR_CONF;
+  in.skip = skip;
+  const char *cm = psh_str(cfg, K("COMMENT"), i);
+  in.comment = cm ? cm[0] : '\0';
+  in.fmtr = psh_str(cfg, K("FORMATTER"), i);
+  for (int d = 0; d < 3; d++) in.pos[d] = psh_str(cfg, K("POSITION"), 3 * i + d);
+  in.wcomp = psh_str(cfg, K("WT_COMP"), i);
+  in.sel = psh_str(cfg, K("SELECTION"), i);
+  if (!c->issim) {
+    in.survey = 1;
+    in.wfkp = psh_str(cfg, K("WT_FKP"), i);
+    in.nz = psh_str(cfg, K("NZ"), i);
+    in.sumw2 = sumw2;
+    in.sumw2n = sumw2n;
+  }
+#undef K
+  if (in.sel && !*in.sel) in.sel = NULL;
+  if (in.wcomp && !*in.wcomp) in.wcomp = NULL;
+  if (in.wfkp && !*in.wfkp) in.wfkp = NULL;
+  if (in.nz && !*in.nz) in.nz = NULL;
+  int rc = fmt == 2 ? psh_read_npy(&in, xyzw, n, wsum, c->verbose)
+                    : psh_read_ascii(&in, xyzw, n, wsum, c->verbose);
+  if (!rc && *n == 0) {
+    fprintf(stderr, "Error: no object read from `%s'\n", in.fname);
+    rc = PSH_ERR_CATA;
+  }
+  return rc;
+}
+
+/* Format, readability and formatter of the DATA or RAND catalogues. */
+static int check_files(psh_cfg *cfg, const Conf *c, const char *which, int *fmt) {
+  char key[32];
+  for (int i = 0; i < c->ndata; i++) {
+    long t = 0;
+    snprintf(key, sizeof key, "%s_FORMAT", which);
+    if (psh_int(cfg, key, i, &t) < 0) return PSH_ERR_CFG;
+    if (t == 1) {
+      fprintf(stderr, "Error: FITS format is not enabled\n");
+      return PSH_ERR_CFG;
+    }
+    if (t != 0 && t != 2) {
+      fprintf(stderr, "Error: invalid `%s': %ld (0: ASCII, 2: NumPy .npy)\n", key, t);
+      return PSH_ERR_CFG;
+    }
+    fmt[i] = (int)t;
+    snprintf(key, sizeof key, "%s_CATALOG", which);
+    const char *fn = psh_str(cfg, key, i);
+    if (access(fn, R_OK)) {
+      fprintf(stderr, "Error: cannot access `%s': `%s'\n", key, fn);
+      return PSH_ERR_FILE;
+    }
+    snprintf(key, sizeof key, "%s_FORMATTER", which);
+    if (t == 0 && psh_size(cfg, key) <= i) {
+      fprintf(stderr, "Error: %s of `%s'\n", psh_size(cfg, key) ? "too few elements" : "not set",
+              key);
+      return PSH_ERR_CFG;
+    }
+  }
+  snprintf(key, sizeof key, "%s_POSITION", which);
+  if (psh_size(cfg, key) < 3 * c->ndata) {
+    fprintf(stderr, "Error: %s `%s'\n", psh_size(cfg, key) ? "too few elements of" : "not set:",
+            key);
+    return PSH_ERR_CFG;
+  }
+  return 0;
+}
+
 static int verify(psh_cfg *cfg, Conf *c) {
   int rc;
   if ((rc = psh_bool(cfg, "CUBIC_SIM", 0, &c->issim))) {
     if (rc == 1) fprintf(stderr, "Error: `CUBIC_SIM' is not set\n");
     return PSH_ERR_CFG;
   }
-  if (!c->issim) {
-    fprintf(stderr, "Error: this program computes periodic simulation boxes only "
-                    "(CUBIC_SIM = T); survey geometries are not supported\n");
+  if (!c->issim && (psh_size(cfg, "DATA_CONVERT") || psh_size(cfg, "RAND_CONVERT"))) {
+    /* set at all, the reference converts (src/load_conf.c:949-968) */
+    fprintf(stderr, "Error: coordinate conversion (`DATA_CONVERT', `RAND_CONVERT') is not "
+                    "supported; give Cartesian comoving coordinates\n");
     return PSH_ERR_CFG;
   }
   c->ovwrite = 0;
@@ -129,36 +214,21 @@ static int verify(psh_cfg *cfg, Conf *c) {
                     "`OUTPUT_CROSS' may require more catalogs)\n");
     return PSH_ERR_CFG;
   }
-  for (int i = 0; i < c->ndata; i++) {
-    long t = 0;
-    if (psh_int(cfg, "DATA_FORMAT", i, &t) < 0) return PSH_ERR_CFG;
-    if (t == 1) {
-      fprintf(stderr, "Error: FITS format is not enabled\n");
+  if ((rc = check_files(cfg, c, "DATA", c->dfmt))) return rc;
+  if (!c->issim) {
+    if (psh_size(cfg, "RAND_CATALOG") < c->ndata) {
+      fprintf(stderr, "Error: %s `RAND_CATALOG'\n",
+              psh_size(cfg, "RAND_CATALOG") ? "too few elements of" : "not set:");
       return PSH_ERR_CFG;
     }
-    if (t != 0 && t != 2) {
-      fprintf(stderr, "Error: invalid `DATA_FORMAT': %ld (0: ASCII, 2: NumPy .npy)\n", t);
-      return PSH_ERR_CFG;
-    }
-    c->dfmt[i] = (int)t;
-    const char *fn = psh_str(cfg, "DATA_CATALOG", i);
-    if (access(fn, R_OK)) {
-      fprintf(stderr, "Error: cannot access `DATA_CATALOG': `%s'\n", fn);
-      return PSH_ERR_FILE;
-    }
-    if (t == 0 && psh_size(cfg, "DATA_FORMATTER") <= i) {
-      fprintf(stderr, "Error: %s of `DATA_FORMATTER'\n",
-              psh_size(cfg, "DATA_FORMATTER") ? "too few elements" : "not set");
+    if ((rc = check_files(cfg, c, "RAND", c->rfmt))) return rc;
+    if (!psh_size(cfg, "DATA_NZ") && !psh_size(cfg, "RAND_NZ")) {
+      fprintf(stderr, "Error: `DATA_NZ' and `RAND_NZ' are both not set\n");
       return PSH_ERR_CFG;
     }
   }
-  if (psh_size(cfg, "DATA_POSITION") < 3 * c->ndata) {
-    fprintf(stderr, "Error: %s `DATA_POSITION'\n",
-            psh_size(cfg, "DATA_POSITION") ? "too few elements of" : "not set:");
-    return PSH_ERR_CFG;
-  }
-  /* LINE_OF_SIGHT: unit vector, default [0, 0, 1] */
-  num = psh_size(cfg, "LINE_OF_SIGHT");
+  /* LINE_OF_SIGHT: unit vector, default [0, 0, 1] (simulation boxes) */
+  num = c->issim ? psh_size(cfg, "LINE_OF_SIGHT") : 0;
   c->los[0] = c->los[1] = 0;
   c->los[2] = 1;
   if (num) {
@@ -174,21 +244,38 @@ static int verify(psh_cfg *cfg, Conf *c) {
       return PSH_ERR_CFG;
     }
   }
-  /* BOX_SIZE: 1 or 3 positive values */
+  /* BOX_SIZE: 1 or 3 positive values; surveys without it fit the box to
+   * the catalogues with BOX_PAD (src/load_conf.c:798-850) */
   num = psh_size(cfg, "BOX_SIZE");
-  if (!num) {
+  c->bset = num > 0;
+  if (!num && c->issim) {
     fprintf(stderr, "Error: `BOX_SIZE' is not set\n");
     return PSH_ERR_CFG;
   }
-  if (num != 1 && num != 3) {
+  if (num && num != 1 && num != 3) {
     fprintf(stderr, "Error: wrong dimension of `BOX_SIZE'");
     return PSH_ERR_CFG;
   }
-  for (int d = 0; d < 3; d++) {
+  for (int d = 0; d < 3 && num; d++) {
     if (psh_dbl(cfg, "BOX_SIZE", num == 1 ? 0 : d, &c->bsize[d])) return PSH_ERR_CFG;
     if (c->bsize[d] <= 0) {
       fprintf(stderr, "Error: `BOX_SIZE' must be > 0\n");
       return PSH_ERR_CFG;
+    }
+  }
+  if (!num) {
+    const int np = psh_size(cfg, "BOX_PAD");
+    if (np && np != 1 && np != 3) {
+      fprintf(stderr, "Error: wrong dimension of `BOX_PAD'");
+      return PSH_ERR_CFG;
+    }
+    for (int d = 0; d < 3; d++) {
+      c->bpad[d] = 0.02;  /* DEFAULT_BOX_PAD */
+      if (np && psh_dbl(cfg, "BOX_PAD", np == 1 ? 0 : d, &c->bpad[d])) return PSH_ERR_CFG;
+      if (c->bpad[d] < 0) {
+        fprintf(stderr, "Error: `BOX_PAD' must be >= 0\n");
+        return PSH_ERR_CFG;
+      }
     }
   }
   long v;
@@ -239,6 +326,11 @@ static int verify(psh_cfg *cfg, Conf *c) {
     return PSH_ERR_CFG;
   }
   for (int i = 0; i < m; i++) c->poles[i] = pl[i];
+  if (!c->issim && (m != 1 || pl[0] != 0)) {
+    fprintf(stderr, "Error: survey catalogues (CUBIC_SIM = F): only `MULTIPOLE' = 0 is "
+                    "supported (l > 0 needs the Yamamoto estimator)\n");
+    return PSH_ERR_CFG;
+  }
   c->kmin = 0;
   if ((rc = psh_dbl(cfg, "KMIN", 0, &c->kmin)) < 0) return PSH_ERR_CFG;
   if (c->kmin < 0) {
@@ -286,7 +378,8 @@ static int verify(psh_cfg *cfg, Conf *c) {
 
 static void header_common(FILE *fp, const Conf *c) {
   fprintf(fp, "# Box size: [%lg, %lg, %lg]\n# Box boundaries: [[%lg,%lg], [%lg,%lg], [%lg,%lg]]\n",
-          c->bsize[0], c->bsize[1], c->bsize[2], 0.0, c->bsize[0], 0.0, c->bsize[1], 0.0, c->bsize[2]);
+          c->bsize[0], c->bsize[1], c->bsize[2], c->bmin[0], c->bmin[0] + c->bsize[0], c->bmin[1],
+          c->bmin[1] + c->bsize[1], c->bmin[2], c->bmin[2] + c->bsize[2]);
   fprintf(fp, "# Grid size: %d , assignment scheme: %s , grid interlacing: %s\n", c->gsize,
           kAssignNames[c->assign], c->intlace ? "enabled" : "disabled");
 }
@@ -304,7 +397,8 @@ static int write_table(FILE *fp, const Conf *c, const ps_gpu_result *r, const do
   return ferror(fp) ? PSH_ERR_FILE : 0;
 }
 
-static int save(const Conf *c, const size_t *ndata, const double *wdata, const ps_gpu_result *r) {
+static int save(const Conf *c, const size_t *ndata, const double *wdata, const size_t *nrand,
+                const double *wrand, const ps_gpu_result *r) {
   printf("Saving outputs ...%s", c->verbose ? "\n" : "");
   fflush(stdout);
   for (int n = 0; n < c->ndata; n++) {
@@ -316,6 +410,8 @@ static int save(const Conf *c, const size_t *ndata, const double *wdata, const p
     }
     if (c->oheader) {
       fprintf(fp, "# Data catalog: %zu objects, total weight: " OFMT_DBL "\n", ndata[n], wdata[n]);
+      if (!c->issim)
+        fprintf(fp, "# Random catalog: %zu objects, total weight: " OFMT_DBL "\n", nrand[n], wrand[n]);
       header_common(fp, c);
       fprintf(fp, "# Shot noise: " OFMT_DBL " , normalisation: " OFMT_DBL " \n", r->shot[n], r->norm[n]);
     }
@@ -339,6 +435,11 @@ static int save(const Conf *c, const size_t *ndata, const double *wdata, const p
               "# Data catalog 1: %zu objects, total weight: " OFMT_DBL
               "\n# Data catalog 2: %zu objects, total weight: " OFMT_DBL "\n",
               ndata[0], wdata[0], ndata[1], wdata[1]);
+      if (!c->issim)
+        fprintf(fp,
+                "# Random catalog 1: %zu objects, total weight: " OFMT_DBL
+                "\n# Random catalog 2: %zu objects, total weight: " OFMT_DBL "\n",
+                nrand[0], wrand[0], nrand[1], wrand[1]);
       header_common(fp, c);
       fprintf(fp, "# Normalisation factor 1: " OFMT_DBL " , Normalisation factor 2: " OFMT_DBL "\n",
               r->norm[0], r->norm[1]);
@@ -382,33 +483,76 @@ int main(int argc, char **argv) {
 
   /* catalogues */
   printf("Reading catalogues ...\n");
-  double *xyzw[2] = {NULL, NULL};
-  size_t ndata[2] = {0, 0};
-  double wsum[2] = {0, 0};
+  double *xyzw[2] = {NULL, NULL}, *rxyzw[2] = {NULL, NULL};
+  size_t ndata[2] = {0, 0}, nrand[2] = {0, 0};
+  double wsum[2] = {0, 0}, wrand[2] = {0, 0}, shot[2] = {0, 0}, norm[2] = {0, 0};
   for (int i = 0; i < c.ndata && !rc; i++) {
-    psh_catalog in;
-    memset(&in, 0, sizeof in);
-    in.fname = psh_str(&cfg, "DATA_CATALOG", i);
-    long skip = 0;
-    if (psh_int(&cfg, "DATA_SKIP", i, &skip) < 0 || skip < 0) {
-      rc = PSH_ERR_CONF;
-      break;
-    }
-    in.skip = skip;
-    const char *cm = psh_str(&cfg, "DATA_COMMENT", i);
-    in.comment = cm ? cm[0] : '\0';
-    in.fmtr = psh_str(&cfg, "DATA_FORMATTER", i);
-    for (int d = 0; d < 3; d++) in.pos[d] = psh_str(&cfg, "DATA_POSITION", 3 * i + d);
-    in.wcomp = psh_str(&cfg, "DATA_WT_COMP", i);
-    in.sel = psh_str(&cfg, "DATA_SELECTION", i);
-    if (in.sel && !*in.sel) in.sel = NULL;
-    if (in.wcomp && !*in.wcomp) in.wcomp = NULL;
-    rc = c.dfmt[i] == 2 ? psh_read_npy(&in, &xyzw[i], &ndata[i], &wsum[i], c.verbose)
-                        : psh_read_ascii(&in, &xyzw[i], &ndata[i], &wsum[i], c.verbose);
-    if (!rc && ndata[i] == 0) {
-      fprintf(stderr, "Error: no object read from `%s'\n", in.fname);
+    double s2[2] = {0, 0}, s2n[2] = {0, 0};
+    rc = read_cat(&cfg, &c, "DATA", i, c.dfmt[i], &xyzw[i], &ndata[i], &wsum[i], &s2[0], &s2n[0]);
+    if (rc || c.issim) continue;
+    rc = read_cat(&cfg, &c, "RAND", i, c.rfmt[i], &rxyzw[i], &nrand[i], &wrand[i], &s2[1], &s2n[1]);
+    if (rc) continue;
+    /* alpha, shot noise and normalisation (src/read_cata.c:165-183) */
+    if (wsum[i] == 0 || s2[0] == 0) {
+      fprintf(stderr, "Error: invalid completeness or FKP weights in the data catalog\n");
       rc = PSH_ERR_CATA;
+    } else if (wrand[i] == 0 || s2[1] == 0) {
+      fprintf(stderr, "Error: invalid completeness or FKP weights in the random catalog\n");
+      rc = PSH_ERR_CATA;
+    } else {
+      const double alpha = wsum[i] / wrand[i];
+      shot[i] = s2[0] + alpha * alpha * s2[1];
+      norm[i] = (s2n[0] == 0 || s2n[1] != 0) ? alpha * s2n[1] : s2n[0];
+      /* data minus alpha x randoms in one catalogue: weights -alpha w */
+      double *all = realloc(xyzw[i], sizeof(double) * 4 * (ndata[i] + nrand[i]));
+      if (!all) {
+        rc = PSH_ERR_MEMORY;
+        continue;
+      }
+      xyzw[i] = all;
+      double *r = all + 4 * ndata[i];
+      for (size_t k = 0; k < nrand[i]; k++) {
+        r[4 * k] = rxyzw[i][4 * k];
+        r[4 * k + 1] = rxyzw[i][4 * k + 1];
+        r[4 * k + 2] = rxyzw[i][4 * k + 2];
+        r[4 * k + 3] = -alpha * rxyzw[i][4 * k + 3];
+      }
+      free(rxyzw[i]);
+      rxyzw[i] = NULL;
     }
+  }
+  if (!rc && !c.issim) {
+    /* the box (src/genr_mesh.c:427-566): bounds of all data and randoms,
+     * centred; BOX_SIZE, or the padded extent rounded up to 10 */
+    double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    for (int i = 0; i < c.ndata; i++)
+      for (size_t k = 0; k < ndata[i] + nrand[i]; k++)
+        for (int d = 0; d < 3; d++) {
+          const double v = xyzw[i][4 * k + d];
+          if (mn[d] > v) mn[d] = v;
+          if (mx[d] < v) mx[d] = v;
+        }
+    for (int d = 0; d < 3 && !rc; d++) {
+      if (c.bset) {
+        if (mx[d] - mn[d] > c.bsize[d]) {
+          fprintf(stderr, "Error: BOX_SIZE is too small for the %c coordinates, should be at least "
+                          OFMT_DBL "\n", "xyz"[d], mx[d] - mn[d]);
+          rc = PSH_ERR_CATA;
+        }
+      } else {
+        c.bsize[d] = ceil((mx[d] - mn[d]) * (1 + c.bpad[d]) / 10) * 10;  /* POWSPEC_BOX_CEIL */
+      }
+      c.bmin[d] = (mx[d] + mn[d] - c.bsize[d]) * 0.5;
+    }
+    if (!rc && c.verbose)
+      printf("  Box size: [%lg, %lg, %lg]\n  Box boundaries: [[%lg,%lg], [%lg,%lg], [%lg,%lg]]\n",
+             c.bsize[0], c.bsize[1], c.bsize[2], c.bmin[0], c.bmin[0] + c.bsize[0], c.bmin[1],
+             c.bmin[1] + c.bsize[1], c.bmin[2], c.bmin[2] + c.bsize[2]);
+    /* positions relative to the box corner: (x - bmin) as the reference's
+     * grid coordinate takes it (src/genr_mesh.c:57-62) */
+    for (int i = 0; i < c.ndata && !rc; i++)
+      for (size_t k = 0; k < ndata[i] + nrand[i]; k++)
+        for (int d = 0; d < 3; d++) xyzw[i][4 * k + d] -= c.bmin[d];
   }
 
   /* estimator */
@@ -453,7 +597,8 @@ int main(int argc, char **argv) {
       res.xpl = xpl;
       if (!res.k || !res.kedge || !res.km || !res.cnt || !res.lcnt || !pl || !xpl) rc = PSH_ERR_MEMORY;
       for (int i = 0; i < c.ndata && !rc; i++) {
-        rc = ps_gpu_assign_aos(ctx, i, xyzw[i], ndata[i], 0);
+        rc = ps_gpu_assign_aos(ctx, i, xyzw[i], ndata[i] + nrand[i], 0);
+        if (!rc && !c.issim) rc = ps_gpu_set_survey(ctx, i, shot[i], norm[i]);
         if (rc) fprintf(stderr, "Error: %s\n", ps_gpu_last_error(ctx));
         free(xyzw[i]);  /* the reference frees the catalogue after assignment */
         xyzw[i] = NULL;
@@ -461,8 +606,11 @@ int main(int argc, char **argv) {
       if (!rc && (rc = ps_gpu_execute(ctx, &res))) fprintf(stderr, "Error: %s\n", ps_gpu_last_error(ctx));
     }
   }
-  if (!rc) rc = save(&c, ndata, wsum, &res);
-  for (int i = 0; i < 2; i++) free(xyzw[i]);
+  if (!rc) rc = save(&c, ndata, wsum, nrand, wrand, &res);
+  for (int i = 0; i < 2; i++) {
+    free(xyzw[i]);
+    free(rxyzw[i]);
+  }
   free(res.k);
   free(res.kedge);
   free(res.km);

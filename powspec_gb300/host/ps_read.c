@@ -295,8 +295,9 @@ typedef struct {
   Field fd[256];
   int nf, ncol;
   char comment;
-  psh_expr *ex[5];  /* x, y, z, weight, selection */
-  int colof[5];     /* an expression that is one column: its index, else -1 */
+  psh_expr *ex[7];  /* x, y, z, completeness weight, selection, FKP weight, n(z) */
+  int colof[7];     /* an expression that is one column: its index, else -1 */
+  int survey;
   const char *buf;  /* ASCII text, or .npy data */
   size_t size;
   /* .npy */
@@ -308,6 +309,7 @@ typedef struct {
   const Reader *rd;
   size_t beg, end;  /* ASCII: byte range of whole lines; .npy: rows */
   double *rec;      /* {x, y, z, w} */
+  double *ext;      /* surveys: {wc, wfkp, nz} per record */
   size_t cnt, cap;
   int err;
   size_t bad;       /* ASCII: offset of the line that failed; SIZE_MAX: none */
@@ -315,6 +317,11 @@ typedef struct {
   int bad_field;
   double *dst;      /* join: where this range's records go */
 } Part;
+
+static double value(const Reader *rd, int k, const double *col, double unset) {
+  if (!rd->ex[k]) return unset;
+  return rd->colof[k] >= 0 ? col[rd->colof[k]] : psh_expr_eval(rd->ex[k], col);
+}
 
 static int push(Part *pt, const double *col) {
   const Reader *rd = pt->rd;
@@ -324,12 +331,24 @@ static int push(Part *pt, const double *col) {
     double *nb = realloc(pt->rec, sizeof(double) * 4 * cap);
     if (!nb) return PSH_ERR_MEMORY;
     pt->rec = nb;
+    if (rd->survey) {
+      double *ne = realloc(pt->ext, sizeof(double) * 3 * cap);
+      if (!ne) return PSH_ERR_MEMORY;
+      pt->ext = ne;
+    }
     pt->cap = cap;
   }
-  double *r = pt->rec + 4 * pt->cnt++;
-  for (int d = 0; d < 3; d++)
-    r[d] = rd->colof[d] >= 0 ? col[rd->colof[d]] : psh_expr_eval(rd->ex[d], col);
-  r[3] = !rd->ex[3] ? 1.0 : rd->colof[3] >= 0 ? col[rd->colof[3]] : psh_expr_eval(rd->ex[3], col);
+  double *r = pt->rec + 4 * pt->cnt;
+  for (int d = 0; d < 3; d++) r[d] = value(rd, d, col, 0.0);
+  r[3] = value(rd, 3, col, 1.0);
+  if (rd->survey) {  /* io/read_ascii.c:880-895 */
+    double *x = pt->ext + 3 * pt->cnt;
+    x[0] = r[3];
+    x[1] = value(rd, 5, col, 1.0);
+    x[2] = value(rd, 6, col, 0.0);
+    r[3] = x[0] * x[1];
+  }
+  pt->cnt++;
   return 0;
 }
 
@@ -435,6 +454,22 @@ static void *copy_part(void *arg) {
   return NULL;
 }
 
+/* Survey sums in file order: completeness weights, (wc wfkp)^2, wc wfkp^2 nz. */
+static void survey_sums(const Part *pt, int np, const psh_catalog *in, double *wsum) {
+  double w = 0, w2 = 0, w2n = 0;
+  for (int i = 0; i < np; i++)
+    for (size_t k = 0; k < pt[i].cnt; k++) {
+      const double *x = pt[i].ext + 3 * k;
+      const double wt = x[0] * x[1];
+      w += x[0];
+      w2 += wt * wt;
+      w2n += x[0] * x[1] * x[1] * x[2];
+    }
+  *wsum = w;
+  if (in->sumw2) *in->sumw2 = w2;
+  if (in->sumw2n) *in->sumw2n = w2n;
+}
+
 /* Runs fn on every part, part 0 on the calling thread. */
 static void run_parts(Part *pt, int np, void *(*fn)(void *)) {
   pthread_t th[256];
@@ -459,25 +494,32 @@ static int join_parts(Part *pt, int np, double **xyzw, size_t *n, double *wsum) 
     pt[i].dst = out + 4 * off;
     off += pt[i].cnt;
   }
+  const int survey = np > 0 && pt[0].rd->survey;
   run_parts(pt, np, copy_part);
   double w = 0;
-  for (size_t i = 0; i < tot; i++) w += out[4 * i + 3];
+  if (!survey)  /* surveys: the completeness weights (survey_sums) */
+    for (size_t i = 0; i < tot; i++) w += out[4 * i + 3];
   *xyzw = out;
   *n = tot;
-  *wsum = w;
+  if (!survey) *wsum = w;
   return 0;
 }
 
 static void free_parts(Part *pt, int np) {
-  for (int i = 0; i < np; i++) free(pt[i].rec);
+  for (int i = 0; i < np; i++) {
+    free(pt[i].rec);
+    free(pt[i].ext);
+  }
 }
 
 /* Compiles the expressions; maxcol: the columns there are. */
 static int compile_exprs(const psh_catalog *in, Reader *rd, int ncol, const char *what) {
-  const char *src[5] = {in->pos[0], in->pos[1], in->pos[2], in->wcomp, in->sel};
+  const char *src[7] = {in->pos[0], in->pos[1], in->pos[2], in->wcomp, in->sel,
+                        in->survey ? in->wfkp : NULL, in->survey ? in->nz : NULL};
   char err[256];
   rd->need = 0;
-  for (int k = 0; k < 5; k++) {
+  rd->survey = in->survey;
+  for (int k = 0; k < 7; k++) {
     rd->ex[k] = NULL;
     rd->colof[k] = -1;
     if (!src[k]) continue;
@@ -499,7 +541,7 @@ static int compile_exprs(const psh_catalog *in, Reader *rd, int ncol, const char
 }
 
 static void free_exprs(Reader *rd) {
-  for (int k = 0; k < 5; k++) psh_expr_free(rd->ex[k]);
+  for (int k = 0; k < 7; k++) psh_expr_free(rd->ex[k]);
 }
 
 /* First line start at or after byte off. */
@@ -570,6 +612,7 @@ int psh_read_ascii(const psh_catalog *in, double **xyzw, size_t *n, double *wsum
       }
     }
   }
+  if (!rc && in->survey) survey_sums(pt, np, in, wsum);
   if (!rc) rc = join_parts(pt, np, xyzw, n, wsum);
   free_parts(pt, np);
   unmap_file(&m);
@@ -696,6 +739,7 @@ int psh_read_npy(const psh_catalog *in, double **xyzw, size_t *n, double *wsum, 
         rc = pt[i].err;
       }
   }
+  if (!rc && in->survey) survey_sums(pt, np, in, wsum);
   if (!rc) rc = join_parts(pt, np, xyzw, n, wsum);
   free_parts(pt, np);
   unmap_file(&m);

@@ -14,8 +14,14 @@ these are the pins of the oracle and of the GPU path:
   every scheme, interlaced.
 * ``cli/``: an ASCII catalogue, a powspec.conf and the reference POWSPEC
   output file for it (the output-format pin).
+* ``survey/``: a survey-like data catalogue (a clustered sphere) and its
+  randoms, with completeness weights, n(z) and FKP weights, and the
+  reference POWSPEC monopole for CUBIC_SIM = F with the box fitted to the
+  catalogues (ref_auto.txt) and with BOX_SIZE given (ref_auto_box.txt).
 
-Usage (in a tree that has the reference sources):  python tests/golden/make_golden.py
+Usage (in a tree that has the reference sources):
+    python tests/golden/make_golden.py          # everything
+    python tests/golden/make_golden.py survey   # the survey fixture only
 """
 from __future__ import annotations
 
@@ -122,5 +128,62 @@ VERBOSE         = F
     print("cli fixture written")
 
 
+SURVEY_CONF = """DATA_CATALOG    = data.txt
+RAND_CATALOG    = rand.txt
+DATA_FORMATTER  = "%lf %lf %lf %lf %lf"
+RAND_FORMATTER  = "%lf %lf %lf %lf %lf"
+DATA_POSITION   = [$1, $2, $3]
+RAND_POSITION   = [$1, $2, $3]
+DATA_WT_COMP    = $4
+RAND_WT_COMP    = $4
+DATA_WT_FKP     = 1/(1+$5*2000)
+RAND_WT_FKP     = 1/(1+$5*2000)
+DATA_NZ         = $5
+RAND_NZ         = $5
+CUBIC_SIM       = F
+GRID_SIZE       = 32
+PARTICLE_ASSIGN = 3
+GRID_INTERLACE  = T
+MULTIPOLE       = 0
+BIN_SIZE        = 0.02
+OUTPUT_AUTO     = {out}
+OVERWRITE       = 1
+VERBOSE         = F
+"""
+
+
+def survey():
+    """Survey fixture: clustered data in a sphere of radius 200 around
+    (600, 300, 450), randoms uniform in the sphere (3x), completeness
+    weights in [0.8, 1.2], a constant n(z) column and FKP weights
+    1 / (1 + n P0), P0 = 2000."""
+    if oracle.build_ref() is None:
+        raise SystemExit("reference sources not found: cannot generate fixtures")
+    d = os.path.join(HERE, "survey")
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(77)
+    cen, rad = np.array([600.0, 300.0, 450.0]), 200.0
+    c = make_cat("lognormal", 9000, 500.0, 31)[:, :3] - 250.0
+    data = c[np.sum(c * c, axis=1) < rad * rad] + cen
+    u = rng.uniform(-rad, rad, (12 * len(data), 3))
+    rand = u[np.sum(u * u, axis=1) < rad * rad][:3 * len(data)] + cen
+    nbar = len(data) / (4.0 / 3.0 * np.pi * rad ** 3)
+    for name, pts in (("data.txt", data), ("rand.txt", rand)):
+        cols = np.column_stack([pts, rng.uniform(0.8, 1.2, len(pts)), np.full(len(pts), nbar)])
+        np.savetxt(os.path.join(d, name), cols, fmt="%.6f %.6f %.6f %.4f %.8e")
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    for conf, extra in (("powspec.conf", ""), ("powspec_box.conf", "BOX_SIZE        = [450, 420, 430]\n")):
+        out = "ref_auto.txt" if not extra else "ref_auto_box.txt"
+        with open(os.path.join(d, conf), "w") as f:
+            f.write(SURVEY_CONF.format(out=out) + extra)
+        subprocess.run([oracle.REF_CLI, "-c", conf], cwd=d, check=True, env=env,
+                       stdout=subprocess.DEVNULL)
+    print("survey fixture written:", len(data), "data,", len(rand), "randoms")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["survey"]:
+        survey()
+    else:
+        main()
+        survey()

@@ -43,10 +43,10 @@ def test_help_and_template(cli, tmp_path):
     assert r.returncode == 0 and "BIN_SIZE" in r.stdout and "LINE_OF_SIGHT" in r.stdout
 
 
-def test_survey_geometry_is_refused(cli, workdir):
-    r = run(cli, ["-c", "powspec.conf", "--sim", "F"], workdir)
+def test_survey_without_randoms_is_refused(cli, workdir):
+    r = run(cli, ["-c", "powspec.conf", "--sim", "F", "--pole", "0"], workdir)
     assert r.returncode != 0
-    assert "CUBIC_SIM" in r.stderr
+    assert "RAND_CATALOG" in r.stderr
 
 
 def test_existing_output_without_overwrite(cli, workdir):
@@ -154,3 +154,61 @@ def test_cli_output_matches_reference_file(cli, workdir):
         assert a.split()[:5] == b.split()[:5]
     scale = np.abs(f[:, 5]) + shot
     assert (np.abs(g[:, 5:] - f[:, 5:]) / scale[:, None]).max() <= 1e-5
+
+
+@pytest.fixture
+def survey_dir(tmp_path):
+    for f in ("data.txt", "rand.txt", "powspec.conf", "powspec_box.conf"):
+        shutil.copy(os.path.join(GOLDEN, "survey", f), tmp_path / f)
+    return tmp_path
+
+
+@pytest.mark.parametrize("args,msg", [
+    (["--pole", "[0, 2]"], "MULTIPOLE"),
+    (["--data-convert", "F"], "coordinate conversion"),
+    (["--rand-pos", "[$1, $2]"], "RAND_POSITION"),
+])
+def test_survey_configuration_errors(cli, survey_dir, args, msg):
+    r = run(cli, ["-c", "powspec.conf", "-a", "o.txt"] + args, survey_dir)
+    assert r.returncode != 0 and msg in r.stderr, r.stderr
+
+
+def test_survey_needs_nz(cli, survey_dir):
+    conf = (survey_dir / "powspec.conf").read_text().replace("DATA_NZ", "#").replace("RAND_NZ", "#")
+    (survey_dir / "nonz.conf").write_text(conf)
+    r = run(cli, ["-c", "nonz.conf", "-a", "o.txt"], survey_dir)
+    assert r.returncode != 0 and "DATA_NZ" in r.stderr
+
+
+def test_survey_catalogues_are_read(cli, survey_dir):
+    r = run(cli, ["-c", "powspec.conf", "-a", "o.txt", "-v", "T"], survey_dir)
+    out = r.stdout
+    assert "2337 objects read from `data.txt'" in out and "7011 objects read from `rand.txt'" in out
+    assert "Box size: [410, 410, 410]" in out, out
+
+
+def _compare(got_path, ref_path):
+    got = open(got_path).read().splitlines()
+    ref = open(ref_path).read().splitlines()
+    assert len(got) == len(ref)
+    assert [l for l in got if l.startswith("#")] == [l for l in ref if l.startswith("#")]
+    rows = [l.split() for l in got if not l.startswith("#")]
+    rrows = [l.split() for l in ref if not l.startswith("#")]
+    assert [x[:5] for x in rows] == [x[:5] for x in rrows]  # k columns and mode counts
+    shot = float(ref[5].split("Shot noise:")[1].split(",")[0])
+    g = np.array([float(x[5]) for x in rows])
+    f = np.array([float(x[5]) for x in rrows])
+    return np.abs(g - f) / (np.abs(f) + shot)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("conf,ref", [("powspec.conf", "ref_auto.txt"),
+                                      ("powspec_box.conf", "ref_auto_box.txt")])
+def test_survey_monopole_matches_reference_file(cli, survey_dir, conf, ref):
+    """Data minus alpha x randoms with FKP weights in the fitted (or given,
+    non-cubic) box: the reference's header lines, k columns and mode counts,
+    and P_0 within 1e-5 of |P_0| + shot noise (bin 0 holds the k = 0 mode)."""
+    r = run(cli, ["-c", conf, "-a", "gpu_auto.txt"], survey_dir)
+    assert r.returncode == 0, r.stdout + r.stderr
+    d = _compare(survey_dir / "gpu_auto.txt", os.path.join(GOLDEN, "survey", ref))
+    assert d.max() <= 1e-5, d

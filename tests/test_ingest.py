@@ -20,7 +20,9 @@ HOST = os.path.join(ROOT, "powspec_gb300", "host")
 class Cat(ctypes.Structure):
     _fields_ = [("fname", ctypes.c_char_p), ("skip", ctypes.c_long), ("comment", ctypes.c_char),
                 ("fmtr", ctypes.c_char_p), ("pos", ctypes.c_char_p * 3),
-                ("wcomp", ctypes.c_char_p), ("sel", ctypes.c_char_p), ("nthread", ctypes.c_int)]
+                ("wcomp", ctypes.c_char_p), ("sel", ctypes.c_char_p), ("nthread", ctypes.c_int),
+                ("survey", ctypes.c_int), ("wfkp", ctypes.c_char_p), ("nz", ctypes.c_char_p),
+                ("sumw2", ctypes.POINTER(ctypes.c_double)), ("sumw2n", ctypes.POINTER(ctypes.c_double))]
 
 
 @pytest.fixture(scope="module")
@@ -231,3 +233,38 @@ def test_npy_one_column_and_errors(host, tmp_path, capfd):
     assert "shorter" in capfd.readouterr().err
     (tmp_path / "t.npy").write_text("1 2 3\n")
     assert read(host, tmp_path / "t.npy", fmtr=None, npy=True)[0] == -3
+
+
+@pytest.mark.parametrize("nthread", [1, 5])
+def test_survey_weights_and_sums(host, tmp_path, nthread):
+    """Survey catalogues (io/read_ascii.c:880-895): record weight wc * wfkp;
+    W = sum wc, sum (wc wfkp)^2 and sum wc wfkp^2 nz, in file order."""
+    rng = np.random.default_rng(9)
+    n = 20000
+    v = np.column_stack([rng.random((n, 3)) * 500, rng.uniform(0.5, 1.5, n),
+                         rng.uniform(1e-4, 3e-4, n)])
+    p = tmp_path / "s.txt"
+    np.savetxt(p, v, fmt="%.10g")
+    w2, w2n = ctypes.c_double(), ctypes.c_double()
+    c = Cat(str(p).encode(), 0, b"#", b"%lf %lf %lf %lf %lf",
+            (ctypes.c_char_p * 3)(b"$1", b"$2", b"$3"), b"$4", b"$5 > 1.2e-4", nthread,
+            1, b"1/(1+$5*10000)", b"$5", ctypes.pointer(w2), ctypes.pointer(w2n))
+    ptr = ctypes.POINTER(ctypes.c_double)()
+    cnt = ctypes.c_size_t()
+    w = ctypes.c_double()
+    assert host.psh_read_ascii(ctypes.byref(c), ctypes.byref(ptr), ctypes.byref(cnt),
+                               ctypes.byref(w), False) == 0
+    a = np.ctypeslib.as_array(ptr, (cnt.value, 4)).copy()
+    LIBC.free(ptr)
+    f = np.loadtxt(p)
+    f = f[f[:, 4] > 1.2e-4]
+    wc, wf, nz = f[:, 3], 1 / (1 + f[:, 4] * 10000), f[:, 4]
+    assert np.array_equal(a[:, :3], f[:, :3])
+    assert np.allclose(a[:, 3], wc * wf, rtol=1e-15, atol=0)
+    s = s2 = s2n = 0.0
+    for x, y, z in zip(wc, wf, nz):  # file order
+        s += x
+        s2 += (x * y) ** 2
+        s2n += x * y * y * z
+    assert w.value == pytest.approx(s, rel=1e-14)
+    assert w2.value == pytest.approx(s2, rel=1e-13) and w2n.value == pytest.approx(s2n, rel=1e-13)
