@@ -22,6 +22,8 @@
 // a decision point of the reference (0, 1/2, 1) is the reference's exact
 // FP64 sequence (pos - bmin) * Ng / L used instead, so cell indices and
 // branches are the reference's while FP64 work stays rare.
+#include <cstddef>
+
 #include "ps_internal.h"
 
 namespace ps {
@@ -72,6 +74,8 @@ struct __align__(16) WRec {
   short base[2][4];   // [mesh][axis]; [mesh][3]: node value bound (k_scatter)
 };
 static_assert(sizeof(WRec) == 112, "weighted record layout");
+static_assert(offsetof(WRec, base) == 96 && sizeof(WRec::w[0]) == 48,
+              "region gather reads w[m] at m * 48 and base[m] at 96 + m * 8");
 constexpr size_t kRecBytes = 112;  // room for either record kind
 
 // round-to-nearest-even of v as int64 from 32-bit conversions only (the

@@ -477,9 +477,12 @@ int main(int argc, char **argv) {
     psh_cfg_free(&cfg);
     return PSH_ERR_CONF;
   }
-  if (c.verbose)
-    printf("  Grid size: %d, assignment: %s, interlacing: %s, box: [%lg, %lg, %lg]\n", c.gsize,
-           kAssignNames[c.assign], c.intlace ? "T" : "F", c.bsize[0], c.bsize[1], c.bsize[2]);
+  if (c.verbose) {
+    printf("  Grid size: %d, assignment: %s, interlacing: %s", c.gsize, kAssignNames[c.assign],
+           c.intlace ? "T" : "F");
+    if (c.issim) printf(", box: [%lg, %lg, %lg]", c.bsize[0], c.bsize[1], c.bsize[2]);
+    printf("\n");
+  }
 
   /* catalogues */
   printf("Reading catalogues ...\n");
