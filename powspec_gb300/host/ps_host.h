@@ -94,4 +94,23 @@ int psh_read_npy(const psh_catalog *in, double **xyzw, size_t *n, double *wsum, 
 /* Decimal string to double with strtod's syntax and correct rounding. */
 double psh_strtod(const char *s, char **end);
 
+/* ---- coordinate conversion: (RA, Dec, z) -> comoving Cartesian ---- */
+typedef struct {
+  double omega_m, omega_l, omega_k, eos_w;  /* OMEGA_M, OMEGA_LAMBDA, DE_EOS_W */
+  double err;                               /* CMVDST_ERR */
+  double widx;                              /* 3 (1 + w), 0 for w = -1 */
+  int order;                                /* Gauss-Legendre order chosen */
+  double x[32], w[32];                      /* its nodes and weights */
+  double *tz, *td, *typp;                   /* Z_CMVDST_CNVT table and spline */
+  size_t ntab;
+} psh_cosmo;
+
+/* Interpolation table `table` (or NULL: quadrature, its order chosen on
+ * the redshift range [zmin, zmax]). */
+int psh_cosmo_init(psh_cosmo *c, const char *table, double zmin, double zmax, bool verbose);
+void psh_cosmo_free(psh_cosmo *c);
+double psh_cosmo_distance(const psh_cosmo *c, double z);
+/* {RA deg, Dec deg, z, w} records -> {x, y, z, w} in place. */
+void psh_cosmo_convert(const psh_cosmo *c, double *xyzw, size_t n, int nthread);
+
 #endif

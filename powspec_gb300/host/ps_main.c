@@ -34,6 +34,9 @@ typedef struct {
   double bmin[3];        /* lower box corner: 0 for simulation boxes */
   double bpad[3];        /* BOX_PAD (surveys without BOX_SIZE) */
   bool bset;             /* BOX_SIZE given */
+  bool cnvt, dcnvt[2], rcnvt[2];  /* coordinate conversion (surveys) */
+  const char *ztab;               /* Z_CMVDST_CNVT */
+  psh_cosmo cosmo;
   long ovwrite;
   double bsize[3], los[3], kmin, kmax, kbin;
   const char *oauto[2], *ocross;
@@ -121,6 +124,65 @@ static int read_cat(psh_cfg *cfg, const Conf *c, const char *which, int i, int f
   return rc;
 }
 
+/* Cosmology of the coordinate conversion (src/load_conf.c:746-785, :970-987). */
+static int check_cosmo(psh_cfg *cfg, Conf *c) {
+  psh_cosmo *k = &c->cosmo;
+  memset(k, 0, sizeof *k);
+  for (int i = 0; i < 2; i++) {
+    c->dcnvt[i] = c->rcnvt[i] = false;
+    if (psh_size(cfg, "DATA_CONVERT") > i && psh_bool(cfg, "DATA_CONVERT", i, &c->dcnvt[i]))
+      return PSH_ERR_CFG;
+    if (psh_size(cfg, "RAND_CONVERT") > i && psh_bool(cfg, "RAND_CONVERT", i, &c->rcnvt[i]))
+      return PSH_ERR_CFG;
+  }
+  c->ztab = psh_str(cfg, "Z_CMVDST_CNVT", 0);
+  if (c->ztab && *c->ztab) {
+    if (access(c->ztab, R_OK)) {
+      fprintf(stderr, "Error: cannot access `Z_CMVDST_CNVT': `%s'\n", c->ztab);
+      return PSH_ERR_FILE;
+    }
+    return 0;
+  }
+  c->ztab = NULL;
+  int rc = psh_dbl(cfg, "OMEGA_M", 0, &k->omega_m);
+  if (rc) {
+    if (rc == 1) fprintf(stderr, "Error: `OMEGA_M' is not set\n");
+    return PSH_ERR_CFG;
+  }
+  if (k->omega_m <= 0 || k->omega_m > 1) {
+    fprintf(stderr, "Error: `OMEGA_M' must be > 0 and <= 1\n");
+    return PSH_ERR_CFG;
+  }
+  if ((rc = psh_dbl(cfg, "OMEGA_LAMBDA", 0, &k->omega_l)) < 0) return PSH_ERR_CFG;
+  if (rc) {
+    k->omega_l = 1 - k->omega_m;
+    k->omega_k = 0;
+  } else if (k->omega_l < 0) {
+    fprintf(stderr, "Error: `OMEGA_LAMBDA' must be >= 0\n");
+    return PSH_ERR_CFG;
+  } else {
+    k->omega_k = 1 - k->omega_m - k->omega_l;
+  }
+  if ((rc = psh_dbl(cfg, "DE_EOS_W", 0, &k->eos_w)) < 0) return PSH_ERR_CFG;
+  if (rc) k->eos_w = -1;
+  else if (k->eos_w > -1 / 3.0) {
+    fprintf(stderr, "Error: `DE_EOS_W' must be <= -1/3\n");
+    return PSH_ERR_CFG;
+  }
+  const double w3 = k->eos_w * 3, wi = w3 + 1;  /* H^2(z) > 0 */
+  if (k->omega_k * pow(k->omega_l * (-wi), wi / w3) <= k->omega_l * w3 * pow(k->omega_m, wi / w3)) {
+    fprintf(stderr, "Error: negative H^2 given the cosmological parameters\n");
+    return PSH_ERR_CFG;
+  }
+  if ((rc = psh_dbl(cfg, "CMVDST_ERR", 0, &k->err)) < 0) return PSH_ERR_CFG;
+  if (rc) k->err = 1e-8;  /* DEFAULT_CMVDST_ERR */
+  else if (k->err < DBL_EPSILON) {
+    fprintf(stderr, "Error: `CMVDST_ERR' is smaller than the machine epsilon\n");
+    return PSH_ERR_CFG;
+  }
+  return 0;
+}
+
 /* Format, readability and formatter of the DATA or RAND catalogues. */
 static int check_files(psh_cfg *cfg, const Conf *c, const char *which, int *fmt) {
   char key[32];
@@ -165,12 +227,11 @@ static int verify(psh_cfg *cfg, Conf *c) {
     if (rc == 1) fprintf(stderr, "Error: `CUBIC_SIM' is not set\n");
     return PSH_ERR_CFG;
   }
-  if (!c->issim && (psh_size(cfg, "DATA_CONVERT") || psh_size(cfg, "RAND_CONVERT"))) {
-    /* set at all, the reference converts (src/load_conf.c:949-968) */
-    fprintf(stderr, "Error: coordinate conversion (`DATA_CONVERT', `RAND_CONVERT') is not "
-                    "supported; give Cartesian comoving coordinates\n");
-    return PSH_ERR_CFG;
-  }
+  /* coordinate conversion: needed when DATA_CONVERT or RAND_CONVERT is set
+   * at all (src/load_conf.c:949-968); each catalogue is converted by its
+   * own value */
+  c->cnvt = !c->issim && (psh_size(cfg, "DATA_CONVERT") || psh_size(cfg, "RAND_CONVERT"));
+  if (c->cnvt && (rc = check_cosmo(cfg, c))) return rc;
   c->ovwrite = 0;
   if (psh_int(cfg, "OVERWRITE", 0, &c->ovwrite) < 0) return PSH_ERR_CFG;
   c->iscross = false;
@@ -452,6 +513,38 @@ static int save(const Conf *c, const size_t *ndata, const double *wdata, const s
   return 0;
 }
 
+/* Converts the catalogues flagged by DATA_CONVERT / RAND_CONVERT
+ * (src/cnvt_coord.c:439-582): the quadrature order is chosen on the range of
+ * all their redshifts. */
+static int convert(Conf *c, double **data, const size_t *nd, double **rand, const size_t *nr) {
+  printf("Converting coordinates ...\n");
+  double zmin = DBL_MAX, zmax = -DBL_MAX;
+  for (int i = 0; i < c->ndata; i++)
+    for (int r = 0; r < 2; r++) {
+      if (!(r ? c->rcnvt[i] : c->dcnvt[i])) continue;
+      const double *p = r ? rand[i] : data[i];
+      const size_t n = r ? nr[i] : nd[i];
+      for (size_t k = 0; k < n; k++) {
+        const double z = p[4 * k + 2];
+        if (z < 0) {
+          fprintf(stderr, "Error: invalid negative redshift in the %s catalog:\n(%g, %g, %g)\n",
+                  r ? "random" : "data", p[4 * k], p[4 * k + 1], z);
+          return PSH_ERR_CATA;
+        }
+        if (zmax < z) zmax = z;
+        if (zmin > z) zmin = z;
+      }
+    }
+  int rc = 0;
+  if (zmin <= zmax || c->ztab) rc = psh_cosmo_init(&c->cosmo, c->ztab, zmin, zmax, c->verbose);
+  for (int i = 0; i < c->ndata && !rc; i++) {
+    if (c->dcnvt[i]) psh_cosmo_convert(&c->cosmo, data[i], nd[i], 0);
+    if (c->rcnvt[i]) psh_cosmo_convert(&c->cosmo, rand[i], nr[i], 0);
+  }
+  psh_cosmo_free(&c->cosmo);
+  return rc;
+}
+
 int main(int argc, char **argv) {
   psh_cfg cfg = {NULL, 0};
   int rc = psh_cfg_init(&cfg);
@@ -489,23 +582,27 @@ int main(int argc, char **argv) {
   double *xyzw[2] = {NULL, NULL}, *rxyzw[2] = {NULL, NULL};
   size_t ndata[2] = {0, 0}, nrand[2] = {0, 0};
   double wsum[2] = {0, 0}, wrand[2] = {0, 0}, shot[2] = {0, 0}, norm[2] = {0, 0};
+  double s2[2][2] = {{0, 0}, {0, 0}}, s2n[2][2] = {{0, 0}, {0, 0}};
   for (int i = 0; i < c.ndata && !rc; i++) {
-    double s2[2] = {0, 0}, s2n[2] = {0, 0};
-    rc = read_cat(&cfg, &c, "DATA", i, c.dfmt[i], &xyzw[i], &ndata[i], &wsum[i], &s2[0], &s2n[0]);
-    if (rc || c.issim) continue;
-    rc = read_cat(&cfg, &c, "RAND", i, c.rfmt[i], &rxyzw[i], &nrand[i], &wrand[i], &s2[1], &s2n[1]);
-    if (rc) continue;
+    rc = read_cat(&cfg, &c, "DATA", i, c.dfmt[i], &xyzw[i], &ndata[i], &wsum[i], &s2[i][0],
+                  &s2n[i][0]);
+    if (!rc && !c.issim)
+      rc = read_cat(&cfg, &c, "RAND", i, c.rfmt[i], &rxyzw[i], &nrand[i], &wrand[i], &s2[i][1],
+                    &s2n[i][1]);
+  }
+  if (!rc && c.cnvt) rc = convert(&c, xyzw, ndata, rxyzw, nrand);
+  for (int i = 0; i < c.ndata && !rc && !c.issim; i++) {
     /* alpha, shot noise and normalisation (src/read_cata.c:165-183) */
-    if (wsum[i] == 0 || s2[0] == 0) {
+    if (wsum[i] == 0 || s2[i][0] == 0) {
       fprintf(stderr, "Error: invalid completeness or FKP weights in the data catalog\n");
       rc = PSH_ERR_CATA;
-    } else if (wrand[i] == 0 || s2[1] == 0) {
+    } else if (wrand[i] == 0 || s2[i][1] == 0) {
       fprintf(stderr, "Error: invalid completeness or FKP weights in the random catalog\n");
       rc = PSH_ERR_CATA;
     } else {
       const double alpha = wsum[i] / wrand[i];
-      shot[i] = s2[0] + alpha * alpha * s2[1];
-      norm[i] = (s2n[0] == 0 || s2n[1] != 0) ? alpha * s2n[1] : s2n[0];
+      shot[i] = s2[i][0] + alpha * alpha * s2[i][1];
+      norm[i] = (s2n[i][0] == 0 || s2n[i][1] != 0) ? alpha * s2n[i][1] : s2n[i][0];
       /* data minus alpha x randoms in one catalogue: weights -alpha w */
       double *all = realloc(xyzw[i], sizeof(double) * 4 * (ndata[i] + nrand[i]));
       if (!all) {

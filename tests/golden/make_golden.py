@@ -17,7 +17,9 @@ these are the pins of the oracle and of the GPU path:
 * ``survey/``: a survey-like data catalogue (a clustered sphere) and its
   randoms, with completeness weights, n(z) and FKP weights, and the
   reference POWSPEC monopole for CUBIC_SIM = F with the box fitted to the
-  catalogues (ref_auto.txt) and with BOX_SIZE given (ref_auto_box.txt).
+  catalogues (ref_auto.txt) and with BOX_SIZE given (ref_auto_box.txt);
+  the same objects as (RA, Dec, z) converted by quadrature
+  (ref_auto_cnvt.txt) and by a distance table (ref_auto_table.txt).
 
 Usage (in a tree that has the reference sources):
     python tests/golden/make_golden.py          # everything
@@ -179,6 +181,44 @@ def survey():
         subprocess.run([oracle.REF_CLI, "-c", conf], cwd=d, check=True, env=env,
                        stdout=subprocess.DEVNULL)
     print("survey fixture written:", len(data), "data,", len(rand), "randoms")
+    survey_converted(d, data, rand, rng, env)
+
+
+def survey_converted(d, data, rand, rng, env):
+    """The same objects as (RA, Dec, redshift) for OMEGA_M = 0.31 (flat,
+    w = -1): redshifts from the comoving distance by inverting a fine table
+    of the adaptive-quadrature distance.  Run with DATA_CONVERT /
+    RAND_CONVERT (Gauss-Legendre, ref_auto_cnvt.txt) and with a
+    Z_CMVDST_CNVT table of 400 samples (ref_auto_table.txt)."""
+    from scipy import integrate
+    om = 0.31
+
+    def dist(z):
+        return integrate.quad(lambda t: 2997.92458 / np.sqrt(om * (1 + t) ** 3 + 1 - om), 0, z,
+                              epsabs=0, epsrel=1e-13)[0]
+
+    zg = np.linspace(0.0, 0.6, 6001)
+    dg = np.array([dist(z) for z in zg])
+    for name, pts in (("data_radecz.txt", data), ("rand_radecz.txt", rand)):
+        r = np.sqrt(np.sum(pts * pts, axis=1))
+        ra = np.degrees(np.arctan2(pts[:, 1], pts[:, 0])) % 360.0
+        dec = np.degrees(np.arcsin(pts[:, 2] / r))
+        z = np.interp(r, dg, zg)
+        cols = np.column_stack([ra, dec, z, rng.uniform(0.8, 1.2, len(pts)),
+                                np.full(len(pts), 1e-4)])
+        np.savetxt(os.path.join(d, name), cols, fmt="%.9f %.9f %.10f %.4f %.8e")
+    zt = np.linspace(0.0, 0.6, 400)
+    np.savetxt(os.path.join(d, "z_dist.txt"), np.column_stack([zt, [dist(z) for z in zt]]),
+               fmt="%.10f %.10f")
+    base = (SURVEY_CONF.replace("data.txt", "data_radecz.txt").replace("rand.txt", "rand_radecz.txt")
+            + "DATA_CONVERT    = T\nRAND_CONVERT    = T\n")
+    for conf, extra, out in (("powspec_cnvt.conf", "OMEGA_M         = 0.31\n", "ref_auto_cnvt.txt"),
+                             ("powspec_table.conf", "Z_CMVDST_CNVT   = z_dist.txt\n", "ref_auto_table.txt")):
+        with open(os.path.join(d, conf), "w") as f:
+            f.write(base.format(out=out) + extra)
+        subprocess.run([oracle.REF_CLI, "-c", conf], cwd=d, check=True, env=env,
+                       stdout=subprocess.DEVNULL)
+    print("converted survey fixture written")
 
 
 if __name__ == "__main__":

@@ -158,14 +158,18 @@ def test_cli_output_matches_reference_file(cli, workdir):
 
 @pytest.fixture
 def survey_dir(tmp_path):
-    for f in ("data.txt", "rand.txt", "powspec.conf", "powspec_box.conf"):
+    for f in ("data.txt", "rand.txt", "powspec.conf", "powspec_box.conf", "data_radecz.txt",
+              "rand_radecz.txt", "z_dist.txt", "powspec_cnvt.conf", "powspec_table.conf"):
         shutil.copy(os.path.join(GOLDEN, "survey", f), tmp_path / f)
     return tmp_path
 
 
 @pytest.mark.parametrize("args,msg", [
     (["--pole", "[0, 2]"], "MULTIPOLE"),
-    (["--data-convert", "F"], "coordinate conversion"),
+    (["--data-convert", "T"], "OMEGA_M"),
+    (["--data-convert", "T", "--omega-m", "1.5"], "OMEGA_M"),
+    (["--data-convert", "T", "--omega-m", "0.3", "--eos-w", "-0.2"], "DE_EOS_W"),
+    (["--data-convert", "T", "--omega-m", "0.3", "--cmvdst-err", "1e-20"], "CMVDST_ERR"),
     (["--rand-pos", "[$1, $2]"], "RAND_POSITION"),
 ])
 def test_survey_configuration_errors(cli, survey_dir, args, msg):
@@ -201,13 +205,24 @@ def _compare(got_path, ref_path):
     return np.abs(g - f) / (np.abs(f) + shot)
 
 
+def test_converted_survey_catalogues_are_read(cli, survey_dir):
+    r = run(cli, ["-c", "powspec_cnvt.conf", "-a", "o.txt", "-v", "T"], survey_dir)
+    assert "Legendre-Gauss order" in r.stdout, r.stdout + r.stderr
+    assert "Box size: [410, 410, 410]" in r.stdout
+    r = run(cli, ["-c", "powspec_table.conf", "-a", "o.txt", "-v", "T"], survey_dir)
+    assert "400 comoving distance samples read" in r.stdout, r.stdout + r.stderr
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("conf,ref", [("powspec.conf", "ref_auto.txt"),
-                                      ("powspec_box.conf", "ref_auto_box.txt")])
+                                      ("powspec_box.conf", "ref_auto_box.txt"),
+                                      ("powspec_cnvt.conf", "ref_auto_cnvt.txt"),
+                                      ("powspec_table.conf", "ref_auto_table.txt")])
 def test_survey_monopole_matches_reference_file(cli, survey_dir, conf, ref):
     """Data minus alpha x randoms with FKP weights in the fitted (or given,
-    non-cubic) box: the reference's header lines, k columns and mode counts,
-    and P_0 within 1e-5 of |P_0| + shot noise (bin 0 holds the k = 0 mode)."""
+    non-cubic) box, from Cartesian or converted (RA, Dec, z) coordinates: the
+    reference's header lines, k columns and mode counts, and P_0 within 1e-5
+    of |P_0| + shot noise (bin 0 holds the k = 0 mode)."""
     r = run(cli, ["-c", conf, "-a", "gpu_auto.txt"], survey_dir)
     assert r.returncode == 0, r.stdout + r.stderr
     d = _compare(survey_dir / "gpu_auto.txt", os.path.join(GOLDEN, "survey", ref))

@@ -268,3 +268,74 @@ def test_survey_weights_and_sums(host, tmp_path, nthread):
         s2n += x * y * y * z
     assert w.value == pytest.approx(s, rel=1e-14)
     assert w2.value == pytest.approx(s2, rel=1e-13) and w2n.value == pytest.approx(s2n, rel=1e-13)
+
+
+class Cosmo(ctypes.Structure):
+    _fields_ = [("omega_m", ctypes.c_double), ("omega_l", ctypes.c_double),
+                ("omega_k", ctypes.c_double), ("eos_w", ctypes.c_double), ("err", ctypes.c_double),
+                ("widx", ctypes.c_double), ("order", ctypes.c_int),
+                ("x", ctypes.c_double * 32), ("w", ctypes.c_double * 32),
+                ("tz", ctypes.POINTER(ctypes.c_double)), ("td", ctypes.POINTER(ctypes.c_double)),
+                ("typp", ctypes.POINTER(ctypes.c_double)), ("ntab", ctypes.c_size_t)]
+
+
+@pytest.fixture(scope="module")
+def cnvt(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("cnvt") / "libpscnvt.so")
+    srcs = [os.path.join(HOST, f) for f in ("ps_cnvt.c", "ps_read.c", "ps_expr.c")]
+    subprocess.run(["gcc", "-std=c99", "-O2", "-Wall", "-shared", "-fPIC", "-pthread", "-I" + HOST,
+                    "-o", out] + srcs + ["-lm"], check=True)
+    lib = ctypes.CDLL(out)
+    lib.psh_cosmo_init.argtypes = [ctypes.POINTER(Cosmo), ctypes.c_char_p, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_bool]
+    lib.psh_cosmo_distance.restype = ctypes.c_double
+    lib.psh_cosmo_distance.argtypes = [ctypes.POINTER(Cosmo), ctypes.c_double]
+    lib.psh_cosmo_convert.argtypes = [ctypes.POINTER(Cosmo), ctypes.c_void_p, ctypes.c_size_t,
+                                      ctypes.c_int]
+    lib.psh_cosmo_free.argtypes = [ctypes.POINTER(Cosmo)]
+    return lib
+
+
+@pytest.mark.parametrize("om,ol,w", [(0.31, 0.69, -1.0), (0.3, 0.6, -0.9)])
+def test_comoving_distance_quadrature(cnvt, om, ol, w):
+    """Gauss-Legendre quadrature of c/(100 km/s) / E(z) at the order that
+    converges to CMVDST_ERR on the redshift range (src/cnvt_coord.c:295-400),
+    against adaptive quadrature; then (RA, Dec, z) -> Cartesian."""
+    integrate = pytest.importorskip("scipy.integrate")
+    c = Cosmo(om, ol, 1 - om - ol, w, 1e-8, 0.0, 0)
+    assert cnvt.psh_cosmo_init(ctypes.byref(c), None, 0.0, 2.0, False) == 0
+    assert 4 <= c.order <= 32
+    wi = 3 * (1 + w)
+
+    def e(z):
+        z1 = 1 + z
+        return np.sqrt(om * z1 ** 3 + (1 - om - ol) * z1 ** 2 + ol * z1 ** wi)
+
+    for z in (0.0, 0.1, 0.57, 1.3, 2.0):
+        ref = integrate.quad(lambda t: 2997.92458 / e(t), 0, z, epsabs=0, epsrel=1e-13)[0]
+        assert cnvt.psh_cosmo_distance(ctypes.byref(c), z) == pytest.approx(ref, rel=1e-9, abs=1e-12)
+    rng = np.random.default_rng(2)
+    rec = np.column_stack([rng.uniform(0, 360, 5000), rng.uniform(-90, 90, 5000),
+                           rng.uniform(0, 2, 5000), np.ones(5000)])
+    out = rec.copy()
+    cnvt.psh_cosmo_convert(ctypes.byref(c), out.ctypes.data, len(out), 3)
+    d = np.array([cnvt.psh_cosmo_distance(ctypes.byref(c), z) for z in rec[:, 2]])
+    ra, dec = np.radians(rec[:, 0]), np.radians(rec[:, 1])
+    assert np.allclose(out[:, 0], d * np.cos(dec) * np.cos(ra), rtol=1e-13, atol=1e-9)
+    assert np.allclose(out[:, 2], d * np.sin(dec), rtol=1e-13, atol=1e-9)
+
+
+def test_comoving_distance_table_spline(cnvt, tmp_path):
+    """Z_CMVDST_CNVT: a natural cubic spline through the (z, D) samples."""
+    interpolate = pytest.importorskip("scipy.interpolate")
+    z = np.linspace(0.0, 1.5, 37) ** 1.3
+    d = 3000 * z / (1 + 0.3 * z)
+    p = tmp_path / "zd.txt"
+    np.savetxt(p, np.column_stack([z, d]), fmt="%.17g", header="z D")
+    c = Cosmo()
+    assert cnvt.psh_cosmo_init(ctypes.byref(c), str(p).encode(), 0.0, 0.0, False) == 0
+    sp = interpolate.CubicSpline(z, d, bc_type="natural")
+    for zz in np.linspace(0, z[-1] * 0.999, 50):
+        assert cnvt.psh_cosmo_distance(ctypes.byref(c), zz) == pytest.approx(float(sp(zz)), rel=1e-12)
+    assert np.isinf(cnvt.psh_cosmo_distance(ctypes.byref(c), z[-1] + 0.1))
+    cnvt.psh_cosmo_free(ctypes.byref(c))
