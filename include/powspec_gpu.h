@@ -115,16 +115,18 @@ int ps_gpu_assign_soa(ps_gpu_ctx *ctx, int cat, const float *x,
                       const float *y, const float *z, const float *w,
                       size_t n, int on_device);
 
-/* Survey catalogue `cat` (CUBIC_SIM = F; monopole only): the context's
- * catalogue holds the data with weights w and the randoms with weights
- * -alpha w, positions minus the box's lower corner (src/genr_mesh.c:797-809,
- * :541-566).  P_0 = (sum / cnt - shot) / norm with the given shot noise and
+/* Survey catalogue `cat` (CUBIC_SIM = F), set before its assign: the
+ * context's catalogue holds the data with weights w and the randoms with
+ * weights -alpha w, positions minus the box's lower corner `origin`
+ * (src/genr_mesh.c:797-809, :541-566); its FP32 mesh keeps its mean.
+ * P_0 = (sum / cnt - shot) / norm with the given shot noise and
  * normalisation (src/read_cata.c:173-183, src/multipole.c:1108-1116); the
  * k = 0 mode is summed when it lies in the first bin (src/multipole.c:593).
- * The result reports shot / norm as its shot noise (src/save_res.c:89).
- * Multipoles l > 0 of surveys (the Yamamoto estimator, src/mp_template.c)
- * are not provided: the context must have poles {0}. */
-int ps_gpu_set_survey(ps_gpu_ctx *ctx, int cat, double shot, double norm);
+ * Multipoles l > 0 (non-interlaced meshes; origin needed, the observer at
+ * 0) come from the spherical-harmonic decomposition of L_l
+ * (src/mp_template.c:48-149): P_l = 4 pi sum Re[F_0 F_l*] / (norm cnt).
+ * The result reports shot / norm as its shot noise (src/save_res.c:89). */
+int ps_gpu_set_survey(ps_gpu_ctx *ctx, int cat, double shot, double norm, const double *origin);
 
 /* Staged input (no counterpart in the reference): ps_gpu_stage_aos starts
  * copying n AoS records from pinned host memory into device slot `slot`

@@ -174,7 +174,8 @@ def lib():
         L.ps_gpu_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ps_gpu_stage_aos.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
         L.ps_gpu_assign_staged.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
-        L.ps_gpu_set_survey.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.ps_gpu_set_survey.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -331,11 +332,15 @@ class Estimator:
                        v(dense_lane_groups), rg], np.int32)
         self._check(lib().ps_gpu_set_tuning(self._ctx, _ptr(ch)))
 
-    def set_survey(self, cat, shot, norm):
-        """Survey normalisation of catalogue `cat` (monopole contexts): P_0 =
-        (sum / cnt - shot) / norm; the catalogue holds the data (weights w)
-        and the randoms (weights -alpha w), relative to the box corner."""
-        self._check(lib().ps_gpu_set_survey(self._ctx, cat, float(shot), float(norm)))
+    def set_survey(self, cat, shot, norm, origin=None):
+        """Survey catalogue `cat`, before its assign: P_0 = (sum / cnt - shot)
+        / norm; multipoles l > 0 by the spherical-harmonic decomposition
+        (non-interlaced meshes; origin = the box corner, the observer at 0).
+        The catalogue holds the data (weights w) and the randoms (weights
+        -alpha w), positions relative to the box corner."""
+        o = None if origin is None else np.ascontiguousarray(origin, dtype=np.float64)
+        self._check(lib().ps_gpu_set_survey(self._ctx, cat, float(shot), float(norm),
+                                            None if o is None else _ptr(o)))
 
     def stage(self, slot, particles):
         """Starts copying host AoS float64 [N, 4] records (pinned memory for

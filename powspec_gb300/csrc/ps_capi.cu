@@ -161,6 +161,13 @@ struct ps_gpu_ctx {
   // survey normalisation per catalogue (ps_gpu_set_survey)
   bool survey[2] = {false, false};
   double survey_shot[2] = {0, 0}, survey_norm[2] = {0, 0};
+  double survey_origin[3] = {0, 0, 0};  // box corner, the observer at 0
+  // survey multipoles l > 0: stored fields F_0 and F_l per catalogue, an
+  // r2c scratch (3 half-complex fields) and a weighted real mesh
+  void* d_yama = nullptr;
+  size_t yama_bytes = 0;
+  float2* d_dc = nullptr;  // F_l at k = 0 per catalogue
+  bool yama_last = false;  // the last execute took the survey-multipole path
   int last_cat = -1;
   Particles last_pt{};
   std::vector<double> kmu;   // last execute's raw (k, |mu|) sums
@@ -266,7 +273,7 @@ int alloc_accum(ps_gpu_ctx* c) {
   c->h_out = nullptr;
   CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)std::max(c->grid_c, c->grid_ct) * width));
   CU(cudaMalloc(&c->d_sums, sizeof(double) * width));
-  CU(cudaMallocHost(&c->h_out, sizeof(double) * (width + 8)));
+  CU(cudaMallocHost(&c->h_out, sizeof(double) * (width + 10)));
   return 0;
 }
 
@@ -520,7 +527,8 @@ void ps_gpu_destroy(ps_gpu_ctx* c) {
   void* bufs[] = {c->d_bintab, c->d_ksq, c->d_win, c->d_phase, c->d_tw_full, c->d_tw_half,
                   c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage,
                   c->d_hist, c->d_bsum, c->d_rank, c->d_rec, c->d_region, c->d_lgeo,
-                  c->d_lx, c->d_lxb, c->d_lc, c->d_lout, c->d_slot[0], c->d_slot[1]};
+                  c->d_lx, c->d_lxb, c->d_lc, c->d_lout, c->d_slot[0], c->d_slot[1],
+                  c->d_yama, c->d_dc};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -628,6 +636,7 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat, size_t n) {
   g.sparse_max = c->gather_sparse_max;
   g.region = use_region(c, n) ? 1 : 0;
   g.regbuf = c->d_region;
+  g.nomean = c->survey[cat] ? 1 : 0;
   g.regflag = c->d_region ? reinterpret_cast<unsigned char*>(c->d_region + region_words(c)) : nullptr;
   return g;
 }
@@ -809,6 +818,18 @@ int finish(ps_gpu_ctx* c, const double* h, const size_t* npart, ps_gpu_result* r
         double v = sums[((size_t)s2 * npole + l) * nbin + i];
         const double cn = (double)c->cnt[i];
         const bool sv = cat >= 0 ? c->survey[cat] : (c->survey[0] && c->survey[1]);
+        if (sv && p.poles[l] > 0 && c->yama_last) {
+          // src/multipole.c:1118-1150: (F_0, F_l) pairs, the k = 0 mode
+          // F_0(0) = W times Re F_l(0) when bin 0 holds it
+          const int a = c->spec_a[s2], b = c->spec_b[s2];
+          const double* dc = h + (size_t)nacc * nkey + 8;  // Re F_l(0) per catalogue
+          if (dc_bin && i == 0)
+            v += (cat >= 0) ? wsum[2 * a] * dc[a] : wsum[2 * a] * dc[b] + wsum[2 * b] * dc[a];
+          if (c->cnt[i])
+            v *= (cat >= 0 ? 4 * M_PI / r->norm[cat] : 2 * M_PI / sqrt(r->norm[0] * r->norm[1])) / cn;
+          dst[(size_t)l * nbin + i] = v;
+          continue;
+        }
         if (sv && dc_bin && i == 0 && p.poles[l] == 0)
           v += wsum[2 * c->spec_a[s2]] * wsum[2 * c->spec_b[s2]];
         if (cat >= 0) {
@@ -959,6 +980,144 @@ int ps_gpu_assign_soa(ps_gpu_ctx* c, int cat, const float* x, const float* y, co
   return assign_common(c, cat, pt);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Plain r2c of a real device mesh into a stored half-complex field
+// [x][y][z/2+1] (the z, y and x passes; a1, a2: scratch fields).
+void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* out) {
+  cudaStream_t s = c->stream;
+  PassAArgs a;
+  memset(&a, 0, sizeof a);
+  a.ng = c->ng;
+  a.ty = c->ty_a;
+  a.fgrid = in;
+  a.out = a1;
+  a.tw_half = c->d_tw_half;
+  a.tw_full = c->d_tw_full;
+  a.plan_half = c->plan_half;
+  a.err = c->d_err + 2;
+  launch_pass_a(a, s);
+  PassBArgs b;
+  memset(&b, 0, sizeof b);
+  b.ng = c->ng;
+  b.tx = c->tx_b;
+  b.in = a1;
+  b.out = a2;
+  b.tw_full = c->d_tw_full;
+  b.plan_full = c->plan_full;
+  b.err = c->d_err + 2;
+  launch_pass_b(b, s);
+  PassCArgs pc;
+  memset(&pc, 0, sizeof pc);
+  pc.ng = c->ng;
+  pc.ty = std::max(1, std::min(c->ng, kPassCElems / c->ng));
+  pc.nfield = 1;
+  pc.ncat = 1;
+  pc.nspec = 1;
+  pc.in[0] = a2;
+  pc.store = out;
+  pc.tw_full = c->d_tw_full;
+  pc.plan_full = c->plan_full;
+  pc.geom = c->geom;
+  launch_pass_c(pc, s);
+  c->launches += 3;
+}
+
+// Per-CTA partial sums of Re[f1 f2*] x window x weight per k bin (the k = 0
+// mode left out), added onto the partials (zeroed by the caller).
+void bin_pair(ps_gpu_ctx* c, const float2* f1, const float2* f2) {
+  BinFieldArgs b;
+  b.ng = c->ng;
+  b.f1 = f1;
+  b.f2 = f2;
+  b.geom = c->geom;
+  b.geom.nmu = 1;
+  b.geom.npole = 1;  // l = 0 weights: the multipole is in the fields
+  for (int q = 0; q < 4; q++) b.geom.lc[0][q] = q == 0 ? 1.f : 0.f;
+  b.geom.lodd = 0;
+  b.partials = c->d_part;
+  b.grid = c->grid_c;
+  launch_bin_fields(b, c->stream);
+  c->launches++;
+}
+
+// Survey catalogues with multipoles l > 0 (src/multipole.c:1179-1250):
+// F_0 of each catalogue's mesh, then per l the field F_l of the harmonic
+// decomposition, and the (F_0, F_l) pair sums; raw sums into c->d_sums as
+// [spec][pole][bin], Re F_l(0) per catalogue into c->d_dc.
+int enqueue_survey_multipoles(ps_gpu_ctx* c) {
+  const ps_gpu_params& p = c->p;
+  cudaStream_t s = c->stream;
+  const size_t cx = c->ncx * sizeof(float2), real = c->ntot * sizeof(float);
+  const size_t need = (size_t)(3 + 2 * p.ncat) * cx + real;
+  if (need > c->yama_bytes) {
+    CU(cudaStreamSynchronize(s));
+    if (c->d_yama) cudaFree(c->d_yama);
+    c->d_yama = nullptr;
+    c->yama_bytes = 0;
+    CU(cudaMalloc(&c->d_yama, need));
+    c->yama_bytes = need;
+  }
+  if (!c->d_dc) CU(cudaMalloc(&c->d_dc, 2 * sizeof(float2)));
+  float2* base = (float2*)c->d_yama;
+  float2 *a1 = base, *a2 = base + c->ncx, *fa = base + 2 * c->ncx;
+  // fields: a1, a2, fa, then F_0 and F_l of catalogue 0 (and 1)
+  float2* f0[2] = {base + 3 * c->ncx, base + 5 * c->ncx};
+  float2* fl[2] = {base + 4 * c->ncx, base + 6 * c->ncx};
+  float* wmesh = (float*)(base + (size_t)(3 + 2 * p.ncat) * c->ncx);
+  CU(cudaEventRecord(c->ev[0], s));
+  for (int k = 0; k < p.ncat; k++) r2c_store(c, (const float*)c->grid[k], a1, a2, f0[k]);
+  CU(cudaEventRecord(c->ev[1], s));
+  CU(cudaEventRecord(c->ev[2], s));
+  const int nbin = c->nbin, npole = p.npole;
+  for (int l = 0; l < npole; l++) {
+    const int ell = p.poles[l];
+    if (ell > 0)
+      for (int k = 0; k < p.ncat; k++) {
+        for (int m = -ell; m <= ell; m++) {
+          double f = 1;  // (l - |m|)! / (l + |m|)!
+          for (int q = ell - abs(m) + 1; q <= ell + abs(m); q++) f /= q;
+          const double kl = sqrt((2 * ell + 1) / (4 * M_PI) * f) * (m ? sqrt(2.0) : 1.0);
+          launch_ylm_real((const float*)c->grid[k], wmesh, c->ng, ell, m, kl, c->survey_origin,
+                          p.box, s);
+          r2c_store(c, wmesh, a1, a2, fa);
+          launch_ylm_acc(fa, fl[k], c->ng, ell, m, kl, p.box, m == -ell, s);
+          c->launches += 2;
+        }
+        CU(cudaMemcpyAsync(c->d_dc + k, fl[k], sizeof(float2), cudaMemcpyDeviceToDevice, s));
+      }
+    for (int sp = 0; sp < c->nspec; sp++) {
+      const int a = c->spec_a[sp], b = c->spec_b[sp];
+      CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)c->grid_c * nbin, s));
+      if (ell == 0) {
+        bin_pair(c, f0[a], f0[b]);
+      } else {
+        bin_pair(c, f0[a], fl[b]);
+        if (a != b) bin_pair(c, f0[b], fl[a]);
+      }
+      launch_reduce(c->d_part, c->grid_c, nbin, c->d_sums + ((size_t)sp * npole + l) * nbin, s);
+      c->launches++;
+    }
+  }
+  CU(cudaEventRecord(c->ev[3], s));
+  CU(cudaEventRecord(c->ev[4], s));
+  CU(cudaGetLastError());
+  return 0;
+}
+
+bool survey_multipoles(const ps_gpu_ctx* c) {
+  bool high = false;
+  for (int l = 0; l < c->p.npole; l++) high |= c->p.poles[l] > 0;
+  for (int k = 0; k < c->p.ncat; k++) high &= c->survey[k];
+  return high;
+}
+
+}  // namespace
+
+extern "C" {
+
 int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   if (!c || !r) return fail(c, PS_GPU_ERR_ARG, "null argument");
   const ps_gpu_params& p = c->p;
@@ -968,13 +1127,19 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   cudaStream_t s = c->stream;
   const int nacc = c->nspec * p.npole;
   const int nkey = c->nbin * c->nmu;
-  int rc = enqueue_passes(c, c->d_sums, true);
+  const bool yama = survey_multipoles(c);
+  c->yama_last = yama;
+  int rc = yama ? enqueue_survey_multipoles(c) : enqueue_passes(c, c->d_sums, true);
   if (rc) return rc;
   double* h = c->h_out;
   CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nkey, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey + 4, c->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+  float2 dc[2] = {{0, 0}, {0, 0}};
+  if (yama) CU(cudaMemcpyAsync(dc, c->d_dc, sizeof(dc), cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
+  h[(size_t)nacc * nkey + 8] = dc[0].x;
+  h[(size_t)nacc * nkey + 9] = dc[1].x;
   float t = 0;
   if (c->assign_started && cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess) c->timings[0] = t;
   for (int i = 0; i < 4; i++)
@@ -985,16 +1150,22 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   return finish(c, h, c->npart, r, true);
 }
 
-int ps_gpu_set_survey(ps_gpu_ctx* c, int cat, double shot, double norm) {
+int ps_gpu_set_survey(ps_gpu_ctx* c, int cat, double shot, double norm, const double* origin) {
   if (!c || cat < 0 || cat >= c->p.ncat) return fail(c, PS_GPU_ERR_ARG, "invalid survey arguments");
-  if (c->p.npole != 1 || c->p.poles[0] != 0)
+  bool high = false;
+  for (int l = 0; l < c->p.npole; l++) high |= c->p.poles[l] > 0;
+  if (high && c->p.interlace)
     return fail(c, PS_GPU_ERR_ARG,
-                "survey catalogues: only the monopole (multipoles l > 0 need the Yamamoto "
-                "estimator, which this library does not provide)");
+                "survey multipoles l > 0 need a mesh without interlacing (the interlaced "
+                "field's inverse transform is not provided)");
+  if (high && !origin) return fail(c, PS_GPU_ERR_ARG, "survey multipoles l > 0 need the box corner");
+  if (high && c->nmu != 1) return fail(c, PS_GPU_ERR_ARG, "survey multipoles take no |mu| sub-bins");
   if (!(norm > 0) || !(shot >= 0)) return fail(c, PS_GPU_ERR_ARG, "survey normalisation must be > 0");
   c->survey[cat] = true;
   c->survey_shot[cat] = shot;
   c->survey_norm[cat] = norm;
+  if (origin)
+    for (int d = 0; d < 3; d++) c->survey_origin[d] = origin[d];
   return 0;
 }
 
@@ -1002,9 +1173,11 @@ int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* p
   if (!c || !m || !r || !pl_corr) return fail(c, PS_GPU_ERR_ARG, "null argument");
   const ps_gpu_params& p = c->p;
   if (p.ncat != 1 || p.npole != 3 || p.poles[0] != 0 || p.poles[1] != 2 || p.poles[2] != 4 ||
-      p.logscale)
+      p.logscale || c->survey[0])
     return fail(c, PS_GPU_ERR_ARG,
-                "the learned correction needs one catalogue, poles (0, 2, 4) and linear bins");
+                "the learned correction needs one simulation-box catalogue, poles (0, 2, 4) and "
+                "linear bins");
+  c->yama_last = false;
   if (!c->assigned[0]) return fail(c, PS_GPU_ERR_STATE, "catalogue 0 not assigned");
   CU(cudaSetDevice(p.device));
   cudaStream_t s = c->stream;
@@ -1263,6 +1436,7 @@ int ps_gpu_batch_create(ps_gpu_ctx* c, int ncat, const double* const* xyzw, cons
   if (!c || !out || ncat < 1 || !xyzw || !n) return fail(c, PS_GPU_ERR_ARG, "invalid batch arguments");
   *out = nullptr;
   if (c->p.ncat != 1) return fail(c, PS_GPU_ERR_ARG, "batches need a single-catalogue context");
+  if (c->survey[0]) return fail(c, PS_GPU_ERR_ARG, "batches take simulation-box catalogues");
   size_t nmax = 0;
   for (int i = 0; i < ncat; i++) {
     if (n[i] && (!xyzw[i] || ((uintptr_t)xyzw[i] & 31)))

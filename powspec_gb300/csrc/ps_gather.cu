@@ -760,7 +760,8 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
   }
   __syncthreads();
   // write the tile: rows of T cells along z
-  const long long off = INT64 ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
+  const long long off =
+      (INT64 || g.nomean) ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
   if constexpr (TT == 16) {
     // 4 consecutive z cells per thread and step; untouched rows are -mean
     const float cst = fix_to_float(-off);
@@ -1029,7 +1030,8 @@ __global__ void __launch_bounds__(256, 4) k_region_sum(const __grid_constant__ G
   static_assert((1 - of) % 2 == 0, "home block of z words starts on a 16-byte boundary");
   const int ng = g.ng, nt = g.nt, nm = g.interlace ? 2 : 1, nq = ng >> 3;
   const size_t per = (size_t)ng * ng * nq;
-  const long long off = INT64 ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
+  const long long off =
+      (INT64 || g.nomean) ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < (size_t)nm * per;
        e += (size_t)gridDim.x * blockDim.x) {
     const int m = (int)(e / per);

@@ -46,6 +46,7 @@ struct GatherArgs {
   int region;              // 1: each record once, into its home tile's region (TSC/PCS, T = 16)
   unsigned long long* regbuf;  // [tiles][meshes][gather_region_words()] region sums
   unsigned char* regflag;      // [tiles] 1: the tile wrote its region (it has records)
+  int nomean;                  // 1: FP32 meshes keep their mean (survey catalogues)
 };
 // Learned correction on the device (ps_mlp.cu), after a binning pass with
 // |mu| sub-bins: cell features, network, corrected multipoles.
@@ -65,6 +66,14 @@ struct LearnedArgs {
 };
 int learned_enqueue(::ps_mlp* m, const LearnedArgs& a, cudaStream_t s);
 int learned_feature_width();
+
+// Survey multipoles l > 0 (ps_yama.cu): out = in * Y_lm(r^) over the real
+// mesh, the observer at the origin, the box corner at `origin`; acc (+)= f *
+// Y_lm(k^) over a stored half-complex field.  kl: the harmonic's constant.
+int launch_ylm_real(const float* in, float* out, int ng, int l, int m, double kl,
+                    const double origin[3], const double box[3], cudaStream_t s);
+int launch_ylm_acc(const float2* f, float2* acc, int ng, int l, int m, double kl,
+                   const double box[3], bool first, cudaStream_t s);
 
 int gather_tile(int ng);    // tile edge for this mesh size, 0 if unsupported
 // Region path: possible for this mesh and scheme; words per tile and mesh.

@@ -6,11 +6,11 @@
  * configuration (src/load_conf.c:876-1130), read the catalogues, build the
  * meshes and evaluate the power spectrum multipoles, save the results
  * (src/save_res.c:35-229, same header lines, columns and number formats).
- * Survey catalogues (CUBIC_SIM = F) are evaluated for the monopole: data
- * minus alpha x randoms with FKP weights in a box fitted to the catalogues
- * (src/read_cata.c:95-185, src/genr_mesh.c:427-566, :797-809).  Multipoles
- * l > 0 of surveys (the Yamamoto estimator), coordinate conversion and FITS
- * catalogues are outside this program and rejected with an error.  Besides
+ * Survey catalogues (CUBIC_SIM = F): data minus alpha x randoms with FKP
+ * weights in a box fitted to the catalogues (src/read_cata.c:95-185,
+ * src/genr_mesh.c:427-566, :797-809), from Cartesian or converted (RA, Dec,
+ * z) coordinates; multipoles l > 0 by the spherical-harmonic decomposition
+ * on non-interlaced meshes.  FITS catalogues are rejected with an error.  Besides
  * ASCII (DATA_FORMAT = 0), DATA_FORMAT = 2 reads NumPy .npy arrays, whose
  * columns take the same position / weight / selection expressions.
  */
@@ -387,9 +387,9 @@ static int verify(psh_cfg *cfg, Conf *c) {
     return PSH_ERR_CFG;
   }
   for (int i = 0; i < m; i++) c->poles[i] = pl[i];
-  if (!c->issim && (m != 1 || pl[0] != 0)) {
-    fprintf(stderr, "Error: survey catalogues (CUBIC_SIM = F): only `MULTIPOLE' = 0 is "
-                    "supported (l > 0 needs the Yamamoto estimator)\n");
+  if (!c->issim && pl[m - 1] > 0 && c->intlace) {
+    fprintf(stderr, "Error: survey catalogues (CUBIC_SIM = F): `MULTIPOLE' l > 0 needs "
+                    "`GRID_INTERLACE' = F\n");
     return PSH_ERR_CFG;
   }
   c->kmin = 0;
@@ -697,8 +697,8 @@ int main(int argc, char **argv) {
       res.xpl = xpl;
       if (!res.k || !res.kedge || !res.km || !res.cnt || !res.lcnt || !pl || !xpl) rc = PSH_ERR_MEMORY;
       for (int i = 0; i < c.ndata && !rc; i++) {
-        rc = ps_gpu_assign_aos(ctx, i, xyzw[i], ndata[i] + nrand[i], 0);
-        if (!rc && !c.issim) rc = ps_gpu_set_survey(ctx, i, shot[i], norm[i]);
+        if (!c.issim) rc = ps_gpu_set_survey(ctx, i, shot[i], norm[i], c.bmin);
+        if (!rc) rc = ps_gpu_assign_aos(ctx, i, xyzw[i], ndata[i] + nrand[i], 0);
         if (rc) fprintf(stderr, "Error: %s\n", ps_gpu_last_error(ctx));
         free(xyzw[i]);  /* the reference frees the catalogue after assignment */
         xyzw[i] = NULL;

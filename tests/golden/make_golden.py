@@ -19,7 +19,9 @@ these are the pins of the oracle and of the GPU path:
   reference POWSPEC monopole for CUBIC_SIM = F with the box fitted to the
   catalogues (ref_auto.txt) and with BOX_SIZE given (ref_auto_box.txt);
   the same objects as (RA, Dec, z) converted by quadrature
-  (ref_auto_cnvt.txt) and by a distance table (ref_auto_table.txt).
+  (ref_auto_cnvt.txt) and by a distance table (ref_auto_table.txt); the
+  multipoles 0, 2, 4 on a non-interlaced mesh (ref_auto_yama.txt) and their
+  cross spectrum of the catalogue with itself (ref_cross_yama.txt).
 
 Usage (in a tree that has the reference sources):
     python tests/golden/make_golden.py          # everything
@@ -181,6 +183,33 @@ def survey():
         subprocess.run([oracle.REF_CLI, "-c", conf], cwd=d, check=True, env=env,
                        stdout=subprocess.DEVNULL)
     print("survey fixture written:", len(data), "data,", len(rand), "randoms")
+    # multipoles l > 0 (non-interlaced mesh): auto, and the cross spectrum
+    # of the catalogue with itself
+    yama = SURVEY_CONF.replace("GRID_INTERLACE  = T", "GRID_INTERLACE  = F").replace(
+        "MULTIPOLE       = 0", "MULTIPOLE       = [0, 2, 4]")
+    with open(os.path.join(d, "powspec_yama.conf"), "w") as f:
+        f.write(yama.format(out="ref_auto_yama.txt"))
+    twice = {"DATA_CATALOG": "[data.txt, data.txt]", "RAND_CATALOG": "[rand.txt, rand.txt]",
+             "DATA_FORMATTER": '["%lf %lf %lf %lf %lf", "%lf %lf %lf %lf %lf"]',
+             "RAND_FORMATTER": '["%lf %lf %lf %lf %lf", "%lf %lf %lf %lf %lf"]',
+             "DATA_POSITION": "[$1, $2, $3, $1, $2, $3]", "RAND_POSITION": "[$1, $2, $3, $1, $2, $3]",
+             "DATA_WT_COMP": "[$4, $4]", "RAND_WT_COMP": "[$4, $4]",
+             "DATA_WT_FKP": "[1/(1+$5*2000), 1/(1+$5*2000)]",
+             "RAND_WT_FKP": "[1/(1+$5*2000), 1/(1+$5*2000)]",
+             "DATA_NZ": "[$5, $5]", "RAND_NZ": "[$5, $5]"}
+    lines = []
+    for line in yama.format(out="").splitlines():
+        key = line.split("=")[0].strip()
+        if key in twice:
+            line = "%-16s= %s" % (key, twice[key])
+        elif key == "OUTPUT_AUTO":
+            line = "OUTPUT_CROSS    = ref_cross_yama.txt"
+        lines.append(line)
+    with open(os.path.join(d, "powspec_cross.conf"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    for conf in ("powspec_yama.conf", "powspec_cross.conf"):
+        subprocess.run([oracle.REF_CLI, "-c", conf], cwd=d, check=True, env=env,
+                       stdout=subprocess.DEVNULL)
     survey_converted(d, data, rand, rng, env)
 
 

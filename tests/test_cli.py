@@ -159,13 +159,14 @@ def test_cli_output_matches_reference_file(cli, workdir):
 @pytest.fixture
 def survey_dir(tmp_path):
     for f in ("data.txt", "rand.txt", "powspec.conf", "powspec_box.conf", "data_radecz.txt",
-              "rand_radecz.txt", "z_dist.txt", "powspec_cnvt.conf", "powspec_table.conf"):
+              "rand_radecz.txt", "z_dist.txt", "powspec_cnvt.conf", "powspec_table.conf",
+              "powspec_yama.conf", "powspec_cross.conf"):
         shutil.copy(os.path.join(GOLDEN, "survey", f), tmp_path / f)
     return tmp_path
 
 
 @pytest.mark.parametrize("args,msg", [
-    (["--pole", "[0, 2]"], "MULTIPOLE"),
+    (["--pole", "[0, 2]"], "GRID_INTERLACE"),
     (["--data-convert", "T"], "OMEGA_M"),
     (["--data-convert", "T", "--omega-m", "1.5"], "OMEGA_M"),
     (["--data-convert", "T", "--omega-m", "0.3", "--eos-w", "-0.2"], "DE_EOS_W"),
@@ -192,6 +193,8 @@ def test_survey_catalogues_are_read(cli, survey_dir):
 
 
 def _compare(got_path, ref_path):
+    """Header lines, k columns and counts equal; |dP_l| / (|P_0| + shot) per
+    row and multipole (shot 0 for cross spectra)."""
     got = open(got_path).read().splitlines()
     ref = open(ref_path).read().splitlines()
     assert len(got) == len(ref)
@@ -199,10 +202,10 @@ def _compare(got_path, ref_path):
     rows = [l.split() for l in got if not l.startswith("#")]
     rrows = [l.split() for l in ref if not l.startswith("#")]
     assert [x[:5] for x in rows] == [x[:5] for x in rrows]  # k columns and mode counts
-    shot = float(ref[5].split("Shot noise:")[1].split(",")[0])
-    g = np.array([float(x[5]) for x in rows])
-    f = np.array([float(x[5]) for x in rrows])
-    return np.abs(g - f) / (np.abs(f) + shot)
+    shot = [float(l.split("Shot noise:")[1].split(",")[0]) for l in ref if "Shot noise:" in l]
+    g = np.array([[float(v) for v in x[5:]] for x in rows])
+    f = np.array([[float(v) for v in x[5:]] for x in rrows])
+    return np.abs(g - f) / (np.abs(f[:, :1]) + (shot[0] if shot else 0.0))
 
 
 def test_converted_survey_catalogues_are_read(cli, survey_dir):
@@ -214,16 +217,19 @@ def test_converted_survey_catalogues_are_read(cli, survey_dir):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("conf,ref", [("powspec.conf", "ref_auto.txt"),
-                                      ("powspec_box.conf", "ref_auto_box.txt"),
-                                      ("powspec_cnvt.conf", "ref_auto_cnvt.txt"),
-                                      ("powspec_table.conf", "ref_auto_table.txt")])
-def test_survey_monopole_matches_reference_file(cli, survey_dir, conf, ref):
+@pytest.mark.parametrize("conf,ref,out", [
+    ("powspec.conf", "ref_auto.txt", "-a"), ("powspec_box.conf", "ref_auto_box.txt", "-a"),
+    ("powspec_cnvt.conf", "ref_auto_cnvt.txt", "-a"),
+    ("powspec_table.conf", "ref_auto_table.txt", "-a"),
+    ("powspec_yama.conf", "ref_auto_yama.txt", "-a"),
+    ("powspec_cross.conf", "ref_cross_yama.txt", "-x")])
+def test_survey_matches_reference_file(cli, survey_dir, conf, ref, out):
     """Data minus alpha x randoms with FKP weights in the fitted (or given,
-    non-cubic) box, from Cartesian or converted (RA, Dec, z) coordinates: the
-    reference's header lines, k columns and mode counts, and P_0 within 1e-5
-    of |P_0| + shot noise (bin 0 holds the k = 0 mode)."""
-    r = run(cli, ["-c", conf, "-a", "gpu_auto.txt"], survey_dir)
+    non-cubic) box, from Cartesian or converted (RA, Dec, z) coordinates;
+    multipoles 0, 2, 4 (non-interlaced) auto and cross: the reference's
+    header lines, k columns and mode counts, and P_l within 1e-5 of
+    |P_0| + shot noise (bin 0 holds the k = 0 mode)."""
+    r = run(cli, ["-c", conf, out, "gpu_out.txt"], survey_dir)
     assert r.returncode == 0, r.stdout + r.stderr
-    d = _compare(survey_dir / "gpu_auto.txt", os.path.join(GOLDEN, "survey", ref))
+    d = _compare(survey_dir / "gpu_out.txt", os.path.join(GOLDEN, "survey", ref))
     assert d.max() <= 1e-5, d
