@@ -122,9 +122,10 @@ int ps_gpu_assign_soa(ps_gpu_ctx *ctx, int cat, const float *x,
  * P_0 = (sum / cnt - shot) / norm with the given shot noise and
  * normalisation (src/read_cata.c:173-183, src/multipole.c:1108-1116); the
  * k = 0 mode is summed when it lies in the first bin (src/multipole.c:593).
- * Multipoles l > 0 (non-interlaced meshes; origin needed, the observer at
- * 0) come from the spherical-harmonic decomposition of L_l
- * (src/mp_template.c:48-149): P_l = 4 pi sum Re[F_0 F_l*] / (norm cnt).
+ * Multipoles l > 0 (origin needed, the observer at 0) come from the
+ * spherical-harmonic decomposition of L_l (src/mp_template.c:48-149):
+ * P_l = 4 pi sum Re[F_0 F_l*] / (norm cnt); with interlacing the harmonics
+ * weight the c2r of the combined field (src/multipole.c:489-500).
  * The result reports shot / norm as its shot noise (src/save_res.c:89). */
 int ps_gpu_set_survey(ps_gpu_ctx *ctx, int cat, double shot, double norm, const double *origin);
 

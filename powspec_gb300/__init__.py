@@ -335,7 +335,8 @@ class Estimator:
     def set_survey(self, cat, shot, norm, origin=None):
         """Survey catalogue `cat`, before its assign: P_0 = (sum / cnt - shot)
         / norm; multipoles l > 0 by the spherical-harmonic decomposition
-        (non-interlaced meshes; origin = the box corner, the observer at 0).
+        (origin = the box corner, the observer at 0; with interlacing, over
+        the c2r of the combined field).
         The catalogue holds the data (weights w) and the randoms (weights
         -alpha w), positions relative to the box corner."""
         o = None if origin is None else np.ascontiguousarray(origin, dtype=np.float64)

@@ -1046,7 +1046,10 @@ void bin_pair(ps_gpu_ctx* c, const float2* f1, const float2* f2) {
 // Survey catalogues with multipoles l > 0 (src/multipole.c:1179-1250):
 // F_0 of each catalogue's mesh, then per l the field F_l of the harmonic
 // decomposition, and the (F_0, F_l) pair sums; raw sums into c->d_sums as
-// [spec][pole][bin], Re F_l(0) per catalogue into c->d_dc.
+// [spec][pole][bin], Re F_l(0) per catalogue into c->d_dc.  With
+// interlacing, F_0 is the combination of the two meshes' fields and the
+// harmonics weight its c2r / Ng^3, which replaces the plain mesh
+// (src/multipole.c:462-500).
 int enqueue_survey_multipoles(ps_gpu_ctx* c) {
   const ps_gpu_params& p = c->p;
   cudaStream_t s = c->stream;
@@ -1068,7 +1071,18 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
   float2* fl[2] = {base + 4 * c->ncx, base + 6 * c->ncx};
   float* wmesh = (float*)(base + (size_t)(3 + 2 * p.ncat) * c->ncx);
   CU(cudaEventRecord(c->ev[0], s));
-  for (int k = 0; k < p.ncat; k++) r2c_store(c, (const float*)c->grid[k], a1, a2, f0[k]);
+  const int mpc = c->mpc;
+  for (int k = 0; k < p.ncat; k++) {
+    r2c_store(c, (const float*)c->grid[k * mpc], a1, a2, f0[k]);
+    if (p.interlace) {
+      r2c_store(c, (const float*)c->grid[k * mpc + 1], a1, a2, fa);
+      launch_inv_lead(f0[k], fa, a1, c->ng, c->geom.phase, c->d_tw_full, c->plan_full, s);
+      launch_inv_lead(a1, nullptr, a2, c->ng, c->geom.phase, c->d_tw_full, c->plan_full, s);
+      launch_c2r_z(a2, (float*)c->grid[k * mpc], c->ng, c->ty_a, c->d_tw_half, c->d_tw_full,
+                   c->plan_half, s);
+      c->launches += 3;
+    }
+  }
   CU(cudaEventRecord(c->ev[1], s));
   CU(cudaEventRecord(c->ev[2], s));
   const int nbin = c->nbin, npole = p.npole;
@@ -1080,7 +1094,7 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
           double f = 1;  // (l - |m|)! / (l + |m|)!
           for (int q = ell - abs(m) + 1; q <= ell + abs(m); q++) f /= q;
           const double kl = sqrt((2 * ell + 1) / (4 * M_PI) * f) * (m ? sqrt(2.0) : 1.0);
-          launch_ylm_real((const float*)c->grid[k], wmesh, c->ng, ell, m, kl, c->survey_origin,
+          launch_ylm_real((const float*)c->grid[k * mpc], wmesh, c->ng, ell, m, kl, c->survey_origin,
                           p.box, s);
           r2c_store(c, wmesh, a1, a2, fa);
           launch_ylm_acc(fa, fl[k], c->ng, ell, m, kl, p.box, m == -ell, s);
@@ -1154,10 +1168,6 @@ int ps_gpu_set_survey(ps_gpu_ctx* c, int cat, double shot, double norm, const do
   if (!c || cat < 0 || cat >= c->p.ncat) return fail(c, PS_GPU_ERR_ARG, "invalid survey arguments");
   bool high = false;
   for (int l = 0; l < c->p.npole; l++) high |= c->p.poles[l] > 0;
-  if (high && c->p.interlace)
-    return fail(c, PS_GPU_ERR_ARG,
-                "survey multipoles l > 0 need a mesh without interlacing (the interlaced "
-                "field's inverse transform is not provided)");
   if (high && !origin) return fail(c, PS_GPU_ERR_ARG, "survey multipoles l > 0 need the box corner");
   if (high && c->nmu != 1) return fail(c, PS_GPU_ERR_ARG, "survey multipoles take no |mu| sub-bins");
   if (!(norm > 0) || !(shot >= 0)) return fail(c, PS_GPU_ERR_ARG, "survey normalisation must be > 0");

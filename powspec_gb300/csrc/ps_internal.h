@@ -74,6 +74,13 @@ int launch_ylm_real(const float* in, float* out, int ng, int l, int m, double kl
                     const double origin[3], const double box[3], cudaStream_t s);
 int launch_ylm_acc(const float2* f, float2* acc, int ng, int l, int m, double kl,
                    const double box[3], bool first, cudaStream_t s);
+// The interlaced field's c2r (ps_yama.cu): inverse along the leading axis
+// of [l][p][kz] into [p][l][kz] (with in2: over the interlace combination,
+// also written back to in), then half-complex z rows -> real rows / Ng^3.
+int launch_inv_lead(float2* in, const float2* in2, float2* out, int ng, const float2* phase,
+                    const float2* tw_full, const FftPlan& plan_full, cudaStream_t s);
+int launch_c2r_z(const float2* in, float* out, int ng, int ty, const float2* tw_half,
+                 const float2* tw_full, const FftPlan& plan_half, cudaStream_t s);
 
 int gather_tile(int ng);    // tile edge for this mesh size, 0 if unsupported
 // Region path: possible for this mesh and scheme; words per tile and mesh.

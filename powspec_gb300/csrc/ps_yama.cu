@@ -14,6 +14,8 @@
 // Two conventions of the reference are kept: the first mesh row
 // (i = j = 0) and the modes on the k_z axis (k_x = k_y = 0) take the
 // harmonic as 1 for every m (src/mp_template.c:71-74, :118-121).
+#include <algorithm>
+
 #include "ps_internal.h"
 
 namespace ps {
@@ -90,7 +92,179 @@ __global__ void k_ylm_acc(const float2* __restrict__ f, float2* __restrict__ acc
   }
 }
 
+// ------------------------------------------------ c2r of the interlaced field
+// With interlacing, the harmonic weights multiply the real-space field of
+// the combined F_0: FFT_EXEC_C2R of (F0 + exp(i theta) F1) / 2, divided by
+// Ng^3 (src/multipole.c:462-500).  The inverse runs as the c2r transform
+// does: inverse complex DFTs along x, then y, over the stored half-complex
+// field, then a half-complex -> real transform of each z row that ignores
+// the imaginary parts of its kz = 0 and kz = Ng/2 terms.  Inverse DFTs are
+// forward ones of the conjugate, conjugated.
+
+struct InvLeadArgs {
+  int ng, tz;             // mesh size; kz values per CTA
+  float2* in;             // [l][p][kz]; receives the combined field if in2
+  const float2* in2;      // shifted mesh's field, or null
+  float2* out;            // [p][l][kz]
+  const float2* phase;    // exp(i pi n / ng), n = signed kx + ky + kz + ng
+  const float2* tw_full;
+  FftPlan plan_full;
+};
+
+// out[p][l][kz] = sum_l' in[l'][p][kz] exp(+2 pi i l l' / ng): the inverse
+// along the leading axis, the two leading axes swapped on the way out, so
+// two launches take [kx][ky][kz] to [x][y][kz].  Each CTA transforms the
+// lines of one p and tz consecutive kz (contiguous in memory).
+template <bool P2>
+__global__ void __launch_bounds__(kFftThreads) k_inv_lead(const __grid_constant__ InvLeadArgs a) {
+  extern __shared__ float2 sm[];
+  const int ng = a.ng, ngk = (ng >> 1) + 1;
+  const int ls = line_stride(ng, P2);
+  const int ntz = (ngk + a.tz - 1) / a.tz;
+  const int p = blockIdx.x / ntz;
+  const int kz0 = (blockIdx.x - p * ntz) * a.tz;
+  const int nl = min(a.tz, ngk - kz0);
+  const int pp = dsigned(p, ng);
+  for (int e = threadIdx.x; e < ng * nl; e += blockDim.x) {
+    const int l = e / nl, r = e - l * nl;
+    const size_t idx = ((size_t)l * ng + p) * ngk + kz0 + r;
+    float2 v = a.in[idx];
+    if (a.in2) {
+      const float2 t = cmul(__ldg(&a.phase[dsigned(l, ng) + pp + kz0 + r + ng]), a.in2[idx]);
+      v = make_float2(0.5f * (v.x + t.x), 0.5f * (v.y + t.y));
+      a.in[idx] = v;
+    }
+    sm[r * ls + lidx<P2>(l)] = make_float2(v.x, -v.y);
+  }
+  __syncthreads();
+  if (P2)
+    fft2_lines(sm, a.plan_full.logn, nl, ls, a.tw_full);
+  else
+    fft_lines(sm, a.plan_full, nl, ls, a.tw_full);
+  float2* ob = a.out + (size_t)p * ng * ngk + kz0;
+  for (int e = threadIdx.x; e < ng * nl; e += blockDim.x) {
+    const int l = e / nl, r = e - l * nl;
+    const float2 v = sm[r * ls + lidx<P2>(l)];
+    ob[(size_t)l * ngk + r] = make_float2(v.x, -v.y);
+  }
+}
+
+struct C2rArgs {
+  int ng, ty;             // mesh size; rows per CTA
+  float scale;            // 1 / Ng^3
+  const float2* in;       // [x][y][0..ng/2]
+  float* out;             // [x][y][0..ng)
+  const float2* tw_half;
+  const float2* tw_full;
+  FftPlan plan_half;
+};
+
+// Half-complex rows -> real rows, times `scale`.  With M = ng / 2 and
+// w_k = exp(2 pi i k / ng),
+//   Z[k] = (X[k] + conj X[M-k]) + i w_k (X[k] - conj X[M-k]),  k < M,
+// is twice the M-point DFT of x[2m] + i x[2m+1], so one inverse M-point
+// transform gives the even and odd samples.  Pairs (k, M - k) go to one
+// thread, which reads both before writing either.
+template <bool P2>
+__global__ void __launch_bounds__(kFftThreads) k_c2r_z(const __grid_constant__ C2rArgs a) {
+  extern __shared__ float2 sm[];
+  const int ng = a.ng, M = ng >> 1, ngk = M + 1;
+  const int ls = line_stride(M + 1, P2);
+  const size_t rows = (size_t)ng * ng, r0 = (size_t)blockIdx.x * a.ty;
+  const int nl = (int)((rows - r0) < (size_t)a.ty ? rows - r0 : (size_t)a.ty);
+  const float2* ib = a.in + r0 * ngk;
+  for (int e = threadIdx.x; e < nl * ngk; e += blockDim.x) {
+    const int r = e / ngk, k = e - r * ngk;
+    sm[r * ls + lidx<P2>(k)] = ib[e];
+  }
+  __syncthreads();
+  const int half = (M >> 1) + 1;
+  for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {
+    const int r = e / half, k = e - r * half;
+    float2* L = sm + r * ls;
+    if (k == 0) {  // imaginary parts of X[0], X[M] ignored; Z[0] stored conjugated
+      const float x0 = L[0].x, xm = L[lidx<P2>(M)].x;
+      L[0] = make_float2(x0 + xm, xm - x0);
+      continue;
+    }
+    const int ik = lidx<P2>(k), imk = lidx<P2>(M - k);
+    const float2 A = L[ik], B = L[imk];
+    const float2 t = __ldg(&a.tw_full[k]);  // exp(-2 pi i k / ng) = conj w_k
+    // Z[k]: S = A + conj B, D = A - conj B, q = w_k D
+    {
+      const float2 S = make_float2(A.x + B.x, A.y - B.y), D = make_float2(A.x - B.x, A.y + B.y);
+      const float2 q = cmul(make_float2(t.x, -t.y), D);
+      L[ik] = make_float2(S.x - q.y, -(S.y + q.x));
+    }
+    if (M - k != k) {  // Z[M-k]: w_(M-k) = -conj w_k
+      const float2 S = make_float2(B.x + A.x, B.y - A.y), D = make_float2(B.x - A.x, B.y + A.y);
+      const float2 q = cmul(make_float2(-t.x, -t.y), D);
+      L[imk] = make_float2(S.x - q.y, -(S.y + q.x));
+    }
+  }
+  __syncthreads();
+  if (P2)
+    fft2_lines(sm, a.plan_half.logn, nl, ls, a.tw_half);
+  else
+    fft_lines(sm, a.plan_half, nl, ls, a.tw_half);
+  float2* ob = reinterpret_cast<float2*>(a.out + r0 * ng);
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+    const int r = e / M, m = e - r * M;
+    const float2 v = sm[r * ls + lidx<P2>(m)];
+    ob[(size_t)r * M + m] = make_float2(v.x * a.scale, -v.y * a.scale);
+  }
+}
+
 }  // namespace
+
+int launch_inv_lead(float2* in, const float2* in2, float2* out, int ng, const float2* phase,
+                    const float2* tw_full, const FftPlan& plan_full, cudaStream_t s) {
+  InvLeadArgs a;
+  a.ng = ng;
+  a.tz = std::max(1, std::min(32, kCtaElems / ng));
+  a.in = in;
+  a.in2 = in2;
+  a.out = out;
+  a.phase = phase;
+  a.tw_full = tw_full;
+  a.plan_full = plan_full;
+  const bool p2 = plan_full.logn >= 0;
+  const size_t smem = (size_t)a.tz * line_stride(ng, p2) * sizeof(float2);
+  const unsigned grid = (unsigned)(ng * ((ng / 2 + 1 + a.tz - 1) / a.tz));
+  if (p2) {
+    cudaFuncSetAttribute(k_inv_lead<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_inv_lead<true><<<grid, kFftThreads, smem, s>>>(a);
+  } else {
+    cudaFuncSetAttribute(k_inv_lead<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_inv_lead<false><<<grid, kFftThreads, smem, s>>>(a);
+  }
+  return 1;
+}
+
+int launch_c2r_z(const float2* in, float* out, int ng, int ty, const float2* tw_half,
+                 const float2* tw_full, const FftPlan& plan_half, cudaStream_t s) {
+  C2rArgs a;
+  a.ng = ng;
+  a.ty = ty;
+  a.scale = (float)(1.0 / ((double)ng * ng * ng));
+  a.in = in;
+  a.out = out;
+  a.tw_half = tw_half;
+  a.tw_full = tw_full;
+  a.plan_half = plan_half;
+  const bool p2 = plan_half.logn >= 0;
+  const size_t smem = (size_t)ty * line_stride(ng / 2 + 1, p2) * sizeof(float2);
+  const size_t rows = (size_t)ng * ng;
+  const unsigned grid = (unsigned)((rows + ty - 1) / ty);
+  if (p2) {
+    cudaFuncSetAttribute(k_c2r_z<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_c2r_z<true><<<grid, kFftThreads, smem, s>>>(a);
+  } else {
+    cudaFuncSetAttribute(k_c2r_z<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_c2r_z<false><<<grid, kFftThreads, smem, s>>>(a);
+  }
+  return 1;
+}
 
 int launch_ylm_real(const float* in, float* out, int ng, int l, int m, double kl,
                     const double origin[3], const double box[3], cudaStream_t s) {

@@ -9,8 +9,8 @@
  * Survey catalogues (CUBIC_SIM = F): data minus alpha x randoms with FKP
  * weights in a box fitted to the catalogues (src/read_cata.c:95-185,
  * src/genr_mesh.c:427-566, :797-809), from Cartesian or converted (RA, Dec,
- * z) coordinates; multipoles l > 0 by the spherical-harmonic decomposition
- * on non-interlaced meshes.  FITS catalogues are rejected with an error.  Besides
+ * z) coordinates; multipoles l > 0 by the spherical-harmonic decomposition,
+ * with or without interlacing.  FITS catalogues are rejected with an error.  Besides
  * ASCII (DATA_FORMAT = 0), DATA_FORMAT = 2 reads NumPy .npy arrays, whose
  * columns take the same position / weight / selection expressions.
  */
@@ -387,11 +387,6 @@ static int verify(psh_cfg *cfg, Conf *c) {
     return PSH_ERR_CFG;
   }
   for (int i = 0; i < m; i++) c->poles[i] = pl[i];
-  if (!c->issim && pl[m - 1] > 0 && c->intlace) {
-    fprintf(stderr, "Error: survey catalogues (CUBIC_SIM = F): `MULTIPOLE' l > 0 needs "
-                    "`GRID_INTERLACE' = F\n");
-    return PSH_ERR_CFG;
-  }
   c->kmin = 0;
   if ((rc = psh_dbl(cfg, "KMIN", 0, &c->kmin)) < 0) return PSH_ERR_CFG;
   if (c->kmin < 0) {

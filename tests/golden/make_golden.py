@@ -21,7 +21,8 @@ these are the pins of the oracle and of the GPU path:
   the same objects as (RA, Dec, z) converted by quadrature
   (ref_auto_cnvt.txt) and by a distance table (ref_auto_table.txt); the
   multipoles 0, 2, 4 on a non-interlaced mesh (ref_auto_yama.txt) and their
-  cross spectrum of the catalogue with itself (ref_cross_yama.txt).
+  cross spectrum of the catalogue with itself (ref_cross_yama.txt); the
+  multipoles 0 to 6 on the interlaced mesh (ref_auto_yama_il.txt).
 
 Usage (in a tree that has the reference sources):
     python tests/golden/make_golden.py          # everything
@@ -207,7 +208,12 @@ def survey():
         lines.append(line)
     with open(os.path.join(d, "powspec_cross.conf"), "w") as f:
         f.write("\n".join(lines) + "\n")
-    for conf in ("powspec_yama.conf", "powspec_cross.conf"):
+    # every multipole up to 6 on the interlaced mesh: the harmonics weight the
+    # c2r of the combined field
+    il = SURVEY_CONF.replace("MULTIPOLE       = 0", "MULTIPOLE       = [0, 1, 2, 3, 4, 5, 6]")
+    with open(os.path.join(d, "powspec_yama_il.conf"), "w") as f:
+        f.write(il.format(out="ref_auto_yama_il.txt"))
+    for conf in ("powspec_yama.conf", "powspec_cross.conf", "powspec_yama_il.conf"):
         subprocess.run([oracle.REF_CLI, "-c", conf], cwd=d, check=True, env=env,
                        stdout=subprocess.DEVNULL)
     survey_converted(d, data, rand, rng, env)
