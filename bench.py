@@ -62,7 +62,13 @@ WORKLOADS = {
     # uniform in [0.5, 1.5], L = 2000 Mpc/h, dk = 0.002
     "large_pcs_il_ng1024_n1.5e8_f32": dict(learned=False, large=True, ng=1024, assign=3, interlace=True),
     "large_pcs_il_ng2048_n1.5e8_f32": dict(learned=False, large=True, ng=2048, assign=3, interlace=True),
+    # survey: 1e6 lognormal data in a sphere of radius 500 Mpc/h centred at
+    # (1500, 800, 1200) from the observer, 3e6 randoms, FKP weights, fitted
+    # box (1020 Mpc/h); P_0, P_2, P_4 by the spherical-harmonic decomposition
+    "survey_pcs_il_ng256_l024_n4e6": dict(learned=False, survey=True, ng=256, assign=3,
+                                          interlace=True, poles=(0, 2, 4)),
 }
+SURVEY_ND, SURVEY_CENTRE, SURVEY_RADIUS = 1_000_000, (1500.0, 800.0, 1200.0), 500.0
 LARGE_N, LARGE_BOX, LARGE_DK = 150_000_000, 2000.0, 0.002
 # mock ensemble: 256 catalogues, N log-uniform in [1e5, 5e6], Ng from
 # {128, 192, 256, 384}, CIC or TSC, interlaced (seeded draws)
@@ -347,6 +353,8 @@ def run_reference(args, world, rank):
         return run_reference_ensemble(args)
     if WORKLOADS[args.workload].get("large"):
         return run_reference_large(args)
+    if WORKLOADS[args.workload].get("survey"):
+        return run_reference_survey(args)
     import oracle
     cat = make_catalogue(SEED)
     threads = os.cpu_count() or 1
@@ -693,6 +701,156 @@ def run_large(args, world, rank, local):
     return 0
 
 
+def survey_bytes(ng, poles, interlace, n):
+    """Algorithmic HBM bytes of one survey evaluation's phases.
+
+    assignment: as for a periodic box; F_0: one r2c per mesh (4 B Ng^3 read,
+    8 B Ncmplx written), with interlacing the combination and its c2r (8 B
+    Ncmplx per field read, 4 B Ng^3 written); each harmonic term (2l + 1 per
+    l > 0): the weighted mesh read (4 B Ng^3), its transform written and read
+    (16 B Ncmplx), the field accumulated (16 B Ncmplx); each (F_0, F_l) pair
+    binned: 16 B Ncmplx.
+    """
+    nmesh = 2 if interlace else 1
+    ntot, ncx = ng ** 3, ng * ng * (ng // 2 + 1)
+    terms = sum(2 * l + 1 for l in poles if l > 0)
+    f0 = nmesh * (4 * ntot + 8 * ncx) + ((16 * ncx + 4 * ntot) if interlace else 0)
+    harm = terms * (4 * ntot + 32 * ncx) + len(poles) * 16 * ncx
+    return {"assign": nmesh * (n * 32 + 4 * ntot), "f0": f0, "harmonics": harm, "terms": terms}
+
+
+def make_survey(seed):
+    from powspec_gb300 import catalog
+    d, r = catalog.survey(SURVEY_ND, centre=SURVEY_CENTRE, radius=SURVEY_RADIUS, seed=seed,
+                          ngen=256)
+    return catalog.prepare_survey([(d, r)])[0], len(d), len(r)
+
+
+def survey_config(name, s, nd, nr):
+    wl = WORKLOADS[name]
+    return {"workload": name, "ng": wl["ng"], "assign": "PCS", "interlace": wl["interlace"],
+            "poles": list(wl["poles"]), "box": list(s.box), "n_data": nd, "n_rand": nr, "dk": DK,
+            "l2": "inputs larger than L2 (128 MB of records, 64 MB meshes)"}
+
+
+def survey_oracle_spec(name, s):
+    import oracle
+    wl = WORKLOADS[name]
+    return oracle.Spec(ng=wl["ng"], box=s.box, assign=wl["assign"], interlace=wl["interlace"],
+                       poles=wl["poles"], dk=DK, isauto=(True, False), iscross=False)
+
+
+def run_reference_survey(args):
+    """The oracle port's survey path on the survey workload's catalogue."""
+    import oracle
+    s, nd, nr = make_survey(SEED)
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    spec = survey_oracle_spec(args.workload, s)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.survey(spec, [s.xyzw], s.origin, [s.shot], [s.norm])
+        times.append(time.perf_counter() - t0)
+        if sum(times) > 150.0:
+            break
+    total = sum(times)
+    value = len(times) / total
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
+        "n_gpus": args.gpus, "steps": len(times), "steps_requested": args.steps, "warmup": 0,
+        "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": survey_config(args.workload, s, nd, nr),
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} evaluation(s) of the workload's catalogue, "
+                                   "150 s cap; FFT by the project's FFTW-API shim"},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+    return 0
+
+
+def run_survey(args, world, rank, local):
+    import torch
+
+    import powspec_gb300 as ps
+    wl = WORKLOADS[args.workload]
+    s, nd, nr = make_survey(SEED + rank)
+    n = len(s.xyzw)
+    torch.cuda.set_device(local)
+    dev = torch.from_numpy(s.xyzw).to(f"cuda:{local}")
+    host = torch.from_numpy(s.xyzw).pin_memory().numpy()
+    est = ps.Estimator(ng=wl["ng"], box=s.box, assign=wl["assign"], interlace=wl["interlace"],
+                       poles=wl["poles"], dk=DK, device=local)
+    est.set_survey(0, s.shot, s.norm, s.origin)
+    stream = torch.cuda.ExternalStream(est.stream(), device=local)
+    phases = np.zeros(6)
+    launches = [0]
+
+    def step():
+        est.assign(0, dev.data_ptr(), on_device=True, n=n)
+        out = est.execute()
+        phases[:] += est.timings()
+        launches[0] += est.launches()
+        return out
+
+    for _ in range(args.warmup):
+        step()
+    phases[:] = 0
+    launches[0] = 0
+    with ClockSampler(local) as clk:
+        barrier(world)
+        dev_ms, _ = timed(stream, args.steps, step)
+        barrier(world)
+    ph = phases / args.steps
+    t_max = reduce(world, dev_ms / 1e3, "max")
+    value = reduce(world, float(args.steps), "sum") / t_max
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        est.assign(0, host)
+        est.execute()
+    e2e_s = reduce(world, time.perf_counter() - t0, "max")
+    if rank == 0:
+        ab = survey_bytes(wl["ng"], wl["poles"], wl["interlace"], n)
+        peak, peak_kind = peaks()
+        frac = lambda b, ms: (b / (ms * 1e-3) / 1e9) / peak if ms > 0 else None
+        cpu = None
+        if not args.no_cpu:
+            import oracle
+            spec = survey_oracle_spec(args.workload, s)
+            t0 = time.perf_counter()
+            reps = 2
+            for _ in range(reps):
+                oracle.survey(spec, [s.xyzw], s.origin, [s.shot], [s.norm])
+            cpu = {"value": reps / (time.perf_counter() - t0), "unit": "evals/s",
+                   "cores": oracle.get_threads(), "kind": "port",
+                   "sample": f"{reps} FP64 evaluations of the same survey catalogue and mesh"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": survey_config(args.workload, s, nd, nr),
+            "phases_ms": {"assign": ph[0], "f0_and_c2r": ph[1], "harmonics_and_binning": ph[3],
+                          "device_total": ph[5]},
+            "roofline": {"bound": "hbm", "kernel": "harmonic terms (weight, r2c, accumulate) "
+                         "and pair binning", "achieved": ab["harmonics"] / (ph[3] * 1e-3) / 1e9,
+                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": frac(ab["harmonics"], ph[3]), "traffic": None,
+                         "per_phase_frac": {"assign": frac(ab["assign"], ph[0]),
+                                            "f0_and_c2r": frac(ab["f0"], ph[1]),
+                                            "harmonics_and_binning": frac(ab["harmonics"], ph[3])},
+                         "harmonic_terms": ab["terms"]},
+            "e2e": {"value": args.steps / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": n * 32,
+                    "d2h_bytes_per_step": 8 * 3 * est.nbin + 8 * 4 + 16},
+            "gpu_launches": launches[0], "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    est.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -710,6 +868,8 @@ def main():
         rc = run_ensemble(args, world, rank, local)
     elif WORKLOADS[args.workload].get("large"):
         rc = run_large(args, world, rank, local)
+    elif WORKLOADS[args.workload].get("survey"):
+        rc = run_survey(args, world, rank, local)
     else:
         rc = run_gpu(args, world, rank, local)
     if world > 1:

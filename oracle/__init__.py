@@ -142,6 +142,8 @@ def port():
         L.ps_oracle_alias_corr.restype = ctypes.c_double
         L.ps_oracle_alias_corr.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double]
         L.ps_oracle_legpoly.argtypes = [ctypes.c_int, ctypes.c_double]
+        L.ps_oracle_ylm.restype = ctypes.c_double
+        L.ps_oracle_ylm.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 4
         _port = L
     return _port
 
@@ -161,6 +163,10 @@ def ref():
 
 def set_threads(n):
     port().ps_oracle_set_threads(int(n))
+
+
+def get_threads():
+    return int(port().ps_oracle_get_threads())
 
 
 def as_aos(cat):
@@ -192,9 +198,9 @@ def _maxbin(spec):
     return int(np.ceil(np.pi * spec.ng / min(spec.box3()) / spec.dk)) + 8 if not spec.logscale else 4096
 
 
-def run(which, spec: Spec, cats, with_c2r=True) -> Result:
-    """Whole periodic-box path on one or two catalogues (float64 [N,4])."""
-    cats = [as_aos(c) for c in cats]
+def _port_call(spec: Spec, cats, with_c2r, call) -> Result:
+    """Marshal spec and the result arrays for a port entry point; call(p,
+    ptrs, ns, r) runs it."""
     nc = len(cats)
     maxbin = _maxbin(spec)
     npole = len(spec.poles)
@@ -205,65 +211,99 @@ def run(which, spec: Spec, cats, with_c2r=True) -> Result:
     lcnt = np.zeros((npole, maxbin))
     pl = np.zeros((2, npole, maxbin))
     xpl = np.zeros((npole, maxbin))
-    box = spec.box3()
-    if which == "port":
-        p = OracleParams()
-        p.ng = spec.ng
-        p.box = (ctypes.c_double * 3)(*box)
-        p.assign = spec.assign
-        p.interlace = int(spec.interlace)
-        p.ncat = nc
-        p.isauto = (ctypes.c_int * 2)(*[int(x) for x in spec.isauto])
-        p.iscross = int(spec.iscross)
-        p.los = (ctypes.c_double * 3)(*spec.los)
-        p.kmin, p.kmax, p.dk = spec.kmin, spec.kmax, spec.dk
-        p.logscale = int(spec.logscale)
-        p.npole = npole
-        p.poles = (ctypes.c_int * 7)(*spec.poles)
-        p.with_c2r = int(with_c2r)
-        r = OracleResult()
-        r.maxbin = maxbin
-        r.k = k.ctypes.data_as(_c_double_p)
-        r.kedge = kedge.ctypes.data_as(_c_double_p)
-        r.km = km.ctypes.data_as(_c_double_p)
-        r.cnt = cnt.ctypes.data_as(_c_size_p)
-        r.lcnt = lcnt.ctypes.data_as(_c_double_p)
-        r.pl = pl.ctypes.data_as(_c_double_p)
-        r.xpl = xpl.ctypes.data_as(_c_double_p)
-        ptrs = (ctypes.c_void_p * 2)(*[c.ctypes.data for c in cats] + [None] * (2 - nc))
-        ns = (ctypes.c_size_t * 2)(*[len(c) for c in cats] + [0] * (2 - nc))
-        rc = port().ps_oracle_run(ctypes.byref(p), ptrs, ns, ctypes.byref(r))
-        if rc:
-            raise RuntimeError(f"oracle port failed: {rc}")
-        nbin = r.nbin
-        shot = np.array(r.shot[:nc])
-        norm = np.array(r.norm[:nc])
-        times = (r.t_mesh, r.t_pk)
-    else:
-        L = ref()
-        nb = ctypes.c_int(0)
-        shot = np.zeros(2)
-        norm = np.zeros(2)
-        times = np.zeros(2)
-        ptrs = (ctypes.c_void_p * 2)(*[c.ctypes.data for c in cats] + [None] * (2 - nc))
-        ns = (ctypes.c_size_t * 2)(*[len(c) for c in cats] + [0] * (2 - nc))
-        isauto = (ctypes.c_int * 2)(*[int(x) for x in spec.isauto])
-        poles = (ctypes.c_int * 7)(*spec.poles)
-        rc = L.ref_powspec(nc, ptrs, ns, spec.ng, (ctypes.c_double * 3)(*box), spec.assign,
-                           int(spec.interlace), (ctypes.c_double * 3)(*spec.los), poles,
-                           npole, ctypes.c_double(spec.kmin), ctypes.c_double(spec.kmax),
-                           ctypes.c_double(spec.dk), int(spec.logscale), isauto,
-                           int(spec.iscross), maxbin, ctypes.byref(nb), _ptr(k), _ptr(kedge),
-                           _ptr(km), _ptr(cnt), _ptr(lcnt), _ptr(pl), _ptr(xpl), _ptr(shot),
-                           _ptr(norm), _ptr(times), 0)
-        if rc:
-            raise RuntimeError(f"reference run failed: {rc}")
-        nbin = nb.value
-        shot, norm, times = shot[:nc], norm[:nc], tuple(times)
+    p = OracleParams()
+    p.ng = spec.ng
+    p.box = (ctypes.c_double * 3)(*spec.box3())
+    p.assign = spec.assign
+    p.interlace = int(spec.interlace)
+    p.ncat = nc
+    p.isauto = (ctypes.c_int * 2)(*[int(x) for x in spec.isauto])
+    p.iscross = int(spec.iscross)
+    p.los = (ctypes.c_double * 3)(*spec.los)
+    p.kmin, p.kmax, p.dk = spec.kmin, spec.kmax, spec.dk
+    p.logscale = int(spec.logscale)
+    p.npole = npole
+    p.poles = (ctypes.c_int * 7)(*spec.poles)
+    p.with_c2r = int(with_c2r)
+    r = OracleResult()
+    r.maxbin = maxbin
+    r.k = k.ctypes.data_as(_c_double_p)
+    r.kedge = kedge.ctypes.data_as(_c_double_p)
+    r.km = km.ctypes.data_as(_c_double_p)
+    r.cnt = cnt.ctypes.data_as(_c_size_p)
+    r.lcnt = lcnt.ctypes.data_as(_c_double_p)
+    r.pl = pl.ctypes.data_as(_c_double_p)
+    r.xpl = xpl.ctypes.data_as(_c_double_p)
+    ptrs = (ctypes.c_void_p * 2)(*[c.ctypes.data for c in cats] + [None] * (2 - nc))
+    ns = (ctypes.c_size_t * 2)(*[len(c) for c in cats] + [0] * (2 - nc))
+    rc = call(ctypes.byref(p), ptrs, ns, ctypes.byref(r))
+    if rc:
+        raise RuntimeError(f"oracle port failed: {rc}")
+    nbin = r.nbin
     return Result(nbin=nbin, k=k[:nbin].copy(), kedge=kedge[:nbin + 1].copy(),
                   km=km[:nbin].copy(), cnt=cnt[:nbin].copy(), lcnt=lcnt[:, :nbin].copy(),
-                  pl=pl[:, :, :nbin].copy(), xpl=xpl[:, :nbin].copy(), shot=shot,
-                  norm=norm, times=times)
+                  pl=pl[:, :, :nbin].copy(), xpl=xpl[:, :nbin].copy(),
+                  shot=np.array(r.shot[:nc]), norm=np.array(r.norm[:nc]),
+                  times=(r.t_mesh, r.t_pk))
+
+
+def run(which, spec: Spec, cats, with_c2r=True) -> Result:
+    """Whole periodic-box path on one or two catalogues (float64 [N,4])."""
+    cats = [as_aos(c) for c in cats]
+    nc = len(cats)
+    if which == "port":
+        return _port_call(spec, cats, with_c2r, port().ps_oracle_run)
+    maxbin = _maxbin(spec)
+    npole = len(spec.poles)
+    k = np.zeros(maxbin)
+    kedge = np.zeros(maxbin + 1)
+    km = np.zeros(maxbin)
+    cnt = np.zeros(maxbin, np.uint64)
+    lcnt = np.zeros((npole, maxbin))
+    pl = np.zeros((2, npole, maxbin))
+    xpl = np.zeros((npole, maxbin))
+    box = spec.box3()
+    L = ref()
+    nb = ctypes.c_int(0)
+    shot = np.zeros(2)
+    norm = np.zeros(2)
+    times = np.zeros(2)
+    ptrs = (ctypes.c_void_p * 2)(*[c.ctypes.data for c in cats] + [None] * (2 - nc))
+    ns = (ctypes.c_size_t * 2)(*[len(c) for c in cats] + [0] * (2 - nc))
+    isauto = (ctypes.c_int * 2)(*[int(x) for x in spec.isauto])
+    poles = (ctypes.c_int * 7)(*spec.poles)
+    rc = L.ref_powspec(nc, ptrs, ns, spec.ng, (ctypes.c_double * 3)(*box), spec.assign,
+                       int(spec.interlace), (ctypes.c_double * 3)(*spec.los), poles,
+                       npole, ctypes.c_double(spec.kmin), ctypes.c_double(spec.kmax),
+                       ctypes.c_double(spec.dk), int(spec.logscale), isauto,
+                       int(spec.iscross), maxbin, ctypes.byref(nb), _ptr(k), _ptr(kedge),
+                       _ptr(km), _ptr(cnt), _ptr(lcnt), _ptr(pl), _ptr(xpl), _ptr(shot),
+                       _ptr(norm), _ptr(times), 0)
+    if rc:
+        raise RuntimeError(f"reference run failed: {rc}")
+    nbin = nb.value
+    return Result(nbin=nbin, k=k[:nbin].copy(), kedge=kedge[:nbin + 1].copy(),
+                  km=km[:nbin].copy(), cnt=cnt[:nbin].copy(), lcnt=lcnt[:, :nbin].copy(),
+                  pl=pl[:, :, :nbin].copy(), xpl=xpl[:, :nbin].copy(), shot=shot[:nc],
+                  norm=norm[:nc], times=tuple(times))
+
+
+def survey(spec: Spec, cats, origin, shot, norm) -> Result:
+    """Survey path (port) on one or two catalogues, each holding its data
+    (weights w) and randoms (weights -alpha w), positions relative to the
+    box corner `origin`; shot and norm per catalogue.  P_0 = (sum / cnt -
+    shot) / norm with the k = 0 mode binned; P_l>0 by the spherical-harmonic
+    decomposition (the c2r of the combined field with interlacing)."""
+    cats = [as_aos(c) for c in cats]
+    o = (ctypes.c_double * 3)(*[float(x) for x in origin])
+    sh = (ctypes.c_double * 2)(*(list(map(float, shot)) + [0.0] * (2 - len(shot))))
+    nm = (ctypes.c_double * 2)(*(list(map(float, norm)) + [1.0] * (2 - len(norm))))
+    return _port_call(spec, cats, False,
+                      lambda p, ptrs, ns, r: port().ps_oracle_survey(p, o, sh, nm, ptrs, ns, r))
+
+
+def ylm(ell, m, ct, st, cp, sp):
+    return port().ps_oracle_ylm(ell, m, ct, st, cp, sp)
 
 
 def bins(spec: Spec):

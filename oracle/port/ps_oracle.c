@@ -584,3 +584,281 @@ done:
   free(alias);
   return rc;
 }
+
+/* ------------------------------------------------------------ survey path */
+
+/* Real spherical harmonics (math/spherical.h:54-262 tabulates one real basis
+ * per ell).  Here Y_l0 = K_l0 P_l(cos t), Y_lm = sqrt2 K_lm P_l^m(cos t)
+ * cos(m p), Y_l,-m = sqrt2 K_lm P_l^m(cos t) sin(m p), K_lm^2 = (2l+1)/(4 pi)
+ * (l-m)!/(l+m)!.  The estimator only uses sums over m of Y_lm(a) Y_lm(b),
+ * which by the addition theorem equal (2l+1)/(4 pi) L_l(a . b) for any
+ * orthonormal real basis. */
+double ps_oracle_ylm(int ell, int m, double ct, double st, double cp, double sp) {
+  const int am = m < 0 ? -m : m;
+  double f = 1;
+  for (int q = ell - am + 1; q <= ell + am; q++) f /= q;
+  double kl = sqrt((2 * ell + 1) / (4 * PS_PI) * f);
+  if (m) kl *= sqrt(2.0);
+  double pmm = 1;
+  for (int i = 1; i <= am; i++) pmm *= (2 * i - 1) * st;
+  double pl = pmm;
+  if (ell > am) {
+    double p0 = pmm, p1 = ct * (2 * am + 1) * pmm;
+    pl = p1;
+    for (int l = am + 2; l <= ell; l++) {
+      pl = ((2 * l - 1) * ct * p1 - (l + am - 1) * p0) / (l - am);
+      p0 = p1;
+      p1 = pl;
+    }
+  }
+  if (!m) return kl * pl;
+  double c = 1, s = 0;
+  for (int i = 0; i < am; i++) {
+    const double c2 = c * cp - s * sp;
+    s = s * cp + c * sp;
+    c = c2;
+  }
+  return kl * pl * (m > 0 ? c : s);
+}
+
+/* src/multipole.c:579-754: sum over the stored modes with a window factor
+ * (the k = 0 mode included) of Re[F1 F2*] x window, twice for the planes
+ * 0 < kz < Ng/2, into pl[kbin]. */
+static void count_survey(int ng, const double box[3], const double *alias,
+                         const double *f1, const double *f2, int logscale,
+                         int nbin, const double *kedge, double dk, double *pl) {
+  const int ngk = ng / 2 + 1;
+  double vec[3];
+  for (int d = 0; d < 3; d++) vec[d] = 2 * PS_PI / box[d];
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+  {
+    double *acc = calloc(nbin, sizeof(double));
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (int i = 0; i < ng; i++) {
+      if (!acc) continue;
+      const size_t idx_i = (size_t)i * ng * ngk;
+      const double ki = vec[0] * ((i <= (ng >> 1)) ? i : i - ng);
+      for (int j = 0; j < ng; j++) {
+        const size_t idx_j = idx_i + (size_t)j * ngk;
+        const double kj = vec[1] * ((j <= (ng >> 1)) ? j : j - ng);
+        const double kmj = ki * ki + kj * kj;
+        for (int k = 0; k < ngk; k++) {
+          const size_t idx = idx_j + k;
+          if (!alias[idx]) continue;
+          const double kk = vec[2] * k;
+          const double km2 = k ? kmj + kk * kk : kmj;
+          const double kmod = logscale ? 0.5 * log10(km2) : sqrt(km2);
+          const int b = (int)((kmod - kedge[0]) / dk);
+          double v = (f1[2 * idx] * f2[2 * idx] + f1[2 * idx + 1] * f2[2 * idx + 1]) * alias[idx];
+          if (k && 2 * k != ng) v *= 2;
+          if (b >= 0 && b < nbin) acc[b] += v;
+        }
+      }
+    }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+    if (acc)
+      for (int b = 0; b < nbin; b++) pl[b] += acc[b];
+    free(acc);
+  }
+}
+
+/* src/mp_template.c:48-149: fl = sum_m Y_lm(k^) FFT[fr Y_lm(r^)] over the
+ * modes with a window factor.  The real-space direction of cell (i, j, k)
+ * is ((i, j, k) + origin Ng / L) x L; the row i = j = 0 and the modes with
+ * kx = ky = 0 take the harmonic as 1. */
+static int harmonic_field(int ng, const double box[3], const double origin[3], int ell,
+                          const double *fr, const double *alias, double *frl, double *fa,
+                          double *fl) {
+  const int ngk = ng / 2 + 1;
+  const size_t ncx = (size_t)ng * ng * ngk;
+  double smin[3], fac[3];
+  for (int d = 0; d < 3; d++) {
+    smin[d] = origin[d] * ng / box[d];
+    fac[d] = 1 / box[d];
+  }
+  memset(fl, 0, sizeof(double) * 2 * ncx);
+  for (int m = -ell; m <= ell; m++) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < ng; i++) {
+      const size_t idx_i = (size_t)i * ng * ng;
+      const double ri = (i + smin[0]) * box[0];
+      for (int j = 0; j < ng; j++) {
+        const size_t idx_j = idx_i + (size_t)j * ng;
+        if (idx_j == 0) {
+          memcpy(frl, fr, sizeof(double) * ng);
+          continue;
+        }
+        const double rj = (j + smin[1]) * box[1];
+        const double r2 = ri * ri + rj * rj, r22 = sqrt(r2);
+        for (int k = 0; k < ng; k++) {
+          const double rk = (k + smin[2]) * box[2];
+          const double r3 = sqrt(r2 + rk * rk);
+          frl[idx_j + k] = fr[idx_j + k] * ps_oracle_ylm(ell, m, rk / r3, r22 / r3, ri / r22, rj / r22);
+        }
+      }
+    }
+    int rc = ps_oracle_r2c(ng, frl, fa);
+    if (rc) return rc;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < ng; i++) {
+      const size_t idx_i = (size_t)i * ng * ngk;
+      const double ki = fac[0] * ((i <= (ng >> 1)) ? i : i - ng);
+      for (int j = 0; j < ng; j++) {
+        const size_t idx_j = idx_i + (size_t)j * ngk;
+        const double kj = fac[1] * ((j <= (ng >> 1)) ? j : j - ng);
+        const double k2 = ki * ki + kj * kj;
+        for (int k = 0; k < ngk; k++) {
+          const size_t idx = idx_j + k;
+          if (!alias[idx]) continue;
+          const double kk = fac[2] * k, k3 = sqrt(k2 + kk * kk);
+          double y = 1;
+          if (k2 != 0 && k3 != 0) {
+            const double k22 = sqrt(k2);
+            y = ps_oracle_ylm(ell, m, kk / k3, k22 / k3, ki / k22, kj / k22);
+          }
+          fl[2 * idx] += fa[2 * idx] * y;
+          fl[2 * idx + 1] += fa[2 * idx + 1] * y;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+int ps_oracle_survey(const ps_oracle_params *p, const double origin[3],
+                     const double shot[2], const double norm[2],
+                     const double *const *xyzw, const size_t *n,
+                     ps_oracle_result *r) {
+  const int ng = p->ng, nc = p->ncat;
+  if (ng < 2 || nc < 1 || nc > 2 || p->npole < 1 || p->npole > 7) return PS_ERR_ARG;
+  const int ngk = ng / 2 + 1;
+  const size_t ntot = (size_t)ng * ng * ng, ncx = (size_t)ng * ng * ngk;
+  const int npole = p->npole;
+  const size_t mb = (size_t)r->maxbin;
+  int rc = 0;
+  double *fr[2] = {0, 0}, *frl[2] = {0, 0}, *fk0[2] = {0, 0}, *fkl[2] = {0, 0};
+  double *alias = NULL, *tmp = NULL, *fa = NULL, *wr = NULL;
+
+  double t0 = wall();
+  for (int c = 0; c < nc; c++) {
+    double w = 0;
+    for (size_t i = 0; i < n[c]; i++) w += xyzw[c][4 * i + 3];
+    r->wdata[c] = w;
+    r->shot[c] = shot[c];
+    r->norm[c] = norm[c];
+    fr[c] = fftw_malloc(sizeof(double) * ntot);
+    fk0[c] = fftw_malloc(sizeof(double) * 2 * ncx);
+    fkl[c] = fftw_malloc(sizeof(double) * 2 * ncx);
+    if (!fr[c] || !fk0[c] || !fkl[c]) { rc = PS_ERR_MEMORY; goto done; }
+    if (p->interlace) {
+      frl[c] = fftw_malloc(sizeof(double) * ntot);
+      if (!frl[c]) { rc = PS_ERR_MEMORY; goto done; }
+    }
+    rc = ps_oracle_assign(xyzw[c], n[c], ng, p->box, p->assign, p->interlace, fr[c], frl[c]);
+    if (rc) goto done;
+  }
+  double t1 = wall();
+
+  int nbin = 0;
+  rc = ps_oracle_bins(ng, p->box, p->kmin, p->kmax, p->dk, p->logscale, r->maxbin, &nbin,
+                      r->kedge, r->k);
+  r->nbin = nbin;
+  if (rc) goto done;
+  alias = malloc(sizeof(double) * ncx);
+  tmp = calloc(nbin, sizeof(double));
+  fa = fftw_malloc(sizeof(double) * 2 * ncx);
+  wr = fftw_malloc(sizeof(double) * ntot);
+  if (!alias || !tmp || !fa || !wr) { rc = PS_ERR_MEMORY; goto done; }
+  rc = ps_oracle_precomp(ng, p->box, p->assign, p->interlace, p->logscale, nbin, r->kedge,
+                         p->dk, alias, r->cnt, r->km);
+  if (rc) goto done;
+
+  /* src/multipole.c:435-505: F_0, and with interlacing the combination and
+   * its c2r / Ng^3 in place of the plain mesh */
+  for (int c = 0; c < nc; c++) {
+    if ((rc = ps_oracle_r2c(ng, fr[c], fk0[c]))) goto done;
+    if (p->interlace) {
+      if ((rc = ps_oracle_r2c(ng, frl[c], fkl[c]))) goto done;
+      ps_oracle_combine(ng, fk0[c], fkl[c]);
+      memcpy(fkl[c], fk0[c], sizeof(double) * 2 * ncx);
+      fftw_plan pc = fftw_plan_dft_c2r_3d(ng, ng, ng, (fftw_complex *)fkl[c], fr[c],
+                                          FFTW_ESTIMATE);
+      if (!pc) { rc = PS_ERR_MEMORY; goto done; }
+      fftw_execute_dft_c2r(pc, (fftw_complex *)fkl[c], fr[c]);
+      fftw_destroy_plan(pc);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+      for (size_t t = 0; t < ntot; t++) fr[c][t] /= ntot;
+    }
+  }
+
+  /* src/multipole.c:1230-1250 with the normalisations of :1090-1160 */
+  for (int l = 0; l < npole; l++) {
+    const int ell = p->poles[l];
+    if (ell > 0)
+      for (int c = 0; c < nc; c++)
+        if ((rc = harmonic_field(ng, p->box, origin, ell, fr[c], alias, wr, fa, fkl[c])))
+          goto done;
+    for (int c = 0; c < nc; c++) {
+      if (!p->isauto[c]) continue;
+      memset(tmp, 0, sizeof(double) * nbin);
+      count_survey(ng, p->box, alias, fk0[c], ell ? fkl[c] : fk0[c], p->logscale, nbin, r->kedge,
+                   p->dk, tmp);
+      double *pl = r->pl + ((size_t)c * npole + l) * mb;
+      for (int i = 0; i < nbin; i++) {
+        double v = tmp[i];
+        if (r->cnt[i]) v = ell ? v * 4 * PS_PI / (norm[c] * r->cnt[i])
+                               : (v / r->cnt[i] - shot[c]) / norm[c];
+        pl[i] = v;
+      }
+    }
+    if (nc == 2 && p->iscross) {
+      memset(tmp, 0, sizeof(double) * nbin);
+      if (ell == 0) {
+        count_survey(ng, p->box, alias, fk0[0], fk0[1], p->logscale, nbin, r->kedge, p->dk, tmp);
+      } else {
+        count_survey(ng, p->box, alias, fk0[0], fkl[1], p->logscale, nbin, r->kedge, p->dk, tmp);
+        count_survey(ng, p->box, alias, fk0[1], fkl[0], p->logscale, nbin, r->kedge, p->dk, tmp);
+      }
+      for (int i = 0; i < nbin; i++) {
+        double v = tmp[i];
+        if (r->cnt[i]) v *= (ell ? 2 * PS_PI : 1.0) / (sqrt(norm[0] * norm[1]) * r->cnt[i]);
+        r->xpl[l * mb + i] = v;
+      }
+    }
+  }
+  if (p->logscale) {  /* src/multipole.c:1267-1274 */
+    for (int i = 0; i < nbin; i++) {
+      r->k[i] = pow(10, r->k[i]);
+      r->km[i] = pow(10, r->k[i]);
+      r->kedge[i] = pow(10, r->k[i]);
+    }
+    r->kedge[nbin] = pow(10, r->kedge[nbin]);
+  }
+  r->t_mesh = t1 - t0;
+  r->t_pk = wall() - t1;
+
+done:
+  for (int c = 0; c < 2; c++) {
+    fftw_free(fr[c]);
+    fftw_free(frl[c]);
+    fftw_free(fk0[c]);
+    fftw_free(fkl[c]);
+  }
+  fftw_free(fa);
+  fftw_free(wr);
+  free(alias);
+  free(tmp);
+  return rc;
+}

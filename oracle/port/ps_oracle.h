@@ -87,6 +87,24 @@ int ps_oracle_count_sim(int ng, const double box[3], const double *alias,
 int ps_oracle_run(const ps_oracle_params *p, const double *const *xyzw,
                   const size_t *n, ps_oracle_result *r);
 
+/* Survey catalogue path (CUBIC_SIM = F), like genr_mesh + powspec for a
+ * survey: xyzw[c] holds catalogue c's data (weights w) and randoms
+ * (weights -alpha w), positions relative to the box corner `origin`; shot
+ * and norm are the catalogue's (src/read_cata.c:165-183).  The k = 0 mode
+ * is binned (src/multipole.c:579-754); multipoles l > 0 come from the
+ * spherical-harmonic decomposition (src/mp_template.c:48-149), over the
+ * c2r / Ng^3 of the combined field with interlacing (src/multipole.c:
+ * 489-500).  los and with_c2r of p are not used.  r->shot, r->norm: the
+ * given values. */
+int ps_oracle_survey(const ps_oracle_params *p, const double origin[3],
+                     const double shot[2], const double norm[2],
+                     const double *const *xyzw, const size_t *n,
+                     ps_oracle_result *r);
+
+/* Real spherical harmonic of degree ell <= 6 and order m of the direction
+ * (cos t, sin t, cos p, sin p), an orthonormal real basis. */
+double ps_oracle_ylm(int ell, int m, double ct, double st, double cp, double sp);
+
 /* Legendre polynomial P_ell(x), ell <= 6 (math/legpoly.h:47-62). */
 double ps_oracle_legpoly(int ell, double x);
 

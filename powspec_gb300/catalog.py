@@ -9,6 +9,11 @@
 
 Outputs are float64 [N, 4] records (x, y, z, w), the reference DATA layout,
 or float32 SoA arrays.
+
+Surveys (``survey``, ``prepare_survey``): a lognormal sample cut to a sphere
+and uniform randoms in the same sphere, with completeness weights and a
+constant n(z); then the reference's survey preparation (src/read_cata.c:
+95-185, src/genr_mesh.c:509-566) into the catalogue the survey path takes.
 """
 from __future__ import annotations
 
@@ -88,4 +93,70 @@ def lognormal(nbar_total, box=1000.0, seed=1, ngen=128, zeldovich=4.0, weights=N
     out = np.empty((n, 4), dtype=dtype)
     out[:, :3] = pos
     out[:, 3] = w
+    return out
+
+
+def survey(ndata, centre=(600.0, 300.0, 450.0), radius=200.0, nrand=3, seed=1, ngen=64):
+    """Synthetic survey: about `ndata` lognormal points in a sphere (data)
+    and nrand x as many uniform points in the same sphere (randoms).  Each
+    row is (x, y, z, wcomp, nz): completeness weights uniform in [0.8, 1.2]
+    and the data's mean density as n(z)."""
+    cen = np.asarray(centre, dtype=np.float64)
+    side = 2.0 * radius
+    c = lognormal(ndata * 6.0 / np.pi, box=side, seed=seed, ngen=ngen)[:, :3] - radius
+    d = c[np.einsum("ij,ij->i", c, c) < radius * radius] + cen
+    rng = np.random.default_rng(seed + 104729)
+    want = nrand * len(d)
+    r = np.empty((0, 3))
+    while len(r) < want:
+        u = rng.uniform(-radius, radius, (int(want * 2.0) + 1024, 3))
+        r = np.concatenate([r, u[np.einsum("ij,ij->i", u, u) < radius * radius]])
+    r = r[:want] + cen
+    nbar = len(d) / (4.0 / 3.0 * np.pi * radius ** 3)
+    out = []
+    for pts in (d, r):
+        out.append(np.column_stack([pts, rng.uniform(0.8, 1.2, len(pts)), np.full(len(pts), nbar)]))
+    return out[0], out[1]
+
+
+class SurveyCatalogue:
+    """What the survey path takes for one catalogue: xyzw = data (weight
+    wc wfkp) then randoms (weight -alpha wc wfkp), positions minus the box
+    corner `origin`; shot noise and normalisation (src/read_cata.c:165-183)."""
+
+    def __init__(self, xyzw, origin, box, alpha, shot, norm):
+        self.xyzw, self.origin, self.box = xyzw, origin, box
+        self.alpha, self.shot, self.norm = alpha, shot, norm
+
+
+def prepare_survey(pairs, p0=2000.0, box=None, pad=0.02):
+    """(data, randoms) pairs of (x, y, z, wcomp, nz) rows -> one
+    SurveyCatalogue per pair, in a common box: FKP weights 1 / (1 + nz p0),
+    alpha = sum wc_d / sum wc_r, shot = sum w_d^2 + alpha^2 sum w_r^2,
+    norm = alpha sum_r wc wfkp^2 nz (sum_d when the randoms' is 0); the box
+    centred on the bounds of every data and random point, `box` or the
+    extent x (1 + pad) rounded up to 10 (src/genr_mesh.c:509-566)."""
+    pts = np.concatenate([a[:, :3] for pr in pairs for a in pr])
+    mn, mx = pts.min(axis=0), pts.max(axis=0)
+    if box is None:
+        size = np.array([np.ceil((mx[a] - mn[a]) * (1 + pad) / 10) * 10 for a in range(3)])
+    else:
+        size = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)).copy()
+        if np.any(mx - mn > size):
+            raise ValueError("box smaller than the catalogues' extent")
+    origin = (mx + mn - size) * 0.5
+    out = []
+    for d, r in pairs:
+        fd, fr = 1.0 / (1.0 + d[:, 4] * p0), 1.0 / (1.0 + r[:, 4] * p0)
+        wd, wr = d[:, 3] * fd, r[:, 3] * fr
+        alpha = d[:, 3].sum() / r[:, 3].sum()
+        shot = (wd * wd).sum() + alpha * alpha * (wr * wr).sum()
+        sd, sr = (d[:, 3] * fd * fd * d[:, 4]).sum(), (r[:, 3] * fr * fr * r[:, 4]).sum()
+        norm = alpha * sr if (sd == 0 or sr != 0) else sd
+        xyzw = np.empty((len(d) + len(r), 4))
+        xyzw[:len(d), :3] = d[:, :3] - origin
+        xyzw[len(d):, :3] = r[:, :3] - origin
+        xyzw[:len(d), 3] = wd
+        xyzw[len(d):, 3] = -alpha * wr
+        out.append(SurveyCatalogue(xyzw, origin, tuple(float(x) for x in size), alpha, shot, norm))
     return out

@@ -176,7 +176,7 @@ struct ps_gpu_ctx {
   double* d_wsum = nullptr;  // [2 cats][2]
   double* d_wpart = nullptr; // [2 * kAssignMaxBlocks]
   int* d_err = nullptr;      // [2 cats]
-  double* h_out = nullptr;   // pinned: sums + wsum + err
+  double* h_out = nullptr;   // pinned: sums + wsum + err (+ Re F_l(0) [pole][cat])
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
   int assigned[2] = {0, 0};
@@ -273,7 +273,7 @@ int alloc_accum(ps_gpu_ctx* c) {
   c->h_out = nullptr;
   CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)std::max(c->grid_c, c->grid_ct) * width));
   CU(cudaMalloc(&c->d_sums, sizeof(double) * width));
-  CU(cudaMallocHost(&c->h_out, sizeof(double) * (width + 10)));
+  CU(cudaMallocHost(&c->h_out, sizeof(double) * (width + 8 + 2 * kMaxPole)));
   return 0;
 }
 
@@ -822,7 +822,7 @@ int finish(ps_gpu_ctx* c, const double* h, const size_t* npart, ps_gpu_result* r
           // src/multipole.c:1118-1150: (F_0, F_l) pairs, the k = 0 mode
           // F_0(0) = W times Re F_l(0) when bin 0 holds it
           const int a = c->spec_a[s2], b = c->spec_b[s2];
-          const double* dc = h + (size_t)nacc * nkey + 8;  // Re F_l(0) per catalogue
+          const double* dc = h + (size_t)nacc * nkey + 8 + 2 * l;  // Re F_l(0) per catalogue
           if (dc_bin && i == 0)
             v += (cat >= 0) ? wsum[2 * a] * dc[a] : wsum[2 * a] * dc[b] + wsum[2 * b] * dc[a];
           if (c->cnt[i])
@@ -1046,7 +1046,7 @@ void bin_pair(ps_gpu_ctx* c, const float2* f1, const float2* f2) {
 // Survey catalogues with multipoles l > 0 (src/multipole.c:1179-1250):
 // F_0 of each catalogue's mesh, then per l the field F_l of the harmonic
 // decomposition, and the (F_0, F_l) pair sums; raw sums into c->d_sums as
-// [spec][pole][bin], Re F_l(0) per catalogue into c->d_dc.  With
+// [spec][pole][bin], F_l(0) into c->d_dc as [pole][catalogue].  With
 // interlacing, F_0 is the combination of the two meshes' fields and the
 // harmonics weight its c2r / Ng^3, which replaces the plain mesh
 // (src/multipole.c:462-500).
@@ -1063,7 +1063,7 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
     CU(cudaMalloc(&c->d_yama, need));
     c->yama_bytes = need;
   }
-  if (!c->d_dc) CU(cudaMalloc(&c->d_dc, 2 * sizeof(float2)));
+  if (!c->d_dc) CU(cudaMalloc(&c->d_dc, 2 * kMaxPole * sizeof(float2)));
   float2* base = (float2*)c->d_yama;
   float2 *a1 = base, *a2 = base + c->ncx, *fa = base + 2 * c->ncx;
   // fields: a1, a2, fa, then F_0 and F_l of catalogue 0 (and 1)
@@ -1100,7 +1100,7 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
           launch_ylm_acc(fa, fl[k], c->ng, ell, m, kl, p.box, m == -ell, s);
           c->launches += 2;
         }
-        CU(cudaMemcpyAsync(c->d_dc + k, fl[k], sizeof(float2), cudaMemcpyDeviceToDevice, s));
+        CU(cudaMemcpyAsync(c->d_dc + 2 * l + k, fl[k], sizeof(float2), cudaMemcpyDeviceToDevice, s));
       }
     for (int sp = 0; sp < c->nspec; sp++) {
       const int a = c->spec_a[sp], b = c->spec_b[sp];
@@ -1149,11 +1149,10 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nkey, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey + 4, c->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
-  float2 dc[2] = {{0, 0}, {0, 0}};
-  if (yama) CU(cudaMemcpyAsync(dc, c->d_dc, sizeof(dc), cudaMemcpyDeviceToHost, s));
+  float2 dc[2 * kMaxPole] = {};
+  if (yama) CU(cudaMemcpyAsync(dc, c->d_dc, sizeof(float2) * 2 * p.npole, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
-  h[(size_t)nacc * nkey + 8] = dc[0].x;
-  h[(size_t)nacc * nkey + 9] = dc[1].x;
+  for (int q = 0; q < 2 * p.npole; q++) h[(size_t)nacc * nkey + 8 + q] = dc[q].x;
   float t = 0;
   if (c->assign_started && cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess) c->timings[0] = t;
   for (int i = 0; i < 4; i++)

@@ -22,7 +22,9 @@ these are the pins of the oracle and of the GPU path:
   (ref_auto_cnvt.txt) and by a distance table (ref_auto_table.txt); the
   multipoles 0, 2, 4 on a non-interlaced mesh (ref_auto_yama.txt) and their
   cross spectrum of the catalogue with itself (ref_cross_yama.txt); the
-  multipoles 0 to 6 on the interlaced mesh (ref_auto_yama_il.txt).
+  multipoles 0 to 6 on the interlaced mesh (ref_auto_yama_il.txt); and
+  multipoles 0, 2, 4 with randoms at 1.5 x the data's n(z), whose k = 0
+  mode is far from 0 (ref_auto_yama_nz.txt).
 
 Usage (in a tree that has the reference sources):
     python tests/golden/make_golden.py          # everything
@@ -213,7 +215,16 @@ def survey():
     il = SURVEY_CONF.replace("MULTIPOLE       = 0", "MULTIPOLE       = [0, 1, 2, 3, 4, 5, 6]")
     with open(os.path.join(d, "powspec_yama_il.conf"), "w") as f:
         f.write(il.format(out="ref_auto_yama_il.txt"))
-    for conf in ("powspec_yama.conf", "powspec_cross.conf", "powspec_yama_il.conf"):
+    # randoms with 1.5 x the data's n(z) (and FKP weights from it): the
+    # weighted field's total W = F(k = 0) is far from 0, so the k = 0 mode
+    # of every multipole counts
+    nz = il.replace("RAND_WT_FKP     = 1/(1+$5*2000)", "RAND_WT_FKP     = 1/(1+$5*3000)").replace(
+        "RAND_NZ         = $5", "RAND_NZ         = $5*1.5").replace(
+        "MULTIPOLE       = [0, 1, 2, 3, 4, 5, 6]", "MULTIPOLE       = [0, 2, 4]")
+    with open(os.path.join(d, "powspec_yama_nz.conf"), "w") as f:
+        f.write(nz.format(out="ref_auto_yama_nz.txt"))
+    for conf in ("powspec_yama.conf", "powspec_cross.conf", "powspec_yama_il.conf",
+                 "powspec_yama_nz.conf"):
         subprocess.run([oracle.REF_CLI, "-c", conf], cwd=d, check=True, env=env,
                        stdout=subprocess.DEVNULL)
     survey_converted(d, data, rand, rng, env)

@@ -160,7 +160,8 @@ def test_cli_output_matches_reference_file(cli, workdir):
 def survey_dir(tmp_path):
     for f in ("data.txt", "rand.txt", "powspec.conf", "powspec_box.conf", "data_radecz.txt",
               "rand_radecz.txt", "z_dist.txt", "powspec_cnvt.conf", "powspec_table.conf",
-              "powspec_yama.conf", "powspec_cross.conf", "powspec_yama_il.conf"):
+              "powspec_yama.conf", "powspec_cross.conf", "powspec_yama_il.conf",
+              "powspec_yama_nz.conf"):
         shutil.copy(os.path.join(GOLDEN, "survey", f), tmp_path / f)
     return tmp_path
 
@@ -223,12 +224,14 @@ def test_converted_survey_catalogues_are_read(cli, survey_dir):
     ("powspec_table.conf", "ref_auto_table.txt", "-a"),
     ("powspec_yama.conf", "ref_auto_yama.txt", "-a"),
     ("powspec_cross.conf", "ref_cross_yama.txt", "-x"),
-    ("powspec_yama_il.conf", "ref_auto_yama_il.txt", "-a")])
+    ("powspec_yama_il.conf", "ref_auto_yama_il.txt", "-a"),
+    ("powspec_yama_nz.conf", "ref_auto_yama_nz.txt", "-a")])
 def test_survey_matches_reference_file(cli, survey_dir, conf, ref, out):
     """Data minus alpha x randoms with FKP weights in the fitted (or given,
     non-cubic) box, from Cartesian or converted (RA, Dec, z) coordinates;
     multipoles 0, 2, 4 (non-interlaced) auto and cross, and 0 to 6 on the
-    interlaced mesh (the c2r of the combined field): the reference's
+    interlaced mesh (the c2r of the combined field), and with randoms at
+    1.5 x the data's n(z) (the k = 0 mode far from 0): the reference's
     header lines, k columns and mode counts, and P_l within 1e-5 of
     |P_0| + shot noise (bin 0 holds the k = 0 mode)."""
     r = run(cli, ["-c", conf, out, "gpu_out.txt"], survey_dir)
