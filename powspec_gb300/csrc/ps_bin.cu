@@ -191,8 +191,11 @@ template <int NSPEC, bool STORE, bool P2>
 __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ PassCArgs a) {
   extern __shared__ float2 sm[];
   const int ng = a.ng, ngk = (ng >> 1) + 1, ls = line_stride(ng, P2), h = ng >> 1;
-  const int nty = (ng + a.ty - 1) / a.ty;
-  const int ntile = ngk * nty;
+  // bin mode: a tile is a.ty lines of consecutive ky at one kz; store mode:
+  // a.ty lines of consecutive kz at one ky, so that the [x][y][kz] stores
+  // of a tile are runs of a.ty consecutive values
+  const int nty = STORE ? (ngk + a.ty - 1) / a.ty : (ng + a.ty - 1) / a.ty;
+  const int ntile = STORE ? ng * nty : ngk * nty;
   const ModeGeom& g = a.geom;
   const int nacc = NSPEC * g.npole;
   const int nkey = g.nbin * g.nmu;  // accumulator key = k bin * nmu + |mu| bin
@@ -211,14 +214,16 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
   }
   int ntiles_acc = 0;
   for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-    const int kz = tile / nty;
-    const int ky0 = (tile - kz * nty) * a.ty;
-    const int nl = min(a.ty, ng - ky0);
+    const int t0 = tile / nty;
+    const int kz = STORE ? (tile - t0 * nty) * a.ty : t0;   // store: first kz
+    const int ky0 = STORE ? t0 : (tile - t0 * nty) * a.ty;  // store: the ky
+    const int nl = STORE ? min(a.ty, ngk - kz) : min(a.ty, ng - ky0);
+    const size_t rstride = STORE ? (size_t)ng * ng : (size_t)ng;  // between lines
     for (int f = 0; f < a.nfield; f++) {
       const float2* src = a.in[f] + ((size_t)kz * ng + ky0) * ng;
       for (int e = threadIdx.x; e < nl * h; e += blockDim.x) {
         const int r = e / h, m = e - r * h;
-        const float4 v = __ldcs(reinterpret_cast<const float4*>(src + (size_t)r * ng) + m);
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(src + r * rstride) + m);
         float2* L = sm + (f * nl + r) * ls;
         L[lidx<P2>(2 * m)] = make_float2(v.x, v.y);
         L[lidx<P2>(2 * m + 1)] = make_float2(v.z, v.w);
@@ -229,10 +234,26 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
                          : fft_lines_pp(sm, sm2, a.plan_full, a.nfield * nl, ls, a.tw_full);
 
     if (STORE) {
-      // FFTW layout [x][y][kz]; strided stores (diagnostic path only).
+      // [x][y][kz]: line r holds kz + r; runs of nl consecutive kz per x.
+      // Accumulate modes weight by Y_lm(k^) (1 for k_x = k_y = 0,
+      // src/mp_template.c:118-121) and add into the field.
+      const int jp = dsigned(ky0, ng);
       for (int e = threadIdx.x; e < nl * ng; e += blockDim.x) {
-        const int r = e / ng, i = e - r * ng;
-        a.store[((size_t)i * ng + ky0 + r) * ngk + kz] = X[r * ls + lidx<P2>(i)];
+        const int i = e / nl, r = e - i * nl;
+        const size_t idx = ((size_t)i * ng + ky0) * ngk + kz + r;
+        float2 v = X[r * ls + lidx<P2>(i)];
+        if (a.acc_mode) {
+          const int ip = dsigned(i, ng);
+          const float y = (ip == 0 && jp == 0)
+                              ? 1.f
+                              : ylm_eval(a.yk, ip * a.kinv[0], jp * a.kinv[1], (kz + r) * a.kinv[2]);
+          v = make_float2(v.x * y, v.y * y);
+          if (a.acc_mode == 2) {
+            const float2 o = a.store[idx];
+            v = make_float2(v.x + o.x, v.y + o.y);
+          }
+        }
+        a.store[idx] = v;
       }
       __syncthreads();
       continue;
@@ -479,10 +500,9 @@ void launch_c(const PassCArgs& a, unsigned grid, size_t smem, cudaStream_t s) {
 template <bool P2>
 void launch_c_p(const PassCArgs& a, cudaStream_t s) {
   const int ngk = a.ng / 2 + 1;
-  const int nty = (a.ng + a.ty - 1) / a.ty;
-  const int ntile = ngk * nty;
-  if (a.store) {
-    launch_c<1, true, P2>(a, (unsigned)ntile, pass_c_smem(a.ng, a.ty, a.nfield, 0, 0, P2), s);
+  if (a.store) {  // tiles of a.ty consecutive kz at one ky
+    const unsigned ntile = (unsigned)(a.ng * ((ngk + a.ty - 1) / a.ty));
+    launch_c<1, true, P2>(a, ntile, pass_c_smem(a.ng, a.ty, a.nfield, 0, 0, P2), s);
     return;
   }
   const size_t smem =

@@ -984,14 +984,20 @@ int ps_gpu_assign_soa(ps_gpu_ctx* c, int cat, const float* x, const float* y, co
 
 namespace {
 
-// Plain r2c of a real device mesh into a stored half-complex field
-// [x][y][z/2+1] (the z, y and x passes; a1, a2: scratch fields).
-void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* out) {
+// r2c of a real device mesh into a stored half-complex field [x][y][z/2+1]
+// (the z, y and x passes; a1, a2: scratch fields; the pipelined z and y
+// passes for power-of-two meshes).  acc_mode 1 / 2: out = / += the
+// transform times the harmonic yk of k^.
+void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* out,
+               int acc_mode = 0, const YlmCoef* yk = nullptr) {
   cudaStream_t s = c->stream;
+  const bool pipe = c->plan_full.logn >= 0 && !getenv("PS_GPU_NO_PIPELINE");
   PassAArgs a;
   memset(&a, 0, sizeof a);
   a.ng = c->ng;
-  a.ty = c->ty_a;
+  a.ty = pipe ? c->ty_ap : c->ty_a;
+  a.pipe_grid = pipe ? (c->radix32_a ? 1 : 2) * c->nsm : 0;
+  a.radix32 = c->radix32_a ? 1 : 0;
   a.fgrid = in;
   a.out = a1;
   a.tw_half = c->d_tw_half;
@@ -1002,7 +1008,9 @@ void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* o
   PassBArgs b;
   memset(&b, 0, sizeof b);
   b.ng = c->ng;
-  b.tx = c->tx_b;
+  b.tx = pipe ? c->tx_bp : c->tx_b;
+  b.pipe_grid = pipe ? (c->radix32_b ? 1 : 2) * c->nsm : 0;
+  b.radix32 = c->radix32_b ? 1 : 0;
   b.in = a1;
   b.out = a2;
   b.tw_full = c->d_tw_full;
@@ -1012,12 +1020,15 @@ void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* o
   PassCArgs pc;
   memset(&pc, 0, sizeof pc);
   pc.ng = c->ng;
-  pc.ty = std::max(1, std::min(c->ng, kPassCElems / c->ng));
+  pc.ty = std::max(1, std::min(c->ng / 2 + 1, kPassCElems / c->ng));
   pc.nfield = 1;
   pc.ncat = 1;
   pc.nspec = 1;
   pc.in[0] = a2;
   pc.store = out;
+  pc.acc_mode = acc_mode;
+  if (yk) pc.yk = *yk;
+  for (int d = 0; d < 3; d++) pc.kinv[d] = (float)(1.0 / c->p.box[d]);
   pc.tw_full = c->d_tw_full;
   pc.plan_full = c->plan_full;
   pc.geom = c->geom;
@@ -1070,6 +1081,7 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
   float2* f0[2] = {base + 3 * c->ncx, base + 5 * c->ncx};
   float2* fl[2] = {base + 4 * c->ncx, base + 6 * c->ncx};
   float* wmesh = (float*)(base + (size_t)(3 + 2 * p.ncat) * c->ncx);
+  CU(cudaMemsetAsync(c->d_err + 2, 0, sizeof(int), s));
   CU(cudaEventRecord(c->ev[0], s));
   const int mpc = c->mpc;
   for (int k = 0; k < p.ncat; k++) {
@@ -1091,14 +1103,11 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
     if (ell > 0)
       for (int k = 0; k < p.ncat; k++) {
         for (int m = -ell; m <= ell; m++) {
-          double f = 1;  // (l - |m|)! / (l + |m|)!
-          for (int q = ell - abs(m) + 1; q <= ell + abs(m); q++) f /= q;
-          const double kl = sqrt((2 * ell + 1) / (4 * M_PI) * f) * (m ? sqrt(2.0) : 1.0);
-          launch_ylm_real((const float*)c->grid[k * mpc], wmesh, c->ng, ell, m, kl, c->survey_origin,
+          launch_ylm_real((const float*)c->grid[k * mpc], wmesh, c->ng, ell, m, c->survey_origin,
                           p.box, s);
-          r2c_store(c, wmesh, a1, a2, fa);
-          launch_ylm_acc(fa, fl[k], c->ng, ell, m, kl, p.box, m == -ell, s);
-          c->launches += 2;
+          const YlmCoef yk = ylm_coef(ell, m);
+          r2c_store(c, wmesh, a1, a2, fl[k], m == -ell ? 1 : 2, &yk);
+          c->launches += 1;
         }
         CU(cudaMemcpyAsync(c->d_dc + 2 * l + k, fl[k], sizeof(float2), cudaMemcpyDeviceToDevice, s));
       }

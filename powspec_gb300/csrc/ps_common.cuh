@@ -704,4 +704,40 @@ __device__ __forceinline__ int mode_bin(const ModeGeom& g, int ia, int ja, int k
 inline int signed_index(int i, int ng) { return (i <= (ng >> 1)) ? i : i - ng; }
 __device__ __forceinline__ int dsigned(int i, int ng) { return (i <= (ng >> 1)) ? i : i - ng; }
 
+// One real spherical harmonic Y_lm, l <= 6, in the basis of the reference's
+// math/spherical.h:54-262 (no Condon-Shortley sign; m > 0: cos(m phi),
+// m < 0: sin(|m| phi)).  Y_lm = sin^|m|(t) q(cos t) trig(|m| phi), where
+// q = K_lm [sqrt 2 if m != 0] d^|m| P_l / dx^|m| holds the normalisation
+// (host: ylm_coef).  The basis matters: the estimator replaces the harmonic
+// by 1 for every m on the k_z axis and at k = 0, where sum_m Y_lm(r^)
+// enters alone.
+struct YlmCoef {
+  int am;        // |m|
+  int trig;      // 0: m = 0; 1: cos(|m| phi); -1: sin(|m| phi)
+  int deg;       // degree of q (l - |m|)
+  float q[7];    // coefficients of q, x^0 .. x^deg
+};
+
+// Y_lm of the direction (x, y, z), not normalised; x = y = 0 gives NaN for
+// m != 0 (callers treat the axis themselves).
+__device__ __forceinline__ float ylm_eval(const YlmCoef& c, float x, float y, float z) {
+  const float rxy2 = fmaf(x, x, y * y);
+  const float rinv = rsqrtf(fmaf(z, z, rxy2));
+  const float ct = z * rinv;
+  float q = c.q[c.deg];
+  for (int d = c.deg - 1; d >= 0; d--) q = fmaf(q, ct, c.q[d]);
+  if (c.am == 0) return q;
+  const float ri = rsqrtf(rxy2);  // 1 / r_xy
+  const float st = rxy2 * ri * rinv;
+  const float cp = x * ri, sp = y * ri;
+  float stm = st, co = cp, si = sp;
+  for (int i = 1; i < c.am; i++) {
+    stm *= st;
+    const float c2 = co * cp - si * sp;
+    si = fmaf(si, cp, co * sp);
+    co = c2;
+  }
+  return q * stm * (c.trig > 0 ? co : si);
+}
+
 }  // namespace ps

@@ -68,12 +68,11 @@ int learned_enqueue(::ps_mlp* m, const LearnedArgs& a, cudaStream_t s);
 int learned_feature_width();
 
 // Survey multipoles l > 0 (ps_yama.cu): out = in * Y_lm(r^) over the real
-// mesh, the observer at the origin, the box corner at `origin`; acc (+)= f *
-// Y_lm(k^) over a stored half-complex field.  kl: the harmonic's constant.
-int launch_ylm_real(const float* in, float* out, int ng, int l, int m, double kl,
-                    const double origin[3], const double box[3], cudaStream_t s);
-int launch_ylm_acc(const float2* f, float2* acc, int ng, int l, int m, double kl,
-                   const double box[3], bool first, cudaStream_t s);
+// mesh, the observer at the origin, the box corner at `origin`; the
+// coefficients of one harmonic (ylm_eval).
+int launch_ylm_real(const float* in, float* out, int ng, int l, int m, const double origin[3],
+                    const double box[3], cudaStream_t s);
+YlmCoef ylm_coef(int l, int m);
 // The interlaced field's c2r (ps_yama.cu): inverse along the leading axis
 // of [l][p][kz] into [p][l][kz] (with in2: over the interlace combination,
 // also written back to in), then half-complex z rows -> real rows / Ng^3.
@@ -135,6 +134,9 @@ struct PassCArgs {
   int spec_a[3], spec_b[3];     // catalogue indices of each spectrum
   const float2* in[4];          // field f = cat * (interlace ? 2 : 1) + mesh
   float2* store;                // store mode target (FFTW layout), or NULL
+  int acc_mode;                 // store mode: 0 store; 1 store x Y(k^); 2 add x Y(k^)
+  YlmCoef yk;                   // acc_mode > 0: the harmonic; 1 on the k_z axis
+  float kinv[3];                // 1 / L per axis (wave-vector direction)
   const float2* tw_full;
   FftPlan plan_full;
   ModeGeom geom;

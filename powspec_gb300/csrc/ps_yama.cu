@@ -4,59 +4,57 @@
 //   F_l(k) = sum_m Y_lm(k^) FFT[ F(r) Y_lm(r^) ](k),
 //   P_l ~ sum_k Re[F_0(k) F_l(k)*],
 // with F the data - alpha x randoms mesh and r^ the direction from the
-// observer (the coordinate origin).  Any orthonormal real basis of the
-// degree-l harmonics gives the same sum over m (the addition theorem,
-// sum_m Y_lm(a) Y_lm(b) = (2l + 1) / (4 pi) L_l(a . b)); the one here is
-// Y_l0 = K_l0 P_l(cos t), Y_lm = sqrt(2) K_lm P_l^m(cos t) cos(m p),
-// Y_l,-m = sqrt(2) K_lm P_l^m(cos t) sin(m p), K_lm^2 = (2l + 1) / (4 pi)
-// (l - m)! / (l + m)!, with P_l^m by the standard recurrences.
+// observer (the coordinate origin).  Each term runs as: the mesh weighted by
+// Y_lm(r^) (k_ylm_real), the r2c passes, and the last pass accumulating
+// Y_lm(k^) times its output into F_l (pass C in accumulate mode, ps_bin.cu).
 //
-// Two conventions of the reference are kept: the first mesh row
-// (i = j = 0) and the modes on the k_z axis (k_x = k_y = 0) take the
-// harmonic as 1 for every m (src/mp_template.c:71-74, :118-121).
+// The harmonics are the reference's real basis (math/spherical.h:54-262),
+// evaluated as sin^|m| t q(cos t) trig(|m| phi) with q's coefficients from
+// the host (ylm_coef).  Two conventions of the reference are kept: the
+// first mesh row (i = j = 0) and the modes on the k_z axis (k_x = k_y = 0)
+// take the harmonic as 1 for every m (src/mp_template.c:71-74, :118-121).
 #include <algorithm>
+#include <cmath>
 
 #include "ps_internal.h"
 
 namespace ps {
-namespace {
 
-// Y_lm of the direction (x, y, z) (need not be normalised); l <= 6.
-__device__ __forceinline__ float ylm(int l, int m, float kl, float x, float y, float z) {
-  const float rxy2 = x * x + y * y, r = sqrtf(rxy2 + z * z);
-  const float ct = z / r, st = sqrtf(rxy2) / r;
-  const int am = abs(m);
-  // P_am^am = (2 am - 1)!! st^am, then up to P_l^am (Condon-Shortley sign
-  // dropped: the sum over m does not depend on it)
-  float pmm = 1.f;
-  for (int i = 1; i <= am; i++) pmm *= (2 * i - 1) * st;
-  float p = pmm;
-  if (l > am) {
-    float p1 = ct * (2 * am + 1) * pmm, p0 = pmm;
-    p = p1;
-    for (int ll = am + 2; ll <= l; ll++) {
-      p = ((2 * ll - 1) * ct * p1 - (ll + am - 1) * p0) / (ll - am);
-      p0 = p1;
-      p1 = p;
-    }
+YlmCoef ylm_coef(int l, int m) {
+  // Legendre P_l coefficients by (n + 1) P_(n+1) = (2n + 1) x P_n - n P_(n-1)
+  double p0[8] = {1}, p1[8] = {0, 1}, pl[8] = {0};
+  if (l == 0) std::copy(p0, p0 + 8, pl);
+  if (l == 1) std::copy(p1, p1 + 8, pl);
+  for (int n = 1; n < l; n++) {
+    double nx[8] = {0};
+    for (int d = 0; d < 7; d++) nx[d + 1] += (2 * n + 1) * p1[d] / (n + 1);
+    for (int d = 0; d < 8; d++) nx[d] -= n * p0[d] / (n + 1);
+    std::copy(p1, p1 + 8, p0);
+    std::copy(nx, nx + 8, p1);
+    std::copy(nx, nx + 8, pl);
   }
-  if (m == 0) return kl * p;
-  // cos(am phi), sin(am phi) from cos phi = x / rxy, sin phi = y / rxy
-  const float ri = rsqrtf(rxy2), cp = x * ri, sp = y * ri;
-  float c = 1.f, s = 0.f;
-  for (int i = 0; i < am; i++) {
-    const float c2 = c * cp - s * sp;
-    s = s * cp + c * sp;
-    c = c2;
-  }
-  return kl * p * (m > 0 ? c : s);
+  const int am = std::abs(m);
+  for (int k = 0; k < am; k++)  // d/dx, |m| times
+    for (int d = 0; d < 7; d++) pl[d] = (d + 1) * pl[d + 1];
+  double f = 1;  // (l - |m|)! / (l + |m|)!
+  for (int q = l - am + 1; q <= l + am; q++) f /= q;
+  double kl = std::sqrt((2 * l + 1) / (4 * M_PI) * f);
+  if (m) kl *= std::sqrt(2.0);
+  YlmCoef c;
+  c.am = am;
+  c.trig = m > 0 ? 1 : (m < 0 ? -1 : 0);
+  c.deg = l - am;
+  for (int d = 0; d < 7; d++) c.q[d] = (float)(d <= c.deg ? kl * pl[d] : 0.0);
+  return c;
 }
+
+namespace {
 
 // out = in * Y_lm(r^) over the real mesh [x][y][z]; cell (i, j, k) sits at
 // (i + o0, j + o1, k + o2) cells from the observer, o = box corner * Ng / L,
 // and directions are taken as cells * L (src/mp_template.c:60-70).
-__global__ void k_ylm_real(const float* __restrict__ in, float* __restrict__ out, int ng, int l,
-                           int m, float kl, float o0, float o1, float o2, float L0, float L1,
+__global__ void k_ylm_real(const float* __restrict__ in, float* __restrict__ out, int ng,
+                           const YlmCoef c, float o0, float o1, float o2, float L0, float L1,
                            float L2) {
   const size_t n = (size_t)ng * ng * ng;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
@@ -65,30 +63,8 @@ __global__ void k_ylm_real(const float* __restrict__ in, float* __restrict__ out
     const size_t row = e / ng;
     const int j = (int)(row % ng), i = (int)(row / ng);
     float y = 1.f;
-    if (row != 0) y = ylm(l, m, kl, (i + o0) * L0, (j + o1) * L1, (k + o2) * L2);
-    out[e] = in[e] * y;
-  }
-}
-
-// acc (+)= f * Y_lm(k^) over the stored half-complex field [x][y][z/2+1];
-// k = (signed i / L0, signed j / L1, k / L2).
-__global__ void k_ylm_acc(const float2* __restrict__ f, float2* __restrict__ acc, int ng, int l,
-                          int m, float kl, float iL0, float iL1, float iL2, int first) {
-  const int ngk = ng / 2 + 1;
-  const size_t n = (size_t)ng * ng * ngk;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e % ngk);
-    const size_t row = e / ngk;
-    const int j = (int)(row % ng), i = (int)(row / ng);
-    const int ip = (2 * i <= ng) ? i : i - ng, jp = (2 * j <= ng) ? j : j - ng;
-    float y = 1.f;
-    if (ip != 0 || jp != 0) y = ylm(l, m, kl, ip * iL0, jp * iL1, k * iL2);
-    const float2 v = f[e];
-    float2 a = first ? make_float2(0.f, 0.f) : acc[e];
-    a.x += v.x * y;
-    a.y += v.y * y;
-    acc[e] = a;
+    if (row != 0) y = ylm_eval(c, (i + o0) * L0, (j + o1) * L1, (k + o2) * L2);
+    out[e] = __ldcs(&in[e]) * y;
   }
 }
 
@@ -266,23 +242,14 @@ int launch_c2r_z(const float2* in, float* out, int ng, int ty, const float2* tw_
   return 1;
 }
 
-int launch_ylm_real(const float* in, float* out, int ng, int l, int m, double kl,
-                    const double origin[3], const double box[3], cudaStream_t s) {
+int launch_ylm_real(const float* in, float* out, int ng, int l, int m, const double origin[3],
+                    const double box[3], cudaStream_t s) {
   const size_t n = (size_t)ng * ng * ng;
   const unsigned blocks = (unsigned)((n + 255) / 256 < 152 * 32 ? (n + 255) / 256 : 152 * 32);
-  k_ylm_real<<<blocks, 256, 0, s>>>(in, out, ng, l, m, (float)kl, (float)(origin[0] * ng / box[0]),
+  k_ylm_real<<<blocks, 256, 0, s>>>(in, out, ng, ylm_coef(l, m), (float)(origin[0] * ng / box[0]),
                                      (float)(origin[1] * ng / box[1]),
                                      (float)(origin[2] * ng / box[2]), (float)box[0],
                                      (float)box[1], (float)box[2]);
-  return 1;
-}
-
-int launch_ylm_acc(const float2* f, float2* acc, int ng, int l, int m, double kl,
-                   const double box[3], bool first, cudaStream_t s) {
-  const size_t n = (size_t)ng * ng * (ng / 2 + 1);
-  const unsigned blocks = (unsigned)((n + 255) / 256 < 152 * 32 ? (n + 255) / 256 : 152 * 32);
-  k_ylm_acc<<<blocks, 256, 0, s>>>(f, acc, ng, l, m, (float)kl, (float)(1.0 / box[0]),
-                                    (float)(1.0 / box[1]), (float)(1.0 / box[2]), first ? 1 : 0);
   return 1;
 }
 
