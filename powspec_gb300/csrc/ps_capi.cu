@@ -701,6 +701,7 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
   if (events) CU(cudaEventRecord(c->ev[0], s));
   for (int f = 0; f < c->nfield; f++) {
     PassAArgs a;
+    memset(&a, 0, sizeof a);
     a.ng = ng;
     a.ty = pipe ? c->ty_ap : c->ty_a;
     a.pipe_grid = pipe ? (c->radix32_a ? 1 : 2) * c->nsm : 0;
@@ -986,8 +987,9 @@ namespace {
 
 // r2c of a real device mesh into a stored half-complex field [x][y][z/2+1]
 // (the z, y and x passes; a1, a2: scratch fields; the pipelined z and y
-// passes for power-of-two meshes).  acc_mode 1 / 2: out = / += the
-// transform times the harmonic yk of k^.
+// passes for power-of-two meshes).  With a harmonic yk: the mesh weighted by
+// yk(r^) on the way in (observer at the origin), and out = (acc_mode 1) or
+// += (acc_mode 2) the transform times yk(k^).
 void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* out,
                int acc_mode = 0, const YlmCoef* yk = nullptr) {
   cudaStream_t s = c->stream;
@@ -999,6 +1001,14 @@ void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* o
   a.pipe_grid = pipe ? (c->radix32_a ? 1 : 2) * c->nsm : 0;
   a.radix32 = c->radix32_a ? 1 : 0;
   a.fgrid = in;
+  if (yk) {
+    a.yw = 1;
+    a.yc = *yk;
+    for (int d = 0; d < 3; d++) {
+      a.org[d] = (float)(c->survey_origin[d] * c->ng / c->p.box[d]);
+      a.len[d] = (float)c->p.box[d];
+    }
+  }
   a.out = a1;
   a.tw_half = c->d_tw_half;
   a.tw_full = c->d_tw_full;
@@ -1064,8 +1074,8 @@ void bin_pair(ps_gpu_ctx* c, const float2* f1, const float2* f2) {
 int enqueue_survey_multipoles(ps_gpu_ctx* c) {
   const ps_gpu_params& p = c->p;
   cudaStream_t s = c->stream;
-  const size_t cx = c->ncx * sizeof(float2), real = c->ntot * sizeof(float);
-  const size_t need = (size_t)(3 + 2 * p.ncat) * cx + real;
+  const size_t cx = c->ncx * sizeof(float2);
+  const size_t need = (size_t)(3 + 2 * p.ncat) * cx;
   if (need > c->yama_bytes) {
     CU(cudaStreamSynchronize(s));
     if (c->d_yama) cudaFree(c->d_yama);
@@ -1080,7 +1090,6 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
   // fields: a1, a2, fa, then F_0 and F_l of catalogue 0 (and 1)
   float2* f0[2] = {base + 3 * c->ncx, base + 5 * c->ncx};
   float2* fl[2] = {base + 4 * c->ncx, base + 6 * c->ncx};
-  float* wmesh = (float*)(base + (size_t)(3 + 2 * p.ncat) * c->ncx);
   CU(cudaMemsetAsync(c->d_err + 2, 0, sizeof(int), s));
   CU(cudaEventRecord(c->ev[0], s));
   const int mpc = c->mpc;
@@ -1103,11 +1112,8 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
     if (ell > 0)
       for (int k = 0; k < p.ncat; k++) {
         for (int m = -ell; m <= ell; m++) {
-          launch_ylm_real((const float*)c->grid[k * mpc], wmesh, c->ng, ell, m, c->survey_origin,
-                          p.box, s);
           const YlmCoef yk = ylm_coef(ell, m);
-          r2c_store(c, wmesh, a1, a2, fl[k], m == -ell ? 1 : 2, &yk);
-          c->launches += 1;
+          r2c_store(c, (const float*)c->grid[k * mpc], a1, a2, fl[k], m == -ell ? 1 : 2, &yk);
         }
         CU(cudaMemcpyAsync(c->d_dc + 2 * l + k, fl[k], sizeof(float2), cudaMemcpyDeviceToDevice, s));
       }
@@ -1322,6 +1328,7 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   float* d_in = (float*)c->grid[0];  // ntot floats fit in the mesh buffer
   CU(cudaMemcpyAsync(d_in, in, c->ntot * sizeof(float), cudaMemcpyHostToDevice, s));
   PassAArgs a;
+  memset(&a, 0, sizeof a);
   a.ng = ng;
   a.ty = c->ty_a;
   a.grid = nullptr;

@@ -724,18 +724,24 @@ __device__ __forceinline__ float ylm_eval(const YlmCoef& c, float x, float y, fl
   const float rxy2 = fmaf(x, x, y * y);
   const float rinv = rsqrtf(fmaf(z, z, rxy2));
   const float ct = z * rinv;
-  float q = c.q[c.deg];
-  for (int d = c.deg - 1; d >= 0; d--) q = fmaf(q, ct, c.q[d]);
+  // fixed-index Horner over all 7 slots (unused ones are 0): no dynamic
+  // indexing, so the coefficients stay in registers
+  float q = c.q[6];
+#pragma unroll
+  for (int d = 5; d >= 0; d--) q = fmaf(q, ct, c.q[d]);
   if (c.am == 0) return q;
   const float ri = rsqrtf(rxy2);  // 1 / r_xy
   const float st = rxy2 * ri * rinv;
   const float cp = x * ri, sp = y * ri;
   float stm = st, co = cp, si = sp;
-  for (int i = 1; i < c.am; i++) {
-    stm *= st;
-    const float c2 = co * cp - si * sp;
-    si = fmaf(si, cp, co * sp);
-    co = c2;
+#pragma unroll
+  for (int i = 1; i < 6; i++) {
+    if (i < c.am) {
+      stm *= st;
+      const float c2 = co * cp - si * sp;
+      si = fmaf(si, cp, co * sp);
+      co = c2;
+    }
   }
   return q * stm * (c.trig > 0 ? co : si);
 }

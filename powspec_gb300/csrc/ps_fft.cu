@@ -18,6 +18,13 @@
 namespace ps {
 namespace {
 
+// Harmonic weight of real cell (i, j, k) for the survey multipoles.
+__device__ __forceinline__ float cell_harmonic(const PassAArgs& a, int i, int j, int k) {
+  return (i == 0 && j == 0) ? 1.f
+                            : ylm_eval(a.yc, (i + a.org[0]) * a.len[0], (j + a.org[1]) * a.len[1],
+                                       (k + a.org[2]) * a.len[2]);
+}
+
 template <bool P2>
 __global__ void __launch_bounds__(kFftThreads, 2) k_pass_a(const __grid_constant__ PassAArgs a) {
   extern __shared__ float2 sm[];
@@ -42,7 +49,12 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_a(const __grid_constant
     const float* base = a.fgrid + ((size_t)x * ng + y0) * ng;
     for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
       const int r = e / M, m = e - r * M;
-      sm[r * ls + lidx<P2>(m)] = __ldcs(reinterpret_cast<const float2*>(base + (size_t)r * ng) + m);
+      float2 v = __ldcs(reinterpret_cast<const float2*>(base + (size_t)r * ng) + m);
+      if (a.yw) {
+        v.x *= cell_harmonic(a, x, y0 + r, 2 * m);
+        v.y *= cell_harmonic(a, x, y0 + r, 2 * m + 1);
+      }
+      sm[r * ls + lidx<P2>(m)] = v;
     }
   }
   __syncthreads();
@@ -170,6 +182,16 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_a_tma
     if (!pipe_wait(bar, it, a.err, &s_abort)) break;
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
+    if (a.yw) {  // weight the staged rows in place; the buffer is refilled
+                 // by the async proxy only after the fence and two barriers
+      for (int e = threadIdx.x; e < nl * ng; e += blockDim.x) {
+        const int r = e / ng, k = e - r * ng;
+        float* row = reinterpret_cast<float*>(stage[s] + (size_t)r * M);
+        row[k] *= cell_harmonic(a, x, y0 + r, k);
+      }
+      fence_proxy_async();
+      __syncthreads();
+    }
     float2* X = fft2_pp_from<false, MAXLOG>(stage[s], M, 0, F, logm, nl, ls, a.tw_half);
     const int half = (M >> 1) + 1;
     for (int e = threadIdx.x; e < nl * half; e += blockDim.x) {

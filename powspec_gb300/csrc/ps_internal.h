@@ -67,11 +67,8 @@ struct LearnedArgs {
 int learned_enqueue(::ps_mlp* m, const LearnedArgs& a, cudaStream_t s);
 int learned_feature_width();
 
-// Survey multipoles l > 0 (ps_yama.cu): out = in * Y_lm(r^) over the real
-// mesh, the observer at the origin, the box corner at `origin`; the
-// coefficients of one harmonic (ylm_eval).
-int launch_ylm_real(const float* in, float* out, int ng, int l, int m, const double origin[3],
-                    const double box[3], cudaStream_t s);
+// Survey multipoles l > 0 (ps_yama.cu): the coefficients of one harmonic
+// (ylm_eval).
 YlmCoef ylm_coef(int l, int m);
 // The interlaced field's c2r (ps_yama.cu): inverse along the leading axis
 // of [l][p][kz] into [p][l][kz] (with in2: over the interlace combination,
@@ -102,9 +99,15 @@ struct PassAArgs {
   const float2* tw_half;        // length ng/2 twiddles
   const float2* tw_full;        // length ng twiddles (r2c split)
   FftPlan plan_half;
-  int pipe_grid;
-  int radix32;  // pipelined kernel: radix-32 passes on 8192-value tiles                // > 0: pipelined persistent kernel with this grid
+  int pipe_grid;                // > 0: pipelined persistent kernel with this grid
+  int radix32;                  // pipelined kernel: radix-32 passes on 8192-value tiles
   int* err;                     // bit 1: pipeline wait timed out
+  // survey harmonics (yw != 0): cell (i, j, k) of the FP32 input is weighted
+  // by Y_lm of ((i, j, k) + org) * len on the way in, 1 on the row i = j = 0
+  // (src/mp_template.c:60-74)
+  int yw;
+  YlmCoef yc;
+  float org[3], len[3];
 };
 int launch_pass_a(const PassAArgs& a, cudaStream_t s);
 

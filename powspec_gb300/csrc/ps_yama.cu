@@ -4,9 +4,10 @@
 //   F_l(k) = sum_m Y_lm(k^) FFT[ F(r) Y_lm(r^) ](k),
 //   P_l ~ sum_k Re[F_0(k) F_l(k)*],
 // with F the data - alpha x randoms mesh and r^ the direction from the
-// observer (the coordinate origin).  Each term runs as: the mesh weighted by
-// Y_lm(r^) (k_ylm_real), the r2c passes, and the last pass accumulating
-// Y_lm(k^) times its output into F_l (pass C in accumulate mode, ps_bin.cu).
+// observer (the coordinate origin).  Each term runs as the r2c passes with
+// the mesh weighted by Y_lm(r^) as pass A reads it (ps_fft.cu) and pass C
+// adding Y_lm(k^) times its output into F_l (ps_bin.cu).  This file holds
+// the harmonics' coefficients and the c2r of the interlaced field.
 //
 // The harmonics are the reference's real basis (math/spherical.h:54-262),
 // evaluated as sin^|m| t q(cos t) trig(|m| phi) with q's coefficients from
@@ -49,24 +50,6 @@ YlmCoef ylm_coef(int l, int m) {
 }
 
 namespace {
-
-// out = in * Y_lm(r^) over the real mesh [x][y][z]; cell (i, j, k) sits at
-// (i + o0, j + o1, k + o2) cells from the observer, o = box corner * Ng / L,
-// and directions are taken as cells * L (src/mp_template.c:60-70).
-__global__ void k_ylm_real(const float* __restrict__ in, float* __restrict__ out, int ng,
-                           const YlmCoef c, float o0, float o1, float o2, float L0, float L1,
-                           float L2) {
-  const size_t n = (size_t)ng * ng * ng;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e % ng);
-    const size_t row = e / ng;
-    const int j = (int)(row % ng), i = (int)(row / ng);
-    float y = 1.f;
-    if (row != 0) y = ylm_eval(c, (i + o0) * L0, (j + o1) * L1, (k + o2) * L2);
-    out[e] = __ldcs(&in[e]) * y;
-  }
-}
 
 // ------------------------------------------------ c2r of the interlaced field
 // With interlacing, the harmonic weights multiply the real-space field of
@@ -239,17 +222,6 @@ int launch_c2r_z(const float2* in, float* out, int ng, int ty, const float2* tw_
     cudaFuncSetAttribute(k_c2r_z<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_c2r_z<false><<<grid, kFftThreads, smem, s>>>(a);
   }
-  return 1;
-}
-
-int launch_ylm_real(const float* in, float* out, int ng, int l, int m, const double origin[3],
-                    const double box[3], cudaStream_t s) {
-  const size_t n = (size_t)ng * ng * ng;
-  const unsigned blocks = (unsigned)((n + 255) / 256 < 152 * 32 ? (n + 255) / 256 : 152 * 32);
-  k_ylm_real<<<blocks, 256, 0, s>>>(in, out, ng, ylm_coef(l, m), (float)(origin[0] * ng / box[0]),
-                                     (float)(origin[1] * ng / box[1]),
-                                     (float)(origin[2] * ng / box[2]), (float)box[0],
-                                     (float)box[1], (float)box[2]);
   return 1;
 }
 
