@@ -720,6 +720,7 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
   if (events) CU(cudaEventRecord(c->ev[1], s));
   for (int f = 0; f < c->nfield; f++) {
     PassBArgs b;
+    memset(&b, 0, sizeof b);
     b.ng = ng;
     b.tx = pipe ? c->tx_bp : c->tx_b;
     b.pipe_grid = pipe ? (c->radix32_b ? 1 : 2) * c->nsm : 0;
@@ -1343,6 +1344,7 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   a.err = c->d_err + 2;
   launch_pass_a(a, s);
   PassBArgs b;
+  memset(&b, 0, sizeof b);
   b.ng = ng;
   b.tx = c->tx_b;
   b.in = c->cbuf[0];
