@@ -1031,7 +1031,10 @@ void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* o
   PassCArgs pc;
   memset(&pc, 0, sizeof pc);
   pc.ng = c->ng;
-  pc.ty = std::max(1, std::min(c->ng / 2 + 1, kPassCElems / c->ng));
+  // 8 kz per tile: 64-byte runs, and small tiles keep more CTAs resident to
+  // hide the accumulator's read-modify-write (Ng = 256: 4.1 ms for the 14
+  // harmonic terms of l = 2, 4 against 4.2 ms at 16 and 4.6 ms at 4)
+  pc.ty = std::max(1, std::min({c->ng / 2 + 1, 8, kPassCElems / c->ng}));
   pc.nfield = 1;
   pc.ncat = 1;
   pc.nspec = 1;
