@@ -718,6 +718,49 @@ struct YlmCoef {
   float q[7];    // coefficients of q, x^0 .. x^deg
 };
 
+// The part of Y_lm that depends on (x, y) only, for a row of cells that
+// share them: r_xy, r_xy^2 and trig(|m| phi).
+struct YlmRow {
+  float rxy, rxy2, trig;
+};
+__device__ __forceinline__ YlmRow ylm_row(const YlmCoef& c, float x, float y) {
+  YlmRow w;
+  w.rxy2 = fmaf(x, x, y * y);
+  w.trig = 1.f;
+  w.rxy = 0.f;
+  if (c.am) {
+    const float ri = rsqrtf(w.rxy2);
+    w.rxy = w.rxy2 * ri;
+    const float cp = x * ri, sp = y * ri;
+    float co = cp, si = sp;
+#pragma unroll
+    for (int i = 1; i < 6; i++) {
+      if (i < c.am) {
+        const float c2 = co * cp - si * sp;
+        si = fmaf(si, cp, co * sp);
+        co = c2;
+      }
+    }
+    w.trig = c.trig > 0 ? co : si;
+  }
+  return w;
+}
+// Y_lm at height z above the row: same value as ylm_eval(c, x, y, z).
+__device__ __forceinline__ float ylm_cell(const YlmCoef& c, const YlmRow& w, float z) {
+  const float rinv = rsqrtf(fmaf(z, z, w.rxy2));
+  const float ct = z * rinv;
+  float q = c.q[6];
+#pragma unroll
+  for (int d = 5; d >= 0; d--) q = fmaf(q, ct, c.q[d]);
+  if (c.am == 0) return q;
+  const float st = w.rxy * rinv;
+  float stm = st;
+#pragma unroll
+  for (int i = 1; i < 6; i++)
+    if (i < c.am) stm *= st;
+  return q * stm * w.trig;
+}
+
 // Y_lm of the direction (x, y, z), not normalised; x = y = 0 gives NaN for
 // m != 0 (callers treat the axis themselves).
 __device__ __forceinline__ float ylm_eval(const YlmCoef& c, float x, float y, float z) {

@@ -183,11 +183,17 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_a_tma
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
     if (a.yw) {  // weight the staged rows in place; the buffer is refilled
-                 // by the async proxy only after the fence and two barriers
-      for (int e = threadIdx.x; e < nl * ng; e += blockDim.x) {
-        const int r = e / ng, k = e - r * ng;
+                 // by the async proxy only after the fence and two barriers.
+                 // tpr threads per row, so the (x, y) part is done per row.
+      const int tpr = max(1, (int)blockDim.x / nl);
+      const int rstep = (int)blockDim.x / tpr;
+      for (int r = threadIdx.x / tpr; r < nl; r += rstep) {
         float* row = reinterpret_cast<float*>(stage[s] + (size_t)r * M);
-        row[k] *= cell_harmonic(a, x, y0 + r, k);
+        const int j = y0 + r;
+        if (x == 0 && j == 0) continue;  // the row i = j = 0 keeps weight 1
+        const YlmRow w = ylm_row(a.yc, (x + a.org[0]) * a.len[0], (j + a.org[1]) * a.len[1]);
+        for (int k = threadIdx.x % tpr; k < ng; k += tpr)
+          row[k] *= ylm_cell(a.yc, w, (k + a.org[2]) * a.len[2]);
       }
       fence_proxy_async();
       __syncthreads();
