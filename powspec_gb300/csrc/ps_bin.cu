@@ -470,13 +470,26 @@ __global__ void __launch_bounds__(256) k_geometry(const __grid_constant__ GeomAr
   }
 }
 
-__global__ void k_reduce(const double* __restrict__ part, int grid, int width,
-                         double* __restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= width) return;
+// out[j] = sum over the grid rows of part[row][j], in a fixed order: warp w
+// of a block adds rows w, w + 16, ... of 32 consecutive columns (coalesced
+// 256-byte rows), then the 16 warp sums are added in warp order.
+constexpr int kReduceWarps = 16;
+__global__ void __launch_bounds__(32 * kReduceWarps) k_reduce(const double* __restrict__ part, int grid,
+                                                             int width, double* __restrict__ out) {
+  __shared__ double sh[kReduceWarps][33];
+  const int j = blockIdx.x * 32 + threadIdx.x, w = threadIdx.y;
   double s = 0.0;
-  for (int gi = 0; gi < grid; gi++) s += part[(size_t)gi * width + j];
-  out[j] = s;
+  if (j < width) {
+#pragma unroll 4
+    for (int gi = w; gi < grid; gi += kReduceWarps) s += __ldg(&part[(size_t)gi * width + j]);
+  }
+  sh[w][threadIdx.x] = s;
+  __syncthreads();
+  if (w == 0 && j < width) {
+    double t = sh[0][threadIdx.x];
+    for (int q = 1; q < kReduceWarps; q++) t += sh[q][threadIdx.x];
+    out[j] = t;
+  }
 }
 
 }  // namespace
@@ -558,7 +571,7 @@ int launch_geometry(const GeomArgs& a, cudaStream_t s) {
 }
 
 int launch_reduce(const double* part, int grid, int width, double* out, cudaStream_t s) {
-  k_reduce<<<(width + 255) / 256, 256, 0, s>>>(part, grid, width, out);
+  k_reduce<<<(width + 31) / 32, dim3(32, kReduceWarps), 0, s>>>(part, grid, width, out);
   return 1;
 }
 
