@@ -101,3 +101,38 @@ def test_ylm_orthonormal_and_addition_theorem():
                 s += ya * yb
             want = (2 * l + 1) / (4 * np.pi) * oracle.port().ps_oracle_legpoly(l, float(u @ v))
             assert abs(s - want) < 1e-12
+
+
+@pytest.mark.parametrize("rand_nz", [1.0, 1.5])
+def test_prepare_survey_matches_restatement(rand_nz):
+    """The package's survey preparation (used by the Python API and the
+    survey workload) gives this file's restatement of the reference's:
+    records, box, corner, shot noise and normalisation."""
+    from powspec_gb300 import catalog
+    d = np.loadtxt(os.path.join(SURVEY, "data.txt"))
+    r = np.loadtxt(os.path.join(SURVEY, "rand.txt"))
+    r[:, 4] *= rand_nz
+    s = catalog.prepare_survey([(d, r)])[0]
+    cats, bmin, box, shot, norm = prepare(rand_nz=rand_nz)
+    assert np.array_equal(s.xyzw, cats[0])
+    assert np.array_equal(s.origin, bmin) and s.box == box
+    assert s.shot == shot[0] and s.norm == norm[0]
+    # a given box: centred on the same bounds; too small is refused
+    t = catalog.prepare_survey([(d, r)], box=(450.0, 420.0, 430.0))[0]
+    assert t.box == (450.0, 420.0, 430.0)
+    pos = np.concatenate([d[:, :3], r[:, :3]])
+    assert np.allclose(t.origin, (pos.min(0) + pos.max(0) - np.array(t.box)) / 2, rtol=0, atol=1e-12)
+    with pytest.raises(ValueError):
+        catalog.prepare_survey([(d, r)], box=100.0)
+
+
+def test_synthetic_survey_is_seeded():
+    from powspec_gb300 import catalog
+    a = catalog.survey(20000, seed=4)
+    b = catalog.survey(20000, seed=4)
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    d, r = a
+    assert len(r) == 3 * len(d) and d.shape[1] == r.shape[1] == 5
+    cen = np.array([600.0, 300.0, 450.0])
+    for p in (d, r):
+        assert np.all(np.linalg.norm(p[:, :3] - cen, axis=1) < 200.0)
