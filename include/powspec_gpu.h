@@ -126,7 +126,10 @@ int ps_gpu_assign_soa(ps_gpu_ctx *ctx, int cat, const float *x,
  * spherical-harmonic decomposition of L_l (src/mp_template.c:48-149):
  * P_l = 4 pi sum Re[F_0 F_l*] / (norm cnt); with interlacing the harmonics
  * weight the c2r of the combined field (src/multipole.c:489-500).
- * The result reports shot / norm as its shot noise (src/save_res.c:89). */
+ * The result reports shot / norm as its shot noise (src/save_res.c:89).
+ * Survey catalogues take no |mu| sub-bins (PS_GPU_ERR_ARG here and from
+ * ps_gpu_set_mu_bins), and ps_gpu_execute refuses (PS_GPU_ERR_STATE) a
+ * two-catalogue context with one survey catalogue. */
 int ps_gpu_set_survey(ps_gpu_ctx *ctx, int cat, double shot, double norm, const double *origin);
 
 /* Staged input (no counterpart in the reference): ps_gpu_stage_aos starts

@@ -1156,6 +1156,8 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   const ps_gpu_params& p = c->p;
   for (int k = 0; k < p.ncat; k++)
     if (!c->assigned[k]) return fail(c, PS_GPU_ERR_STATE, "catalogue %d not assigned", k);
+  if (p.ncat == 2 && c->survey[0] != c->survey[1])
+    return fail(c, PS_GPU_ERR_STATE, "both catalogues must be survey catalogues, or neither");
   CU(cudaSetDevice(p.device));
   cudaStream_t s = c->stream;
   const int nacc = c->nspec * p.npole;
@@ -1187,7 +1189,7 @@ int ps_gpu_set_survey(ps_gpu_ctx* c, int cat, double shot, double norm, const do
   bool high = false;
   for (int l = 0; l < c->p.npole; l++) high |= c->p.poles[l] > 0;
   if (high && !origin) return fail(c, PS_GPU_ERR_ARG, "survey multipoles l > 0 need the box corner");
-  if (high && c->nmu != 1) return fail(c, PS_GPU_ERR_ARG, "survey multipoles take no |mu| sub-bins");
+  if (c->nmu != 1) return fail(c, PS_GPU_ERR_ARG, "survey catalogues take no |mu| sub-bins");
   if (!(norm > 0) || !(shot >= 0)) return fail(c, PS_GPU_ERR_ARG, "survey normalisation must be > 0");
   c->survey[cat] = true;
   c->survey_shot[cat] = shot;
@@ -1278,6 +1280,8 @@ int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* p
 
 int ps_gpu_set_mu_bins(ps_gpu_ctx* c, int nmu) {
   if (!c || nmu < 1 || nmu > 64) return fail(c, PS_GPU_ERR_ARG, "number of mu bins must be 1..64");
+  if (nmu != 1 && (c->survey[0] || c->survey[1]))
+    return fail(c, PS_GPU_ERR_ARG, "survey catalogues take no |mu| sub-bins");
   CU(cudaSetDevice(c->p.device));
   CU(cudaStreamSynchronize(c->stream));
   const int old_nmu = c->nmu;

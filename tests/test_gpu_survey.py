@@ -104,3 +104,30 @@ def test_survey_unbalanced_weights_k0_mode(gpu_lib):
     for err in _cross(gpu_lib, _pair(unbalanced=True), True):
         assert err[:, 1:].max() <= TOL, err[:, 1:].max(axis=1)
         assert err[:, 0].max() <= 2e-4, err[:, 0]
+
+
+def test_survey_misuse_is_refused(gpu_lib):
+    """|mu| sub-bins with a survey catalogue, in either order, and a
+    two-catalogue context with one survey catalogue are refused; the
+    context stays usable."""
+    d, r = catalog.survey(20000, seed=5)
+    s = catalog.prepare_survey([(d, r)])[0]
+    with gpu_lib.Estimator(ng=32, box=s.box, assign=2, poles=(0, 2), dk=0.02) as e:
+        e.set_survey(0, s.shot, s.norm, s.origin)
+        with pytest.raises(gpu_lib.PowspecError):
+            e.set_mu_bins(4)
+    with gpu_lib.Estimator(ng=32, box=s.box, assign=2, poles=(0,), dk=0.02) as e:
+        e.set_mu_bins(4)
+        with pytest.raises(gpu_lib.PowspecError):
+            e.set_survey(0, s.shot, s.norm, s.origin)
+    with gpu_lib.Estimator(ng=32, box=s.box, assign=2, ncat=2, poles=(0,), dk=0.02) as e:
+        e.set_survey(0, s.shot, s.norm, s.origin)
+        e.assign(0, s.xyzw)
+        e.assign(1, s.xyzw)
+        with pytest.raises(gpu_lib.PowspecError):
+            e.execute()
+        e.set_survey(1, s.shot, s.norm, s.origin)
+        e.assign(0, s.xyzw)
+        e.assign(1, s.xyzw)
+        spec = e.execute()
+        assert np.isfinite(spec.pl[:2, 0]).all() and np.isfinite(spec.xpl[0]).all()
