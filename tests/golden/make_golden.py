@@ -24,7 +24,9 @@ these are the pins of the oracle and of the GPU path:
   cross spectrum of the catalogue with itself (ref_cross_yama.txt); the
   multipoles 0 to 6 on the interlaced mesh (ref_auto_yama_il.txt); and
   multipoles 0, 2, 4 with randoms at 1.5 x the data's n(z), whose k = 0
-  mode is far from 0 (ref_auto_yama_nz.txt).
+  mode is far from 0 (ref_auto_yama_nz.txt); the cross spectrum of the
+  catalogue with a 60% subsample of it and half the randoms
+  (ref_cross2_il.txt); and log-scale bins (ref_auto_log.txt).
 
 Usage (in a tree that has the reference sources):
     python tests/golden/make_golden.py          # everything
@@ -223,8 +225,34 @@ def survey():
         "MULTIPOLE       = [0, 1, 2, 3, 4, 5, 6]", "MULTIPOLE       = [0, 2, 4]")
     with open(os.path.join(d, "powspec_yama_nz.conf"), "w") as f:
         f.write(nz.format(out="ref_auto_yama_nz.txt"))
+    # two different catalogues: a 60% subsample of the data with every
+    # second random, crossed with the full ones (interlaced, l = 0, 2, 4)
+    fmt = "%.6f %.6f %.6f %.4f %.8e"
+    dd = np.loadtxt(os.path.join(d, "data.txt"))
+    rr = np.loadtxt(os.path.join(d, "rand.txt"))
+    np.savetxt(os.path.join(d, "data2.txt"), dd[np.random.default_rng(91).random(len(dd)) < 0.6],
+               fmt=fmt)
+    np.savetxt(os.path.join(d, "rand2.txt"), rr[::2], fmt=fmt)
+    il024 = il.replace("MULTIPOLE       = [0, 1, 2, 3, 4, 5, 6]", "MULTIPOLE       = [0, 2, 4]")
+    lines = []
+    for line in il024.format(out="").splitlines():
+        key = line.split("=")[0].strip()
+        if key in twice:
+            line = "%-16s= %s" % (key, twice[key])
+            line = line.replace("[data.txt, data.txt]", "[data.txt, data2.txt]").replace(
+                "[rand.txt, rand.txt]", "[rand.txt, rand2.txt]")
+        elif key == "OUTPUT_AUTO":
+            line = "OUTPUT_CROSS    = ref_cross2_il.txt"
+        lines.append(line)
+    with open(os.path.join(d, "powspec_cross2.conf"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    # log-scale bins (KMIN 0.01, 0.1 dex), interlaced, l = 0, 2, 4
+    lg = il024.replace("BIN_SIZE        = 0.02",
+                       "BIN_SIZE        = 0.1\nLOG_SCALE       = T\nKMIN            = 0.01")
+    with open(os.path.join(d, "powspec_log.conf"), "w") as f:
+        f.write(lg.format(out="ref_auto_log.txt"))
     for conf in ("powspec_yama.conf", "powspec_cross.conf", "powspec_yama_il.conf",
-                 "powspec_yama_nz.conf"):
+                 "powspec_yama_nz.conf", "powspec_cross2.conf", "powspec_log.conf"):
         subprocess.run([oracle.REF_CLI, "-c", conf], cwd=d, check=True, env=env,
                        stdout=subprocess.DEVNULL)
     survey_converted(d, data, rand, rng, env)

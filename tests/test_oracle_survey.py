@@ -20,22 +20,33 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SURVEY = os.path.join(HERE, "golden", "survey")
 
 
-def prepare(ncat=1, pad=0.02, rand_nz=1.0):
-    """rand_nz: the randoms' n(z) as this multiple of the file's column."""
-    d = np.loadtxt(os.path.join(SURVEY, "data.txt"))
-    r = np.loadtxt(os.path.join(SURVEY, "rand.txt"))
-    r[:, 4] *= rand_nz
-    fkp = lambda a: 1.0 / (1.0 + a[:, 4] * 2000)
-    wd, wr = d[:, 3] * fkp(d), r[:, 3] * fkp(r)
-    alpha = d[:, 3].sum() / r[:, 3].sum()
-    shot = (wd * wd).sum() + alpha * alpha * (wr * wr).sum()
-    norm = alpha * (r[:, 3] * fkp(r) ** 2 * r[:, 4]).sum()
-    pos = np.concatenate([d[:, :3], r[:, :3]])
+def _prepare(pairs, pad=0.02):
+    """(data, randoms) row pairs -> catalogues in one box fitted to all."""
+    pos = np.concatenate([a[:, :3] for pr in pairs for a in pr])
     mn, mx = pos.min(axis=0), pos.max(axis=0)
     box = np.array([math.ceil((mx[a] - mn[a]) * (1 + pad) / 10) * 10 for a in range(3)])
     bmin = (mx + mn - box) * 0.5
-    cat = np.column_stack([pos - bmin, np.concatenate([wd, -alpha * wr])])
-    return [cat] * ncat, bmin, tuple(box), [shot] * ncat, [norm] * ncat
+    cats, shots, norms = [], [], []
+    fkp = lambda a: 1.0 / (1.0 + a[:, 4] * 2000)
+    for d, r in pairs:
+        wd, wr = d[:, 3] * fkp(d), r[:, 3] * fkp(r)
+        alpha = d[:, 3].sum() / r[:, 3].sum()
+        shots.append((wd * wd).sum() + alpha * alpha * (wr * wr).sum())
+        norms.append(alpha * (r[:, 3] * fkp(r) ** 2 * r[:, 4]).sum())
+        p = np.concatenate([d[:, :3], r[:, :3]])
+        cats.append(np.column_stack([p - bmin, np.concatenate([wd, -alpha * wr])]))
+    return cats, bmin, tuple(box), shots, norms
+
+
+def _load(name):
+    return np.loadtxt(os.path.join(SURVEY, name))
+
+
+def prepare(ncat=1, pad=0.02, rand_nz=1.0):
+    """rand_nz: the randoms' n(z) as this multiple of the file's column."""
+    d, r = _load("data.txt"), _load("rand.txt")
+    r[:, 4] *= rand_nz
+    return _prepare([(d, r)] * ncat, pad)
 
 
 def read_ref(name):
@@ -65,6 +76,40 @@ def test_oracle_survey_matches_reference_output(ref, interlace, poles, cross, ra
     got = res.xpl if cross else res.pl[0]
     scale = np.abs(want[:, 5]) + (0.0 if cross else shot[0] / norm[0])
     err = np.abs(got.T - want[:, 5:]) / scale[:, None]
+    assert err.max() <= 1e-8, err.max()
+
+
+def test_oracle_survey_cross_of_two_catalogues():
+    """The catalogue crossed with a 60% subsample of it and half the
+    randoms, interlaced, l = 0, 2, 4 (ref_cross2_il.txt)."""
+    cats, bmin, box, shot, norm = _prepare([(_load("data.txt"), _load("rand.txt")),
+                                            (_load("data2.txt"), _load("rand2.txt"))])
+    spec = oracle.Spec(ng=32, box=box, assign=3, interlace=True, poles=(0, 2, 4), dk=0.02,
+                       isauto=(False, False), iscross=True)
+    res = oracle.survey(spec, cats, bmin, shot, norm)
+    want = read_ref("ref_cross2_il.txt")
+    assert res.nbin == len(want)
+    assert np.array_equal(res.cnt, want[:, 4].astype(np.uint64))
+    err = np.abs(res.xpl.T - want[:, 5:]) / np.abs(want[:, 5:6])
+    assert err.max() <= 1e-8, err.max()
+
+
+def test_oracle_survey_log_bins():
+    """Log-scale bins (KMIN 0.01, 0.1 dex), interlaced, l = 0, 2, 4: counts,
+    the k columns with the reference's rescaling, and P_l
+    (ref_auto_log.txt)."""
+    cats, bmin, box, shot, norm = prepare()
+    spec = oracle.Spec(ng=32, box=box, assign=3, interlace=True, poles=(0, 2, 4),
+                       kmin=math.log10(0.01), dk=0.1, logscale=True, isauto=(True, False),
+                       iscross=False)
+    res = oracle.survey(spec, cats, bmin, shot, norm)
+    want = read_ref("ref_auto_log.txt")
+    assert res.nbin == len(want)
+    assert np.array_equal(res.cnt, want[:, 4].astype(np.uint64))
+    assert np.allclose(res.k, want[:, 0], rtol=1e-9, atol=0)
+    assert np.allclose(res.km, want[:, 3], rtol=1e-9, atol=0)
+    scale = np.abs(want[:, 5]) + shot[0] / norm[0]
+    err = np.abs(res.pl[0].T - want[:, 5:]) / scale[:, None]
     assert err.max() <= 1e-8, err.max()
 
 
