@@ -730,7 +730,8 @@ def survey_config(name, s, nd, nr):
     wl = WORKLOADS[name]
     return {"workload": name, "ng": wl["ng"], "assign": "PCS", "interlace": wl["interlace"],
             "poles": list(wl["poles"]), "box": list(s.box), "n_data": nd, "n_rand": nr, "dk": DK,
-            "l2": "inputs larger than L2 (128 MB of records, 64 MB meshes)"}
+            "l2": "no flush: each evaluation's working set (128 MB of records, two 64 MB "
+                  "meshes, seven 68 MB fields) is about 1 GB, far above the 129 MB L2"}
 
 
 def survey_oracle_spec(name, s):
