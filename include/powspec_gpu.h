@@ -202,11 +202,15 @@ int ps_gpu_bin_fields_host(ps_gpu_ctx *ctx, const float *f1, const float *f2,
  * [ng][ng][ng/2+1] (re, im); pl: device output [npole][nbin] doubles, written
  * asynchronously on `stream` (a cudaStream_t; NULL = legacy default stream).
  * The per-CTA partial sums live in one static device array per GPU (4,096,000
- * bytes): npole * nbin must be <= 3200, else PS_GPU_ERR_RANGE.  The first call
- * on a device looks that array up (cudaGetSymbolAddress); make it before any
- * stream capture.  All calls on one device share the array: calls whose
- * stream work can overlap race and corrupt each other's sums, so order them
- * on one stream. */
+ * bytes): npole * nbin must be <= 3200, else PS_GPU_ERR_RANGE.  ps_gpu_create
+ * makes the array resident on the context's device (the module load that
+ * places it), so the per-step call does not; should that fail there, the
+ * first call of this entry point does it, and that call should come before
+ * any stream capture.  Every call looks the array's address up anew
+ * (cudaGetSymbolAddress) and gives the caller's current device back on
+ * return.  All calls on one device share the array: calls whose stream work
+ * can overlap race and corrupt each other's sums, so order them on one
+ * stream. */
 int ps_gpu_bin_fields_noalloc(ps_gpu_ctx *ctx, const float *f1, const float *f2,
                               double *pl, void *stream);
 
@@ -244,6 +248,15 @@ int ps_gpu_autotune(ps_gpu_ctx *ctx, const double *xyzw, size_t n, int reps, int
  * returns the region gather to its default: on when there is a particle
  * for every 32 cells or more. */
 int ps_gpu_set_tuning(ps_gpu_ctx *ctx, const int *choice);
+
+/* ---- Test hook (no counterpart in the reference) */
+
+/* Fake of an out-of-memory allocation: n > 0 makes the n-th next device or
+ * pinned-host allocation made by this library's context and batch entry
+ * points fail as cudaErrorMemoryAllocation without calling CUDA; n <= 0
+ * disarms it.  The entry point that hits it returns PS_GPU_ERR_MEMORY, where
+ * the reference exits with POWSPEC_ERR_MEMORY (src/multipole.c:121-126). */
+void ps_gpu_debug_fail_alloc(int n);
 
 #ifdef __cplusplus
 }

@@ -29,7 +29,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "libps_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpowspec_ref.so")
 REF_CLI = os.path.join(HERE, "_ref", "POWSPEC")
-REF_SRC = os.environ.get("POWSPEC_REF_DIR", "/root/reference")
+# Where the reference tree is read from: POWSPEC_REF_DIR, else the default
+# of the build recipe (oracle/Makefile, REF).
+REF_SRC = os.environ.get("POWSPEC_REF_DIR", "")
 
 _c_double_p = ctypes.POINTER(ctypes.c_double)
 _c_size_p = ctypes.POINTER(ctypes.c_size_t)
@@ -121,11 +123,22 @@ def build_port(force=False):
     return PORT_SO
 
 
+def ref_dir():
+    """The reference tree the recipe compiles: POWSPEC_REF_DIR or the
+    recipe's own default."""
+    if REF_SRC:
+        return REF_SRC
+    r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"],
+                       capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
 def build_ref():
     """Compile the reference from source (only where its tree exists)."""
-    if not os.path.isdir(os.path.join(REF_SRC, "src")):
+    ref = ref_dir()
+    if not ref or not os.path.isdir(os.path.join(ref, "src")):
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True)
     return REF_SO
 
 

@@ -38,6 +38,7 @@ EXPORTED = [
     "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
     "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune", "ps_gpu_set_tuning",
     "ps_gpu_execute_learned", "ps_gpu_stage_aos", "ps_gpu_assign_staged", "ps_gpu_set_survey",
+    "ps_gpu_debug_fail_alloc",
 ]
 
 

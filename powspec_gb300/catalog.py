@@ -54,14 +54,16 @@ def gaussian_field(ngen, box, seed, slope=-1.5, kcut=0.5):
 
 
 def lognormal(nbar_total, box=1000.0, seed=1, ngen=128, zeldovich=4.0, weights=None,
-              dtype=np.float64, soa=False):
+              dtype=np.float64, soa=False, sample_seed=None):
     """Poisson sample of ~nbar_total points from a lognormal field.
 
     zeldovich: rms displacement (Mpc/h) along z added to every particle.
+    sample_seed: seed of the Poisson sampling (default seed + 7919); two
+    samples of one field (the same `seed`) differ only in it.
     """
     g, gk, kz, k2 = gaussian_field(ngen, box, seed)
     dens = np.exp(g - 0.5)  # sigma_G^2 = 1
-    rng = np.random.default_rng(seed + 7919)
+    rng = np.random.default_rng(seed + 7919 if sample_seed is None else sample_seed)
     cell = box / ngen
     lam = dens.ravel() * (nbar_total / dens.size) / dens.mean()
     counts = rng.poisson(lam)

@@ -306,7 +306,9 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_cons
     srange[1] = -1;
   }
   __syncthreads();
+  int nissued = 0;  // copies issued (thread 0)
   auto issue = [&](int tile, int s) {
+    nissued++;
     const int kz = tile / nty, ky0 = (tile - kz * nty) * a.ty;
     const int nl = min(a.ty, ng - ky0);
     mbar_expect_tx(&bar[s], (uint32_t)(a.nfield * nl * ng * 8));
@@ -340,10 +342,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_cons
   }
   if (ntiles_acc && !s_abort) merge_tile(tacc, srange, part, nacc, nkey);
   // never exit with a bulk copy in flight into this CTA's memory
-  if (threadIdx.x == 0 && s_abort) {
-    mbar_wait(&bar[0], 0);
-    mbar_wait(&bar[1], 0);
-  }
+  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued);
 }
 
 // Stand-alone binning of FFTW-layout fields [x][y][kz]: one line per (x, y).

@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "powspec_gpu.h"
@@ -200,16 +201,49 @@ int fail(ps_gpu_ctx* c, int code, const char* fmt, ...) {
   return code;
 }
 
+// A failed allocation is PS_GPU_ERR_MEMORY (the reference's
+// POWSPEC_ERR_MEMORY, which it raises with exit() inside its OpenMP region,
+// src/multipole.c:121-126); any other CUDA failure is PS_GPU_ERR_CUDA.
 #define CU(call)                                                                      \
   do {                                                                                \
     cudaError_t e_ = (call);                                                          \
-    if (e_ != cudaSuccess)                                                            \
-      return fail(c, PS_GPU_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    if (e_ != cudaSuccess) {                                                          \
+      (void)cudaGetLastError();                                                       \
+      return fail(c, e_ == cudaErrorMemoryAllocation ? PS_GPU_ERR_MEMORY : PS_GPU_ERR_CUDA, \
+                  "%s failed: %s", #call, cudaGetErrorString(e_));                    \
+    }                                                                                 \
   } while (0)
+
+// Test hook of ps_gpu_debug_fail_alloc: n > 0 makes the n-th next device or
+// pinned allocation of this file fail as out of memory (a fake of the
+// failing call; the device is never touched by it).
+std::atomic<int> g_fail_alloc{0};
+bool fake_alloc_failure() {
+  int n = g_fail_alloc.load();
+  while (n > 0 && !g_fail_alloc.compare_exchange_weak(n, n - 1)) {
+  }
+  return n == 1;
+}
+template <typename T>
+cudaError_t dev_malloc(T** p, size_t bytes) {
+  if (fake_alloc_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc((void**)p, bytes);
+}
+template <typename T>
+cudaError_t host_malloc(T** p, size_t bytes) {
+  if (fake_alloc_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocHost((void**)p, bytes);
+}
 
 template <typename T>
 int upload(ps_gpu_ctx* c, T** dst, const std::vector<T>& v) {
-  CU(cudaMalloc((void**)dst, sizeof(T) * (v.empty() ? 1 : v.size())));
+  CU(dev_malloc(dst, sizeof(T) * (v.empty() ? 1 : v.size())));
   if (!v.empty()) CU(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
   return 0;
 }
@@ -271,9 +305,9 @@ int alloc_accum(ps_gpu_ctx* c) {
   c->d_part = nullptr;
   c->d_sums = nullptr;
   c->h_out = nullptr;
-  CU(cudaMalloc(&c->d_part, sizeof(double) * (size_t)std::max(c->grid_c, c->grid_ct) * width));
-  CU(cudaMalloc(&c->d_sums, sizeof(double) * width));
-  CU(cudaMallocHost(&c->h_out, sizeof(double) * (width + 8 + 2 * kMaxPole)));
+  CU(dev_malloc(&c->d_part, sizeof(double) * (size_t)std::max(c->grid_c, c->grid_ct) * width));
+  CU(dev_malloc(&c->d_sums, sizeof(double) * width));
+  CU(host_malloc(&c->h_out, sizeof(double) * (width + 8 + 2 * kMaxPole)));
   return 0;
 }
 
@@ -352,10 +386,14 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   if (cudaGetDeviceCount(&dcount) != cudaSuccess || dcount < 1)
     return fail(c, PS_GPU_ERR_CUDA, "no CUDA device available");
   if (p.device < 0 || p.device >= dcount) return fail(c, PS_GPU_ERR_ARG, "invalid device %d", p.device);
-  CU(cudaSetDevice(p.device));
+  DeviceScope dev_scope_(p.device);
+  CU(dev_scope_.err);
   CU(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, p.device));
   CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   for (auto& e : c->ev) CU(cudaEventCreate(&e));
+  // place ps_gpu_bin_fields_noalloc's static scratch now, not on its first
+  // call; a failure here is cleared and reported by that entry point
+  if (noalloc_prepare(p.device) != cudaSuccess) (void)cudaGetLastError();
 
   // ---- geometry tables (FP64 on the host)
   const int ng = p.ng, h = c->ngk;
@@ -466,15 +504,15 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   // per field: the FP32 mesh, later reused for the y-pass output (8 B * Ncmplx
   // >= 4 B * Ng^3), and the z-pass output
   for (int f = 0; f < c->nfield; f++) {
-    CU(cudaMalloc(&c->grid[f], c->ncx * sizeof(float2)));
-    CU(cudaMalloc(&c->cbuf[f], c->ncx * sizeof(float2)));
+    CU(dev_malloc(&c->grid[f], c->ncx * sizeof(float2)));
+    CU(dev_malloc(&c->cbuf[f], c->ncx * sizeof(float2)));
   }
-  CU(cudaMalloc(&c->d_hist, (c->nkeys + 1) * sizeof(unsigned)));
-  CU(cudaMalloc(&c->d_bsum, ((c->nkeys + 4095) / 4096 + 1) * sizeof(unsigned)));
+  CU(dev_malloc(&c->d_hist, (c->nkeys + 1) * sizeof(unsigned)));
+  CU(dev_malloc(&c->d_bsum, ((c->nkeys + 4095) / 4096 + 1) * sizeof(unsigned)));
   if ((rc = alloc_accum(c))) return rc;
-  CU(cudaMalloc(&c->d_wsum, sizeof(double) * 4));
-  CU(cudaMalloc(&c->d_wpart, sizeof(double) * 2 * kAssignMaxBlocks));
-  CU(cudaMalloc(&c->d_err, sizeof(int) * 4));
+  CU(dev_malloc(&c->d_wsum, sizeof(double) * 4));
+  CU(dev_malloc(&c->d_wpart, sizeof(double) * 2 * kAssignMaxBlocks));
+  CU(dev_malloc(&c->d_err, sizeof(int) * 4));
   CU(cudaMemset(c->d_wsum, 0, sizeof(double) * 4));
   CU(cudaMemset(c->d_err, 0, sizeof(int) * 4));
 
@@ -482,9 +520,9 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   {
     unsigned long long* d_cnt = nullptr;
     double *d_ks = nullptr, *d_lc = nullptr;
-    CU(cudaMalloc(&d_cnt, sizeof(unsigned long long) * c->nbin));
-    CU(cudaMalloc(&d_ks, sizeof(double) * c->nbin));
-    CU(cudaMalloc(&d_lc, sizeof(double) * (size_t)p.npole * c->nbin));
+    CU(dev_malloc(&d_cnt, sizeof(unsigned long long) * c->nbin));
+    CU(dev_malloc(&d_ks, sizeof(double) * c->nbin));
+    CU(dev_malloc(&d_lc, sizeof(double) * (size_t)p.npole * c->nbin));
     CU(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * c->nbin, c->stream));
     CU(cudaMemsetAsync(d_ks, 0, sizeof(double) * c->nbin, c->stream));
     CU(cudaMemsetAsync(d_lc, 0, sizeof(double) * (size_t)p.npole * c->nbin, c->stream));
@@ -571,7 +609,7 @@ int ensure_stage(ps_gpu_ctx* c, size_t bytes) {
     c->d_stage = nullptr;
     c->stage_bytes = 0;
   }
-  CU(cudaMalloc(&c->d_stage, bytes));
+  CU(dev_malloc(&c->d_stage, bytes));
   c->stage_bytes = bytes;
   return 0;
 }
@@ -601,7 +639,7 @@ int ensure_region(ps_gpu_ctx* c) {
   if (c->d_region) cudaFree(c->d_region);
   c->d_region = nullptr;
   c->region_bytes = 0;
-  CU(cudaMalloc(&c->d_region, need));
+  CU(dev_malloc(&c->d_region, need));
   c->region_bytes = need;
   return 0;
 }
@@ -650,8 +688,8 @@ int ensure_gather_capacity(ps_gpu_ctx* c, size_t n) {
   c->d_rank = nullptr;
   c->d_rec = nullptr;
   c->gcap = 0;
-  CU(cudaMalloc(&c->d_rank, n * sizeof(unsigned)));
-  CU(cudaMalloc(&c->d_rec, n * gather_record_bytes()));
+  CU(dev_malloc(&c->d_rank, n * sizeof(unsigned)));
+  CU(dev_malloc(&c->d_rec, n * gather_record_bytes()));
   c->gcap = n;
   return 0;
 }
@@ -660,7 +698,8 @@ int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
   // ranks and bucket offsets are 32-bit
   if (pt.n >= 0xffffffffull)
     return fail(c, PS_GPU_ERR_RANGE, "%zu particles: at most 2^32 - 2 per catalogue", pt.n);
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   if (!c->assign_started) {
     CU(cudaEventRecord(c->ev[6], c->stream));
     c->assign_started = true;
@@ -914,7 +953,8 @@ int ps_gpu_assign_aos(ps_gpu_ctx* c, int cat, const double* xyzw, size_t n, int 
 
 int ps_gpu_stage_aos(ps_gpu_ctx* c, int slot, const double* xyzw, size_t n) {
   if (!c || slot < 0 || slot > 1 || (!xyzw && n)) return fail(c, PS_GPU_ERR_ARG, "invalid stage arguments");
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   if (!c->copy_stream) {
     CU(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     for (int k = 0; k < 2; k++) {
@@ -931,7 +971,7 @@ int ps_gpu_stage_aos(ps_gpu_ctx* c, int slot, const double* xyzw, size_t n) {
     if (c->d_slot[slot]) cudaFree(c->d_slot[slot]);
     c->d_slot[slot] = nullptr;
     c->slot_bytes[slot] = 0;
-    CU(cudaMalloc(&c->d_slot[slot], bytes));
+    CU(dev_malloc(&c->d_slot[slot], bytes));
     c->slot_bytes[slot] = bytes;
   }
   // the copy waits for the kernels that read this slot's previous catalogue
@@ -947,7 +987,8 @@ int ps_gpu_assign_staged(ps_gpu_ctx* c, int cat, int slot) {
   if (!c || cat < 0 || cat >= c->p.ncat || slot < 0 || slot > 1)
     return fail(c, PS_GPU_ERR_ARG, "invalid assign arguments");
   if (!c->slot_full[slot]) return fail(c, PS_GPU_ERR_STATE, "staging slot %d holds no catalogue", slot);
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   CU(cudaStreamWaitEvent(c->stream, c->copied[slot], 0));
   Particles pt{};
   pt.n = c->slot_n[slot];
@@ -1085,10 +1126,10 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
     if (c->d_yama) cudaFree(c->d_yama);
     c->d_yama = nullptr;
     c->yama_bytes = 0;
-    CU(cudaMalloc(&c->d_yama, need));
+    CU(dev_malloc(&c->d_yama, need));
     c->yama_bytes = need;
   }
-  if (!c->d_dc) CU(cudaMalloc(&c->d_dc, 2 * kMaxPole * sizeof(float2)));
+  if (!c->d_dc) CU(dev_malloc(&c->d_dc, 2 * kMaxPole * sizeof(float2)));
   float2* base = (float2*)c->d_yama;
   float2 *a1 = base, *a2 = base + c->ncx, *fa = base + 2 * c->ncx;
   // fields: a1, a2, fa, then F_0 and F_l of catalogue 0 (and 1)
@@ -1158,7 +1199,8 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
     if (!c->assigned[k]) return fail(c, PS_GPU_ERR_STATE, "catalogue %d not assigned", k);
   if (p.ncat == 2 && c->survey[0] != c->survey[1])
     return fail(c, PS_GPU_ERR_STATE, "both catalogues must be survey catalogues, or neither");
-  CU(cudaSetDevice(p.device));
+  DeviceScope dev_scope_(p.device);
+  CU(dev_scope_.err);
   cudaStream_t s = c->stream;
   const int nacc = c->nspec * p.npole;
   const int nkey = c->nbin * c->nmu;
@@ -1209,7 +1251,8 @@ int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* p
                 "linear bins");
   c->yama_last = false;
   if (!c->assigned[0]) return fail(c, PS_GPU_ERR_STATE, "catalogue 0 not assigned");
-  CU(cudaSetDevice(p.device));
+  DeviceScope dev_scope_(p.device);
+  CU(dev_scope_.err);
   cudaStream_t s = c->stream;
   const int nbin = c->nbin, nmu = c->nmu, nkey = nbin * nmu, nacc = p.npole;
   if (c->lcells != nkey) {  // per-context buffers and constants
@@ -1229,13 +1272,13 @@ int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* p
       geo[nbin + b] = (double)c->cnt[b];
     }
     memcpy(geo.data() + 2 * nbin, c->lcnt.data(), sizeof(double) * (size_t)nacc * nbin);
-    CU(cudaMalloc(&c->d_lgeo, sizeof(double) * geo.size()));
+    CU(dev_malloc(&c->d_lgeo, sizeof(double) * geo.size()));
     CU(cudaMemcpy(c->d_lgeo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice));
-    CU(cudaMalloc(&c->d_lx, sizeof(float) * (size_t)nkey * fw));
-    CU(cudaMalloc(&c->d_lxb, 2 * (size_t)nkey * fw));
-    CU(cudaMalloc(&c->d_lc, sizeof(float) * (size_t)nkey));
-    CU(cudaMalloc(&c->d_lout, sizeof(double) * (size_t)nacc * nbin));
-    CU(cudaMallocHost(&c->h_lout, sizeof(double) * (size_t)nacc * nbin));
+    CU(dev_malloc(&c->d_lx, sizeof(float) * (size_t)nkey * fw));
+    CU(dev_malloc(&c->d_lxb, 2 * (size_t)nkey * fw));
+    CU(dev_malloc(&c->d_lc, sizeof(float) * (size_t)nkey));
+    CU(dev_malloc(&c->d_lout, sizeof(double) * (size_t)nacc * nbin));
+    CU(host_malloc(&c->h_lout, sizeof(double) * (size_t)nacc * nbin));
     c->lcells = nkey;
   }
   int rc = enqueue_passes(c, c->d_sums, true);
@@ -1282,7 +1325,8 @@ int ps_gpu_set_mu_bins(ps_gpu_ctx* c, int nmu) {
   if (!c || nmu < 1 || nmu > 64) return fail(c, PS_GPU_ERR_ARG, "number of mu bins must be 1..64");
   if (nmu != 1 && (c->survey[0] || c->survey[1]))
     return fail(c, PS_GPU_ERR_ARG, "survey catalogues take no |mu| sub-bins");
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   CU(cudaStreamSynchronize(c->stream));
   const int old_nmu = c->nmu;
   c->nmu = nmu;
@@ -1309,9 +1353,10 @@ int ps_gpu_read_mesh(ps_gpu_ctx* c, int cat, int m, double* out) {
     return fail(c, PS_GPU_ERR_ARG, "invalid read_mesh arguments");
   if (c->last_cat != cat || !c->assigned[cat])
     return fail(c, PS_GPU_ERR_STATE, "read_mesh: catalogue %d is not the last one assigned", cat);
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   long long* tmp = nullptr;
-  CU(cudaMalloc(&tmp, c->ntot * sizeof(long long) * c->mpc));
+  CU(dev_malloc(&tmp, c->ntot * sizeof(long long) * c->mpc));
   GatherArgs g = gather_args(c, cat, c->last_pt.n);
   for (int k = 0; k < c->mpc; k++) g.out64[k] = tmp + (size_t)k * c->ntot;
   launch_gather_assign(c->last_pt, g, c->stream, true);
@@ -1330,7 +1375,8 @@ int ps_gpu_read_mesh(ps_gpu_ctx* c, int cat, int m, double* out) {
 
 int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   if (!c || !in || !out) return fail(c, PS_GPU_ERR_ARG, "null argument");
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   cudaStream_t s = c->stream;
   const int ng = c->ng;
   float* d_in = (float*)c->grid[0];  // ntot floats fit in the mesh buffer
@@ -1383,7 +1429,8 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
 
 int ps_gpu_bin_fields_host(ps_gpu_ctx* c, const float* f1, const float* f2, double* pl) {
   if (!c || !f1 || !f2 || !pl) return fail(c, PS_GPU_ERR_ARG, "null argument");
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   cudaStream_t s = c->stream;
   const int npole = c->p.npole, nbin = c->nbin;
   float2* d1 = c->cbuf[0];
@@ -1478,7 +1525,8 @@ int ps_gpu_batch_create(ps_gpu_ctx* c, int ncat, const double* const* xyzw, cons
     if (n[i] >= 0xffffffffull) return fail(c, PS_GPU_ERR_RANGE, "batch catalogue %d: too many particles", i);
     nmax = std::max(nmax, n[i]);
   }
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   int rc = ensure_gather_capacity(c, nmax);
   for (int i = 0; i < ncat && !rc; i++)
     if (n[i] && use_region(c, n[i])) rc = ensure_region(c);
@@ -1489,12 +1537,14 @@ int ps_gpu_batch_create(ps_gpu_ctx* c, int ncat, const double* const* xyzw, cons
   b->n.assign(n, n + ncat);
   const int nacc = c->nspec * c->p.npole, nkey = c->nbin * c->nmu;
   b->stride = (size_t)nacc * nkey + 6;
-  cudaError_t e = cudaMalloc(&b->d_res, sizeof(double) * b->stride * ncat);
-  if (e == cudaSuccess) e = cudaMallocHost(&b->h_res, sizeof(double) * b->stride * ncat);
+  cudaError_t e = dev_malloc(&b->d_res, sizeof(double) * b->stride * ncat);
+  if (e == cudaSuccess) e = host_malloc(&b->h_res, sizeof(double) * b->stride * ncat);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
     batch_free(b);
-    return fail(c, PS_GPU_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e));
+    (void)cudaGetLastError();
+    return fail(c, e == cudaErrorMemoryAllocation ? PS_GPU_ERR_MEMORY : PS_GPU_ERR_CUDA,
+                "batch set-up: %s", cudaGetErrorString(e));
   }
   // Record every launch; the capture is always ended, also on an error.
   e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
@@ -1526,7 +1576,8 @@ int ps_gpu_batch_create(ps_gpu_ctx* c, int ncat, const double* const* xyzw, cons
 int ps_gpu_batch_launch(ps_gpu_batch* b, int wait) {
   if (!b) return PS_GPU_ERR_ARG;
   ps_gpu_ctx* c = b->c;
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   CU(cudaGraphLaunch(b->exec, c->stream));
   c->launches = b->launches;
   if (wait) CU(cudaStreamSynchronize(c->stream));
@@ -1536,7 +1587,8 @@ int ps_gpu_batch_launch(ps_gpu_batch* b, int wait) {
 int ps_gpu_batch_wait(ps_gpu_batch* b) {
   if (!b) return PS_GPU_ERR_ARG;
   ps_gpu_ctx* c = b->c;
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   CU(cudaStreamSynchronize(c->stream));
   return 0;
 }
@@ -1550,7 +1602,7 @@ int ps_gpu_batch_launches(const ps_gpu_batch* b) { return b ? b->launches : PS_G
 
 void ps_gpu_batch_destroy(ps_gpu_batch* b) {
   if (!b) return;
-  cudaSetDevice(b->c->p.device);
+  DeviceScope dev_scope_(b->c->p.device);
   cudaStreamSynchronize(b->c->stream);
   batch_free(b);
 }
@@ -1561,7 +1613,8 @@ int ps_gpu_set_tuning(ps_gpu_ctx* c, const int* choice) {
   if (!c || !choice) return fail(c, PS_GPU_ERR_ARG, "invalid set_tuning arguments");
   if (choice[0] != -1 && choice[0] != 0 && choice[0] != 256 && choice[0] != 512)
     return fail(c, PS_GPU_ERR_ARG, "gather threads: 0 (by density), 256 or 512");
-  CU(cudaSetDevice(c->p.device));
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
   CU(cudaStreamSynchronize(c->stream));
   if (choice[0] >= 0) c->gather_threads = choice[0];
   if (choice[1] >= 0) c->radix32_a = choice[1] != 0;
@@ -1660,5 +1713,7 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
   }
   return 0;
 }
+
+void ps_gpu_debug_fail_alloc(int n) { g_fail_alloc.store(n > 0 ? n : 0); }
 
 }  // extern "C"

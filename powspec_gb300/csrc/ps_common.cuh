@@ -505,6 +505,17 @@ __device__ __forceinline__ bool pipe_wait(uint64_t* bar, int it, int* err, int* 
   return *s_abort == 0;
 }
 
+// Abort drain of a two-stage pipeline, by the thread that issued every copy:
+// `issued` copies went out, copy j on stage j & 1, where it completes that
+// stage's phase j >> 1.  Only the last two can still be in flight; wait
+// (bounded) for exactly their phases, so that the CTA never exits with a
+// bulk copy landing in its shared memory.  An older phase's parity would
+// not do: a wait on a phase that completed earlier returns at once.
+__device__ __forceinline__ void pipe_drain(uint64_t* bar, int issued) {
+  for (int j = issued >= 2 ? issued - 2 : 0; j < issued; j++)
+    mbar_wait(&bar[j & 1], (uint32_t)((j >> 1) & 1));
+}
+
 // First radix pass of a pipelined transform: reads lines of n = 2^logn
 // from an unpadded staging buffer (line stride sstride), writes the padded
 // FFT buffer (line stride ls).

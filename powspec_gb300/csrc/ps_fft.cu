@@ -163,7 +163,9 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_a_tma
   }
   __syncthreads();
   // real rows of ng floats, staged as M complex values (x[2m], x[2m+1])
+  int nissued = 0;  // copies issued (thread 0)
   auto issue = [&](int tile, int s) {
+    nissued++;
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
     mbar_expect_tx(&bar[s], (uint32_t)(nl * ng * 4));
@@ -228,10 +230,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_a_tma
     __syncthreads();
   }
   // drain: never exit with a bulk copy in flight into this CTA's memory
-  if (threadIdx.x == 0 && s_abort) {
-    mbar_wait(&bar[0], 0);
-    mbar_wait(&bar[1], 0);
-  }
+  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued);
 }
 
 // MAXLOG 5: radix-32 passes, 8192-value tiles, one CTA per SM (long lines);
@@ -258,7 +257,9 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma
     s_abort = 0;
   }
   __syncthreads();
+  int nissued = 0;  // copies issued (thread 0)
   auto issue = [&](int tile, int s) {
+    nissued++;
     const int kz = tile / ntx, x0 = (tile - kz * ntx) * a.tx;
     const int nl = min(a.tx, ng - x0);
     mbar_expect_tx(&bar[s], (uint32_t)(nl * ng * 8));
@@ -285,10 +286,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0 && s_abort) {
-    mbar_wait(&bar[0], 0);
-    mbar_wait(&bar[1], 0);
-  }
+  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued);
 }
 
 }  // namespace

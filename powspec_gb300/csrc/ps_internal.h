@@ -186,6 +186,28 @@ int launch_reduce(const double* part, int grid, int width, double* out, cudaStre
 // Minimum shared memory per CTA the passes need (bytes).
 size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin, bool pow2);
 
+// Makes `dev` the current device for the scope of one entry point and gives
+// the caller's current device back on every return path, so that a call on
+// a context never changes the device the calling thread works on.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceScope(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) err = cudaSetDevice(dev);
+    else prev = -1;  // already current: nothing to give back
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
+// Loads the no-allocation entry point's static scratch array on the current
+// device (ps_noalloc.cu).
+cudaError_t noalloc_prepare(int dev);
+
 // Read-only view of a context for entry points outside ps_capi.cu.
 struct CtxView {
   int ng, device;

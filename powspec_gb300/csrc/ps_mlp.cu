@@ -558,7 +558,8 @@ int ps_mlp_create(int device, ps_mlp** out) {
   if (!m) return PS_GPU_ERR_MEMORY;
   *out = m;
   m->device = device;
-  MCU(cudaSetDevice(device));
+  ps::DeviceScope dev_scope_(device);
+  MCU(dev_scope_.err);
   MCU(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
   MCU(cudaMalloc(&m->d_params, kNParam * sizeof(float)));
   MCU(cudaMalloc(&m->d_m, kNParam * sizeof(float)));

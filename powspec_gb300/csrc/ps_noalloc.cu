@@ -15,8 +15,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <mutex>
-
 #include "powspec_gpu.h"
 #include "ps_internal.h"
 
@@ -27,35 +25,33 @@ constexpr int kNoAllocMaxCtas = 160;     // partial-sum rows (one per CTA)
 constexpr int kNoAllocMaxWidth = 3200;   // npole * nbin
 constexpr size_t kNoAllocScratchBytes =  // 4,096,000 bytes
     (size_t)kNoAllocMaxCtas * kNoAllocMaxWidth * sizeof(double);
-constexpr int kMaxDevices = 64;
 
 // Per-CTA partial sums [grid][npole * nbin] of every call on this device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-std::mutex g_setup_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
-int g_nsm[kMaxDevices] = {};
-
-// Once per device, with that device current: the scratch array's device
-// address and the SM count.
-cudaError_t setup_device(int dev, void** ptr, int* nsm) {
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    int n = 0;
-    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    g_nsm[dev] = n;
-    g_scratch_ptr[dev] = p;
-  }
-  *ptr = g_scratch_ptr[dev];
-  *nsm = g_nsm[dev];
-  return cudaSuccess;
+// With the context's device current: the scratch array's device address and
+// the SM count.  Looked up on every call rather than cached, so that an
+// address never outlives the CUDA context it belongs to (a caller may reset
+// the device between calls); the lookup is cheap once the module is loaded.
+cudaError_t scratch_of_current_device(int dev, void** ptr, int* nsm) {
+  cudaError_t e = cudaGetSymbolAddress(ptr, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  return cudaDeviceGetAttribute(nsm, cudaDevAttrMultiProcessorCount, dev);
 }
 
 }  // namespace
+
+// Called by ps_gpu_create with the context's device current: the first
+// lookup of the array loads this file's module, which is when the driver
+// places the array in device memory.  Doing it at context creation keeps
+// that one-time placement off the per-step call.  Returns the CUDA status;
+// the caller clears a failure, which the entry point then reports.
+cudaError_t noalloc_prepare(int dev) {
+  void* p = nullptr;
+  int nsm = 0;
+  return scratch_of_current_device(dev, &p, &nsm);
+}
+
 }  // namespace ps
 
 using namespace ps;
@@ -73,12 +69,12 @@ extern "C" int ps_gpu_bin_fields_noalloc(ps_gpu_ctx* c, const float* f1, const f
     return ctx_fail(c, PS_GPU_ERR_RANGE,
                     "bin_fields_noalloc: npole * nbin = %d exceeds the scratch limit %d", width,
                     kNoAllocMaxWidth);
-  if (v.device < 0 || v.device >= kMaxDevices)
-    return ctx_fail(c, PS_GPU_ERR_ARG, "bin_fields_noalloc: device %d out of range", v.device);
-  cudaError_t e = cudaSetDevice(v.device);
+  // the caller's current device is given back on return (DeviceScope)
+  DeviceScope dev_scope(v.device);
+  cudaError_t e = dev_scope.err;
   void* scratch = nullptr;
   int nsm = 0;
-  if (e == cudaSuccess) e = setup_device(v.device, &scratch, &nsm);
+  if (e == cudaSuccess) e = scratch_of_current_device(v.device, &scratch, &nsm);
   if (e != cudaSuccess)
     return ctx_fail(c, PS_GPU_ERR_CUDA, "bin_fields_noalloc set-up: %s", cudaGetErrorString(e));
   const int grid = nsm < kNoAllocMaxCtas ? nsm : kNoAllocMaxCtas;

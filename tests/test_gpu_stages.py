@@ -76,3 +76,46 @@ def test_binning_alone_matches_oracle(gpu_lib, oracle_mod, assign, interlace):
     with gpu_lib.Estimator(ng=ng, assign=assign, interlace=interlace, dk=0.01, poles=poles) as e:
         got = e.bin_fields(fk.astype(np.complex64))
     assert (np.abs(got - pl) / np.abs(pl[0])).max() <= 2e-6
+
+
+def _host_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) / 2 ** 20
+    except OSError:
+        pass
+    return 0.0
+
+
+@pytest.mark.parametrize("ng", [512, 1024])
+def test_fft_r2c_matches_cufft(gpu_lib, ng):
+    """The hand-written r2c (z, y and x passes) against cuFFT, called through
+    torch.fft.rfftn on the same FP32 cube (the reference's transform is
+    FFTW's r2c, src/fftw_define.h:56, called at src/multipole.c:444,459).
+    cuFFT in FP64 is the truth; the FP32 error of ours must be within a
+    norm-scaled bound and at most twice cuFFT's own FP32 error."""
+    torch = pytest.importorskip("torch")
+    need = 4 * ng ** 3 * 3.2 / 2 ** 30
+    if _host_gb() < need + 8:
+        pytest.skip(f"needs about {need:.0f} GB of host memory")
+    g = torch.Generator(device="cuda").manual_seed(ng)
+    xd = torch.randn((ng, ng, ng), device="cuda", dtype=torch.float32, generator=g)
+    x = xd.cpu().numpy()
+    with gpu_lib.Estimator(ng=ng, dk=2 * np.pi / 1000) as e:
+        got = e.fft_r2c(x)
+    ref64 = torch.fft.rfftn(xd.double())
+    cu32 = torch.fft.rfftn(xd)
+    gd = torch.from_numpy(got).cuda()
+    del got
+    err = (gd.to(torch.complex128) - ref64).abs()
+    err_cu = (cu32.to(torch.complex128) - ref64).abs()
+    norm = torch.sqrt((xd.double() ** 2).sum()).item()
+    emax, ecu_max = err.max().item(), err_cu.max().item()
+    rms = torch.sqrt((err ** 2).mean()).item()
+    rms_cu = torch.sqrt((err_cu ** 2).mean()).item()
+    print(f"ng={ng}: max |ours - fp64| = {emax:.3e}, cuFFT fp32 {ecu_max:.3e}; "
+          f"rms {rms:.3e} vs cuFFT {rms_cu:.3e}; ||x|| = {norm:.3e}")
+    assert emax <= 6e-8 * np.log2(ng ** 3) * norm
+    assert rms <= 2.0 * rms_cu

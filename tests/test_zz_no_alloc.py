@@ -56,3 +56,34 @@ def test_noalloc_rejects_oversized_binning(gpu_lib):
         rc = L.ps_gpu_bin_fields_noalloc(e._ctx, d.data_ptr(), d.data_ptr(), out.data_ptr(), None)
         assert rc == -22
         assert b"scratch limit" in L.ps_gpu_last_error(e._ctx)
+
+
+def test_noalloc_allocates_nothing_and_outlives_a_context(gpu_lib):
+    """A warm call leaves the device's free memory unchanged, and the call
+    stays correct on a context created after another one was destroyed
+    (the scratch address is looked up on every call, never cached)."""
+    import torch
+    ng = 48
+    rng = np.random.default_rng(5)
+    shape = (ng, ng, ng // 2 + 1)
+    f = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    L = gpu_lib.lib()
+    d = torch.from_numpy(f.view(np.float32)).cuda()
+    dev_before = torch.cuda.current_device()
+    for _ in range(2):  # the second context is created after the first is gone
+        with gpu_lib.Estimator(ng=ng, assign=2, interlace=False, dk=0.01) as e:
+            ref = e.bin_fields(f)
+            out = torch.zeros(3 * e.nbin, dtype=torch.float64, device="cuda")
+            stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+            assert L.ps_gpu_bin_fields_noalloc(e._ctx, d.data_ptr(), d.data_ptr(),
+                                               out.data_ptr(), stream) == 0
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
+            out.fill_(float("nan"))
+            assert L.ps_gpu_bin_fields_noalloc(e._ctx, d.data_ptr(), d.data_ptr(),
+                                               out.data_ptr(), stream) == 0
+            torch.cuda.synchronize()
+            assert torch.cuda.mem_get_info()[0] == free0, "the warm call allocated device memory"
+            got = out.cpu().numpy().reshape(3, e.nbin)
+            assert (np.abs(got - ref) / np.abs(ref[0]).max()).max() <= 2e-6
+    assert torch.cuda.current_device() == dev_before
