@@ -213,18 +213,37 @@ def roofline(phases_ms, ng, interlace, n, traffic=None, assign=3, bp=32):
             "eval_frac": ab["total"] / (phases_ms[5] * 1e-3) / 1e9 / peak}
 
 
-def cpu_eval(cat, threads=None):
-    """One plain Ng = 1024 PCS interlaced evaluation with the oracle's C
-    restatement (FP64, OpenMP)."""
+def cpu_eval(cat, threads=None, ref=None):
+    """One plain evaluation (default Ng = 1024 PCS interlaced) with the
+    oracle's C restatement (FP64, OpenMP); returns (seconds, result)."""
     import oracle
     if threads:
         oracle.set_threads(threads)
-    spec = oracle.Spec(ng=PLAIN_REF["ng"], box=BOX, assign=PLAIN_REF["assign"],
-                       interlace=PLAIN_REF["interlace"], poles=(0, 2, 4), dk=DK,
+    ref = ref or PLAIN_REF
+    spec = oracle.Spec(ng=ref["ng"], box=BOX, assign=ref["assign"],
+                       interlace=ref["interlace"], poles=(0, 2, 4), dk=DK,
                        isauto=(True, False), iscross=False)
     t0 = time.perf_counter()
-    oracle.run("port", spec, [cat])
-    return time.perf_counter() - t0
+    res = oracle.run("port", spec, [cat])
+    return time.perf_counter() - t0, res
+
+
+def parity(got, ref):
+    """Error of a GPU evaluation against the FP64 oracle on the same
+    catalogue: mode counts bit-exact?, max |dP_l| / (|P_0| + shot) over every
+    bin, max |dP_l| / |P_0| over the bins where |P_0| >= shot, and over
+    every bin (unbounded where P_0, shot noise subtracted, crosses 0)."""
+    d = np.abs(got.pl[0] - ref.pl[0])
+    p0 = np.abs(ref.pl[0][0])
+    strong = p0 >= ref.shot[0]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        every = float(np.nanmax(d / p0))
+    return {"counts_exact": bool(np.array_equal(got.cnt, ref.cnt)),
+            "max_dP_over_P0_plus_shot": float((d / (p0 + ref.shot[0])).max()),
+            "max_dP_over_P0": float((d[:, strong] / p0[strong]).max()) if strong.any() else None,
+            "bins_P0_ge_shot": int(strong.sum()), "bins": int(len(p0)),
+            "max_dP_over_P0_every_bin": every, "tolerance": 1e-5,
+            "oracle": "FP64 C restatement of the reference (bit-identical to it at one thread)"}
 
 
 def ensemble_plan(seed):
@@ -364,8 +383,11 @@ def run_reference(args, world, rank):
     for _ in range(args.warmup):  # warm-up: small evaluations of the same catalogue
         oracle.run("port", small, [cat])
     times = []
+    wl = WORKLOADS[args.workload]
+    pref = PLAIN_REF if wl["learned"] else dict(ng=wl["ng"], assign=wl["assign"],
+                                                 interlace=wl["interlace"])
     for _ in range(args.steps):
-        times.append(cpu_eval(cat))
+        times.append(cpu_eval(cat, ref=pref)[0])
         if sum(times) > 150.0:  # bounded sample: keep the run within a few minutes
             break
     total = sum(times)
@@ -376,7 +398,7 @@ def run_reference(args, world, rank):
         "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": config_of(args.workload, len(cat)),
-        "reference_computes": "plain Ng=1024 PCS interlaced (genr_mesh + powspec)",
+        "reference_computes": f"plain Ng={pref['ng']} PCS interlaced (genr_mesh + powspec)",
         "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
                          "sample": f"{len(times)} full evaluation(s), 150 s cap; FFT by the "
                                    "project's FFTW-API shim, not FFTW"},
@@ -427,10 +449,13 @@ def run_gpu(args, world, rank, local):
     phases_plain = np.zeros(6)
     tuning = {"plain": plain.autotune(d_cat.data_ptr(), nreal)}  # set-up, not timed
 
+    rp_last = [None]
+
     def step_plain():
         plain.assign(0, d_cat.data_ptr(), on_device=True, n=nreal)
         r = plain.execute()
         phases_plain[:] += plain.timings()
+        rp_last[0] = r
         return r
 
     if wl["learned"]:
@@ -535,7 +560,10 @@ def run_gpu(args, world, rank, local):
         }
         line.update(extra)
         if world == 1 and not args.no_cpu:
-            cpu_s = cpu_eval(cat, threads=os.cpu_count())
+            cpu_s, cpu_res = cpu_eval(cat, threads=os.cpu_count(), ref=pref)
+            # the plain evaluation's error against the FP64 oracle, same catalogue
+            line["parity"] = dict(parity(rp_last[0], cpu_res),
+                                  evaluation=f"plain Ng={pref['ng']} PCS interlaced")
             line["cpu_baseline"] = {
                 "value": 1.0 / cpu_s, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",
                 "sample": "one plain Ng=1024 PCS interlaced evaluation of the same catalogue "
