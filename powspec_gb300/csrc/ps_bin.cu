@@ -100,11 +100,107 @@ __device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int
   __syncthreads();
 }
 
+// Moment form of the accumulation, for pole sets of even multipoles only
+// (MOM = lmax / 2 + 1 moments): per (k, mu) key the FP32 run and tile sums
+// hold M_j = sum p mu^(2j), j < MOM, two multiplies and MOM adds a mode
+// instead of a Horner evaluation per pole.  The merge turns them into the
+// Legendre sums in FP64, sum p L_l(mu) = sum_j c_lj M_j with the exact
+// coefficients of L_l in mu^2 (math/legpoly.h:47-62).
+template <int NSPEC, int MOM>
+struct MomAcc {
+  int bin;
+  float v[NSPEC][MOM];
+};
+
+template <int NSPEC, int MOM>
+__device__ __forceinline__ void mom_flush(MomAcc<NSPEC, MOM>& ra, float* tacc, int nkey, int& lo,
+                                          int& hi) {
+  if (ra.bin < 0) return;
+#pragma unroll
+  for (int s = 0; s < NSPEC; s++)
+#pragma unroll
+    for (int j = 0; j < MOM; j++) {
+      if (ra.v[s][j] != 0.f) atomicAdd(&tacc[(s * MOM + j) * nkey + ra.bin], ra.v[s][j]);
+      ra.v[s][j] = 0.f;
+    }
+  lo = min(lo, ra.bin);
+  hi = max(hi, ra.bin);
+}
+
+template <int NSPEC, int MOM>
+__device__ __forceinline__ void mom_add(MomAcc<NSPEC, MOM>& ra, int b, int nkey,
+                                        const float (&p)[NSPEC], float mu, float* tacc, int& lo,
+                                        int& hi) {
+  if (b != ra.bin) {
+    mom_flush<NSPEC, MOM>(ra, tacc, nkey, lo, hi);
+    ra.bin = b;
+  }
+  const float m2 = mu * mu;
+#pragma unroll
+  for (int s = 0; s < NSPEC; s++) {
+    float t = p[s];
+    ra.v[s][0] += t;
+#pragma unroll
+    for (int j = 1; j < MOM; j++) {
+      t *= m2;
+      ra.v[s][j] += t;
+    }
+  }
+}
+
+// Merge of moment tile sums: the Legendre sums of the touched keys are added
+// into the CTA's FP64 slice [NSPEC][npole][nkey], the moments cleared.
+template <int NSPEC, int MOM>
+__device__ void merge_tile_mom(float* tacc, int* srange, double* part, const ModeGeom& g,
+                               int nkey) {
+  __syncthreads();
+  const int blo = srange[0], bhi = srange[1];
+  if (bhi >= blo) {
+    const int w = bhi - blo + 1;
+    for (int e = threadIdx.x; e < NSPEC * w; e += blockDim.x) {
+      const int s = e / w, key = blo + (e - s * w);
+      double m[MOM];
+#pragma unroll
+      for (int j = 0; j < MOM; j++) {
+        float* t = &tacc[(s * MOM + j) * nkey + key];
+        m[j] = (double)*t;
+        *t = 0.f;
+      }
+      for (int l = 0; l < g.npole; l++) {
+        double v = 0.0;
+#pragma unroll
+        for (int j = 0; j < MOM; j++) v = fma((double)g.lc[l][j], m[j], v);
+        part[(s * g.npole + l) * nkey + key] += v;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    srange[0] = 0x7fffffff;
+    srange[1] = -1;
+  }
+  __syncthreads();
+}
+
+template <int NSPEC, int MOM>
+__device__ __forceinline__ void merge_any(float* tacc, int* srange, double* part,
+                                          const ModeGeom& g, int nkey) {
+  if (MOM > 0) merge_tile_mom<NSPEC, (MOM > 0 ? MOM : 1)>(tacc, srange, part, g, nkey);
+  else merge_tile(tacc, srange, part, NSPEC * g.npole, nkey);
+}
+
+// Accumulators of the tile sums: moments or pole sums.
+template <int NSPEC, int MOM>
+__device__ __forceinline__ int tile_accs(const ModeGeom& g) {
+  return NSPEC * (MOM > 0 ? MOM : g.npole);
+}
+
 // Binning of one transformed tile: lines f * nl + r of X (field f, row ky0 + r
 // of plane kz), each mode windowed, combined and added to the tile sums.
-template <int NSPEC, bool P2>
+template <int NSPEC, bool P2, int MOM>
 __device__ __forceinline__ void bin_lines(const PassCArgs& a, const float2* X, int ls, int kz,
                                           int ky0, int nl, float* tacc, int& lo, int& hi) {
+  constexpr int MM = MOM > 0 ? MOM : 1;
   const int ng = a.ng;
   const ModeGeom& g = a.geom;
   const int nkey = g.nbin * g.nmu;
@@ -130,12 +226,21 @@ __device__ __forceinline__ void bin_lines(const PassCArgs& a, const float2* X, i
     const float mu_yz = kyf * g.los[1] + kzf * g.los[2];
     const float k2_yz = kyf * kyf + kzf * kzf;
     const int n_yz = ja * ja + kz * kz;
-    RunAcc<NSPEC> ra;
+    RunAcc<(MOM > 0 ? 1 : NSPEC)> ra;  // pole sums (MOM == 0)
+    MomAcc<NSPEC, MM> rm;               // moments (MOM > 0)
     ra.bin = -1;
+    rm.bin = -1;
+    if (MOM == 0) {
 #pragma unroll
-    for (int s = 0; s < NSPEC; s++)
+      for (int s = 0; s < (MOM > 0 ? 1 : NSPEC); s++)
 #pragma unroll
-      for (int l = 0; l < kMaxPole; l++) ra.v[s][l] = 0.f;
+        for (int l = 0; l < kMaxPole; l++) ra.v[s][l] = 0.f;
+    } else {
+#pragma unroll
+      for (int s = 0; s < NSPEC; s++)
+#pragma unroll
+        for (int j = 0; j < MM; j++) rm.v[s][j] = 0.f;
+    }
     const int iend = min(i0 + kRun, ng);
     for (int i = i0; i < iend; i++) {
       const int ip = dsigned(i, ng), ia = abs(ip);
@@ -180,14 +285,22 @@ __device__ __forceinline__ void bin_lines(const PassCArgs& a, const float2* X, i
       }
       const float mu = (kxf * g.los[0] + mu_yz) * rq;
       const int key = (g.nmu == 1) ? b : b * g.nmu + min(g.nmu - 1, (int)(fabsf(mu) * g.nmu));
-      run_add<NSPEC>(ra, g, key, nkey, p, mu, twice, tacc, lo, hi);
+      if (MOM > 0) {
+        mom_add<NSPEC, MM>(rm, key, nkey, p, mu, tacc, lo, hi);
+      } else {
+        float q[MOM > 0 ? 1 : NSPEC];
+#pragma unroll
+        for (int s = 0; s < (MOM > 0 ? 1 : NSPEC); s++) q[s] = p[s];
+        run_add<(MOM > 0 ? 1 : NSPEC)>(ra, g, key, nkey, q, mu, twice, tacc, lo, hi);
+      }
     }
-    run_flush<NSPEC>(ra, tacc, g.npole, nkey, lo, hi);
+    if (MOM > 0) mom_flush<NSPEC, MM>(rm, tacc, nkey, lo, hi);
+    else run_flush<(MOM > 0 ? 1 : NSPEC)>(ra, tacc, g.npole, nkey, lo, hi);
   }
 }
 
 // Pass C.  Lines of tile: field f, row r -> smem line f * nl + r.
-template <int NSPEC, bool STORE, bool P2>
+template <int NSPEC, bool STORE, bool P2, int MOM>
 __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ PassCArgs a) {
   extern __shared__ float2 sm[];
   const int ng = a.ng, ngk = (ng >> 1) + 1, ls = line_stride(ng, P2), h = ng >> 1;
@@ -205,7 +318,7 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
   __shared__ int srange[2];
   double* part = STORE ? nullptr : a.partials + (size_t)blockIdx.x * nacc * nkey;
   if (!STORE) {
-    for (int e = threadIdx.x; e < nacc * nkey; e += blockDim.x) tacc[e] = 0.f;
+    for (int e = threadIdx.x; e < tile_accs<NSPEC, MOM>(g) * nkey; e += blockDim.x) tacc[e] = 0.f;
     if (threadIdx.x == 0) {
       srange[0] = 0x7fffffff;
       srange[1] = -1;
@@ -260,16 +373,16 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
     }
 
     int lo = 0x7fffffff, hi = -1;
-    bin_lines<NSPEC, P2>(a, X, ls, kz, ky0, nl, tacc, lo, hi);
+    bin_lines<NSPEC, P2, MOM>(a, X, ls, kz, ky0, nl, tacc, lo, hi);
     note_range(srange, lo, hi);
     if (++ntiles_acc == kMergeEvery) {
-      merge_tile(tacc, srange, part, nacc, nkey);
+      merge_any<NSPEC, MOM>(tacc, srange, part, g, nkey);
       ntiles_acc = 0;
     } else {
       __syncthreads();
     }
   }
-  if (!STORE && ntiles_acc) merge_tile(tacc, srange, part, nacc, nkey);
+  if (!STORE && ntiles_acc) merge_any<NSPEC, MOM>(tacc, srange, part, g, nkey);
 }
 
 // Pass C, pipelined (power-of-two Ng): persistent CTAs, the lines of the next
@@ -277,7 +390,7 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
 // transformed (ping-pong between its stage buffer and F) and binned.  Every
 // mbarrier wait is bounded; on a timeout the kernel flags a.err, drains its
 // copies and stops.
-template <int NSPEC>
+template <int NSPEC, int MOM>
 __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_constant__ PassCArgs a) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int s_abort;
@@ -296,7 +409,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_cons
   float2* F = stage[1] + selems;
   float* tacc = reinterpret_cast<float*>(F + selems);
   double* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
-  for (int e = threadIdx.x; e < nacc * nkey; e += blockDim.x) tacc[e] = 0.f;
+  for (int e = threadIdx.x; e < tile_accs<NSPEC, MOM>(g) * nkey; e += blockDim.x) tacc[e] = 0.f;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -331,16 +444,16 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_cons
     const float2* X = fft2_pp_from<false, 4>(stage[s], ng, 0, F, a.plan_full.logn, a.nfield * nl,
                                              ls, a.tw_full);
     int lo = 0x7fffffff, hi = -1;
-    bin_lines<NSPEC, true>(a, X, ls, kz, ky0, nl, tacc, lo, hi);
+    bin_lines<NSPEC, true, MOM>(a, X, ls, kz, ky0, nl, tacc, lo, hi);
     note_range(srange, lo, hi);
     if (++ntiles_acc == kMergeEvery) {
-      merge_tile(tacc, srange, part, nacc, nkey);
+      merge_any<NSPEC, MOM>(tacc, srange, part, g, nkey);
       ntiles_acc = 0;
     } else {
       __syncthreads();
     }
   }
-  if (ntiles_acc && !s_abort) merge_tile(tacc, srange, part, nacc, nkey);
+  if (ntiles_acc && !s_abort) merge_any<NSPEC, MOM>(tacc, srange, part, g, nkey);
   // never exit with a bulk copy in flight into this CTA's memory
   if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued);
 }
@@ -493,6 +606,16 @@ __global__ void __launch_bounds__(32 * kReduceWarps) k_reduce(const double* __re
 
 }  // namespace
 
+int pass_c_moments(const int* poles, int npole) {
+  int lmax = 0;
+  for (int l = 0; l < npole; l++) {
+    if (poles[l] & 1) return 0;
+    lmax = poles[l] > lmax ? poles[l] : lmax;
+  }
+  const int mom = lmax / 2 + 1;
+  return mom < 2 ? 2 : mom;
+}
+
 size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin, bool pow2) {
   return 2 * (size_t)nfield * ty * line_stride(ng, pow2) * sizeof(float2) +
          (size_t)nacc * nbin * sizeof(float);
@@ -503,11 +626,32 @@ size_t pass_c_tma_smem(int ng, int ty, int nfield, int nacc, int nkey) {
 }
 
 namespace {
-template <int NSPEC, bool STORE, bool P2>
+template <int NSPEC, bool STORE, bool P2, int MOM = 0>
 void launch_c(const PassCArgs& a, unsigned grid, size_t smem, cudaStream_t s) {
-  cudaFuncSetAttribute(k_pass_c<NSPEC, STORE, P2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  k_pass_c<NSPEC, STORE, P2><<<grid, kFftThreads, smem, s>>>(a);
+  cudaFuncSetAttribute(k_pass_c<NSPEC, STORE, P2, MOM>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_pass_c<NSPEC, STORE, P2, MOM><<<grid, kFftThreads, smem, s>>>(a);
+}
+template <int MOM, bool P2>
+void launch_c_bin(const PassCArgs& a, size_t smem, cudaStream_t s) {
+  switch (a.nspec) {
+    case 1: launch_c<1, false, P2, MOM>(a, (unsigned)a.grid, smem, s); break;
+    case 2: launch_c<2, false, P2, MOM>(a, (unsigned)a.grid, smem, s); break;
+    default: launch_c<3, false, P2, MOM>(a, (unsigned)a.grid, smem, s); break;
+  }
+}
+template <int MOM>
+void launch_c_tma(const PassCArgs& a, size_t smem, cudaStream_t s) {
+#define PS_C_TMA(NS)                                                                    \
+  cudaFuncSetAttribute(k_pass_c_tma<NS, MOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)smem);                                                      \
+  k_pass_c_tma<NS, MOM><<<(unsigned)a.grid, kFftThreads, smem, s>>>(a);
+  switch (a.nspec) {
+    case 1: PS_C_TMA(1); break;
+    case 2: PS_C_TMA(2); break;
+    default: PS_C_TMA(3); break;
+  }
+#undef PS_C_TMA
 }
 template <bool P2>
 void launch_c_p(const PassCArgs& a, cudaStream_t s) {
@@ -517,26 +661,23 @@ void launch_c_p(const PassCArgs& a, cudaStream_t s) {
     launch_c<1, true, P2>(a, ntile, pass_c_smem(a.ng, a.ty, a.nfield, 0, 0, P2), s);
     return;
   }
-  const size_t smem =
-      pass_c_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole, a.geom.nbin * a.geom.nmu, P2);
+  const int nacc_t = a.nspec * pass_c_accs(a.geom.npole, a.mom);
+  const size_t smem = pass_c_smem(a.ng, a.ty, a.nfield, nacc_t, a.geom.nbin * a.geom.nmu, P2);
   if (P2 && a.pipe) {
-    const size_t sm2 = pass_c_tma_smem(a.ng, a.ty, a.nfield, a.nspec * a.geom.npole,
-                                       a.geom.nbin * a.geom.nmu);
-#define PS_C_TMA(NS)                                                                        \
-  cudaFuncSetAttribute(k_pass_c_tma<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2); \
-  k_pass_c_tma<NS><<<(unsigned)a.grid, kFftThreads, sm2, s>>>(a);
-    switch (a.nspec) {
-      case 1: PS_C_TMA(1); break;
-      case 2: PS_C_TMA(2); break;
-      default: PS_C_TMA(3); break;
+    const size_t sm2 = pass_c_tma_smem(a.ng, a.ty, a.nfield, nacc_t, a.geom.nbin * a.geom.nmu);
+    switch (a.mom) {
+      case 2: launch_c_tma<2>(a, sm2, s); break;
+      case 3: launch_c_tma<3>(a, sm2, s); break;
+      case 4: launch_c_tma<4>(a, sm2, s); break;
+      default: launch_c_tma<0>(a, sm2, s); break;
     }
-#undef PS_C_TMA
     return;
   }
-  switch (a.nspec) {
-    case 1: launch_c<1, false, P2>(a, (unsigned)a.grid, smem, s); break;
-    case 2: launch_c<2, false, P2>(a, (unsigned)a.grid, smem, s); break;
-    default: launch_c<3, false, P2>(a, (unsigned)a.grid, smem, s); break;
+  switch (a.mom) {
+    case 2: launch_c_bin<2, P2>(a, smem, s); break;
+    case 3: launch_c_bin<3, P2>(a, smem, s); break;
+    case 4: launch_c_bin<4, P2>(a, smem, s); break;
+    default: launch_c_bin<0, P2>(a, smem, s); break;
   }
 }
 }  // namespace

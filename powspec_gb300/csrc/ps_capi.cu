@@ -272,7 +272,8 @@ void plan_pipes(ps_gpu_ctx* c) {
 // tile (rows per field) that lets two CTAs share an SM, else one CTA.
 int plan_pass_c(ps_gpu_ctx* c) {
   const int ng = c->ng;
-  const int nacc = c->nspec * c->p.npole, nkey = c->nbin * c->nmu;
+  const int nacc = c->nspec * pass_c_accs(c->p.npole, pass_c_moments(c->p.poles, c->p.npole));
+  const int nkey = c->nbin * c->nmu;
   c->ty_c = std::max(1, std::min(ng, kPassCElems / (c->nfield * ng)));
   const size_t smem_c = pass_c_smem(ng, c->ty_c, c->nfield, nacc, nkey, c->plan_full.logn >= 0);
   if (smem_c > 227 * 1024)
@@ -781,6 +782,7 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
   pc.ng = ng;
   pc.ty = pipe_c ? c->ty_ct : c->ty_c;
   pc.pipe = pipe_c ? 1 : 0;
+  pc.mom = pass_c_moments(p.poles, p.npole);
   pc.err = c->d_err + 2;
   pc.nfield = c->nfield;
   pc.interlace = p.interlace;

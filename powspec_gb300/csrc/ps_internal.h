@@ -146,8 +146,14 @@ struct PassCArgs {
   double* partials;             // [grid][nspec*npole*nbin] FP64
   int grid;                     // persistent CTAs (bin mode)
   int pipe;                     // power-of-two Ng: the cp.async.bulk-pipelined kernel
+  int mom;                      // 0: pole sums; 2..4: mu^2 moments (even poles, lmax = 2 (mom - 1))
   int* err;                     // bit 1: a pipeline wait timed out
 };
+// mu^2 moments the binning pass accumulates for a pole set (0: a Horner sum
+// per pole, for sets with odd multipoles), and its FP32 tile accumulators
+// per spectrum.
+int pass_c_moments(const int* poles, int npole);
+inline int pass_c_accs(int npole, int mom) { return mom > 0 ? (mom > npole ? mom : npole) : npole; }
 int launch_pass_c(const PassCArgs& a, cudaStream_t s);
 // Dynamic shared memory of the pipelined pass C (barriers, 2 stages + FFT
 // buffer, tile sums); complex elements of one of its buffers.

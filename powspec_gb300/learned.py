@@ -12,8 +12,9 @@ The correction is applied per (k bin, |mu| bin) cell of the coarse binning
 shot-noise term, P_l(b) = (2l+1) (sum_j c_bj A_bjl - B_bl).  The network
 (6 -> 64 -> 64 -> 64 -> 1, GELU, BF16 tensor cores) is trained and evaluated
 by the CUDA kernels of libpowspec_gpu.so (include/powspec_learned.h).  The
-plain fine-mesh method stays the fallback: k bins whose held-out error
-exceeds the tolerance are flagged and the correction is not trusted there.
+plain fine-mesh method stays the fallback and the judge of the error: k bins
+whose held-out error exceeds the tolerance are disabled, and the fine mesh's
+values replace the surrogate's there (LearnedEstimator, fallback=True).
 """
 from __future__ import annotations
 
@@ -371,13 +372,20 @@ class LearnedEstimator:
 
     run(cat) evaluates the coarse mesh on the GPU with 16 |mu| sub-bins, runs
     the correction network on the (k, |mu|) cells (GPU kernel) and returns
-    (k, P_l corrected [3, nbin], trusted [nbin]).  `trusted` is False on k
-    bins beyond the trained range or flagged by the held-out report (their
-    values are the corrected ones, but the plain fine mesh is the method to
-    use there)."""
+    (k, P_l [3, nbin], trusted [nbin]).  `trusted` is False on k bins beyond
+    the trained range (k > frac k_Nyq).
+
+    The plain fine mesh (Ng = 1024, PCS, interlaced) is the fallback: on the
+    bins where the held-out report puts the corrected error above the
+    tolerance, the surrogate is disabled.  With fallback=True (default) the
+    fine mesh is evaluated on the same catalogue whenever the configuration
+    has such bins, and its multipoles replace the surrogate's there (its
+    cost is part of the evaluation; `last_fallback` marks those bins).  With
+    fallback=False those bins keep the corrected values and are reported as
+    not trusted."""
 
     def __init__(self, ng=256, assign=3, interlace=True, box=1000.0, dk=0.005, device=0,
-                 weights=DEFAULT_WEIGHTS, frac=0.8):
+                 weights=DEFAULT_WEIGHTS, frac=0.8, fallback=True):
         self.cfg = (ng, assign, interlace)
         self.est = Estimator(ng=ng, box=box, assign=assign, interlace=interlace, poles=POLES,
                              dk=dk, device=device)
@@ -392,6 +400,16 @@ class LearnedEstimator:
                 r = json.load(f)
             key = f"ng{ng}_{['NGP', 'CIC', 'TSC', 'PCS'][assign]}_{'il' if interlace else 'noil'}"
             self.disabled = set(r.get(key, {}).get("disabled_bins", []))
+        kny = np.pi * ng / max(self.est.params.box)
+        kcen = (np.arange(self.est.nbin) + 0.5) * dk + self.est.params.kmin
+        # disabled bins inside the trained range: the ones the fallback replaces
+        self.fallback_bins = sorted(b for b in self.disabled
+                                    if b < self.est.nbin and kcen[b] <= frac * kny)
+        self.fine = None
+        if fallback and self.fallback_bins:
+            self.fine = Estimator(ng=FINE["ng"], box=box, assign=FINE["assign"],
+                                  interlace=FINE["interlace"], poles=POLES, dk=dk, device=device)
+        self.last_fallback = np.zeros(self.est.nbin, bool)
         self._last = None
         self._x = None
         self._trusted = None
@@ -399,6 +417,8 @@ class LearnedEstimator:
     def close(self):
         self.est.close()
         self.mlp.close()
+        if self.fine is not None:
+            self.fine.close()
 
     def __enter__(self):
         return self
@@ -409,17 +429,25 @@ class LearnedEstimator:
     def run(self, cat=None, *, device_ptr=None, n=None):
         """One learned evaluation (ps_gpu_execute_learned: the passes, the
         cell features, the network and the corrected multipoles all on the
-        GPU, one copy back).  cat: host AoS float64 [N, 4]; or a device
+        GPU, one copy back), plus the fine-mesh fallback where the
+        configuration needs it.  cat: host AoS float64 [N, 4]; or a device
         pointer with n."""
         if device_ptr is not None:
             self.est.assign(0, device_ptr, on_device=True, n=n)
+            if self.fine is not None:
+                self.fine.assign(0, device_ptr, on_device=True, n=n)
         else:
             self.est.assign(0, cat)
+            if self.fine is not None:
+                self.fine.assign(0, cat)
         return self._execute()
 
     def run_stream(self, cats):
         """run() over host catalogues, the copy of each overlapping the
-        evaluation of the one before (two staging slots)."""
+        evaluation of the one before (two staging slots).  A configuration
+        that needs the fine-mesh fallback evaluates them one at a time."""
+        if self.fine is not None:
+            return (self.run(c) for c in cats)
         return self.est.run_stream(cats, execute=self._execute)
 
     def _execute(self):
@@ -437,7 +465,17 @@ class LearnedEstimator:
                 if b < len(trusted):
                     trusted[b] = False
             self._trusted = trusted
-        return spec.k, pc, self._trusted.copy()
+        trusted = self._trusted.copy()
+        self.last_fallback[:] = False
+        if self.fine is not None:
+            # the plain fine mesh on the bins where the surrogate is disabled
+            # (the same bin edges: kmin + i dk on both meshes)
+            ref = self.fine.execute()
+            fb = np.asarray(self.fallback_bins, dtype=np.int64)
+            pc[:, fb] = ref.pl[0][:, fb]
+            trusted[fb] = True
+            self.last_fallback[fb] = True
+        return spec.k, pc, trusted
 
     @property
     def last_cells(self):
@@ -462,6 +500,15 @@ class LearnedEstimator:
         for b in self.disabled:
             if b < len(trusted):
                 trusted[b] = False
+        if self.fine is not None:
+            if device_ptr is not None:
+                self.fine.assign(0, device_ptr, on_device=True, n=n)
+            else:
+                self.fine.assign(0, cat)
+            ref = self.fine.execute()
+            fb = np.asarray(self.fallback_bins, dtype=np.int64)
+            pc[:, fb] = ref.pl[0][:, fb]
+            trusted[fb] = True
         return cells.kcen, pc, trusted
 
 
