@@ -249,6 +249,16 @@ int ps_gpu_autotune(ps_gpu_ctx *ctx, const double *xyzw, size_t n, int reps, int
  * for every 32 cells or more. */
 int ps_gpu_set_tuning(ps_gpu_ctx *ctx, const int *choice);
 
+/* Warp-register transforms of power-of-two meshes (no counterpart in the
+ * reference): each warp transforms whole lines in registers, with no block
+ * barrier inside a transform.  mask bit 0: the z pass (Ng = 256..2048), bit
+ * 1: the y pass, bit 2: the x pass with the combine and binning (Ng = 256..
+ * 1024); bits without a warp form for the mesh size are dropped.  They are
+ * on by default, and ps_gpu_autotune times both forms of each pass.
+ * mask < 0 only reads the setting.  Returns the mask in effect, or a status
+ * < 0. */
+int ps_gpu_set_warp_fft(ps_gpu_ctx *ctx, int mask);
+
 /* ---- Test hook (no counterpart in the reference) */
 
 /* Fake of an out-of-memory allocation: n > 0 makes the n-th next device or

@@ -38,7 +38,7 @@ EXPORTED = [
     "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
     "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune", "ps_gpu_set_tuning",
     "ps_gpu_execute_learned", "ps_gpu_stage_aos", "ps_gpu_assign_staged", "ps_gpu_set_survey",
-    "ps_gpu_debug_fail_alloc",
+    "ps_gpu_debug_fail_alloc", "ps_gpu_set_warp_fft",
 ]
 
 
@@ -173,6 +173,7 @@ def lib():
         L.ps_gpu_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                       ctypes.c_void_p]
         L.ps_gpu_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.ps_gpu_set_warp_fft.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.ps_gpu_stage_aos.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
         L.ps_gpu_assign_staged.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.ps_gpu_set_survey.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
@@ -320,7 +321,15 @@ class Estimator:
                                           _ptr(ch)))
         return dict(gather_threads=int(ch[0]), z_radix32=bool(ch[1]), y_radix32=bool(ch[2]),
                     pipelined_pass_c=bool(ch[3]), dense_lane_groups=bool(ch[4]),
-                    region_gather=bool(ch[5]))
+                    region_gather=bool(ch[5]), warp_fft=self.warp_fft())
+
+    def warp_fft(self, mask=None):
+        """Warp-register transforms in use (bit 0 z, 1 y, 2 x pass); with a
+        mask, sets them first (bits without a warp form are dropped)."""
+        rc = lib().ps_gpu_set_warp_fft(self._ctx, -1 if mask is None else int(mask))
+        if rc < 0:
+            raise PowspecError(rc, self.last_error())
+        return rc
 
     def set_tuning(self, gather_threads=None, z_radix32=None, y_radix32=None,
                    pipelined_pass_c=None, dense_lane_groups=None, region_gather=None):

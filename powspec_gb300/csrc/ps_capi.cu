@@ -91,6 +91,24 @@ bool make_plan(int n, FftPlan& p) {
   return m == 1;
 }
 
+// Table of the warp transform of length n held as L lanes x V values:
+// t[k1 L + l] = exp(-2 pi i l k1 / n), l < L, k1 < V (l k1 < n), FP64
+// angles reduced as above.
+std::vector<float2> warp_twiddles(int n) {
+  int L = 0, V = 0;
+  wfft_shape(n, &L, &V);
+  std::vector<float2> t((size_t)L * V);
+  for (int k1 = 0; k1 < V; k1++)
+    for (int l = 0; l < L; l++) {
+      const int m = (l * k1) % n;
+      const int mm = (2 * m <= n) ? m : n - m;
+      const double a = 2.0 * kPi * (double)mm / (double)n;
+      const double sn = (2 * m <= n) ? -sin(a) : sin(a);
+      t[(size_t)k1 * L + l] = make_float2((float)cos(a), (float)sn);
+    }
+  return t;
+}
+
 std::vector<float2> twiddles(int n) {
   std::vector<float2> t(n);
   for (int m = 0; m < n; m++) {
@@ -134,6 +152,13 @@ struct ps_gpu_ctx {
   int gather_region = -1;  // region gather: 1 on, 0 off, -1 by density (TSC/PCS, 16^3 tiles)
   bool pipe_c_on = true;
   int ty_ct = 1, grid_ct = 0;  // pipelined pass C (grid 0: not available)
+  // warp-register transforms (ps_wfft.cu): bit 0 z pass, 1 y pass, 2 x pass
+  // + binning, each where the mesh size has one; their tables; the x pass's
+  // persistent grid (0: not available)
+  int wfft = 0;
+  float2* d_twl_half = nullptr;
+  float2* d_twl_full = nullptr;
+  int grid_cw = 0;
   int nmu = 1;               // |mu| sub-bins of the binning pass
   // tile assignment
   int gT = 0, gnt = 0;
@@ -167,7 +192,8 @@ struct ps_gpu_ctx {
   // r2c scratch (3 half-complex fields) and a weighted real mesh
   void* d_yama = nullptr;
   size_t yama_bytes = 0;
-  float2* d_dc = nullptr;  // F_l at k = 0 per catalogue
+  double* d_dc = nullptr;  // F_l at k = 0 per catalogue [pole][cat], FP64
+  double* d_dcpart = nullptr;  // its per-CTA partial sums
   bool yama_last = false;  // the last execute took the survey-multipole path
   int last_cat = -1;
   Particles last_pt{};
@@ -293,6 +319,17 @@ int plan_pass_c(ps_gpu_ctx* c) {
       c->grid_ct = std::min(c->ngk * ((ng + ty - 1) / ty), c->nsm * per);
     }
   }
+  // warp x pass: as many persistent CTAs per SM as shared memory and 2048
+  // threads allow
+  c->grid_cw = 0;
+  if (c->d_twl_full) {
+    const size_t smw = pass_c_w_smem(ng, c->nfield, nacc, nkey);
+    if (smw && smw <= 227 * 1024) {
+      int per = std::max(1, (int)((228 * 1024) / (smw + 1024)));
+      per = std::min(per, 2048 / pass_c_w_threads());
+      c->grid_cw = c->nsm * per;
+    }
+  }
   return 0;
 }
 
@@ -306,7 +343,8 @@ int alloc_accum(ps_gpu_ctx* c) {
   c->d_part = nullptr;
   c->d_sums = nullptr;
   c->h_out = nullptr;
-  CU(dev_malloc(&c->d_part, sizeof(double) * (size_t)std::max(c->grid_c, c->grid_ct) * width));
+  CU(dev_malloc(&c->d_part,
+                sizeof(double) * (size_t)std::max({c->grid_c, c->grid_ct, c->grid_cw}) * width));
   CU(dev_malloc(&c->d_sums, sizeof(double) * width));
   CU(host_malloc(&c->h_out, sizeof(double) * (width + 8 + 2 * kMaxPole)));
   return 0;
@@ -433,6 +471,14 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   if ((rc = upload(c, &c->d_phase, phase))) return rc;
   if ((rc = upload(c, &c->d_tw_full, twiddles(ng)))) return rc;
   if ((rc = upload(c, &c->d_tw_half, twiddles(ng / 2)))) return rc;
+  if (wfft_supported(ng, 0)) {
+    if ((rc = upload(c, &c->d_twl_half, warp_twiddles(ng / 2)))) return rc;
+    c->wfft |= 1;
+  }
+  if (wfft_supported(ng, 1)) {
+    if ((rc = upload(c, &c->d_twl_full, warp_twiddles(ng)))) return rc;
+    c->wfft |= 2 | 4;
+  }
 
   ModeGeom& g = c->geom;
   g.ng = ng;
@@ -498,7 +544,7 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   size_t freeb = 0, totalb = 0;
   CU(cudaMemGetInfo(&freeb, &totalb));
   const size_t need = (size_t)c->nfield * (c->ncx * 16) +
-                      (size_t)std::max(c->grid_c, c->grid_ct) * nacc * c->nbin * 8 + c->nkeys * 8 +
+                      (size_t)std::max({c->grid_c, c->grid_ct, c->grid_cw}) * nacc * c->nbin * 8 + c->nkeys * 8 +
                       (64u << 20);
   if (need > freeb)
     return fail(c, PS_GPU_ERR_MEMORY, "need %.1f GB of device memory, %.1f GB free", need / 1e9, freeb / 1e9);
@@ -564,10 +610,10 @@ void ps_gpu_destroy(ps_gpu_ctx* c) {
     if (c->cbuf[f]) cudaFree(c->cbuf[f]);
   }
   void* bufs[] = {c->d_bintab, c->d_ksq, c->d_win, c->d_phase, c->d_tw_full, c->d_tw_half,
-                  c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage,
+                  c->d_twl_full, c->d_twl_half, c->d_part, c->d_sums, c->d_wsum, c->d_wpart, c->d_err, c->d_stage,
                   c->d_hist, c->d_bsum, c->d_rank, c->d_rec, c->d_region, c->d_lgeo,
                   c->d_lx, c->d_lxb, c->d_lc, c->d_lout, c->d_slot[0], c->d_slot[1],
-                  c->d_yama, c->d_dc};
+                  c->d_yama, c->d_dc, c->d_dcpart};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -754,6 +800,7 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
     a.tw_half = c->d_tw_half;
     a.tw_full = c->d_tw_full;
     a.plan_half = c->plan_half;
+    a.twl = (c->wfft & 1) ? c->d_twl_half : nullptr;
     c->launches += launch_pass_a(a, s);
   }
   CU(cudaGetLastError());
@@ -770,12 +817,14 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
     b.out = (float2*)c->grid[f];
     b.tw_full = c->d_tw_full;
     b.plan_full = c->plan_full;
+    b.twl = (c->wfft & 2) ? c->d_twl_full : nullptr;
     c->launches += launch_pass_b(b, s);
   }
   CU(cudaGetLastError());
   if (events) CU(cudaEventRecord(c->ev[2], s));
-  const bool pipe_c = pipe && c->pipe_c_on && c->grid_ct > 0;
-  const int grid_c = pipe_c ? c->grid_ct : c->grid_c;
+  const bool warp_c = (c->wfft & 4) && c->grid_cw > 0;
+  const bool pipe_c = !warp_c && pipe && c->pipe_c_on && c->grid_ct > 0;
+  const int grid_c = warp_c ? c->grid_cw : pipe_c ? c->grid_ct : c->grid_c;
   CU(cudaMemsetAsync(c->d_part, 0, sizeof(double) * (size_t)grid_c * nacc * nkey, s));
   PassCArgs pc;
   memset(&pc, 0, sizeof pc);
@@ -783,6 +832,7 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
   pc.ty = pipe_c ? c->ty_ct : c->ty_c;
   pc.pipe = pipe_c ? 1 : 0;
   pc.mom = pass_c_moments(p.poles, p.npole);
+  pc.twl = warp_c ? c->d_twl_full : nullptr;
   pc.err = c->d_err + 2;
   pc.nfield = c->nfield;
   pc.interlace = p.interlace;
@@ -1131,7 +1181,14 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
     CU(dev_malloc(&c->d_yama, need));
     c->yama_bytes = need;
   }
-  if (!c->d_dc) CU(dev_malloc(&c->d_dc, 2 * kMaxPole * sizeof(float2)));
+  if (!c->d_dc) CU(dev_malloc(&c->d_dc, 2 * kMaxPole * sizeof(double)));
+  const int grid_dc = std::min(c->ng * c->ng, 4 * c->nsm);
+  if (!c->d_dcpart) CU(dev_malloc(&c->d_dcpart, (size_t)4 * c->nsm * sizeof(double)));
+  double dc_org[3], dc_len[3];
+  for (int d = 0; d < 3; d++) {
+    dc_org[d] = c->survey_origin[d] * c->ng / c->p.box[d];
+    dc_len[d] = c->p.box[d];
+  }
   float2* base = (float2*)c->d_yama;
   float2 *a1 = base, *a2 = base + c->ncx, *fa = base + 2 * c->ncx;
   // fields: a1, a2, fa, then F_0 and F_l of catalogue 0 (and 1)
@@ -1162,7 +1219,11 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
           const YlmCoef yk = ylm_coef(ell, m);
           r2c_store(c, (const float*)c->grid[k * mpc], a1, a2, fl[k], m == -ell ? 1 : 2, &yk);
         }
-        CU(cudaMemcpyAsync(c->d_dc + 2 * l + k, fl[k], sizeof(float2), cudaMemcpyDeviceToDevice, s));
+        // F_l(0) in FP64 from the same mesh the harmonic terms weight
+        if (launch_dc_sum((const float*)c->grid[k * mpc], c->ng, ell, dc_org, dc_len,
+                          c->d_dcpart, grid_dc, c->d_dc + 2 * l + k, s) < 0)
+          return fail(c, PS_GPU_ERR_ARG, "survey multipoles: unsupported multipole %d", ell);
+        c->launches += 2;
       }
     for (int sp = 0; sp < c->nspec; sp++) {
       const int a = c->spec_a[sp], b = c->spec_b[sp];
@@ -1214,10 +1275,10 @@ int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nkey, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey + 4, c->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
-  float2 dc[2 * kMaxPole] = {};
-  if (yama) CU(cudaMemcpyAsync(dc, c->d_dc, sizeof(float2) * 2 * p.npole, cudaMemcpyDeviceToHost, s));
+  double dc[2 * kMaxPole] = {};
+  if (yama) CU(cudaMemcpyAsync(dc, c->d_dc, sizeof(double) * 2 * p.npole, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
-  for (int q = 0; q < 2 * p.npole; q++) h[(size_t)nacc * nkey + 8 + q] = dc[q].x;
+  for (int q = 0; q < 2 * p.npole; q++) h[(size_t)nacc * nkey + 8 + q] = dc[q];
   float t = 0;
   if (c->assign_started && cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess) c->timings[0] = t;
   for (int i = 0; i < 4; i++)
@@ -1397,11 +1458,13 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   a.pipe_grid = 0;
   a.radix32 = 0;
   a.err = c->d_err + 2;
+  a.twl = (c->wfft & 1) ? c->d_twl_half : nullptr;
   launch_pass_a(a, s);
   PassBArgs b;
   memset(&b, 0, sizeof b);
   b.ng = ng;
   b.tx = c->tx_b;
+  b.twl = (c->wfft & 2) ? c->d_twl_full : nullptr;
   b.in = c->cbuf[0];
   b.out = (float2*)c->grid[0];
   b.tw_full = c->d_tw_full;
@@ -1611,6 +1674,18 @@ void ps_gpu_batch_destroy(ps_gpu_batch* b) {
 
 // ---- autotuner ----------------------------------------------------------
 
+int ps_gpu_set_warp_fft(ps_gpu_ctx* c, int mask) {
+  if (!c) return PS_GPU_ERR_ARG;
+  const int avail = (c->d_twl_half ? 1 : 0) | (c->d_twl_full && c->grid_cw > 0 ? 6 : 0);
+  if (mask >= 0) {
+    DeviceScope dev_scope_(c->p.device);
+    CU(dev_scope_.err);
+    CU(cudaStreamSynchronize(c->stream));
+    c->wfft = mask & avail;
+  }
+  return c->wfft;
+}
+
 int ps_gpu_set_tuning(ps_gpu_ctx* c, const int* choice) {
   if (!c || !choice) return fail(c, PS_GPU_ERR_ARG, "invalid set_tuning arguments");
   if (choice[0] != -1 && choice[0] != 0 && choice[0] != 256 && choice[0] != 512)
@@ -1703,6 +1778,23 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
       }
       *v = arg;
       plan_pipes(c);
+    }
+  }
+  // warp-register form of each pass against the block-tiled one (phases
+  // 1, 2, 3), where the mesh size has one
+  {
+    const int avail = (c->d_twl_half ? 1 : 0) | (c->d_twl_full && c->grid_cw > 0 ? 6 : 0);
+    for (int bit = 0; bit < 3; bit++) {
+      const int m = 1 << bit;
+      if (!(avail & m)) continue;
+      float best = 1e30f;
+      int arg = c->wfft & m;
+      for (int k = 0; k < 2; k++) {
+        c->wfft = k ? (c->wfft | m) : (c->wfft & ~m);
+        if ((rc = measure(t))) return rc;
+        if (t[1 + bit] < best) { best = t[1 + bit]; arg = k ? m : 0; }
+      }
+      c->wfft = (c->wfft & ~m) | arg;
     }
   }
   if (choice) {

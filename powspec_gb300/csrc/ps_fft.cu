@@ -292,6 +292,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma
 }  // namespace
 
 int launch_pass_a(const PassAArgs& a, cudaStream_t s) {
+  if (a.twl && !a.grid && !a.yw && launch_pass_a_w(a, s)) return 1;
   const int M = a.ng / 2;
   const bool p2 = a.plan_half.logn >= 0;
   const size_t smem = (size_t)a.ty * line_stride(M + 1, p2) * sizeof(float2);
@@ -317,6 +318,7 @@ int launch_pass_a(const PassAArgs& a, cudaStream_t s) {
 }
 
 int launch_pass_b(const PassBArgs& a, cudaStream_t s) {
+  if (a.twl && launch_pass_b_w(a, s)) return 1;
   const bool p2 = a.plan_full.logn >= 0;
   const size_t smem = (size_t)a.tx * line_stride(a.ng, p2) * sizeof(float2);
   const int ntx = (a.ng + a.tx - 1) / a.tx;

@@ -70,6 +70,12 @@ int learned_feature_width();
 // Survey multipoles l > 0 (ps_yama.cu): the coefficients of one harmonic
 // (ylm_eval).
 YlmCoef ylm_coef(int l, int m);
+void ylm_poly(int l, int am, double* q);  // FP64 polynomial of Y_l,+-am in cos(theta)
+// F_l(0) = sum_r F(r) sum_m Y_lm(r^) of an FP32 mesh [ng][ng][ng] in FP64
+// (harmonics included) into *out (device), through `grid` CTA partials in
+// `part`.  Returns the launches made, or < 0 for l outside 0..6.
+int launch_dc_sum(const float* mesh, int ng, int ell, const double* org, const double* len,
+                  double* part, int grid, double* out, cudaStream_t s);
 // The interlaced field's c2r (ps_yama.cu): inverse along the leading axis
 // of [l][p][kz] into [p][l][kz] (with in2: over the interlace combination,
 // also written back to in), then half-complex z rows -> real rows / Ng^3.
@@ -101,6 +107,7 @@ struct PassAArgs {
   FftPlan plan_half;
   int pipe_grid;                // > 0: pipelined persistent kernel with this grid
   int radix32;                  // pipelined kernel: radix-32 passes on 8192-value tiles
+  const float2* twl;            // non-NULL: the warp transform (ps_wfft.cu), its table
   int* err;                     // bit 1: pipeline wait timed out
   // survey harmonics (yw != 0): cell (i, j, k) of the FP32 input is weighted
   // by Y_lm of ((i, j, k) + org) * len on the way in, 1 on the row i = j = 0
@@ -121,6 +128,7 @@ struct PassBArgs {
   FftPlan plan_full;
   int pipe_grid;
   int radix32;  // pipelined kernel: radix-32 passes on 8192-value tiles
+  const float2* twl;            // non-NULL: the warp transform (ps_wfft.cu), its table
   int* err;
 };
 int launch_pass_b(const PassBArgs& a, cudaStream_t s);
@@ -147,6 +155,7 @@ struct PassCArgs {
   int grid;                     // persistent CTAs (bin mode)
   int pipe;                     // power-of-two Ng: the cp.async.bulk-pipelined kernel
   int mom;                      // 0: pole sums; 2..4: mu^2 moments (even poles, lmax = 2 (mom - 1))
+  const float2* twl;            // bin mode, non-NULL: the warp transform (ps_wfft.cu)
   int* err;                     // bit 1: a pipeline wait timed out
 };
 // mu^2 moments the binning pass accumulates for a pole set (0: a Horner sum
@@ -161,6 +170,19 @@ size_t pass_c_tma_smem(int ng, int ty, int nfield, int nacc, int nkey);
 __host__ __device__ inline size_t pass_c_tma_elems(int ng, int ty, int nfield) {
   return ((size_t)nfield * ty * line_stride(ng, true) + 1) & ~(size_t)1;  // 16-byte multiple
 }
+
+// Warp-register transforms (ps_wfft.cu) for power-of-two meshes: pass 0
+// (z, Ng = 256..2048), passes 1 and 2 (y, x + binning; Ng = 256..1024).
+// Line length n is held as L lanes x V values; the table of a length-n
+// transform is twl[k1 L + l] = exp(-2 pi i l k1 / n), n entries.
+bool wfft_supported(int ng, int pass);
+void wfft_shape(int n, int* L, int* V);
+int launch_pass_a_w(const PassAArgs& a, cudaStream_t s);  // 0: shape not supported
+int launch_pass_b_w(const PassBArgs& a, cudaStream_t s);
+int launch_pass_c_w(const PassCArgs& a, cudaStream_t s);
+// Dynamic shared memory and block size of the warp x pass (persistent CTAs).
+size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey);
+int pass_c_w_threads();
 
 // Binning of standard-layout half-complex fields [x][y][kz].
 struct BinFieldArgs {

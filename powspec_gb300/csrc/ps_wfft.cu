@@ -1,0 +1,366 @@
+// ps_wfft.cu -- warp-register FFT passes for power-of-two meshes.
+//
+// Each warp transforms whole lines in registers, with no block barrier
+// inside a transform.  A line of N = L * V complex values is held by L lanes,
+// V values each, lane l holding x[l + L m] (G = 32 / L lines per warp, so
+// every load instruction reads 32 consecutive values of G lines):
+//
+//   X[k1 + V k2] = sum_l W_L^(l k2) W_N^(l k1) sum_m x[l + L m] W_V^(m k1)
+//
+//   1. a V-point DFT over m in each lane's registers;
+//   2. the twiddles W_N^(l k1), read as one coalesced row per k1 from a
+//      table twl[k1 L + l] built on the host in FP64;
+//   3. a transpose through the warp's own shared memory (__syncwarp only);
+//   4. R = V / L L-point DFTs over l per lane.
+//
+// After step 4 lane l of line g holds X[(l R + j) + V k2] in x[j L + k2].
+// Shapes: N = 128 (L 8, V 16), 256 (L 16, V 16), 512 (L 16, V 32), 1024
+// (L 32, V 32).  The passes that use it:
+//
+//   k_pass_a_w  z transform of the real mesh rows [x][y][z] (length M =
+//               Ng / 2 complex, the half-length r2c), the r2c split and the
+//               transposed store A[x][kz][y] from a tile of consecutive y;
+//   k_pass_b_w  y transform A[x][kz][y] -> B[kz][ky][x] from a tile of
+//               consecutive x, stored through shared memory in runs over x;
+//   k_pass_c_w  x transform of every field's line B[kz][ky][.], then the
+//               interlace combine, window and binning of ps_bin.cu's
+//               bin_lines on the warp's own lines.
+//
+// The reference transform is FFTW's unnormalised forward r2c
+// (src/fftw_define.h:56, called at src/multipole.c:444,459).
+#include "ps_bin_core.cuh"
+
+namespace ps {
+namespace {
+
+template <int N>
+struct WShape;
+template <>
+struct WShape<128> {
+  static constexpr int L = 8, V = 16;
+};
+template <>
+struct WShape<256> {
+  static constexpr int L = 16, V = 16;
+};
+template <>
+struct WShape<512> {
+  static constexpr int L = 16, V = 32;
+};
+template <>
+struct WShape<1024> {
+  static constexpr int L = 32, V = 32;
+};
+
+template <int N>
+struct WF {
+  static constexpr int L = WShape<N>::L, V = WShape<N>::V;
+  static constexpr int G = 32 / L;          // lines per warp
+  static constexpr int R = V / L;           // L-point DFTs per lane
+  static constexpr int SROW = L + 1;        // transpose row (complex)
+  static constexpr int SLINE = V * SROW;    // transpose area of one line
+  static constexpr int SWARP = G * SLINE;   // of one warp
+};
+
+// Forward DFT of the G lines a warp holds (see the file comment).  S: the
+// warp's transpose area, WF<N>::SWARP complex values.
+template <int N>
+__device__ __forceinline__ void wfft(float2 (&x)[WF<N>::V], float2* S,
+                                     const float2* __restrict__ twl, int lane) {
+  constexpr int L = WF<N>::L, V = WF<N>::V, R = WF<N>::R, SROW = WF<N>::SROW;
+  const int g = lane / L, l = lane - g * L;
+  dft<V>(x);
+#pragma unroll
+  for (int k1 = 1; k1 < V; k1++) x[k1] = cmul(x[k1], ldtw(&twl[k1 * L + l]));
+  float2* Sg = S + g * WF<N>::SLINE;
+#pragma unroll
+  for (int k1 = 0; k1 < V; k1++) Sg[k1 * SROW + l] = x[k1];
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < R; j++)
+#pragma unroll
+    for (int q = 0; q < L; q++) x[j * L + q] = Sg[(l * R + j) * SROW + q];
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < R; j++) {
+    float2 t[L];
+#pragma unroll
+    for (int q = 0; q < L; q++) t[q] = x[j * L + q];
+    dft<L>(t);
+#pragma unroll
+    for (int q = 0; q < L; q++) x[j * L + q] = t[q];
+  }
+}
+
+constexpr int kWarpsAB = 4;  // warps per CTA of the z and y passes
+
+// z transform: real rows of the FP32 mesh (minus its mean) -> A[x][kz][y].
+template <int NG>
+__global__ void __launch_bounds__(32 * kWarpsAB) k_pass_a_w(const __grid_constant__ PassAArgs a) {
+  constexpr int M = NG / 2;
+  using S = WF<M>;
+  constexpr int TY = kWarpsAB * S::G;  // y rows per tile
+  constexpr int TL = M + 1;            // tile line (odd)
+  extern __shared__ float2 wsm[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane / S::L, l = lane - g * S::L;
+  float2* T = wsm;                                  // [TY][TL]
+  float2* scr = wsm + TY * TL + w * S::SWARP;
+  constexpr int nty = NG / TY;
+  const int x = blockIdx.x / nty, y0 = (blockIdx.x - x * nty) * TY;
+  const int r = w * S::G + g;
+  const float2* src =
+      reinterpret_cast<const float2*>(a.fgrid + ((size_t)x * NG + y0 + r) * NG) + l;
+  float2 v[S::V];
+#pragma unroll
+  for (int m = 0; m < S::V; m++) v[m] = __ldcs(src + m * S::L);
+  wfft<M>(v, scr, a.twl, lane);
+#pragma unroll
+  for (int j = 0; j < S::R; j++)
+#pragma unroll
+    for (int k2 = 0; k2 < S::L; k2++) T[r * TL + (l * S::R + j) + S::V * k2] = v[j * S::L + k2];
+  __syncthreads();
+  // r2c split of Z = FFT(x[2m] + i x[2m+1]): X[k] = E[k] + W_NG^k O[k],
+  // E = (Z[k] + Z*[M-k]) / 2, O = -i (Z[k] - Z*[M-k]) / 2; stored as runs
+  // of TY consecutive y
+  float2* dst = a.out + (size_t)x * (M + 1) * NG + y0;
+  for (int e = threadIdx.x; e < (M + 1) * TY; e += blockDim.x) {
+    const int kz = e / TY, rr = e - kz * TY;
+    const float2* Lr = T + rr * TL;
+    float2 X;
+    if (kz == 0 || kz == M) {
+      const float2 z = Lr[0];
+      X = make_float2(kz == 0 ? z.x + z.y : z.x - z.y, 0.f);
+    } else {
+      const float2 A = Lr[kz], B = Lr[M - kz];
+      const float2 E = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y - B.y));
+      const float2 O = make_float2(0.5f * (A.y + B.y), -0.5f * (A.x - B.x));
+      X = cadd(E, cmul(__ldg(&a.tw_full[kz]), O));
+    }
+    dst[(size_t)kz * NG + rr] = X;
+  }
+}
+
+// y transform: A[x][kz][y] -> B[kz][ky][x].
+template <int N>
+__global__ void __launch_bounds__(32 * kWarpsAB) k_pass_b_w(const __grid_constant__ PassBArgs a) {
+  using S = WF<N>;
+  constexpr int TX = kWarpsAB * S::G;  // x lines per tile
+  constexpr int TP = TX + 1;           // tile row (odd)
+  constexpr int ngk = N / 2 + 1;
+  constexpr int ntx = N / TX;
+  extern __shared__ float2 wsm[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane / S::L, l = lane - g * S::L;
+  float2* T = wsm;                                  // [N][TP]
+  float2* scr = wsm + N * TP + w * S::SWARP;
+  const int kz = blockIdx.x / ntx, x0 = (blockIdx.x - kz * ntx) * TX;
+  const int col = w * S::G + g;
+  const float2* src = a.in + ((size_t)(x0 + col) * ngk + kz) * N + l;
+  float2 v[S::V];
+#pragma unroll
+  for (int m = 0; m < S::V; m++) v[m] = __ldcs(src + m * S::L);
+  wfft<N>(v, scr, a.twl, lane);
+#pragma unroll
+  for (int j = 0; j < S::R; j++)
+#pragma unroll
+    for (int k2 = 0; k2 < S::L; k2++) T[((l * S::R + j) + S::V * k2) * TP + col] = v[j * S::L + k2];
+  __syncthreads();
+  float2* dst = a.out + (size_t)kz * N * N + x0;
+  for (int e = threadIdx.x; e < N * TX; e += blockDim.x) {
+    const int ky = e / TX, xl = e - ky * TX;
+    dst[(size_t)ky * N + xl] = T[ky * TP + xl];
+  }
+}
+
+// Complex values per warp of the x pass: NP positions x nfield lines in the
+// padded layout, plus what the transpose area needs beyond G lines.
+template <int N>
+__host__ __device__ constexpr int wc_np(int nfield) {
+  return WF<N>::G > nfield ? WF<N>::G / nfield : 1;
+}
+template <int N>
+__host__ __device__ constexpr int wc_line() {
+  return N + (N - 1) / 32;  // padded line (odd), as line_stride(N, true)
+}
+template <int N>
+__host__ __device__ constexpr int wc_warp_elems(int nfield) {
+  return ((wc_np<N>(nfield) * nfield * wc_line<N>() +
+           (WF<N>::SWARP > WF<N>::G * wc_line<N>() ? WF<N>::SWARP - WF<N>::G * wc_line<N>() : 0)) +
+          1) &
+         ~1;
+}
+constexpr int kWarpsC = 4;  // warps per CTA of the x pass
+
+// x transform + combine + window + binning.  A work item of a warp is NP
+// consecutive ky at one kz (NP > 1 when a transform holds more lines than
+// there are fields); every CTA step gives one item to each warp, and the
+// tile sums are merged into the CTA's FP64 partials every kMergeEvery steps.
+template <int N, int NSPEC, int MOM>
+__global__ void __launch_bounds__(32 * kWarpsC) k_pass_c_w(const __grid_constant__ PassCArgs a) {
+  using S = WF<N>;
+  constexpr int LS = wc_line<N>();
+  extern __shared__ __align__(16) float2 wsm[];
+  __shared__ int srange[2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane / S::L, l = lane - g * S::L;
+  const int nfield = a.nfield;
+  const int NP = wc_np<N>(nfield);
+  const int nline = NP * nfield;
+  const int wel = wc_warp_elems<N>(nfield);
+  float2* X = wsm + w * wel;  // this warp's lines [field][pos][LS]
+  float* tacc = reinterpret_cast<float*>(wsm + kWarpsC * wel);
+  const ModeGeom& gm = a.geom;
+  const int nacc = NSPEC * gm.npole;
+  const int nkey = gm.nbin * gm.nmu;
+  double* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
+  for (int e = threadIdx.x; e < tile_accs<NSPEC, MOM>(gm) * nkey; e += blockDim.x) tacc[e] = 0.f;
+  if (threadIdx.x == 0) {
+    srange[0] = 0x7fffffff;
+    srange[1] = -1;
+  }
+  __syncthreads();
+  const int nitem = (N / 2 + 1) * (N / NP);  // (kz, ky0) with ky0 a multiple of NP
+  const int nstep = (nitem + (int)gridDim.x * kWarpsC - 1) / ((int)gridDim.x * kWarpsC);
+  int nacc_steps = 0;
+  for (int st = 0; st < nstep; st++) {
+    const int item = (st * (int)gridDim.x + (int)blockIdx.x) * kWarpsC + w;
+    int lo = 0x7fffffff, hi = -1;
+    if (item < nitem) {
+      const int kz = item / (N / NP), ky0 = (item - kz * (N / NP)) * NP;
+      // lines e = pos * nfield + f, G at a time; line e -> buffer f * NP + pos
+      for (int e0 = 0; e0 < nline; e0 += S::G) {
+        const int e = e0 + g, f = e % nfield, pos = e / nfield;
+        const float2* src = a.in[f] + ((size_t)kz * N + ky0 + pos) * N + l;
+        float2 v[S::V];
+#pragma unroll
+        for (int m = 0; m < S::V; m++) v[m] = __ldcs(src + m * S::L);
+        wfft<N>(v, X + e0 * LS, a.twl, lane);  // transpose area: this group's lines onward
+        float2* out = X + (f * NP + pos) * LS;
+#pragma unroll
+        for (int j = 0; j < S::R; j++)
+#pragma unroll
+          for (int k2 = 0; k2 < S::L; k2++) {
+            const int kx = (l * S::R + j) + S::V * k2;
+            out[kx + (kx >> 5)] = v[j * S::L + k2];
+          }
+        __syncwarp();
+      }
+      bin_lines<NSPEC, true, MOM>(a, X, LS, kz, ky0, NP, tacc, lo, hi, lane, 32);
+    }
+    note_range(srange, lo, hi);
+    if (++nacc_steps == kMergeEvery) {
+      merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
+      nacc_steps = 0;
+    } else {
+      __syncthreads();
+    }
+  }
+  if (nacc_steps) merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
+}
+
+template <int N, int NSPEC, int MOM>
+void launch_c_w(const PassCArgs& a, cudaStream_t s) {
+  const size_t smem = pass_c_w_smem(a.ng, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
+                                    a.geom.nbin * a.geom.nmu);
+  cudaFuncSetAttribute(k_pass_c_w<N, NSPEC, MOM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  k_pass_c_w<N, NSPEC, MOM><<<(unsigned)a.grid, 32 * kWarpsC, smem, s>>>(a);
+}
+
+template <int N, int MOM>
+void launch_c_w_ns(const PassCArgs& a, cudaStream_t s) {
+  switch (a.nspec) {
+    case 1: launch_c_w<N, 1, MOM>(a, s); break;
+    case 2: launch_c_w<N, 2, MOM>(a, s); break;
+    default: launch_c_w<N, 3, MOM>(a, s); break;
+  }
+}
+
+template <int N>
+void launch_c_w_mom(const PassCArgs& a, cudaStream_t s) {
+  switch (a.mom) {
+    case 2: launch_c_w_ns<N, 2>(a, s); break;
+    case 3: launch_c_w_ns<N, 3>(a, s); break;
+    case 4: launch_c_w_ns<N, 4>(a, s); break;
+    default: launch_c_w_ns<N, 0>(a, s); break;
+  }
+}
+
+}  // namespace
+
+bool wfft_supported(int ng, int pass) {
+  if (pass == 0) return ng == 256 || ng == 512 || ng == 1024 || ng == 2048;
+  return ng == 256 || ng == 512 || ng == 1024;
+}
+
+void wfft_shape(int n, int* L, int* V) {
+  switch (n) {
+    case 128: *L = WShape<128>::L; *V = WShape<128>::V; break;
+    case 256: *L = WShape<256>::L; *V = WShape<256>::V; break;
+    case 512: *L = WShape<512>::L; *V = WShape<512>::V; break;
+    case 1024: *L = WShape<1024>::L; *V = WShape<1024>::V; break;
+    default: *L = *V = 0; break;
+  }
+}
+
+size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey) {
+  int wel = 0;
+  switch (ng) {
+    case 256: wel = wc_warp_elems<256>(nfield); break;
+    case 512: wel = wc_warp_elems<512>(nfield); break;
+    case 1024: wel = wc_warp_elems<1024>(nfield); break;
+    default: return 0;
+  }
+  return (size_t)kWarpsC * wel * sizeof(float2) + (size_t)nacc * nkey * sizeof(float);
+}
+
+int pass_c_w_threads() { return 32 * kWarpsC; }
+
+int launch_pass_a_w(const PassAArgs& a, cudaStream_t s) {
+#define PS_A_W(NG)                                                                              \
+  {                                                                                             \
+    constexpr int M = (NG) / 2, TY = kWarpsAB * WF<M>::G;                                       \
+    const size_t smem = ((size_t)TY * (M + 1) + (size_t)kWarpsAB * WF<M>::SWARP) * sizeof(float2); \
+    cudaFuncSetAttribute(k_pass_a_w<NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    k_pass_a_w<NG><<<(unsigned)((NG) * ((NG) / TY)), 32 * kWarpsAB, smem, s>>>(a);              \
+    return 1;                                                                                   \
+  }
+  switch (a.ng) {
+    case 256: PS_A_W(256)
+    case 512: PS_A_W(512)
+    case 1024: PS_A_W(1024)
+    case 2048: PS_A_W(2048)
+    default: return 0;
+  }
+#undef PS_A_W
+}
+
+int launch_pass_b_w(const PassBArgs& a, cudaStream_t s) {
+#define PS_B_W(N)                                                                               \
+  {                                                                                             \
+    constexpr int TX = kWarpsAB * WF<N>::G;                                                     \
+    const size_t smem = ((size_t)(N) * (TX + 1) + (size_t)kWarpsAB * WF<N>::SWARP) * sizeof(float2); \
+    cudaFuncSetAttribute(k_pass_b_w<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    k_pass_b_w<N><<<(unsigned)(((N) / 2 + 1) * ((N) / TX)), 32 * kWarpsAB, smem, s>>>(a);       \
+    return 1;                                                                                   \
+  }
+  switch (a.ng) {
+    case 256: PS_B_W(256)
+    case 512: PS_B_W(512)
+    case 1024: PS_B_W(1024)
+    default: return 0;
+  }
+#undef PS_B_W
+}
+
+int launch_pass_c_w(const PassCArgs& a, cudaStream_t s) {
+  switch (a.ng) {
+    case 256: launch_c_w_mom<256>(a, s); return 1;
+    case 512: launch_c_w_mom<512>(a, s); return 1;
+    case 1024: launch_c_w_mom<1024>(a, s); return 1;
+    default: return 0;
+  }
+}
+
+}  // namespace ps

@@ -16,12 +16,16 @@
 // take the harmonic as 1 for every m (src/mp_template.c:71-74, :118-121).
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "ps_internal.h"
 
 namespace ps {
 
-YlmCoef ylm_coef(int l, int m) {
+// FP64 coefficients of the polynomial in cos(theta) of Y_l,m for |m| = am:
+// kl times the am-th derivative of P_l, kl the normalisation (with sqrt 2
+// for am > 0); q[d] for d <= l - am, 0 above.
+void ylm_poly(int l, int am, double* q) {
   // Legendre P_l coefficients by (n + 1) P_(n+1) = (2n + 1) x P_n - n P_(n-1)
   double p0[8] = {1}, p1[8] = {0, 1}, pl[8] = {0};
   if (l == 0) std::copy(p0, p0 + 8, pl);
@@ -34,18 +38,24 @@ YlmCoef ylm_coef(int l, int m) {
     std::copy(nx, nx + 8, p1);
     std::copy(nx, nx + 8, pl);
   }
-  const int am = std::abs(m);
   for (int k = 0; k < am; k++)  // d/dx, |m| times
     for (int d = 0; d < 7; d++) pl[d] = (d + 1) * pl[d + 1];
   double f = 1;  // (l - |m|)! / (l + |m|)!
-  for (int q = l - am + 1; q <= l + am; q++) f /= q;
+  for (int r = l - am + 1; r <= l + am; r++) f /= r;
   double kl = std::sqrt((2 * l + 1) / (4 * M_PI) * f);
-  if (m) kl *= std::sqrt(2.0);
+  if (am) kl *= std::sqrt(2.0);
+  for (int d = 0; d < 7; d++) q[d] = d <= l - am ? kl * pl[d] : 0.0;
+}
+
+YlmCoef ylm_coef(int l, int m) {
+  const int am = std::abs(m);
+  double q[7];
+  ylm_poly(l, am, q);
   YlmCoef c;
   c.am = am;
   c.trig = m > 0 ? 1 : (m < 0 ? -1 : 0);
   c.deg = l - am;
-  for (int d = 0; d < 7; d++) c.q[d] = (float)(d <= c.deg ? kl * pl[d] : 0.0);
+  for (int d = 0; d < 7; d++) c.q[d] = (float)q[d];
   return c;
 }
 
@@ -223,6 +233,102 @@ int launch_c2r_z(const float2* in, float* out, int ng, int ty, const float2* tw_
     k_c2r_z<false><<<grid, kFftThreads, smem, s>>>(a);
   }
   return 1;
+}
+
+// ------------------------------------------------- F_l(0) in FP64
+// The k = 0 term of F_l is sum_m sum_r F(r) Y_lm(r^) (the harmonic of k^ is
+// 1 at k = 0, src/mp_template.c:118-121), a sum that cancels to a small
+// fraction of its terms, and the first bin of a survey multipole is W times
+// it.  Summed here directly over the mesh in FP64, harmonics included (an
+// FP32 harmonic, 1e-7 off, leaves ~1e-4 of the noise scale in that bin when
+// W is far from 0).  The +m (cos) and -m (sin) harmonics share their
+// polynomial in cos(theta), so sum_m Y_lm = sum_am q_am(cos t) sin^am(t)
+// (cos(am phi) + sin(am phi)); the row i = j = 0 takes 1 for every m
+// (src/mp_template.c:71-74).  Per-CTA sums, then a fixed-order reduce.
+namespace {
+
+struct DcArgs {
+  int ng, ell;
+  const float* mesh;
+  double q[7][7];  // [am][degree]: kl q of Y_l,am (sqrt 2 included for am > 0)
+  double org[3], len[3];
+  double* part;    // [gridDim.x]
+};
+
+__global__ void __launch_bounds__(256) k_dc_sum(const __grid_constant__ DcArgs a) {
+  const int ng = a.ng, ell = a.ell;
+  const size_t nrow = (size_t)ng * ng;
+  double acc = 0.0;
+  for (size_t row = blockIdx.x; row < nrow; row += gridDim.x) {
+    const int i = (int)(row / ng), j = (int)(row - (size_t)i * ng);
+    const float* r = a.mesh + row * ng;
+    if (i == 0 && j == 0) {
+      double t = 0.0;
+      for (int k = threadIdx.x; k < ng; k += blockDim.x) t += (double)r[k];
+      acc = fma(t, (double)(2 * ell + 1), acc);
+      continue;
+    }
+    const double X = (i + a.org[0]) * a.len[0], Y = (j + a.org[1]) * a.len[1];
+    const double rxy2 = fma(X, X, Y * Y), rxy = sqrt(rxy2);
+    const double cp = X / rxy, sp = Y / rxy;
+    double T[7];  // cos(am phi) + sin(am phi)
+    T[0] = 1.0;
+    double co = 1.0, si = 0.0;
+    for (int am = 1; am <= ell; am++) {
+      const double c2 = co * cp - si * sp;
+      si = fma(si, cp, co * sp);
+      co = c2;
+      T[am] = co + si;
+    }
+    for (int k = threadIdx.x; k < ng; k += blockDim.x) {
+      const double Z = (k + a.org[2]) * a.len[2];
+      const double rinv = rsqrt(fma(Z, Z, rxy2));
+      const double ct = Z * rinv, st = rxy * rinv;
+      double ysum = 0.0, stm = 1.0;
+      for (int am = 0; am <= ell; am++) {
+        double q = 0.0;
+        for (int d = ell - am; d >= 0; d--) q = fma(q, ct, a.q[am][d]);
+        ysum = fma(q * stm, T[am], ysum);
+        stm *= st;
+      }
+      acc = fma((double)r[k], ysum, acc);
+    }
+  }
+  __shared__ double sh[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+    a.part[blockIdx.x] = t;
+  }
+}
+
+}  // namespace
+
+int launch_dc_sum(const float* mesh, int ng, int ell, const double* org, const double* len,
+                  double* part, int grid, double* out, cudaStream_t s) {
+  if (ell < 0 || ell > 6) return -1;
+  DcArgs a;
+  memset(&a, 0, sizeof a);
+  a.ng = ng;
+  a.ell = ell;
+  a.mesh = mesh;
+  for (int am = 0; am <= ell; am++) {
+    double q[7];
+    ylm_poly(ell, am, q);
+    for (int d = 0; d < 7; d++) a.q[am][d] = q[d];
+  }
+  for (int d = 0; d < 3; d++) {
+    a.org[d] = org[d];
+    a.len[d] = len[d];
+  }
+  a.part = part;
+  k_dc_sum<<<grid, 256, 0, s>>>(a);
+  launch_reduce(part, grid, 1, out, s);
+  return 2;
 }
 
 }  // namespace ps

@@ -42,10 +42,16 @@ def test_mesh_matches_oracle_and_is_deterministic(gpu_lib, oracle_mod, assign, i
         assert np.abs(runs[0][m] - ref[m]).max() <= MESH_RTOL * np.abs(ref[m]).max()
 
 
-@pytest.mark.parametrize("ng", [8, 12, 16, 20, 24, 30, 32, 40, 48, 60, 64, 96, 128, 192, 256])
-def test_fft_r2c_matches_numpy(gpu_lib, ng):
+@pytest.mark.parametrize("ng,warp", [(n, False) for n in (8, 12, 16, 20, 24, 30, 32, 40, 48, 60, 64,
+                                                     96, 128, 192, 256)] + [(256, True), (512, True),
+                                                                            (512, False)])
+def test_fft_r2c_matches_numpy(gpu_lib, ng, warp):
+    """warp: the warp-register z and y passes (ps_wfft.cu) where the size has
+    them, else the block-tiled passes."""
     x = np.random.default_rng(ng).standard_normal((ng, ng, ng)).astype(np.float32)
     with gpu_lib.Estimator(ng=ng, dk=2 * np.pi / 1000) as e:
+        m = e.warp_fft(7 if warp else 0)
+        assert bool(m & 3) == (warp and ng >= 256)
         got = e.fft_r2c(x)
     ref = np.fft.rfftn(x.astype(np.float64))
     # FP32 transform: error ~ eps * log2(n) * ||x||_2
