@@ -236,6 +236,18 @@ int ps_gpu_batch_result(ps_gpu_batch *batch, int i, ps_gpu_result *r);
 int ps_gpu_batch_launches(const ps_gpu_batch *batch);
 void ps_gpu_batch_destroy(ps_gpu_batch *batch);
 
+/* One CUDA graph over several batches (no counterpart in the reference):
+ * each batch's graph becomes a child node with no dependency on the
+ * others, so batches of different contexts run concurrently from a single
+ * graph launch on the ensemble's own stream.  The batches (one per context)
+ * must outlive the ensemble; their results are read with
+ * ps_gpu_batch_result after ps_gpu_ensemble_wait. */
+typedef struct ps_gpu_ensemble ps_gpu_ensemble;
+int ps_gpu_ensemble_create(ps_gpu_batch *const *batches, int nbatch, ps_gpu_ensemble **ens);
+int ps_gpu_ensemble_launch(ps_gpu_ensemble *ens, int wait);
+int ps_gpu_ensemble_wait(ps_gpu_ensemble *ens);
+void ps_gpu_ensemble_destroy(ps_gpu_ensemble *ens);
+
 /* Autotuner (no counterpart in the reference): times the alternative launch
  * configurations on one catalogue -- region or tile gather, gather CTA size
  * and dense-tile mapping, radix-16 / radix-32 z and y passes, pipelined or
@@ -267,6 +279,14 @@ int ps_gpu_set_warp_fft(ps_gpu_ctx *ctx, int mask);
  * disarms it.  The entry point that hits it returns PS_GPU_ERR_MEMORY, where
  * the reference exits with POWSPEC_ERR_MEMORY (src/multipole.c:121-126). */
 void ps_gpu_debug_fail_alloc(int n);
+
+/* Bounded-wait check: in the next evaluation, CTA 0 of each bulk-copy
+ * pipelined pass (the block-tiled z, y and x passes) arms the barrier of
+ * its second tile but issues no copy for it, and every barrier wait of
+ * those passes gives up after `polls` polls.  The wait runs out, the CTA
+ * drains its copies in flight and stops, and ps_gpu_execute returns
+ * PS_GPU_ERR_CUDA; the context stays usable.  No fault is involved. */
+int ps_gpu_debug_stall_pipeline(ps_gpu_ctx *ctx, int polls);
 
 #ifdef __cplusplus
 }

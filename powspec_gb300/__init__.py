@@ -38,7 +38,9 @@ EXPORTED = [
     "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
     "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune", "ps_gpu_set_tuning",
     "ps_gpu_execute_learned", "ps_gpu_stage_aos", "ps_gpu_assign_staged", "ps_gpu_set_survey",
-    "ps_gpu_debug_fail_alloc", "ps_gpu_set_warp_fft",
+    "ps_gpu_debug_fail_alloc", "ps_gpu_set_warp_fft", "ps_gpu_debug_stall_pipeline",
+    "ps_gpu_ensemble_create", "ps_gpu_ensemble_launch", "ps_gpu_ensemble_wait",
+    "ps_gpu_ensemble_destroy",
 ]
 
 
@@ -174,6 +176,13 @@ def lib():
                                       ctypes.c_void_p]
         L.ps_gpu_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ps_gpu_set_warp_fft.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ps_gpu_debug_stall_pipeline.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ps_gpu_ensemble_create.argtypes = [ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_void_p)]
+        L.ps_gpu_ensemble_launch.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ps_gpu_ensemble_wait.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_ensemble_destroy.argtypes = [ctypes.c_void_p]
+        L.ps_gpu_ensemble_destroy.restype = None
         L.ps_gpu_stage_aos.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
         L.ps_gpu_assign_staged.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.ps_gpu_set_survey.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,

@@ -143,6 +143,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_cons
     const int kz = tile / nty, ky0 = (tile - kz * nty) * a.ty;
     const int nl = min(a.ty, ng - ky0);
     mbar_expect_tx(&bar[s], (uint32_t)(a.nfield * nl * ng * 8));
+    if (a.stall && blockIdx.x == 0 && nissued == 2) return;  // test hook: no copy
     for (int f = 0; f < a.nfield; f++)
       for (int r = 0; r < nl; r++)
         bulk_g2s(stage[s] + (size_t)(f * nl + r) * ng, a.in[f] + ((size_t)kz * ng + ky0 + r) * ng,
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_cons
       fence_proxy_async();
       issue(tile + gridDim.x, s ^ 1);
     }
-    if (!pipe_wait(bar, it, a.err, &s_abort)) break;
+    if (!pipe_wait(bar, it, a.err, &s_abort, wait_limit(a.wait_limit))) break;
     const int kz = tile / nty, ky0 = (tile - kz * nty) * a.ty;
     const int nl = min(a.ty, ng - ky0);
     const float2* X = fft2_pp_from<false, 4>(stage[s], ng, 0, F, a.plan_full.logn, a.nfield * nl,
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_cons
   }
   if (ntiles_acc && !s_abort) merge_any<NSPEC, MOM>(tacc, srange, part, g, nkey);
   // never exit with a bulk copy in flight into this CTA's memory
-  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued);
+  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued, wait_limit(a.wait_limit));
 }
 
 // Stand-alone binning of FFTW-layout fields [x][y][kz]: one line per (x, y).

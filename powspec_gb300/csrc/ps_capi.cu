@@ -156,6 +156,7 @@ struct ps_gpu_ctx {
   // + binning, each where the mesh size has one; their tables; the x pass's
   // persistent grid (0: not available)
   int wfft = 0;
+  int stall = 0;  // test hook: poll limit of the next evaluation's stalled pipeline
   float2* d_twl_half = nullptr;
   float2* d_twl_full = nullptr;
   int grid_cw = 0;
@@ -801,6 +802,8 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
     a.tw_full = c->d_tw_full;
     a.plan_half = c->plan_half;
     a.twl = (c->wfft & 1) ? c->d_twl_half : nullptr;
+    a.stall = c->stall ? 1 : 0;
+    a.wait_limit = c->stall;
     c->launches += launch_pass_a(a, s);
   }
   CU(cudaGetLastError());
@@ -818,6 +821,8 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
     b.tw_full = c->d_tw_full;
     b.plan_full = c->plan_full;
     b.twl = (c->wfft & 2) ? c->d_twl_full : nullptr;
+    b.stall = c->stall ? 1 : 0;
+    b.wait_limit = c->stall;
     c->launches += launch_pass_b(b, s);
   }
   CU(cudaGetLastError());
@@ -833,6 +838,9 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
   pc.pipe = pipe_c ? 1 : 0;
   pc.mom = pass_c_moments(p.poles, p.npole);
   pc.twl = warp_c ? c->d_twl_full : nullptr;
+  pc.stall = c->stall ? 1 : 0;
+  pc.wait_limit = c->stall;
+  c->stall = 0;  // one evaluation only
   pc.err = c->d_err + 2;
   pc.nfield = c->nfield;
   pc.interlace = p.interlace;
@@ -1658,6 +1666,83 @@ int ps_gpu_batch_wait(ps_gpu_batch* b) {
   return 0;
 }
 
+// ---- one graph over several batches
+struct ps_gpu_ensemble {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<ps_gpu_batch*> batches;
+};
+
+static void ensemble_free(ps_gpu_ensemble* e) {
+  if (!e) return;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+int ps_gpu_ensemble_create(ps_gpu_batch* const* batches, int nbatch, ps_gpu_ensemble** out) {
+  if (!batches || nbatch < 1 || !out) return PS_GPU_ERR_ARG;
+  *out = nullptr;
+  for (int i = 0; i < nbatch; i++)
+    if (!batches[i] || batches[i]->c->p.device != batches[0]->c->p.device) return PS_GPU_ERR_ARG;
+  ps_gpu_ctx* c = batches[0]->c;
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
+  for (int i = 0; i < nbatch; i++)
+    for (int j = 0; j < i; j++)
+      if (batches[i]->c == batches[j]->c)
+        return fail(c, PS_GPU_ERR_ARG, "ensemble: batches %d and %d share a context", j, i);
+  ps_gpu_ensemble* e = new ps_gpu_ensemble;
+  e->device = c->p.device;
+  e->batches.assign(batches, batches + nbatch);
+  cudaError_t err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (err == cudaSuccess) err = cudaGraphCreate(&e->graph, 0);
+  // each batch a child graph without dependencies: their contexts' buffers
+  // are disjoint, so the batches run concurrently
+  for (int i = 0; i < nbatch && err == cudaSuccess; i++) {
+    cudaGraphNode_t node;
+    err = cudaGraphAddChildGraphNode(&node, e->graph, nullptr, 0, batches[i]->graph);
+  }
+  if (err == cudaSuccess) err = cudaGraphInstantiate(&e->exec, e->graph, 0);
+  if (err != cudaSuccess) {
+    (void)cudaGetLastError();
+    ensemble_free(e);
+    return fail(c, err == cudaErrorMemoryAllocation ? PS_GPU_ERR_MEMORY : PS_GPU_ERR_CUDA,
+                "ensemble graph: %s", cudaGetErrorString(err));
+  }
+  *out = e;
+  return 0;
+}
+
+int ps_gpu_ensemble_launch(ps_gpu_ensemble* e, int wait) {
+  if (!e) return PS_GPU_ERR_ARG;
+  ps_gpu_ctx* c = e->batches[0]->c;
+  DeviceScope dev_scope_(e->device);
+  CU(dev_scope_.err);
+  CU(cudaGraphLaunch(e->exec, e->stream));
+  if (wait) CU(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int ps_gpu_ensemble_wait(ps_gpu_ensemble* e) {
+  if (!e) return PS_GPU_ERR_ARG;
+  ps_gpu_ctx* c = e->batches[0]->c;
+  DeviceScope dev_scope_(e->device);
+  CU(dev_scope_.err);
+  CU(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+void ps_gpu_ensemble_destroy(ps_gpu_ensemble* e) {
+  if (!e) return;
+  DeviceScope dev_scope_(e->device);
+  ensemble_free(e);
+}
+
 int ps_gpu_batch_result(ps_gpu_batch* b, int i, ps_gpu_result* r) {
   if (!b || !r || i < 0 || i >= b->ncat) return b ? fail(b->c, PS_GPU_ERR_ARG, "invalid batch result index") : PS_GPU_ERR_ARG;
   return finish(b->c, b->h_res + (size_t)i * b->stride, &b->n[i], r, false);
@@ -1809,5 +1894,11 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
 }
 
 void ps_gpu_debug_fail_alloc(int n) { g_fail_alloc.store(n > 0 ? n : 0); }
+
+int ps_gpu_debug_stall_pipeline(ps_gpu_ctx* c, int polls) {
+  if (!c || polls < 1) return PS_GPU_ERR_ARG;
+  c->stall = polls;
+  return 0;
+}
 
 }  // extern "C"

@@ -488,16 +488,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Bounded wait: gives up after `limit` polls (each poll may suspend the
 // thread for a hardware-defined time) and reports failure.
 constexpr long long kWaitLimit = 1ll << 24;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < kWaitLimit; i++)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          long long limit = kWaitLimit) {
+  for (long long i = 0; i < limit; i++)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// A pass's poll limit: its own (> 0, set by the stall test hook) or the default.
+__device__ __forceinline__ long long wait_limit(int lim) { return lim > 0 ? lim : kWaitLimit; }
 
 // Wait for stage it & 1 of a two-stage pipeline (all threads).  On timeout:
 // sets bit 1 of *err and the block's abort flag; returns false once aborted.
-__device__ __forceinline__ bool pipe_wait(uint64_t* bar, int it, int* err, int* s_abort) {
-  if (!mbar_wait(&bar[it & 1], (uint32_t)((it >> 1) & 1))) {
+__device__ __forceinline__ bool pipe_wait(uint64_t* bar, int it, int* err, int* s_abort,
+                                          long long limit = kWaitLimit) {
+  if (!mbar_wait(&bar[it & 1], (uint32_t)((it >> 1) & 1), limit)) {
     atomicOr(err, 2);
     *s_abort = 1;
   }
@@ -511,9 +515,9 @@ __device__ __forceinline__ bool pipe_wait(uint64_t* bar, int it, int* err, int* 
 // (bounded) for exactly their phases, so that the CTA never exits with a
 // bulk copy landing in its shared memory.  An older phase's parity would
 // not do: a wait on a phase that completed earlier returns at once.
-__device__ __forceinline__ void pipe_drain(uint64_t* bar, int issued) {
+__device__ __forceinline__ void pipe_drain(uint64_t* bar, int issued, long long limit = kWaitLimit) {
   for (int j = issued >= 2 ? issued - 2 : 0; j < issued; j++)
-    mbar_wait(&bar[j & 1], (uint32_t)((j >> 1) & 1));
+    mbar_wait(&bar[j & 1], (uint32_t)((j >> 1) & 1), limit);
 }
 
 // First radix pass of a pipelined transform: reads lines of n = 2^logn

@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_a_tma
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
     mbar_expect_tx(&bar[s], (uint32_t)(nl * ng * 4));
+    if (a.stall && blockIdx.x == 0 && nissued == 2) return;  // test hook: no copy
     const float* src = a.fgrid + ((size_t)x * ng + y0) * ng;
     for (int r = 0; r < nl; r++)
       bulk_g2s(stage[s] + (size_t)r * M, src + (size_t)r * ng, (uint32_t)(ng * 4), &bar[s]);
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_a_tma
       fence_proxy_async();
       issue(tile + gridDim.x, s ^ 1);
     }
-    if (!pipe_wait(bar, it, a.err, &s_abort)) break;
+    if (!pipe_wait(bar, it, a.err, &s_abort, wait_limit(a.wait_limit))) break;
     const int x = tile / nty, y0 = (tile - x * nty) * a.ty;
     const int nl = min(a.ty, ng - y0);
     if (a.yw) {  // weight the staged rows in place; the buffer is refilled
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_a_tma
     __syncthreads();
   }
   // drain: never exit with a bulk copy in flight into this CTA's memory
-  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued);
+  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued, wait_limit(a.wait_limit));
 }
 
 // MAXLOG 5: radix-32 passes, 8192-value tiles, one CTA per SM (long lines);
@@ -263,6 +264,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma
     const int kz = tile / ntx, x0 = (tile - kz * ntx) * a.tx;
     const int nl = min(a.tx, ng - x0);
     mbar_expect_tx(&bar[s], (uint32_t)(nl * ng * 8));
+    if (a.stall && blockIdx.x == 0 && nissued == 2) return;  // test hook: no copy
     for (int r = 0; r < nl; r++)
       bulk_g2s(stage[s] + (size_t)r * ng, a.in + ((size_t)(x0 + r) * ngk + kz) * ng,
                (uint32_t)(ng * 8), &bar[s]);
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma
       fence_proxy_async();
       issue(tile + gridDim.x, s ^ 1);
     }
-    if (!pipe_wait(bar, it, a.err, &s_abort)) break;
+    if (!pipe_wait(bar, it, a.err, &s_abort, wait_limit(a.wait_limit))) break;
     const int kz = tile / ntx, x0 = (tile - kz * ntx) * a.tx;
     const int nl = min(a.tx, ng - x0);
     const float2* X = fft2_pp_from<false, MAXLOG>(stage[s], ng, 0, F, logn, nl, ls, a.tw_full);
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued);
+  if (threadIdx.x == 0 && s_abort) pipe_drain(bar, nissued, wait_limit(a.wait_limit));
 }
 
 }  // namespace

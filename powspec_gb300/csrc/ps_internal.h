@@ -115,6 +115,11 @@ struct PassAArgs {
   int yw;
   YlmCoef yc;
   float org[3], len[3];
+  // test hook (ps_gpu_debug_stall_pipeline): CTA 0 of a pipelined kernel
+  // arms its second copy but issues none, and every wait gives up after
+  // wait_limit polls (0: the default bound)
+  int stall;
+  int wait_limit;
 };
 int launch_pass_a(const PassAArgs& a, cudaStream_t s);
 
@@ -130,6 +135,11 @@ struct PassBArgs {
   int radix32;  // pipelined kernel: radix-32 passes on 8192-value tiles
   const float2* twl;            // non-NULL: the warp transform (ps_wfft.cu), its table
   int* err;
+  // test hook (ps_gpu_debug_stall_pipeline): CTA 0 of a pipelined kernel
+  // arms its second copy but issues none, and every wait gives up after
+  // wait_limit polls (0: the default bound)
+  int stall;
+  int wait_limit;
 };
 int launch_pass_b(const PassBArgs& a, cudaStream_t s);
 
@@ -157,6 +167,11 @@ struct PassCArgs {
   int mom;                      // 0: pole sums; 2..4: mu^2 moments (even poles, lmax = 2 (mom - 1))
   const float2* twl;            // bin mode, non-NULL: the warp transform (ps_wfft.cu)
   int* err;                     // bit 1: a pipeline wait timed out
+  // test hook (ps_gpu_debug_stall_pipeline): CTA 0 of a pipelined kernel
+  // arms its second copy but issues none, and every wait gives up after
+  // wait_limit polls (0: the default bound)
+  int stall;
+  int wait_limit;
 };
 // mu^2 moments the binning pass accumulates for a pole set (0: a Horner sum
 // per pole, for sets with odd multipoles), and its FP32 tile accumulators

@@ -1,6 +1,7 @@
 """Mock ensembles: catalogues of uneven size, mesh and scheme evaluated
-through per-group CUDA graphs (ps_gpu_batch_*) after autotuning
-(ps_gpu_autotune), against one-at-a-time evaluations in fresh contexts."""
+through one ensemble CUDA graph (ps_gpu_ensemble_*) over per-context graphs
+(ps_gpu_batch_*) after autotuning (ps_gpu_autotune), against one-at-a-time
+evaluations in fresh contexts."""
 import numpy as np
 import pytest
 
@@ -59,3 +60,33 @@ def test_empty_catalogue_in_a_batch(gpu_lib):
             assert ei.value.code == -11
         finally:
             b.close()
+
+
+def test_group_split_over_lanes(gpu_lib):
+    """One configuration's catalogues split over several contexts (lanes)
+    whose graphs run concurrently inside the ensemble graph: the same
+    results as the per-context graph launches and as single evaluations."""
+    torch = pytest.importorskip("torch")
+    from powspec_gb300 import catalog
+    from powspec_gb300.ensemble import Ensemble
+    cats = [catalog.lognormal(8000 + 3000 * s, box=1000.0, seed=40 + s, ngen=32) for s in range(8)]
+    dev = [torch.from_numpy(c).cuda() for c in cats]
+    cfg = [(48, 2, True)] * 8
+    ens = Ensemble(dev, cfg, dk=0.01, lanes=3, min_per_lane=2)
+    try:
+        assert len(ens.lanes) == 3
+        got = ens.run()
+        ens.launch_groups()
+        ens.wait_groups()
+        again = ens.results()
+    finally:
+        ens.close()
+    for cat, g, g2 in zip(cats, got, again):
+        with gpu_lib.Estimator(ng=48, assign=2, interlace=True, dk=0.01) as e:
+            e.assign(0, cat)
+            ref = e.execute()
+        assert np.array_equal(g.cnt, ref.cnt)
+        scale = np.abs(ref.pl[0][0]) + ref.shot[0]
+        use = ref.cnt > 0
+        for x in (g, g2):
+            assert (np.abs(x.pl[0] - ref.pl[0])[:, use] / scale[use]).max() <= 5e-6

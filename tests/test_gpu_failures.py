@@ -58,3 +58,28 @@ def test_assign_reports_out_of_memory_and_recovers(gpu_lib, oracle_mod, fail_all
     assert np.array_equal(r.cnt, ref.cnt)
     scale = np.abs(ref.pl[0, 0]) + ref.shot[0]
     assert (np.abs(r.pl[0] - ref.pl[0]) / scale).max() <= 1e-5
+
+
+def test_bounded_wait_runs_out_and_the_context_recovers(gpu_lib, oracle_mod):
+    """The bulk-copy pipelines' barrier waits are bounded: with one copy
+    armed but never issued (ps_gpu_debug_stall_pipeline) and a short poll
+    limit, the wait runs out, the kernel drains its other copy and stops,
+    and the evaluation reports PS_GPU_ERR_CUDA -- no fault, no hang.  The
+    next evaluation on the same context is correct."""
+    cat = _small_cat()
+    spec = oracle_mod.Spec(ng=256, assign=3, interlace=True, dk=0.01, isauto=(True, False),
+                           iscross=False)
+    ref = oracle_mod.run("port", spec, [cat])
+    L = gpu_lib.lib()
+    with gpu_lib.Estimator(ng=256, assign=3, interlace=True, dk=0.01) as e:
+        e.warp_fft(0)                      # the bulk-copy pipelined passes
+        e.set_tuning(pipelined_pass_c=True)
+        assert L.ps_gpu_debug_stall_pipeline(e._ctx, 2048) == 0
+        e.assign(0, cat)
+        with pytest.raises(gpu_lib.PowspecError) as ei:
+            e.execute()
+        assert ei.value.code == -20 and "timed out" in str(ei.value)
+        r = e.run([cat])
+    assert np.array_equal(r.cnt, ref.cnt)
+    scale = np.abs(ref.pl[0, 0]) + ref.shot[0]
+    assert (np.abs(r.pl[0] - ref.pl[0]) / scale).max() <= 1e-5

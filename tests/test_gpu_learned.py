@@ -144,7 +144,8 @@ def test_device_correction_matches_host_correction(gpu_lib, ng, assign, interlac
     path agrees to the binning's run-to-run FP32 summation error."""
     from powspec_gb300 import catalog, learned
     cat = catalog.lognormal(600_000, seed=23, ngen=128)
-    with learned.LearnedEstimator(ng=ng, assign=assign, interlace=interlace) as le:
+    # the surrogate alone on every bin (no fine-mesh fallback)
+    with learned.LearnedEstimator(ng=ng, assign=assign, interlace=interlace, fallback=False) as le:
         k1, p1, t1 = le.run(cat)
         cells = le.last_cells
         x = learned.features(cells.kcen, cells.kny, assign, interlace, cells.shot_ratio())
