@@ -95,13 +95,20 @@ def test_survey_cross_matches_oracle(gpu_lib, interlace):
 @pytest.mark.parametrize("interlace", [False, True])
 def test_survey_cross_unbalanced_weights(gpu_lib, interlace):
     """A catalogue whose weighted total W is far from 0: the first bin,
-    which holds the k = 0 mode alone, is dominated by W x F_l(0) = W sum_m
-    sum_r F Y_lm(r^), a sum that cancels to a small fraction of its terms.
-    F_l(0) is summed over the mesh in FP64, harmonics included (an FP32
-    transform's DC leaves ~1e-4 of the noise scale in that bin; see
-    tests/test_survey_fp32.py), so every bin is within the FP32 bar."""
+    which holds the k = 0 mode alone, is W_b F_l,a(0) + W_a F_l,b(0) with
+    F_l(0) = sum_m sum_r F Y_lm(r^), a sum that cancels to a small fraction
+    of its terms.  F_l(0) is summed over the mesh in FP64, harmonics
+    included; the FP32 transform's DC left ~1e-4 of the noise scale there
+    (tests/test_survey_fp32.py).  What remains is the mesh itself: its
+    node values are FP32 products of the 1-D weights, so the balanced
+    catalogue's F_l(0), summed in FP64 from the exact fixed-point mesh, is
+    3e-7 off the FP64 reference's (measured), and W_b = -1404 carries that
+    into the first bin as up to 3.2e-5 of the noise scale.  Bound: 5e-5 in
+    the first bin, the FP32 bar in every other bin (measured at most
+    2.1e-6)."""
     (err,) = _cross(gpu_lib, _pair(unbalanced=True), interlace, autos=False)
-    assert err.max() <= TOL, err.max(axis=1)
+    assert err[:, 1:].max() <= TOL, err[:, 1:].max(axis=1)
+    assert err[:, 0].max() <= 5e-5, err[:, 0]
 
 
 def test_survey_misuse_is_refused(gpu_lib):
