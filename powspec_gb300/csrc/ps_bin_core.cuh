@@ -198,10 +198,122 @@ __device__ __forceinline__ int tile_accs(const ModeGeom& g) {
 
 // Binning of one transformed tile: lines f * nl + r of X (field f, row ky0 + r
 // of plane kz), each mode windowed, combined and added to the tile sums.
+// Power of the mode at x index xi (signed ip) of line r: the combined field
+// of each catalogue, (F0 + exp(i theta) F1) / 2 with interlacing, windowed.
+template <int NSPEC, bool P2>
+__device__ __forceinline__ void mode_power(const PassCArgs& a, const float2* X, int ls, int nl,
+                                           int r, int xi, int ip, int jp, int kz, float wjk,
+                                           const int (&spec_a)[NSPEC], const int (&spec_b)[NSPEC],
+                                           float (&p)[NSPEC]) {
+  const int ng = a.ng;
+  const ModeGeom& g = a.geom;
+  const int mpc = a.interlace ? 2 : 1;
+  const int li = lidx<P2>(xi);
+  float2 G0 = X[r * ls + li], G1 = G0;
+  float2 ph = make_float2(1.f, 0.f);
+  if (a.interlace) {
+    ph = __ldg(&g.phase[ip + jp + kz + ng]);
+    const float2 t = cmul(ph, X[(nl + r) * ls + li]);
+    G0 = make_float2(0.5f * (G0.x + t.x), 0.5f * (G0.y + t.y));
+  }
+  if (a.ncat > 1) {
+    G1 = X[(mpc * nl + r) * ls + li];
+    if (a.interlace) {
+      const float2 t = cmul(ph, X[((mpc + 1) * nl + r) * ls + li]);
+      G1 = make_float2(0.5f * (G1.x + t.x), 0.5f * (G1.y + t.y));
+    }
+  }
+  const float wwin = __ldg(&g.win[xi]) * wjk;
+#pragma unroll
+  for (int s = 0; s < NSPEC; s++) {
+    const float2 A = spec_a[s] ? G1 : G0;
+    const float2 B = spec_b[s] ? G1 : G0;
+    p[s] = (A.x * B.x + A.y * B.y) * wwin;
+  }
+}
+
+// Moment binning when the line of sight has no x component: the modes at
+// +k_x and -k_x of a line share |k|, mu, the bin and the |mu| sub-bin, so
+// they are binned as one: the geometry once and one accumulation of the
+// two powers (the window and the interlace phase stay per mode).  Lanes
+// walk runs of consecutive |k_x| in [0, Ng/2): kRun long, or shorter so
+// that a line gives every lane of a warp a run; the run that ends at Ng/2
+// also takes the Nyquist plane k_x = Ng/2.
+template <int NSPEC, bool P2, int MOM>
+__device__ __forceinline__ void bin_lines_pair(const PassCArgs& a, const float2* X, int ls,
+                                               int kz, int ky0, int nl, float* tacc, int& lo,
+                                               int& hi, int tid, int nthr) {
+  const int ng = a.ng, half = ng >> 1;
+  const ModeGeom& g = a.geom;
+  const int nkey = g.nbin * g.nmu;
+  int spec_a[NSPEC], spec_b[NSPEC];
+#pragma unroll
+  for (int s = 0; s < NSPEC; s++) {
+    spec_a[s] = a.spec_a[s];
+    spec_b[s] = a.spec_b[s];
+  }
+  const bool twice = !(kz == 0 || 2 * kz == ng);
+  const float wk = twice ? 2.f : 1.f;
+  const float kzf = g.vec[2] * (float)kz;
+  const int runp = max(1, min(kRun, half / 32));
+  const int chunks = (half + runp - 1) / runp;
+  for (int e = tid; e < nl * chunks; e += nthr) {
+    const int r = e / chunks;
+    const int i0 = (e - r * chunks) * runp;
+    const int ky = ky0 + r;
+    const int jp = dsigned(ky, ng), ja = abs(jp);
+    const float wjk = __ldg(&g.win[ng + ky]) * __ldg(&g.win[2 * ng + kz]) * wk;
+    const float kyf = g.vec[1] * (float)jp;
+    const float mu_yz = kyf * g.los[1] + kzf * g.los[2];
+    const float k2_yz = kyf * kyf + kzf * kzf;
+    const int n_yz = ja * ja + kz * kz;
+    MomAcc<NSPEC, MOM> rm;
+    rm.bin = -1;
+#pragma unroll
+    for (int s = 0; s < NSPEC; s++)
+#pragma unroll
+      for (int j = 0; j < MOM; j++) rm.v[s][j] = 0.f;
+    int iend = min(i0 + runp, half);
+    if (iend == half) iend = half + 1;
+    for (int i = i0; i < iend; i++) {
+      const int n = i * i + n_yz;
+      if (n == 0) continue;  // DC (src/multipole.c:806)
+      const float kxf = g.vec[0] * (float)i;
+      const float rq = rsqrtf(kxf * kxf + k2_yz);
+      int b;
+      if (g.fastbin) {
+        const float t = (fmaf(kxf, kxf, k2_yz) * rq - g.k0f) * g.inv_dkf;
+        const float fl = floorf(t), fr = t - fl;
+        b = (fr > g.eps_t && fr < 1.f - g.eps_t) ? ((fl < 0.f || fl >= (float)g.nbin) ? -1 : (int)fl)
+                                                 : mode_bin(g, i, ja, kz, n);
+      } else {
+        b = mode_bin(g, i, ja, kz, n);
+      }
+      if (b < 0) continue;
+      const float mu = mu_yz * rq;
+      const int key = (g.nmu == 1) ? b : b * g.nmu + min(g.nmu - 1, (int)(fabsf(mu) * g.nmu));
+      float p[NSPEC];
+      mode_power<NSPEC, P2>(a, X, ls, nl, r, i, i, jp, kz, wjk, spec_a, spec_b, p);
+      if (i != 0 && i != half) {  // the mode at -k_x (x index ng - i)
+        float q[NSPEC];
+        mode_power<NSPEC, P2>(a, X, ls, nl, r, ng - i, -i, jp, kz, wjk, spec_a, spec_b, q);
+#pragma unroll
+        for (int s = 0; s < NSPEC; s++) p[s] += q[s];
+      }
+      mom_add<NSPEC, MOM>(rm, key, nkey, p, mu, tacc, lo, hi);
+    }
+    mom_flush<NSPEC, MOM>(rm, tacc, nkey, lo, hi);
+  }
+}
+
 template <int NSPEC, bool P2, int MOM>
 __device__ __forceinline__ void bin_lines(const PassCArgs& a, const float2* X, int ls, int kz,
                                           int ky0, int nl, float* tacc, int& lo, int& hi,
                                           int tid, int nthr) {
+  if (MOM > 0 && a.geom.los[0] == 0.f) {
+    bin_lines_pair<NSPEC, P2, (MOM > 0 ? MOM : 1)>(a, X, ls, kz, ky0, nl, tacc, lo, hi, tid, nthr);
+    return;
+  }
   constexpr int MM = MOM > 0 ? MOM : 1;
   const int ng = a.ng;
   const ModeGeom& g = a.geom;
