@@ -1191,7 +1191,7 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
   }
   if (!c->d_dc) CU(dev_malloc(&c->d_dc, 2 * kMaxPole * sizeof(double)));
   const int grid_dc = std::min(c->ng * c->ng, 4 * c->nsm);
-  if (!c->d_dcpart) CU(dev_malloc(&c->d_dcpart, (size_t)4 * c->nsm * sizeof(double)));
+  if (!c->d_dcpart) CU(dev_malloc(&c->d_dcpart, ((size_t)4 * c->nsm + 1) * sizeof(double)));
   double dc_org[3], dc_len[3];
   for (int d = 0; d < 3; d++) {
     dc_org[d] = c->survey_origin[d] * c->ng / c->p.box[d];
@@ -1228,10 +1228,11 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
           r2c_store(c, (const float*)c->grid[k * mpc], a1, a2, fl[k], m == -ell ? 1 : 2, &yk);
         }
         // F_l(0) in FP64 from the same mesh the harmonic terms weight
-        if (launch_dc_sum((const float*)c->grid[k * mpc], c->ng, ell, dc_org, dc_len,
-                          c->d_dcpart, grid_dc, c->d_dc + 2 * l + k, s) < 0)
-          return fail(c, PS_GPU_ERR_ARG, "survey multipoles: unsupported multipole %d", ell);
-        c->launches += 2;
+        const int nl = launch_dc_sum((const float*)c->grid[k * mpc], c->ng, ell, dc_org, dc_len,
+                                     c->d_wsum, p.ncat, fl[k], c->d_dcpart, grid_dc,
+                                     c->d_dc + 2 * l + k, s);
+        if (nl < 0) return fail(c, PS_GPU_ERR_ARG, "survey multipoles: unsupported multipole %d", ell);
+        c->launches += nl;
       }
     for (int sp = 0; sp < c->nspec; sp++) {
       const int a = c->spec_a[sp], b = c->spec_b[sp];

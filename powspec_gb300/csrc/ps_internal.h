@@ -71,11 +71,15 @@ int learned_feature_width();
 // (ylm_eval).
 YlmCoef ylm_coef(int l, int m);
 void ylm_poly(int l, int am, double* q);  // FP64 polynomial of Y_l,+-am in cos(theta)
-// F_l(0) = sum_r F(r) sum_m Y_lm(r^) of an FP32 mesh [ng][ng][ng] in FP64
-// (harmonics included) into *out (device), through `grid` CTA partials in
-// `part`.  Returns the launches made, or < 0 for l outside 0..6.
+// F_l(0) into *out (device): sum_r F(r) sum_m Y_lm(r^) of an FP32 mesh
+// [ng][ng][ng] in FP64 (harmonics included), through `grid` CTA partials
+// in `part` (grid + 1 doubles), when some catalogue's |sum w| exceeds kDcGate
+// times its sum |w| (wsum: [ncat][2] on the device); else the FP32
+// transform's DC *dc32.  Returns the launches made, or < 0 for l outside 0..6.
+constexpr double kDcGate = 1e-4;
 int launch_dc_sum(const float* mesh, int ng, int ell, const double* org, const double* len,
-                  double* part, int grid, double* out, cudaStream_t s);
+                  const double* wsum, int ncat, const float2* dc32, double* part, int grid,
+                  double* out, cudaStream_t s);
 // The interlaced field's c2r (ps_yama.cu): inverse along the leading axis
 // of [l][p][kz] into [p][l][kz] (with in2: over the interlace combination,
 // also written back to in), then half-complex z rows -> real rows / Ng^3.

@@ -253,9 +253,21 @@ struct DcArgs {
   double q[7][7];  // [am][degree]: kl q of Y_l,am (sqrt 2 included for am > 0)
   double org[3], len[3];
   double* part;    // [gridDim.x]
+  const double* wsum;  // [ncat][2]: each catalogue's sum of w and of |w|
+  int ncat;
 };
 
+// The FP64 sum is needed only when a catalogue's weighted total W, which
+// multiplies F_l(0) in the first bin, is not small against its sum of |w|;
+// otherwise the transform's FP32 DC is kept.
+__device__ __forceinline__ bool dc_needed(const double* wsum, int ncat) {
+  bool need = false;
+  for (int k = 0; k < ncat; k++) need |= fabs(wsum[2 * k]) > kDcGate * wsum[2 * k + 1];
+  return need;
+}
+
 __global__ void __launch_bounds__(256) k_dc_sum(const __grid_constant__ DcArgs a) {
+  if (!dc_needed(a.wsum, a.ncat)) return;
   const int ng = a.ng, ell = a.ell;
   const size_t nrow = (size_t)ng * ng;
   double acc = 0.0;
@@ -306,10 +318,17 @@ __global__ void __launch_bounds__(256) k_dc_sum(const __grid_constant__ DcArgs a
   }
 }
 
+// out = the FP64 sum (when needed) or the FP32 transform's DC.
+__global__ void k_dc_select(const double* sum, const float2* dc32, const double* wsum, int ncat,
+                            double* out) {
+  *out = dc_needed(wsum, ncat) ? *sum : (double)dc32->x;
+}
+
 }  // namespace
 
 int launch_dc_sum(const float* mesh, int ng, int ell, const double* org, const double* len,
-                  double* part, int grid, double* out, cudaStream_t s) {
+                  const double* wsum, int ncat, const float2* dc32, double* part, int grid,
+                  double* out, cudaStream_t s) {
   if (ell < 0 || ell > 6) return -1;
   DcArgs a;
   memset(&a, 0, sizeof a);
@@ -326,9 +345,12 @@ int launch_dc_sum(const float* mesh, int ng, int ell, const double* org, const d
     a.len[d] = len[d];
   }
   a.part = part;
+  a.wsum = wsum;
+  a.ncat = ncat;
   k_dc_sum<<<grid, 256, 0, s>>>(a);
-  launch_reduce(part, grid, 1, out, s);
-  return 2;
+  launch_reduce(part, grid, 1, part + grid, s);
+  k_dc_select<<<1, 1, 0, s>>>(part + grid, dc32, wsum, ncat, out);
+  return 3;
 }
 
 }  // namespace ps
