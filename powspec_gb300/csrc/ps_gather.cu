@@ -23,6 +23,7 @@
 // FP64 sequence (pos - bmin) * Ng / L used instead, so cell indices and
 // branches are the reference's while FP64 work stays rare.
 #include <cstddef>
+#include <type_traits>
 
 #include "ps_internal.h"
 
@@ -509,6 +510,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
   __shared__ unsigned bstart[128];
   __shared__ unsigned boff[125];
   __shared__ unsigned rowmask[2][8];  // T = 16: touched (x, y) rows per mesh
+  __shared__ float bound_sum[2];
   const int T = TT ? TT : g.T;
   const int nt = g.nt, ng = g.ng;
   const int T3 = T * T * T;
@@ -590,7 +592,25 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
   const bool sparse = (S >= 3) && total <= g.sparse_max;
   if (threadIdx.x < 16) rowmask[threadIdx.x >> 3][threadIdx.x & 7] = (sparse && TT == 16) ? 0u : ~0u;
   __syncthreads();
+  bool split_used = false;  // the tile sums are in the split 32-bit form
   if constexpr (S >= 3) {
+    // Accumulators: 64-bit adds, or (TT == 16, every tile of at most 65535
+    // records) the split form of the region gather: q mod 2^32 summed at
+    // word idx, q >> 16 summed at HW + idx, native 32-bit shared adds in
+    // place of a 64-bit compare-and-swap loop, in the same bytes.  A tile
+    // whose records' node bounds sum to 2^46 or more is redone with 64-bit
+    // adds.  The cell value 2^16 H + L is the same integer either way.
+    unsigned* const w32 = reinterpret_cast<unsigned*>(acc);
+    const int HW = nmesh * (T3 + kMeshPad);
+    auto add = [&](auto split, int idx, long long q) {
+      if constexpr (decltype(split)::value) {
+        atomicAdd(&w32[idx], (unsigned)q);
+        atomicAdd(reinterpret_cast<int*>(&w32[HW + idx]), (int)(q >> 16));
+      } else {
+        atomicAdd(&acc[idx], (unsigned long long)q);
+      }
+    };
+    auto run = [&](auto split) {
    if (sparse) {
     // Lane = (record, mesh, z node), 4 lanes per record and mesh: all the
     // records of the tile in one step.  The z = 0 lane flags the rows.
@@ -605,6 +625,8 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
         if (b + step < 126 && bstart[b + step] <= i) b += step;
       const WRec* rp = recs + boff[b] + (i - bstart[b]);
       const short4 bs = *reinterpret_cast<const short4*>(&rp->base[m][0]);
+      if (decltype(split)::value && kz == 0)
+        atomicAdd(&bound_sum[m], __int_as_float((min(bs.w & 0xff, 127) + 127) << 23));
       const float4 wx4 = *reinterpret_cast<const float4*>(&rp->w[m][0][0]);
       const float4 wy4 = *reinterpret_cast<const float4*>(&rp->w[m][1][0]);
       const float wz = rp->w[m][2][kz];
@@ -639,7 +661,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
           const int col = kSwz ? (lz ^ ((ly & 3) << 2)) : lz;
           const float v = wxs[x] * wyz[y];
           const long long q = (bs.w & 0x100) ? round_small(v) : round_fix(v);
-          atomicAdd(&A[(lx * T + ly) * T + col], (unsigned long long)q);
+          add(split, (int)(A - acc) + (lx * T + ly) * T + col, q);
         }
       }
     }
@@ -657,6 +679,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
       float4 wx;
       float wy, wz;
       int b0, b1, b2, small;
+      float bound;  // 2^e above every node value of the record (2^-32 units)
     };
     auto load = [&](unsigned i, int& b) {
       while (bstart[b + 1] <= i) b++;  // warp-uniform; i only grows
@@ -670,6 +693,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
       L.b1 = bs.y;
       L.b2 = bs.z;
       L.small = bs.w & 0x100;
+      L.bound = __int_as_float((min(bs.w & 0xff, 127) + 127) << 23);
       return L;
     };
     int b = 0;
@@ -679,6 +703,8 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
     for (; i < total; i += nw) {
       const Ld cur = nxt;
       if (i + nw < total) nxt = load(i + nw, b);
+      if (decltype(split)::value && yy == 0 && zz == 0 && (nmesh == 2 || half == 0))
+        atomicAdd(&bound_sum[m], cur.bound);
       if (!act) continue;
       const int ly = rel(cur.b1, 1) + yy, lz = rel(cur.b2, 2) + zz;
       if ((unsigned)ly >= (unsigned)T || (unsigned)lz >= (unsigned)T) continue;
@@ -694,10 +720,29 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
         if ((unsigned)lx >= (unsigned)T) continue;
         const float v = wxs[x] * wyz;
         const long long q = cur.small ? round_small(v) : round_fix(v);  // warp-uniform
-        atomicAdd(&A[lx * T * T], (unsigned long long)q);
+        add(split, (int)(A - acc) + lx * T * T, q);
       }
     }
    }
+    };
+    bool done = false;
+    if constexpr (TT == 16) {
+      if (total <= 65535u) {
+        if (threadIdx.x < 2) bound_sum[threadIdx.x] = 0.f;
+        __syncthreads();
+        run(std::integral_constant<bool, true>());
+        __syncthreads();
+        done = bound_sum[0] < 70368744177664.f && bound_sum[1] < 70368744177664.f;  // 2^46
+        split_used = done;
+        if (!done) {
+          ulonglong2* a2 = reinterpret_cast<ulonglong2*>(acc);
+          for (int e = threadIdx.x; e < nmesh * (T3 + kMeshPad) / 2; e += blockDim.x)
+            a2[e] = make_ulonglong2(0ull, 0ull);
+          __syncthreads();
+        }
+      }
+    }
+    if (!done) run(std::integral_constant<bool, false>());
   } else {
     // Work item = (record, mesh, z node): P lanes per mesh (P = S rounded up
     // to a power of two), G = nmesh * P lanes per record, aligned within the
@@ -772,11 +817,24 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
       const bool touched = (rowmask[m][row >> 5] >> (row & 31)) & 1u;
       ulonglong2 u0 = make_ulonglong2(0ull, 0ull), u1 = u0;
       if (touched) {
-        const ulonglong2* Ar =
-            reinterpret_cast<const ulonglong2*>(acc + m * (T3 + kMeshPad) + row * 16);
         const int pq = kSwz ? (q ^ (ly & 3)) : q;  // stored block of z cells [4q, 4q + 4)
-        u0 = Ar[2 * pq];
-        u1 = Ar[2 * pq + 1];
+        if (split_used) {
+          const unsigned* w32 = reinterpret_cast<const unsigned*>(acc);
+          const int idx = m * (T3 + kMeshPad) + row * 16 + 4 * pq;
+          const uint4 lo = *reinterpret_cast<const uint4*>(w32 + idx);
+          const int4 hi = *reinterpret_cast<const int4*>(w32 + nmesh * (T3 + kMeshPad) + idx);
+          auto join = [](unsigned l, int h) {
+            return (unsigned long long)(((long long)h << 16) +
+                                        (long long)(unsigned)(l - ((unsigned)h << 16)));
+          };
+          u0 = make_ulonglong2(join(lo.x, hi.x), join(lo.y, hi.y));
+          u1 = make_ulonglong2(join(lo.z, hi.z), join(lo.w, hi.w));
+        } else {
+          const ulonglong2* Ar =
+              reinterpret_cast<const ulonglong2*>(acc + m * (T3 + kMeshPad) + row * 16);
+          u0 = Ar[2 * pq];
+          u1 = Ar[2 * pq + 1];
+        }
       }
       if (INT64) {
         longlong2* o = reinterpret_cast<longlong2*>(g.out64[m] + cell);

@@ -54,8 +54,10 @@ def test_region_gather_equals_tile_gather(gpu_lib, assign, interlace, ng):
     assert np.array_equal(sr.cnt, st.cnt)
     scale = np.abs(st.pl[0][0]) + st.shot[0]
     use = st.cnt > 0
-    # the same FP32 mesh; the binning's FP32 sums may add in another order
-    assert (np.abs(sr.pl[0] - st.pl[0])[:, use] / scale[use]).max() <= 1e-6
+    # the same FP32 mesh; the binning's FP32 sums may add in another order,
+    # and its mu^2 moments (P_4 = 4.375 M_2 - 3.75 M_1 + 0.375 M_0) carry
+    # that order's rounding into P_l at a few 1e-7 of the monopole
+    assert (np.abs(sr.pl[0] - st.pl[0])[:, use] / scale[use]).max() <= 5e-6
 
 
 def test_region_gather_with_empty_tiles(gpu_lib):
