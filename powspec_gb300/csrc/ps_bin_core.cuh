@@ -105,8 +105,9 @@ __device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int
 // (MOM = lmax / 2 + 1 moments): per (k, mu) key the FP32 run and tile sums
 // hold M_j = sum p mu^(2j), j < MOM, two multiplies and MOM adds a mode
 // instead of a Horner evaluation per pole.  The merge turns them into the
-// Legendre sums in FP64, sum p L_l(mu) = sum_j c_lj M_j with the exact
-// coefficients of L_l in mu^2 (math/legpoly.h:47-62).
+// Legendre sums, sum p L_l(mu) = sum_j c_lj M_j with the exact coefficients
+// of L_l in mu^2 (math/legpoly.h:47-62), combined in FP32 and added into
+// the FP64 partials.
 template <int NSPEC, int MOM>
 struct MomAcc {
   int bin;
@@ -160,18 +161,23 @@ __device__ void merge_tile_mom(float* tacc, int* srange, double* part, const Mod
     const int w = bhi - blo + 1;
     for (int e = threadIdx.x; e < NSPEC * w; e += blockDim.x) {
       const int s = e / w, key = blo + (e - s * w);
-      double m[MOM];
+      float m[MOM];
+      bool any = false;
 #pragma unroll
       for (int j = 0; j < MOM; j++) {
         float* t = &tacc[(s * MOM + j) * nkey + key];
-        m[j] = (double)*t;
+        m[j] = *t;
+        any |= m[j] != 0.f;
         *t = 0.f;
       }
+      if (!any) continue;  // a key of the range that no mode reached
+      // the combination in FP32 (FP64 arithmetic is slow on this GPU; the
+      // moments are FP32 sums already), added into the FP64 partials
       for (int l = 0; l < g.npole; l++) {
-        double v = 0.0;
+        float v = 0.f;
 #pragma unroll
-        for (int j = 0; j < MOM; j++) v = fma((double)g.lc[l][j], m[j], v);
-        part[(s * g.npole + l) * nkey + key] += v;
+        for (int j = 0; j < MOM; j++) v = fmaf(g.lc[l][j], m[j], v);
+        part[(s * g.npole + l) * nkey + key] += (double)v;
       }
     }
   }

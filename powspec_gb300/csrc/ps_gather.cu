@@ -131,26 +131,35 @@ __device__ __forceinline__ bool near_edge(float d) {
   return d < kEdge || d > 1.f - kEdge || fabsf(d - 0.5f) < kEdge;
 }
 
-// Both grids' axis for one coordinate.  pos_hi + pos_lo = pos; s_hi + s_lo = Ng / L.
-__device__ __forceinline__ void axis_pair(int assign, double pos, float pos_hi, float pos_lo,
-                                          float s_hi, float s_lo, double L, int ng, bool il,
-                                          Axis& a0, Axis& a1) {
+// The plain grid's axis for one coordinate; i, d: the double-float cell and
+// fraction it started from.  pos_hi + pos_lo = pos; s_hi + s_lo = Ng / L.
+__device__ __forceinline__ Axis plain_axis(int assign, double pos, float pos_hi, float pos_lo,
+                                           float s_hi, float s_lo, double L, int ng, int& i,
+                                           float& d) {
   // x = pos * s in double-float: p + t
   const float p = pos_hi * s_hi;
   const float e = fmaf(pos_hi, s_hi, -p);
   const float t = e + fmaf(pos_hi, s_lo, pos_lo * s_hi);
-  int i = (int)floorf(p);
-  float d = (p - (float)i) + t;
+  i = (int)floorf(p);
+  d = (p - (float)i) + t;
   if (d < 0.f) { i -= 1; d += 1.f; }
   if (d >= 1.f) { i += 1; d -= 1.f; }
   if (near_edge(d) || i < 0 || i >= ng) {
     int i0;
     double dd;
     exact_coord(pos, L, ng, false, i0, dd);
-    a0 = make_axis(assign, i0, dd, ng);
-  } else {
-    a0 = make_axis(assign, i, (double)d, ng);
+    return make_axis(assign, i0, dd, ng);
   }
+  return make_axis(assign, i, (double)d, ng);
+}
+
+// Both grids' axis for one coordinate.
+__device__ __forceinline__ void axis_pair(int assign, double pos, float pos_hi, float pos_lo,
+                                          float s_hi, float s_lo, double L, int ng, bool il,
+                                          Axis& a0, Axis& a1) {
+  int i;
+  float d;
+  a0 = plain_axis(assign, pos, pos_hi, pos_lo, s_hi, s_lo, L, ng, i, d);
   if (!il) {
     a1 = a0;
     return;
@@ -297,15 +306,39 @@ __device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs&
   return true;
 }
 
+// Key of a particle for the region gather, which takes every record of its
+// home tile (the tile of the plain grid's base node) from one bucket: class
+// 0 of that tile, from the plain grid alone.  The same tile as make_record's.
+__device__ __forceinline__ bool region_key(const Particle& q, const GatherArgs& g, unsigned& key) {
+  if (!q.ok) return false;
+  int tile[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    int i;
+    float d;
+    const Axis a0 = plain_axis(g.assign, q.aos ? q.pos[a] : (double)q.hi[a], q.hi[a], q.lo[a],
+                               g.s_hi[a], g.s_lo[a], g.box[a], g.ng, i, d);
+    tile[a] = a0.base / g.T;
+  }
+  key = (((unsigned)tile[0] * g.nt + tile[1]) * g.nt + tile[2]) * 27u;
+  return true;
+}
+
 __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ GatherArgs g, Particles p) {
   double ws = 0.0, wa = 0.0;
   int bad = 0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
        i += (size_t)gridDim.x * blockDim.x) {
     const Particle q = load_particle(p, g, i);
-    Rec r;
     unsigned key;
-    if (!make_record(q, g, r, key)) {
+    bool ok;
+    if (g.region) {
+      ok = region_key(q, g, key);
+    } else {
+      Rec r;
+      ok = make_record(q, g, r, key);
+    }
+    if (!ok) {
       bad = 1;
       g.rank[i] = 0xffffffffu;
       continue;
@@ -369,6 +402,7 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ GatherA
     Rec r;
     unsigned key;
     make_record(q, g, r, key);
+    if (g.region) key -= key % 27u;  // one bucket per home tile (region_key)
     const unsigned slot = g.hist[key] + rk;
     if (g.assign >= 2) {
       WRec v;
