@@ -127,6 +127,21 @@ __device__ __forceinline__ Axis make_axis(int assign, int i0, double d, int ng) 
   return a;
 }
 
+// The same from a float fraction (the fast path): d - 1 is exact for d in
+// [1/2, 1), so the parameter equals the FP64 form's.
+__device__ __forceinline__ Axis make_axis(int assign, int i0, float d, int ng) {
+  Axis a;
+  if (assign == 0 || assign == 2) {
+    const bool up = d >= 0.5f;
+    a.base = up ? ((i0 == ng - 1) ? 0 : i0 + 1) : i0;
+    a.par = up ? d - 1.f : d;
+  } else {
+    a.base = i0;
+    a.par = d;
+  }
+  return a;
+}
+
 __device__ __forceinline__ bool near_edge(float d) {
   return d < kEdge || d > 1.f - kEdge || fabsf(d - 0.5f) < kEdge;
 }
@@ -150,7 +165,7 @@ __device__ __forceinline__ Axis plain_axis(int assign, double pos, float pos_hi,
     exact_coord(pos, L, ng, false, i0, dd);
     return make_axis(assign, i0, dd, ng);
   }
-  return make_axis(assign, i, (double)d, ng);
+  return make_axis(assign, i, d, ng);
 }
 
 // Both grids' axis for one coordinate.
@@ -175,7 +190,7 @@ __device__ __forceinline__ void axis_pair(int assign, double pos, float pos_hi, 
     exact_coord(pos, L, ng, true, i0, dd);
     a1 = make_axis(assign, i0, dd, ng);
   } else {
-    a1 = make_axis(assign, i1, (double)d1, ng);
+    a1 = make_axis(assign, i1, d1, ng);
   }
 }
 
@@ -393,7 +408,7 @@ struct RegGeom {
   static constexpr int SM = (R * R * RZ + 1) & ~1;  // shared words per mesh
 };
 
-__global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ GatherArgs g, Particles p) {
+__global__ void __launch_bounds__(256, 4) k_scatter(const __grid_constant__ GatherArgs g, Particles p) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
        i += (size_t)gridDim.x * blockDim.x) {
     const unsigned rk = g.rank[i];
@@ -993,19 +1008,22 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
   };
   // Split path.  With q = 2^16 h + l (0 <= l < 2^16), H = sum h and
   // L = sum l: at most 65535 records put at most 65535 terms in a cell, so
-  // 0 <= L < 2^32 and L = (sum q - 2^16 H) mod 2^32; with the records'
-  // bounds summing below 2^46, H fits in int32.  The cell value is then
-  // 2^16 H + L exactly.  A tile past the bound sum is redone below.
-  bool split = end - beg <= 65535u;
+  // 0 <= L < 2^32 and L = (sum q - 2^16 H) mod 2^32.  A record whose node
+  // values are all below 2^31 (flag 0x100) adds |h| <= 2^15 to a cell; one
+  // with larger values adds |h| <= 2^(e - 16), e its bound exponent.  So
+  // |H| < 2^31 when n 2^31 + sum over the large records of 2^e < 2^47 (n
+  // records): then the cell value is 2^16 H + L exactly.  A tile past that
+  // bound is redone below.
+  const unsigned nrec = end - beg;
+  bool split = nrec <= 65535u;
   if (split) {
     zero();
     if (threadIdx.x < 2) bound_sum[threadIdx.x] = 0.f;
     __syncthreads();
-    float bsum = 0.f;
+    float bsum = 0.f;  // sum of 2^e over this lane's large-value records (exact: powers >= 2^31)
     const int lbase = (yy * RZ + zz) * NM + m;
     auto proc = [&](const Ld& cur) {
       if (!act) return;
-      bsum += __int_as_float((min(cur.bs.w & 0xff, 127) + 127) << 23);
       unsigned* A = w32 + lbase + cur.bs.x * NM;
       const float wyz = cur.wy * cur.wz;
       const float wxs[4] = {cur.wx.x, cur.wx.y, cur.wx.z, cur.wx.w};
@@ -1017,6 +1035,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
           atomicAdd(reinterpret_cast<int*>(A + HW) + x * R * RZ * NM, q >> 16);
         }
       } else {
+        bsum += __int_as_float((min(cur.bs.w & 0xff, 127) + 127) << 23);
 #pragma unroll
         for (int x = 0; x < S; x++) {
           const long long q = round_fix(wxs[x] * wyz);
@@ -1028,23 +1047,20 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     records(proc);
     if (lane == 0 || lane == 16) atomicAdd(&bound_sum[(NM == 2) ? half : 0], bsum);
     __syncthreads();
-    split = bound_sum[0] < 70368744177664.f && bound_sum[1] < 70368744177664.f;  // 2^46
+    const float room = 2147483648.f * (float)(65536u - nrec);  // 2^47 - n 2^31, exact
+    split = bound_sum[0] < room && bound_sum[1] < room;
     if (split) {
-      // one z row per warp and step, out as [NM][R][R][RG]
-      unsigned long long* o = g.regbuf + (size_t)tile * NM * RP;
-      int mm = 0, row = warp;  // this warp's row, advanced by nw rows a step
-      for (int rw = warp; rw < NM * R * R; rw += nw) {
-        if (lane < R) {
-          const int w = (row * RZ + lane) * NM + mm;
-          const int h = (int)w32[HW + w];
-          const unsigned l = w32[w] - ((unsigned)h << 16);
-          o[mm * RP + row * RG + lane] = (unsigned long long)(((long long)h << 16) + (long long)l);
-        }
-        row += nw;
-        if (row >= R * R) {
-          row -= R * R;
-          mm++;
-        }
+      // out as [R][R][RG][NM] (meshes interleaved): a pair of words per
+      // thread and step, one 16-byte store; the padding column z = R reads
+      // zeros
+      longlong2* o = reinterpret_cast<longlong2*>(g.regbuf + (size_t)tile * NM * RP);
+      constexpr int ROW = RG * NM;
+      for (int e = threadIdx.x; e < NM * RP / 2; e += blockDim.x) {
+        const int row = (2 * e) / ROW, w = row * RZ * NM + (2 * e - row * ROW);
+        const uint2 lo = *reinterpret_cast<const uint2*>(w32 + w);
+        const int2 hi = *reinterpret_cast<const int2*>(w32 + HW + w);
+        o[e] = make_longlong2(((long long)hi.x << 16) + (long long)(lo.x - ((unsigned)hi.x << 16)),
+                              ((long long)hi.y << 16) + (long long)(lo.y - ((unsigned)hi.y << 16)));
       }
       if (threadIdx.x == 0) g.regflag[tile] = 1;
       return;
@@ -1074,16 +1090,18 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     records(proc);
   }
   __syncthreads();
-  // out with z rows of RG words: [NM][R][R][RG]
-  unsigned long long* o = g.regbuf + (size_t)tile * NM * RP;
-  int mm = 0, row = warp;
-  for (int rw = warp; rw < NM * R * R; rw += nw) {
-    if (lane < R) o[mm * RP + row * RG + lane] = acc[mm * SM + row * RZ + lane];
-    row += nw;
-    if (row >= R * R) {
-      row -= R * R;
-      mm++;
+  // out as [R][R][RG][NM], as above
+  longlong2* o = reinterpret_cast<longlong2*>(g.regbuf + (size_t)tile * NM * RP);
+  constexpr int ROW = RG * NM;
+  for (int e = threadIdx.x; e < NM * RP / 2; e += blockDim.x) {
+    const int row = (2 * e) / ROW, rem = 2 * e - row * ROW;
+    long long v[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int c = (rem + j) / NM, mm = (rem + j) % NM;
+      v[j] = (long long)acc[mm * SM + row * RZ + c];
     }
+    o[e] = make_longlong2(v[0], v[1]);
   }
   if (threadIdx.x == 0) g.regflag[tile] = 1;
 }
@@ -1110,89 +1128,97 @@ __device__ __forceinline__ int region_sources(int c, int nt, int* t, int* idx) {
   return 1;
 }
 
-// Mesh from the regions: 8 consecutive z cells per thread, the FP32 value
-// minus the mean cell value (or the exact fixed-point sum).  The home
-// tile's 8 words are four 16-byte loads; a tile without records wrote
-// neither its region nor a flag of 1, and its words (loaded alongside the
-// flag) are dropped.
-template <int S, bool INT64>
-__global__ void __launch_bounds__(256, 4) k_region_sum(const __grid_constant__ GatherArgs g) {
+// Two consecutive cells of every mesh from a region row: words [c NM + m]
+// (cell-major, mesh-minor), one 32- or 16-byte load.
+template <int NM>
+__device__ __forceinline__ void load_pair(const unsigned long long* p, long long (&v)[2 * NM]) {
+  if constexpr (NM == 2) {
+    const longlong4_32a q = *reinterpret_cast<const longlong4_32a*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+  } else {
+    const longlong2 q = *reinterpret_cast<const longlong2*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+  }
+}
+
+// Mesh from the regions: a pair of consecutive z cells of every mesh per
+// thread (a warp reads 32 consecutive pairs: whole sectors), the FP32 value
+// minus the mean cell value (or the exact fixed-point sum).  Regions are
+// [R][R][RG][NM] words; a cell pair starts on an even region cell.  A tile
+// without records wrote neither its region nor a flag of 1, and its words
+// (loaded alongside the flag) are dropped.
+template <int S, int NM, bool INT64>
+__global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ GatherArgs g) {
   constexpr int T = kRegT, R = RegGeom<S>::R, RG = RegGeom<S>::RG, RP = RegGeom<S>::RP;
   constexpr int of = (S >= 3) ? -1 : 0;
-  static_assert((1 - of) % 2 == 0, "home block of z words starts on a 16-byte boundary");
-  const int ng = g.ng, nt = g.nt, nm = g.interlace ? 2 : 1, nq = ng >> 3;
-  const size_t per = (size_t)ng * ng * nq;
+  constexpr int NB = S + of;      // cells u < NB also take the tile before (cell u + T - of + 1)
+  constexpr int NA = T + of - 1;  // cells u >= NA also take the tile after (cell u - T - of + 1)
+  static_assert((1 - of) % 2 == 0 && RG % 2 == 0 && NA % 2 == 0,
+                "cell pairs start on even region cells; a pair never straddles NA");
+  static_assert(NB % 2 == 0 || (NB + T - of + 1 == R && RG > R),
+                "a pair straddling NB reads the padding column as its second cell");
+  const int ng = g.ng, nt = g.nt, nh = ng >> 1;
+  const size_t work = (size_t)ng * ng * nh;
   const long long off =
       (INT64 || g.nomean) ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < (size_t)nm * per;
+  const unsigned long long* const rb = g.regbuf;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < work;
        e += (size_t)gridDim.x * blockDim.x) {
-    const int m = (int)(e / per);
-    size_t r = e - (size_t)m * per;
-    const int zq = (int)(r % (size_t)nq);
-    r /= (size_t)nq;
+    const int zh = (int)(e % (size_t)nh);
+    const size_t r = e / (size_t)nh;
     const int y = (int)(r % (size_t)ng), x = (int)(r / (size_t)ng);
     int tx[2], ix[2], ty[2], iy[2];
     const int nx = region_sources<S>(x, nt, tx, ix), ny = region_sources<S>(y, nt, ty, iy);
-    const int z0 = 8 * zq, tz0 = z0 / T, uz = z0 - tz0 * T;  // uz = 0 or 8
-    const int tzp = (tz0 == 0) ? nt - 1 : tz0 - 1, tzn = (tz0 == nt - 1) ? 0 : tz0 + 1;
-    long long s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int z = 2 * zh, tz = z / T, uz = z - tz * T;  // uz even
+    // the second z source: the tile before for uz < NB (for PCS the pair
+    // (2, 3) reads its cells (R - 1, R): cell 3 gets the zero padding
+    // column), the tile after for uz >= NA
+    int tz2 = -1, cz2 = 0;
+    if (uz < NB) {
+      tz2 = (tz == 0) ? nt - 1 : tz - 1;
+      cz2 = uz + T - of + 1;
+    } else if (uz >= NA) {
+      tz2 = (tz == nt - 1) ? 0 : tz + 1;
+      cz2 = uz - T - of + 1;
+    }
+    long long s[2 * NM];
+#pragma unroll
+    for (int k = 0; k < 2 * NM; k++) s[k] = 0;
     for (int a = 0; a < nx; a++)
       for (int b = 0; b < ny; b++) {
         const unsigned tb = ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt;
         const int row = (ix[a] * R + iy[b]) * RG;
-        {
-          const unsigned t = tb + tz0;
-          const bool f = g.regflag[t] != 0;
-          const longlong2* p = reinterpret_cast<const longlong2*>(
-              g.regbuf + ((size_t)t * nm + m) * RP + row + uz - of + 1);
-          const longlong2 v0 = p[0], v1 = p[1], v2 = p[2], v3 = p[3];
-          if (f) {
-            s[0] += v0.x;
-            s[1] += v0.y;
-            s[2] += v1.x;
-            s[3] += v1.y;
-            s[4] += v2.x;
-            s[5] += v2.y;
-            s[6] += v3.x;
-            s[7] += v3.y;
-          }
+        const unsigned t0 = tb + tz;
+        const bool f0 = g.regflag[t0] != 0;
+        long long v0[2 * NM], v1[2 * NM];
+        load_pair<NM>(rb + ((size_t)t0 * RP + row + uz - of + 1) * NM, v0);
+        bool f1 = false;
+        if (tz2 >= 0) {
+          const unsigned t1 = tb + tz2;
+          f1 = g.regflag[t1] != 0;
+          load_pair<NM>(rb + ((size_t)t1 * RP + row + cz2) * NM, v1);
         }
-        if (uz == 0) {  // cells u < S + of: the tile before, words u + T - of + 1
-          const unsigned t = tb + tzp;
-          const bool f = g.regflag[t] != 0;
-          const unsigned long long* p = g.regbuf + ((size_t)t * nm + m) * RP + row + T - of + 1;
-          long long v[S + of];
+        if (f0) {
 #pragma unroll
-          for (int k = 0; k < S + of; k++) v[k] = (long long)p[k];
-          if (f) {
+          for (int k = 0; k < 2 * NM; k++) s[k] += v0[k];
+        }
+        if (f1) {
 #pragma unroll
-            for (int k = 0; k < S + of; k++) s[k] += v[k];
-          }
-        } else {  // cells u >= T + of - 1: the tile after, words u - T - of + 1
-          const unsigned t = tb + tzn;
-          const bool f = g.regflag[t] != 0;
-          constexpr int k0 = T + of - 1 - 8;
-          const unsigned long long* p = g.regbuf + ((size_t)t * nm + m) * RP + row;
-          long long v[8 - k0];
-#pragma unroll
-          for (int k = k0; k < 8; k++) v[k - k0] = (long long)p[8 + k - T - of + 1];
-          if (f) {
-#pragma unroll
-            for (int k = k0; k < 8; k++) s[k] += v[k - k0];
-          }
+          for (int k = 0; k < 2 * NM; k++) s[k] += v1[k];
         }
       }
-    const size_t cell = ((size_t)x * ng + y) * ng + z0;
-    if (INT64) {
-      longlong2* o = reinterpret_cast<longlong2*>(g.out64[m] + cell);
+    const size_t cell = ((size_t)x * ng + y) * ng + z;
 #pragma unroll
-      for (int k = 0; k < 4; k++) o[k] = make_longlong2(s[2 * k], s[2 * k + 1]);
-    } else {
-      float4* o = reinterpret_cast<float4*>(g.out[m] + cell);
-      o[0] = make_float4(fix_to_float(s[0] - off), fix_to_float(s[1] - off),
-                         fix_to_float(s[2] - off), fix_to_float(s[3] - off));
-      o[1] = make_float4(fix_to_float(s[4] - off), fix_to_float(s[5] - off),
-                         fix_to_float(s[6] - off), fix_to_float(s[7] - off));
+    for (int m = 0; m < NM; m++) {
+      if (INT64)
+        *reinterpret_cast<longlong2*>(g.out64[m] + cell) = make_longlong2(s[m], s[NM + m]);
+      else
+        *reinterpret_cast<float2*>(g.out[m] + cell) =
+            make_float2(fix_to_float(s[m] - off), fix_to_float(s[NM + m] - off));
     }
   }
 }
@@ -1255,8 +1281,9 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
     const dim3 ntile((unsigned)g.nt, (unsigned)g.nt, (unsigned)g.nt);
     const int nm = g.interlace ? 2 : 1;
     const size_t smem = gather_region_smem(g.assign, g.interlace);
-    const size_t work = (size_t)nm * g.ng * g.ng * (g.ng / 8);
-    const unsigned sblocks = (unsigned)((work + 255) / 256 < 152 * 16 ? (work + 255) / 256 : 152 * 16);
+    // two waves of the resident CTAs
+    const size_t work = (size_t)g.ng * g.ng * (g.ng / 2), cap = (size_t)152 * 12;
+    const unsigned sblocks = (unsigned)((work + 255) / 256 < cap ? (work + 255) / 256 : cap);
 #define PS_REGION(SS)                                                                          \
   if (nm == 2) {                                                                               \
     cudaFuncSetAttribute(k_gather_region<SS, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
@@ -1267,10 +1294,14 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
                          (int)smem);                                                           \
     k_gather_region<SS, 1><<<ntile, 512, smem, s>>>(g);                                        \
   }                                                                                            \
-  if (int64_out)                                                                               \
-    k_region_sum<SS, true><<<sblocks, 256, 0, s>>>(g);                                         \
+  if (int64_out && nm == 2)                                                                    \
+    k_region_sum<SS, 2, true><<<sblocks, 256, 0, s>>>(g);                                      \
+  else if (int64_out)                                                                          \
+    k_region_sum<SS, 1, true><<<sblocks, 256, 0, s>>>(g);                                      \
+  else if (nm == 2)                                                                            \
+    k_region_sum<SS, 2, false><<<sblocks, 256, 0, s>>>(g);                                     \
   else                                                                                         \
-    k_region_sum<SS, false><<<sblocks, 256, 0, s>>>(g);
+    k_region_sum<SS, 1, false><<<sblocks, 256, 0, s>>>(g);
     if (g.assign == 2) {
       PS_REGION(3)
     } else {

@@ -44,7 +44,7 @@ struct GatherArgs {
   unsigned sparse_max;     // tiles with at most this many records: lane groups, rows flagged;
                            // more: one record per warp (TSC/PCS)
   int region;              // 1: each record once, into its home tile's region (TSC/PCS, T = 16)
-  unsigned long long* regbuf;  // [tiles][meshes][gather_region_words()] region sums
+  unsigned long long* regbuf;  // [tiles][gather_region_words()][meshes] region sums
   unsigned char* regflag;      // [tiles] 1: the tile wrote its region (it has records)
   int nomean;                  // 1: FP32 meshes keep their mean (survey catalogues)
 };
