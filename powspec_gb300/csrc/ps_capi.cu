@@ -201,7 +201,7 @@ struct ps_gpu_ctx {
   std::vector<double> kmu;   // last execute's raw (k, |mu|) sums
   double* d_part = nullptr;
   double* d_sums = nullptr;
-  double* d_wsum = nullptr;  // [2 cats][2]
+  double* d_wsum = nullptr;  // [2 cats][2], then [2 cats] int64 mean cell values
   double* d_wpart = nullptr; // [2 * kAssignMaxBlocks]
   int* d_err = nullptr;      // [2 cats]
   double* h_out = nullptr;   // pinned: sums + wsum + err (+ Re F_l(0) [pole][cat])
@@ -558,10 +558,11 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   CU(dev_malloc(&c->d_hist, (c->nkeys + 1) * sizeof(unsigned)));
   CU(dev_malloc(&c->d_bsum, ((c->nkeys + 4095) / 4096 + 1) * sizeof(unsigned)));
   if ((rc = alloc_accum(c))) return rc;
-  CU(dev_malloc(&c->d_wsum, sizeof(double) * 4));
+  // [2 cats][2] sums, then [2 cats] mean cell values in fixed point (int64)
+  CU(dev_malloc(&c->d_wsum, sizeof(double) * 6));
   CU(dev_malloc(&c->d_wpart, sizeof(double) * 2 * kAssignMaxBlocks));
   CU(dev_malloc(&c->d_err, sizeof(int) * 4));
-  CU(cudaMemset(c->d_wsum, 0, sizeof(double) * 4));
+  CU(cudaMemset(c->d_wsum, 0, sizeof(double) * 6));
   CU(cudaMemset(c->d_err, 0, sizeof(int) * 4));
 
   // ---- geometry sweep: counts, mean |k|, multipole mode weights
@@ -701,6 +702,10 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat, size_t n) {
   g.nt = c->gnt;
   for (int d = 0; d < 3; d++) {
     g.box[d] = c->p.box[d];
+    // the reference's shifted-grid edges (src/genr_mesh.c), correctly rounded
+    const double half = 0.5 * c->p.box[d];
+    g.bmin[d] = 0.0 - half / (double)c->ng;
+    g.bmax[d] = g.bmin[d] + c->p.box[d];
     const double s = (double)c->ng / c->p.box[d];
     g.s_hi[d] = (float)s;
     g.s_lo[d] = (float)(s - (double)g.s_hi[d]);
@@ -716,6 +721,7 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat, size_t n) {
   g.rec = c->d_rec;
   for (int m = 0; m < c->mpc; m++) g.out[m] = (float*)c->grid[cat * c->mpc + m];
   g.wsum = c->d_wsum + 2 * cat;
+  g.moff = reinterpret_cast<long long*>(c->d_wsum + 4) + cat;
   g.wpart = c->d_wpart;
   g.err = c->d_err + cat;
   g.threads = c->gather_threads;

@@ -35,8 +35,12 @@ constexpr int kMeshPad = 8;  // words between the two meshes' accumulators (bank
 constexpr float kEdge = 4e-6f;
 
 // wsum[0..1] = sums of the per-block partials: lane l adds blocks l, l + 32,
-// ... in order, then a fixed shuffle tree (same order every run).
-__global__ void k_wsum(const double* __restrict__ wpart, int nblocks, double* wsum) {
+// ... in order, then a fixed shuffle tree (same order every run).  *moff =
+// the mean cell value in fixed point (0 with nomean), computed once here:
+// FP64 division is slow on this GPU, and the gather kernels' threads would
+// each repeat it.
+__global__ void k_wsum(const double* __restrict__ wpart, int nblocks, double* wsum,
+                       long long* moff, int ng, int nomean) {
   double t0 = 0, t1 = 0;
   for (int b = threadIdx.x; b < nblocks; b += 32) {
     t0 += wpart[2 * b];
@@ -50,6 +54,7 @@ __global__ void k_wsum(const double* __restrict__ wpart, int nblocks, double* ws
   if (threadIdx.x == 0) {
     wsum[0] = t0;
     wsum[1] = t1;
+    *moff = nomean ? 0 : __double2ll_rn(t0 * 4294967296.0 / ((double)ng * ng * ng));
   }
 }
 
@@ -98,12 +103,15 @@ __host__ __device__ inline int first_off(int assign) { return assign >= 2 ? -1 :
 __host__ __device__ inline int width(int assign) { return assign + 1; }
 
 // Exact reference grid coordinate (FP64, correctly rounded operations).
-__device__ __forceinline__ void exact_coord(double pos, double L, int ng, bool shift, int& i0,
-                                            double& d) {
-  double bmin = 0.0;
+// Shifted grid: its lower edge bmin = -(L / 2) / Ng and bmax = bmin + L,
+// computed on the host (loop-invariant FP64 divisions would otherwise be
+// hoisted into every thread's preamble).
+__device__ __forceinline__ void exact_coord(double pos, double L, int ng, bool shift, double bmin,
+                                            double bmax, int& i0, double& d) {
   if (shift) {
-    bmin = __dsub_rn(0.0, __ddiv_rn(__dmul_rn(0.5, L), (double)ng));
-    if (pos >= __dadd_rn(bmin, L)) pos = __dsub_rn(pos, L);
+    if (pos >= bmax) pos = __dsub_rn(pos, L);
+  } else {
+    bmin = 0.0;
   }
   const double x = __ddiv_rn(__dmul_rn(__dsub_rn(pos, bmin), (double)ng), L);
   i0 = (int)x;
@@ -148,7 +156,10 @@ __device__ __forceinline__ bool near_edge(float d) {
 
 // The plain grid's axis for one coordinate; i, d: the double-float cell and
 // fraction it started from.  pos_hi + pos_lo = pos; s_hi + s_lo = Ng / L.
-__device__ __forceinline__ Axis plain_axis(int assign, double pos, float pos_hi, float pos_lo,
+// pos() gives the FP64 coordinate, asked for only on the exact path (FP64
+// conversions run on this GPU's narrow FP64 pipe).
+template <class Pos>
+__device__ __forceinline__ Axis plain_axis(int assign, Pos pos, float pos_hi, float pos_lo,
                                            float s_hi, float s_lo, double L, int ng, int& i,
                                            float& d) {
   // x = pos * s in double-float: p + t
@@ -162,16 +173,17 @@ __device__ __forceinline__ Axis plain_axis(int assign, double pos, float pos_hi,
   if (near_edge(d) || i < 0 || i >= ng) {
     int i0;
     double dd;
-    exact_coord(pos, L, ng, false, i0, dd);
+    exact_coord(pos(), L, ng, false, 0.0, 0.0, i0, dd);
     return make_axis(assign, i0, dd, ng);
   }
   return make_axis(assign, i, d, ng);
 }
 
 // Both grids' axis for one coordinate.
-__device__ __forceinline__ void axis_pair(int assign, double pos, float pos_hi, float pos_lo,
-                                          float s_hi, float s_lo, double L, int ng, bool il,
-                                          Axis& a0, Axis& a1) {
+template <class Pos>
+__device__ __forceinline__ void axis_pair(int assign, Pos pos, float pos_hi, float pos_lo,
+                                          float s_hi, float s_lo, double L, double bmin,
+                                          double bmax, int ng, bool il, Axis& a0, Axis& a1) {
   int i;
   float d;
   a0 = plain_axis(assign, pos, pos_hi, pos_lo, s_hi, s_lo, L, ng, i, d);
@@ -187,7 +199,7 @@ __device__ __forceinline__ void axis_pair(int assign, double pos, float pos_hi, 
   if (near_edge(d1) || near_edge(d) || i1 < 0 || i1 >= ng) {
     int i0;
     double dd;
-    exact_coord(pos, L, ng, true, i0, dd);
+    exact_coord(pos(), L, ng, true, bmin, bmax, i0, dd);
     a1 = make_axis(assign, i0, dd, ng);
   } else {
     a1 = make_axis(assign, i1, d1, ng);
@@ -218,9 +230,35 @@ __device__ __forceinline__ void node_weights(float par, float (&w)[4]) {
   }
 }
 
-// 2^k as a float (0 below the normal range).
+// 2^k as a float (0 below the normal range, infinity above it).
 __device__ __forceinline__ float exp2i(int k) {
-  return k < -126 ? 0.f : __int_as_float((k + 127) << 23);
+  return k < -126 ? 0.f : (k > 127 ? __int_as_float(0x7f800000) : __int_as_float((k + 127) << 23));
+}
+
+// round-to-nearest-even of m 2^sh as an integer (m >= 0, m < 2^53, sh <=
+// 10), integer operations only; negated if neg.
+__device__ __forceinline__ long long round_shift(long long m, int sh, bool neg) {
+  long long r;
+  if (sh >= 0) {
+    r = m << min(sh, 10);
+  } else if (sh < -53) {
+    r = 0;  // m 2^sh < 1/2
+  } else {
+    const int t = -sh;
+    r = m >> t;
+    const long long rem = m & ((1LL << t) - 1), half = 1LL << (t - 1);
+    if (rem > half || (rem == half && (r & 1))) r++;
+  }
+  return neg ? -r : r;
+}
+
+// llrint(w 2^32) from the bits of the double w (|w| < 2^31, which the
+// total-weight limit checked on the host implies): equals
+// __double2ll_rn(w * 4294967296.0), without FP64 arithmetic.
+__device__ __forceinline__ long long fix_from_bits(long long b) {
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0) return 0;  // zero or subnormal: |w| 2^32 < 2^-990
+  return round_shift((b & 0xfffffffffffffLL) | 0x10000000000000LL, e - 1043, b < 0);
 }
 
 // Non-negative double (bit pattern b) as hi + lo floats with integer
@@ -245,10 +283,13 @@ __device__ __forceinline__ void split_pos(long long b, float& hi, float& lo) {
 struct Particle {
   double pos[3];     // AoS input: the coordinates as given (exact path only)
   float hi[3], lo[3];
-  double w;
+  float wh, wl;      // weight = wh + wl (FP64 input: to about 2^-48 relative)
+  long long wbits;   // the weight as FP64 bits (NGP node value)
   float wf;          // weight as float
   bool ok;           // inside [0, L) on every axis
   bool aos;          // FP64 input (pos holds the coordinates)
+  // the FP64 coordinate of axis a, for the exact path
+  __device__ __forceinline__ double exact(int a) const { return aos ? pos[a] : (double)hi[a]; }
 };
 
 __device__ __forceinline__ Particle load_particle(const Particles& p, const GatherArgs& g, size_t i) {
@@ -268,10 +309,13 @@ __device__ __forceinline__ Particle load_particle(const Particles& p, const Gath
       if (b < 0 || b >= g.box_bits[a]) q.ok = false;
       split_pos(b, q.hi[a], q.lo[a]);
     }
-    q.w = r.w;
     const long long wb = __double_as_longlong(r.w);
     float wh, wl;
     split_pos(wb & 0x7fffffffffffffffLL, wh, wl);
+    if (((wb >> 52) & 0x7ff) == 0x7ff) wh = __int_as_float(0x7fc00000);  // inf, NaN: NaN sums
+    q.wh = (wb < 0) ? -wh : wh;
+    q.wl = (wb < 0) ? -wl : wl;
+    q.wbits = wb;
     q.wf = (wb < 0) ? -(wh + wl) : (wh + wl);
   } else {
     const float v[3] = {p.x[i], p.y[i], p.z[i]};
@@ -283,7 +327,13 @@ __device__ __forceinline__ Particle load_particle(const Particles& p, const Gath
       if (!(v[a] >= 0.f && v[a] < g.box_f[a])) q.ok = false;  // box_f: smallest float >= L
     }
     q.wf = p.w ? p.w[i] : 1.f;
-    q.w = (double)q.wf;
+    q.wh = q.wf;
+    q.wl = 0.f;
+    // the float's value as FP64 bits (zero for subnormals, whose node value
+    // rounds to 0 anyway)
+    const unsigned fb = __float_as_uint(q.wf), ef = (fb >> 23) & 0xff;
+    q.wbits = (long long)((unsigned long long)(fb >> 31) << 63) |
+              (ef ? ((long long)(ef + 1023 - 127) << 52) | ((long long)(fb & 0x7fffff) << 29) : 0);
   }
   return q;
 }
@@ -296,8 +346,8 @@ __device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs&
   if (!q.ok) return false;
   for (int a = 0; a < 3; a++) {
     Axis a0, a1;
-    axis_pair(g.assign, q.aos ? q.pos[a] : (double)q.hi[a], q.hi[a], q.lo[a], g.s_hi[a], g.s_lo[a],
-              g.box[a], ng, g.interlace != 0, a0, a1);
+    axis_pair(g.assign, [&] { return q.exact(a); }, q.hi[a], q.lo[a], g.s_hi[a], g.s_lo[a],
+              g.box[a], g.bmin[a], g.bmax[a], ng, g.interlace != 0, a0, a1);
     r.base[0][a] = (short)a0.base;
     r.base[1][a] = (short)a1.base;
     r.par[0][a] = a0.par;
@@ -315,7 +365,7 @@ __device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs&
     cls[a] = (lo_r < 0) ? 1 : ((hi_r >= g.T) ? 2 : 0);
   }
   r.wf = q.wf * kFixScale;
-  r.q = (g.assign == 0) ? __double2ll_rn(q.w * 4294967296.0) : 0;  // NGP node value only
+  r.q = (g.assign == 0) ? fix_from_bits(q.wbits) : 0;  // NGP node value only
   const unsigned t = ((unsigned)tile[0] * g.nt + tile[1]) * g.nt + tile[2];
   key = t * 27u + (unsigned)(cls[0] + 3 * cls[1] + 9 * cls[2]);
   return true;
@@ -331,7 +381,7 @@ __device__ __forceinline__ bool region_key(const Particle& q, const GatherArgs& 
   for (int a = 0; a < 3; a++) {
     int i;
     float d;
-    const Axis a0 = plain_axis(g.assign, q.aos ? q.pos[a] : (double)q.hi[a], q.hi[a], q.lo[a],
+    const Axis a0 = plain_axis(g.assign, [&] { return q.exact(a); }, q.hi[a], q.lo[a],
                                g.s_hi[a], g.s_lo[a], g.box[a], g.ng, i, d);
     tile[a] = a0.base / g.T;
   }
@@ -339,8 +389,22 @@ __device__ __forceinline__ bool region_key(const Particle& q, const GatherArgs& 
   return true;
 }
 
+// s += a + b as an unevaluated FP32 pair (hi, lo), renormalised after
+// each add: TwoSum of hi and a (exact), the low parts added, then hi + lo
+// recombined (Fast2Sum).  Each add loses about 2^-48 of the running sum.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float a, float b) {
+  const float t = hi + a, bp = t - hi;
+  const float err = (hi - (t - bp)) + (a - bp);
+  const float l = lo + err + b;
+  hi = t + l;
+  lo = l - (hi - t);
+}
+
 __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ GatherArgs g, Particles p) {
-  double ws = 0.0, wa = 0.0;
+  // weight sums: the signed one as an FP32 pair (the per-particle FP64 add
+  // would load this GPU's narrow FP64 pipe), |w| in FP32 (only compared
+  // against limits)
+  float ws_hi = 0.f, ws_lo = 0.f, waf = 0.f;
   int bad = 0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -358,8 +422,8 @@ __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ Gather
       g.rank[i] = 0xffffffffu;
       continue;
     }
-    ws += q.w;
-    wa += fabs(q.w);
+    df_add(ws_hi, ws_lo, q.wh, q.wl);
+    waf += fabsf(q.wh + q.wl);
     // Rank within the key, aggregated over the lanes of this warp that share
     // it (catalogues are often spatially ordered: whole warps hit one key).
     const unsigned peers = __match_any_sync(__activemask(), key);
@@ -369,25 +433,29 @@ __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ Gather
     base = __shfl_sync(peers, base, leader);
     g.rank[i] = base + __popc(peers & ((1u << lane) - 1u));
   }
+  // block partials, still as FP32 pairs (FP64 once per block)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    ws += __shfl_down_sync(0xffffffffu, ws, o);
-    wa += __shfl_down_sync(0xffffffffu, wa, o);
+    const float oh = __shfl_down_sync(0xffffffffu, ws_hi, o);
+    const float ol = __shfl_down_sync(0xffffffffu, ws_lo, o);
+    waf += __shfl_down_sync(0xffffffffu, waf, o);
+    df_add(ws_hi, ws_lo, oh, ol);
   }
-  __shared__ double sws[8], swa[8];
+  __shared__ float sws[8][2], swa[8];
   if ((threadIdx.x & 31) == 0) {
-    sws[threadIdx.x >> 5] = ws;
-    swa[threadIdx.x >> 5] = wa;
+    sws[threadIdx.x >> 5][0] = ws_hi;
+    sws[threadIdx.x >> 5][1] = ws_lo;
+    swa[threadIdx.x >> 5] = waf;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t0 = 0, t1 = 0;
+    float th = 0.f, tl = 0.f, ta = 0.f;
     for (int k = 0; k < 8; k++) {
-      t0 += sws[k];
-      t1 += swa[k];
+      df_add(th, tl, sws[k][0], sws[k][1]);
+      ta += swa[k];
     }
-    g.wpart[2 * blockIdx.x] = t0;
-    g.wpart[2 * blockIdx.x + 1] = t1;
+    g.wpart[2 * blockIdx.x] = (double)th + (double)tl;
+    g.wpart[2 * blockIdx.x + 1] = (double)ta;
   }
   if (bad) atomicOr(g.err, 1);
 }
@@ -408,69 +476,102 @@ struct RegGeom {
   static constexpr int SM = (R * R * RZ + 1) & ~1;  // shared words per mesh
 };
 
-__global__ void __launch_bounds__(256, 4) k_scatter(const __grid_constant__ GatherArgs g, Particles p) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const unsigned rk = g.rank[i];
-    if (rk == 0xffffffffu) continue;
-    const Particle q = load_particle(p, g, i);
-    Rec r;
-    unsigned key;
-    make_record(q, g, r, key);
-    if (g.region) key -= key % 27u;  // one bucket per home tile (region_key)
-    const unsigned slot = g.hist[key] + rk;
-    if (g.assign >= 2) {
-      WRec v;
+// Gather record of a TSC/PCS particle: the node weights of both meshes per
+// axis (weight * 2^32 folded into x), the region word offset and the node
+// value bound.
+__device__ __forceinline__ WRec weighted_record(const Rec& r, const GatherArgs& g) {
+  WRec v;
 #pragma unroll
-      for (int m = 0; m < 2; m++) {
+  for (int m = 0; m < 2; m++) {
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-          float w[4];
-          if (g.assign == 2) {
-            node_weights<3>(r.par[m][a], w);
-            w[3] = 0.f;
-          } else {
-            node_weights<4>(r.par[m][a], w);
-          }
-#pragma unroll
-          for (int k = 0; k < 4; k++) v.w[m][a][k] = (a == 0) ? w[k] * r.wf : w[k];
-          v.base[m][a] = r.base[m][a];
-        }
-        if (g.region) {
-          // Region word offset of the first node: region index = base -
-          // home tile origin + 1 per axis, wrapped into [0, T + 1] (the
-          // shifted grid's base may sit one cell outside the home tile,
-          // across the periodic edge).
-          int l[3];
-#pragma unroll
-          for (int a = 0; a < 3; a++) {
-            l[a] = (int)r.base[m][a] - ((int)r.base[0][a] / g.T) * g.T + 1;
-            l[a] += (l[a] < 0) ? g.ng : 0;
-            l[a] -= (l[a] > g.T + 1) ? g.ng : 0;
-            if (l[a] < 0 || l[a] > g.T + 1) {  // the grids' bases differ by at most a cell
-              atomicOr(g.err, 2);
-              l[a] = 0;
-            }
-          }
-          const int R = (g.assign == 2) ? RegGeom<3>::R : RegGeom<4>::R;
-          const int RZ = (g.assign == 2) ? RegGeom<3>::RZ : RegGeom<4>::RZ;
-          v.base[m][0] = (short)((l[0] * R + l[1]) * RZ + l[2]);
-          v.base[m][1] = v.base[m][2] = 0;
-        }
-        // bound of every node value of this mesh: product of the axis maxima
-        float bound = 1.f;
-#pragma unroll
-        for (int a = 0; a < 3; a++)
-          bound *= fmaxf(fmaxf(fabsf(v.w[m][a][0]), fabsf(v.w[m][a][1])),
-                         fmaxf(fabsf(v.w[m][a][2]), fabsf(v.w[m][a][3])));
-        // [mesh][3]: bit 8 set when every node value is below 2^31 (one
-        // 32-bit conversion); bits 0-7 the least e >= 0 with bound < 2^e
-        const int e = max(0, ((__float_as_int(bound) >> 23) & 0xff) - 126);
-        v.base[m][3] = (short)((bound < 0.999f * 2147483648.f ? 0x100 : 0) | min(e, 255));
+    for (int a = 0; a < 3; a++) {
+      float w[4];
+      if (g.assign == 2) {
+        node_weights<3>(r.par[m][a], w);
+        w[3] = 0.f;
+      } else {
+        node_weights<4>(r.par[m][a], w);
       }
-      reinterpret_cast<WRec*>(g.rec)[slot] = v;
-    } else {
-      reinterpret_cast<Rec*>(g.rec)[slot] = r;
+#pragma unroll
+      for (int k = 0; k < 4; k++) v.w[m][a][k] = (a == 0) ? w[k] * r.wf : w[k];
+      v.base[m][a] = r.base[m][a];
+    }
+    if (g.region) {
+      // Region word offset of the first node: region index = base -
+      // home tile origin + 1 per axis, wrapped into [0, T + 1] (the
+      // shifted grid's base may sit one cell outside the home tile,
+      // across the periodic edge).
+      int l[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        l[a] = (int)r.base[m][a] - ((int)r.base[0][a] / g.T) * g.T + 1;
+        l[a] += (l[a] < 0) ? g.ng : 0;
+        l[a] -= (l[a] > g.T + 1) ? g.ng : 0;
+        if (l[a] < 0 || l[a] > g.T + 1) {  // the grids' bases differ by at most a cell
+          atomicOr(g.err, 2);
+          l[a] = 0;
+        }
+      }
+      const int R = (g.assign == 2) ? RegGeom<3>::R : RegGeom<4>::R;
+      const int RZ = (g.assign == 2) ? RegGeom<3>::RZ : RegGeom<4>::RZ;
+      v.base[m][0] = (short)((l[0] * R + l[1]) * RZ + l[2]);
+      v.base[m][1] = v.base[m][2] = 0;
+    }
+    // bound of every node value of this mesh: product of the axis maxima
+    float bound = 1.f;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+      bound *= fmaxf(fmaxf(fabsf(v.w[m][a][0]), fabsf(v.w[m][a][1])),
+                     fmaxf(fabsf(v.w[m][a][2]), fabsf(v.w[m][a][3])));
+    // [mesh][3]: bit 8 set when every node value is below 2^31 (one
+    // 32-bit conversion); bits 0-7 the least e >= 0 with bound < 2^e
+    const int e = max(0, ((__float_as_int(bound) >> 23) & 0xff) - 126);
+    v.base[m][3] = (short)((bound < 0.999f * 2147483648.f ? 0x100 : 0) | min(e, 255));
+    if (g.region) v.base[m][1] = v.base[m][3];  // (offset, flags): one 32-bit read
+  }
+  return v;
+}
+
+// Records to their slots.  TSC/PCS: a warp's 32 records are staged in shared
+// memory and written 4 at a time by 28 lanes, 7 x 16 bytes each, so that a
+// record's 112 bytes leave as one contiguous run (and a run of consecutive
+// slots, as spatially ordered catalogues give, as whole sectors).
+constexpr int kScatterWarps = 8;
+__global__ void __launch_bounds__(32 * kScatterWarps, 4) k_scatter(const __grid_constant__ GatherArgs g,
+                                                                   Particles p) {
+  __shared__ __align__(16) WRec stage[kScatterWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const size_t step = (size_t)gridDim.x * kScatterWarps * 32;
+  for (size_t base = ((size_t)blockIdx.x * kScatterWarps + w) * 32; base < p.n; base += step) {
+    const size_t i = base + lane;
+    const unsigned rk = (i < p.n) ? g.rank[i] : 0xffffffffu;
+    const bool valid = rk != 0xffffffffu;
+    unsigned slot = 0;
+    if (valid) {
+      const Particle q = load_particle(p, g, i);
+      Rec r;
+      unsigned key;
+      make_record(q, g, r, key);
+      if (g.region) key -= key % 27u;  // one bucket per home tile (region_key)
+      slot = g.hist[key] + rk;
+      if (g.assign >= 2)
+        stage[w][lane] = weighted_record(r, g);
+      else
+        reinterpret_cast<Rec*>(g.rec)[slot] = r;
+    }
+    if (g.assign >= 2) {
+      __syncwarp();
+      const int jr = lane / 7, part = lane - 7 * jr;
+#pragma unroll
+      for (int it = 0; it < 8; it++) {
+        const int j = (it * 4 + jr) & 31;  // lanes 28-31 idle
+        const unsigned sj = __shfl_sync(0xffffffffu, slot, j);
+        const bool vj = __shfl_sync(0xffffffffu, valid ? 1 : 0, j) != 0;
+        if (lane < 28 && vj)
+          reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(g.rec) + (size_t)sj * sizeof(WRec))[part] =
+              reinterpret_cast<const uint4*>(&stage[w][j])[part];
+      }
+      __syncwarp();  // the stage is rewritten next step
     }
   }
 }
@@ -854,8 +955,7 @@ __global__ void __launch_bounds__(kGatherThreads, 3) k_gather(const __grid_const
   }
   __syncthreads();
   // write the tile: rows of T cells along z
-  const long long off =
-      (INT64 || g.nomean) ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
+  const long long off = INT64 ? 0 : *g.moff;  // mean cell value (k_wsum)
   if constexpr (TT == 16) {
     // 4 consecutive z cells per thread and step; untouched rows are -mean
     const float cst = fix_to_float(-off);
@@ -958,7 +1058,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
   struct Ld {
     float4 wx;
     float wy, wz;
-    short4 bs;
+    short2 bs;  // region word offset, flags
   };
   // This warp's records, in stages of 4 consecutive ones (with one mesh
   // the half-warps take alternate records), two stages in flight: a stage
@@ -985,17 +1085,24 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
       cp_async_wait<1>();
       __syncwarp();  // every lane's part of stage k has landed
       const unsigned i0 = w0 + k * step;
+      const unsigned char* const slot = ring + (k & 1) * Q * sizeof(WRec);
+      auto one = [&](int j) {
+        const unsigned char* rp = slot + j * sizeof(WRec);
+        Ld L;
+        L.wx = *reinterpret_cast<const float4*>(rp + m * 48);
+        L.wy = *reinterpret_cast<const float*>(rp + m * 48 + 16 + yy * 4);
+        L.wz = *reinterpret_cast<const float*>(rp + m * 48 + 32 + zz * 4);
+        L.bs = *reinterpret_cast<const short2*>(rp + 96 + m * 8);
+        proc(L);
+      };
+      if (i0 + Q <= end) {  // a full stage
 #pragma unroll
-      for (int jj = 0; jj < ((NM == 2) ? Q : Q / 2); jj++) {
-        const int j = (NM == 2) ? jj : 2 * jj + half;
-        if (i0 + (unsigned)j < end) {
-          const unsigned char* rp = ring + ((k & 1) * Q + j) * sizeof(WRec);
-          Ld L;
-          L.wx = *reinterpret_cast<const float4*>(rp + m * 48);
-          L.wy = *reinterpret_cast<const float*>(rp + m * 48 + 16 + yy * 4);
-          L.wz = *reinterpret_cast<const float*>(rp + m * 48 + 32 + zz * 4);
-          L.bs = *reinterpret_cast<const short4*>(rp + 96 + m * 8);
-          proc(L);
+        for (int jj = 0; jj < ((NM == 2) ? Q : Q / 2); jj++) one((NM == 2) ? jj : 2 * jj + half);
+      } else {
+#pragma unroll
+        for (int jj = 0; jj < ((NM == 2) ? Q : Q / 2); jj++) {
+          const int j = (NM == 2) ? jj : 2 * jj + half;
+          if (i0 + (unsigned)j < end) one(j);
         }
       }
     }
@@ -1027,7 +1134,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
       unsigned* A = w32 + lbase + cur.bs.x * NM;
       const float wyz = cur.wy * cur.wz;
       const float wxs[4] = {cur.wx.x, cur.wx.y, cur.wx.z, cur.wx.w};
-      if (cur.bs.w & 0x100) {
+      if (cur.bs.y & 0x100) {
 #pragma unroll
         for (int x = 0; x < S; x++) {
           const int q = __float2int_rn(wxs[x] * wyz);
@@ -1035,7 +1142,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
           atomicAdd(reinterpret_cast<int*>(A + HW) + x * R * RZ * NM, q >> 16);
         }
       } else {
-        bsum += __int_as_float((min(cur.bs.w & 0xff, 127) + 127) << 23);
+        bsum += __int_as_float((min(cur.bs.y & 0xff, 127) + 127) << 23);
 #pragma unroll
         for (int x = 0; x < S; x++) {
           const long long q = round_fix(wxs[x] * wyz);
@@ -1077,7 +1184,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
       unsigned long long* A = acc + lofs + cur.bs.x;
       const float wyz = cur.wy * cur.wz;
       const float wxs[4] = {cur.wx.x, cur.wx.y, cur.wx.z, cur.wx.w};
-      if (cur.bs.w & 0x100) {
+      if (cur.bs.y & 0x100) {
 #pragma unroll
         for (int x = 0; x < S; x++)
           atomicAdd(A + x * R * RZ, (unsigned long long)round_small(wxs[x] * wyz));
@@ -1163,8 +1270,7 @@ __global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ Gath
                 "a pair straddling NB reads the padding column as its second cell");
   const int ng = g.ng, nt = g.nt, nh = ng >> 1;
   const size_t work = (size_t)ng * ng * nh;
-  const long long off =
-      (INT64 || g.nomean) ? 0 : __double2ll_rn(*g.wsum * 4294967296.0 / ((double)ng * ng * ng));
+  const long long off = INT64 ? 0 : *g.moff;  // mean cell value (k_wsum)
   const unsigned long long* const rb = g.regbuf;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < work;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -1267,14 +1373,14 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
     if (blocks < 1) blocks = 1;
     k_classify<<<(unsigned)blocks, 256, 0, s>>>(g, p);
     n++;
-    k_wsum<<<1, 32, 0, s>>>(g.wpart, (int)blocks, g.wsum);
+    k_wsum<<<1, 32, 0, s>>>(g.wpart, (int)blocks, g.wsum, g.moff, g.ng, g.nomean);
     n++;
     const int nb = (int)((nkeys + kScanBlock - 1) / kScanBlock);
     k_scan_reduce<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum);
     k_scan_blocks<<<1, 256, 0, s>>>(g.bsum, nb);
     k_scan_apply<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum, nb);
     n += 3;
-    k_scatter<<<(unsigned)blocks, 256, 0, s>>>(g, p);
+    k_scatter<<<(unsigned)blocks, 32 * kScatterWarps, 0, s>>>(g, p);
     n++;
   }
   if (g.region) {

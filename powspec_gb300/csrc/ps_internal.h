@@ -28,6 +28,7 @@ struct GatherArgs {
   int ng, assign, interlace;
   int T, nt;               // tile edge (cells) and tiles per axis
   double box[3];
+  double bmin[3], bmax[3]; // shifted grid's edges: -(L / 2) / Ng and that + L (FP64)
   float s_hi[3], s_lo[3];  // Ng / L as a double-float pair per axis
   long long box_bits[3];   // bit pattern of L (AoS FP64 bound check)
   float box_f[3];          // smallest float >= L (SoA FP32 bound check)
@@ -38,6 +39,7 @@ struct GatherArgs {
   float* out[2];           // FP32 meshes minus the mean cell value
   long long* out64[2];     // or exact fixed-point meshes (diagnostics)
   double* wsum;            // [2]
+  long long* moff;         // mean cell value in fixed point (0 with nomean), set by k_wsum
   double* wpart;           // [2 * kAssignMaxBlocks]
   int* err;                // bit 0: particle outside [0, L); bit 1: region index out of range
   int threads;             // CTA size of the gather: 256, 512 or 0 (by density)
