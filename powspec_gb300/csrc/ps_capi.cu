@@ -160,6 +160,7 @@ struct ps_gpu_ctx {
   float2* d_twl_half = nullptr;
   float2* d_twl_full = nullptr;
   int grid_cw = 0;
+  int wpc_cw = 4;  // warps per CTA of the warp x pass
   int nmu = 1;               // |mu| sub-bins of the binning pass
   // tile assignment
   int gT = 0, gnt = 0;
@@ -321,14 +322,26 @@ int plan_pass_c(ps_gpu_ctx* c) {
     }
   }
   // warp x pass: as many persistent CTAs per SM as shared memory and 2048
-  // threads allow
+  // threads allow, of the CTA size (4 warps, or 16 sharing the tile sums:
+  // one spectrum of the poles 0, 2, 4 at Ng = 256) that keeps the most warps resident
+  // (the smaller on a tie).  16-warp CTAs are built for two per SM (64
+  // registers a thread).
   c->grid_cw = 0;
+  c->wpc_cw = 4;
   if (c->d_twl_full) {
-    const size_t smw = pass_c_w_smem(ng, c->nfield, nacc, nkey);
-    if (smw && smw <= 227 * 1024) {
+    const bool big_ok = ng == 256 && c->nspec == 1 && pass_c_moments(c->p.poles, c->p.npole) == 3;
+    int best = 0;
+    for (int wpc : {4, 16}) {
+      if (wpc == 16 && !big_ok) continue;
+      const size_t smw = pass_c_w_smem(ng, c->nfield, nacc, nkey, wpc);
+      if (!smw || smw > 227 * 1024) continue;
       int per = std::max(1, (int)((228 * 1024) / (smw + 1024)));
-      per = std::min(per, 2048 / pass_c_w_threads());
-      c->grid_cw = c->nsm * per;
+      per = std::min(per, wpc == 16 ? 2 : 2048 / (32 * wpc));
+      if (per * wpc > best) {
+        best = per * wpc;
+        c->wpc_cw = wpc;
+        c->grid_cw = c->nsm * per;
+      }
     }
   }
   return 0;
@@ -844,6 +857,7 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
   pc.pipe = pipe_c ? 1 : 0;
   pc.mom = pass_c_moments(p.poles, p.npole);
   pc.twl = warp_c ? c->d_twl_full : nullptr;
+  pc.wpc = c->wpc_cw;
   pc.stall = c->stall ? 1 : 0;
   pc.wait_limit = c->stall;
   c->stall = 0;  // one evaluation only

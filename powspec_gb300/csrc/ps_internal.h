@@ -172,6 +172,7 @@ struct PassCArgs {
   int pipe;                     // power-of-two Ng: the cp.async.bulk-pipelined kernel
   int mom;                      // 0: pole sums; 2..4: mu^2 moments (even poles, lmax = 2 (mom - 1))
   const float2* twl;            // bin mode, non-NULL: the warp transform (ps_wfft.cu)
+  int wpc;                      // warp x pass: warps per CTA (4, 8 or 16)
   int* err;                     // bit 1: a pipeline wait timed out
   // test hook (ps_gpu_debug_stall_pipeline): CTA 0 of a pipelined kernel
   // arms its second copy but issues none, and every wait gives up after
@@ -202,8 +203,7 @@ int launch_pass_a_w(const PassAArgs& a, cudaStream_t s);  // 0: shape not suppor
 int launch_pass_b_w(const PassBArgs& a, cudaStream_t s);
 int launch_pass_c_w(const PassCArgs& a, cudaStream_t s);
 // Dynamic shared memory and block size of the warp x pass (persistent CTAs).
-size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey);
-int pass_c_w_threads();
+size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey, int wpc);
 
 // Binning of standard-layout half-complex fields [x][y][kz].
 struct BinFieldArgs {

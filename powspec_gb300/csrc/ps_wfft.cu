@@ -190,26 +190,31 @@ __host__ __device__ constexpr int wc_warp_elems(int nfield) {
           1) &
          ~1;
 }
-constexpr int kWarpsC = 4;  // warps per CTA of the x pass
+constexpr int kMaxWarpsC = 16;  // warps per CTA of the x pass: 4 or 16 (host's choice)
 
 // x transform + combine + window + binning.  A work item of a warp is NP
 // consecutive ky at one kz (NP > 1 when a transform holds more lines than
 // there are fields); every CTA step gives one item to each warp, and the
-// tile sums are merged into the CTA's FP64 partials every kMergeEvery steps.
-template <int N, int NSPEC, int MOM>
-__global__ void __launch_bounds__(32 * kWarpsC) k_pass_c_w(const __grid_constant__ PassCArgs a) {
+// tile sums are merged into the CTA's FP64 partials every kMergeEvery steps
+// of 4 warps' items (fewer steps with more warps).  Large tile sums (|mu|
+// sub-bins) take the CTA's shared memory: then 8 or 16 warps share them, so
+// that more warps are resident.
+template <int N, int NSPEC, int MOM, int WPC>
+__global__ void __launch_bounds__(32 * WPC, WPC == 4 ? 0 : 2) k_pass_c_w(const __grid_constant__ PassCArgs a) {
   using S = WF<N>;
   constexpr int LS = wc_line<N>();
   extern __shared__ __align__(16) float2 wsm[];
   __shared__ int srange[2];
+  constexpr int nwc = WPC;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int g = lane / S::L, l = lane - g * S::L;
   const int nfield = a.nfield;
+  constexpr int merge_every = (kMergeEvery * 4 / WPC > 1) ? kMergeEvery * 4 / WPC : 1;
   const int NP = wc_np<N>(nfield);
   const int nline = NP * nfield;
   const int wel = wc_warp_elems<N>(nfield);
   float2* X = wsm + w * wel;  // this warp's lines [field][pos][LS]
-  float* tacc = reinterpret_cast<float*>(wsm + kWarpsC * wel);
+  float* tacc = reinterpret_cast<float*>(wsm + nwc * wel);
   const ModeGeom& gm = a.geom;
   const int nacc = NSPEC * gm.npole;
   const int nkey = gm.nbin * gm.nmu;
@@ -221,10 +226,10 @@ __global__ void __launch_bounds__(32 * kWarpsC) k_pass_c_w(const __grid_constant
   }
   __syncthreads();
   const int nitem = (N / 2 + 1) * (N / NP);  // (kz, ky0) with ky0 a multiple of NP
-  const int nstep = (nitem + (int)gridDim.x * kWarpsC - 1) / ((int)gridDim.x * kWarpsC);
+  const int nstep = (nitem + (int)gridDim.x * nwc - 1) / ((int)gridDim.x * nwc);
   int nacc_steps = 0;
   for (int st = 0; st < nstep; st++) {
-    const int item = (st * (int)gridDim.x + (int)blockIdx.x) * kWarpsC + w;
+    const int item = (st * (int)gridDim.x + (int)blockIdx.x) * nwc + w;
     int lo = 0x7fffffff, hi = -1;
     if (item < nitem) {
       const int kz = item / (N / NP), ky0 = (item - kz * (N / NP)) * NP;
@@ -249,7 +254,7 @@ __global__ void __launch_bounds__(32 * kWarpsC) k_pass_c_w(const __grid_constant
       bin_lines<NSPEC, true, MOM>(a, X, LS, kz, ky0, NP, tacc, lo, hi, lane, 32);
     }
     note_range(srange, lo, hi);
-    if (++nacc_steps == kMergeEvery) {
+    if (++nacc_steps == merge_every) {
       merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
       nacc_steps = 0;
     } else {
@@ -259,13 +264,27 @@ __global__ void __launch_bounds__(32 * kWarpsC) k_pass_c_w(const __grid_constant
   if (nacc_steps) merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
 }
 
+template <int N, int NSPEC, int MOM, int WPC>
+void launch_c_w_at(const PassCArgs& a, cudaStream_t s) {
+  const size_t smem = pass_c_w_smem(a.ng, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
+                                    a.geom.nbin * a.geom.nmu, WPC);
+  cudaFuncSetAttribute(k_pass_c_w<N, NSPEC, MOM, WPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  k_pass_c_w<N, NSPEC, MOM, WPC><<<(unsigned)a.grid, 32 * WPC, smem, s>>>(a);
+}
+
+// 16 warps per CTA only at Ng = 256 for one spectrum of the poles 0, 2, 4
+// (the learned form's |mu| sub-bins; larger transforms would spill at the
+// 64 registers two such CTAs an SM allow); the host plans by the same rule
 template <int N, int NSPEC, int MOM>
 void launch_c_w(const PassCArgs& a, cudaStream_t s) {
-  const size_t smem = pass_c_w_smem(a.ng, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
-                                    a.geom.nbin * a.geom.nmu);
-  cudaFuncSetAttribute(k_pass_c_w<N, NSPEC, MOM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  k_pass_c_w<N, NSPEC, MOM><<<(unsigned)a.grid, 32 * kWarpsC, smem, s>>>(a);
+  if constexpr (N == 256 && NSPEC == 1 && MOM == 3) {
+    if (a.wpc == kMaxWarpsC) {
+      launch_c_w_at<N, NSPEC, MOM, kMaxWarpsC>(a, s);
+      return;
+    }
+  }
+  launch_c_w_at<N, NSPEC, MOM, 4>(a, s);
 }
 
 template <int N, int MOM>
@@ -304,7 +323,7 @@ void wfft_shape(int n, int* L, int* V) {
   }
 }
 
-size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey) {
+size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey, int wpc) {
   int wel = 0;
   switch (ng) {
     case 256: wel = wc_warp_elems<256>(nfield); break;
@@ -312,10 +331,9 @@ size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey) {
     case 1024: wel = wc_warp_elems<1024>(nfield); break;
     default: return 0;
   }
-  return (size_t)kWarpsC * wel * sizeof(float2) + (size_t)nacc * nkey * sizeof(float);
+  if (wpc != 4 && wpc != kMaxWarpsC) return 0;
+  return (size_t)wpc * wel * sizeof(float2) + (size_t)nacc * nkey * sizeof(float);
 }
-
-int pass_c_w_threads() { return 32 * kWarpsC; }
 
 int launch_pass_a_w(const PassAArgs& a, cudaStream_t s) {
 #define PS_A_W(NG)                                                                              \
