@@ -713,6 +713,9 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat, size_t n) {
   g.interlace = c->p.interlace;
   g.T = c->gT;
   g.nt = c->gnt;
+  g.tshift = -1;
+  for (int k = 0; k < 31; k++)
+    if ((1 << k) == g.T) g.tshift = k;
   for (int d = 0; d < 3; d++) {
     g.box[d] = c->p.box[d];
     // the reference's shifted-grid edges (src/genr_mesh.c), correctly rounded

@@ -338,6 +338,12 @@ __device__ __forceinline__ Particle load_particle(const Particles& p, const Gath
   return q;
 }
 
+// Tile of a base node: a shift when the tile edge is a power of two (the
+// usual 16), else an integer division.
+__device__ __forceinline__ int tile_of(int base, const GatherArgs& g) {
+  return g.tshift >= 0 ? (base >> g.tshift) : base / g.T;
+}
+
 // Record and key of one particle; returns false if it lies outside the box.
 __device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs& g, Rec& r,
                                             unsigned& key) {
@@ -356,7 +362,7 @@ __device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs&
     int diff = a1.base - a0.base;
     if (diff > ng / 2) diff -= ng;
     if (diff < -ng / 2) diff += ng;
-    const int t = a0.base / g.T;
+    const int t = tile_of(a0.base, g);
     const int rel = a0.base - t * g.T;
     const int of = first_off(g.assign), S = width(g.assign);
     const int lo_r = rel + of + (g.interlace ? min(0, diff) : 0);
@@ -383,7 +389,7 @@ __device__ __forceinline__ bool region_key(const Particle& q, const GatherArgs& 
     float d;
     const Axis a0 = plain_axis(g.assign, [&] { return q.exact(a); }, q.hi[a], q.lo[a],
                                g.s_hi[a], g.s_lo[a], g.box[a], g.ng, i, d);
-    tile[a] = a0.base / g.T;
+    tile[a] = tile_of(a0.base, g);
   }
   key = (((unsigned)tile[0] * g.nt + tile[1]) * g.nt + tile[2]) * 27u;
   return true;
@@ -504,7 +510,7 @@ __device__ __forceinline__ WRec weighted_record(const Rec& r, const GatherArgs& 
       int l[3];
 #pragma unroll
       for (int a = 0; a < 3; a++) {
-        l[a] = (int)r.base[m][a] - ((int)r.base[0][a] / g.T) * g.T + 1;
+        l[a] = (int)r.base[m][a] - tile_of(r.base[0][a], g) * g.T + 1;
         l[a] += (l[a] < 0) ? g.ng : 0;
         l[a] -= (l[a] > g.T + 1) ? g.ng : 0;
         if (l[a] < 0 || l[a] > g.T + 1) {  // the grids' bases differ by at most a cell

@@ -27,6 +27,7 @@ constexpr int kAssignMaxBlocks = 2048;  // per-block weight partials
 struct GatherArgs {
   int ng, assign, interlace;
   int T, nt;               // tile edge (cells) and tiles per axis
+  int tshift;              // log2 T when T is a power of two, else -1
   double box[3];
   double bmin[3], bmax[3]; // shifted grid's edges: -(L / 2) / Ng and that + L (FP64)
   float s_hi[3], s_lo[3];  // Ng / L as a double-float pair per axis
