@@ -97,15 +97,20 @@ bool make_plan(int n, FftPlan& p) {
 std::vector<float2> warp_twiddles(int n) {
   int L = 0, V = 0;
   wfft_shape(n, &L, &V);
+  auto w = [n](int m) {  // W_n^m, the angle reduced to [0, pi]
+    m %= n;
+    const int mm = (2 * m <= n) ? m : n - m;
+    const double a = 2.0 * kPi * (double)mm / (double)n;
+    const double sn = (2 * m <= n) ? -sin(a) : sin(a);
+    return make_float2((float)cos(a), (float)sn);
+  };
   std::vector<float2> t((size_t)L * V);
   for (int k1 = 0; k1 < V; k1++)
-    for (int l = 0; l < L; l++) {
-      const int m = (l * k1) % n;
-      const int mm = (2 * m <= n) ? m : n - m;
-      const double a = 2.0 * kPi * (double)mm / (double)n;
-      const double sn = (2 * m <= n) ? -sin(a) : sin(a);
-      t[(size_t)k1 * L + l] = make_float2((float)cos(a), (float)sn);
-    }
+    for (int l = 0; l < L; l++) t[(size_t)k1 * L + l] = w(l * k1);
+  // the pair-of-warps form (L = 64 lanes over two warps) ends with 64-point
+  // DFTs split in two: W_64^k2 = W_n^(32 k2) after the table
+  if (L == 64)
+    for (int k2 = 0; k2 < 32; k2++) t.push_back(w(32 * k2));
   return t;
 }
 
@@ -298,6 +303,14 @@ void plan_pipes(ps_gpu_ctx* c) {
 // of (k, mu) accumulators.  Plain kernel: kPassCElems complex per tile, as
 // many CTAs per SM as fit.  Pipelined kernel (power-of-two Ng): the largest
 // tile (rows per field) that lets two CTAs share an SM, else one CTA.
+// Passes with a warp-register form for the context (ps_gpu_set_warp_fft's
+// mask): z (bit 0), y (bit 1) and x (bit 2); at Ng = 2048 only z and x.
+int warp_avail(const ps_gpu_ctx* c) {
+  int m = c->d_twl_half ? 1 : 0;
+  if (c->d_twl_full && c->grid_cw > 0) m |= (c->ng == 2048) ? 4 : 6;
+  return m;
+}
+
 int plan_pass_c(ps_gpu_ctx* c) {
   const int ng = c->ng;
   const int nacc = c->nspec * pass_c_accs(c->p.npole, pass_c_moments(c->p.poles, c->p.npole));
@@ -328,7 +341,17 @@ int plan_pass_c(ps_gpu_ctx* c) {
   // registers a thread).
   c->grid_cw = 0;
   c->wpc_cw = 4;
-  if (c->d_twl_full) {
+  if (c->d_twl_full && ng == 2048) {
+    // pairs of warps: as many as shared memory holds, up to 8 (16 warps)
+    for (int wpc = 16; wpc >= 2; wpc -= 2) {
+      const size_t smw = pass_c_w_smem(ng, c->nfield, nacc, nkey, wpc);
+      if (smw && smw <= 227 * 1024) {
+        c->wpc_cw = wpc;
+        c->grid_cw = c->nsm;
+        break;
+      }
+    }
+  } else if (c->d_twl_full) {
     const bool big_ok = ng == 256 && c->nspec == 1 && pass_c_moments(c->p.poles, c->p.npole) == 3;
     int best = 0;
     for (int wpc : {4, 16}) {
@@ -492,6 +515,9 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   if (wfft_supported(ng, 1)) {
     if ((rc = upload(c, &c->d_twl_full, warp_twiddles(ng)))) return rc;
     c->wfft |= 2 | 4;
+  } else if (ng == 2048 && c->nfield <= 2) {  // the x pass only, by pairs of warps
+    if ((rc = upload(c, &c->d_twl_full, warp_twiddles(ng)))) return rc;
+    c->wfft |= 4;
   }
 
   ModeGeom& g = c->geom;
@@ -1785,7 +1811,7 @@ void ps_gpu_batch_destroy(ps_gpu_batch* b) {
 
 int ps_gpu_set_warp_fft(ps_gpu_ctx* c, int mask) {
   if (!c) return PS_GPU_ERR_ARG;
-  const int avail = (c->d_twl_half ? 1 : 0) | (c->d_twl_full && c->grid_cw > 0 ? 6 : 0);
+  const int avail = warp_avail(c);
   if (mask >= 0) {
     DeviceScope dev_scope_(c->p.device);
     CU(dev_scope_.err);
@@ -1892,7 +1918,7 @@ int ps_gpu_autotune(ps_gpu_ctx* c, const double* xyzw, size_t n, int reps, int* 
   // warp-register form of each pass against the block-tiled one (phases
   // 1, 2, 3), where the mesh size has one
   {
-    const int avail = (c->d_twl_half ? 1 : 0) | (c->d_twl_full && c->grid_cw > 0 ? 6 : 0);
+    const int avail = warp_avail(c);
     for (int bit = 0; bit < 3; bit++) {
       const int m = 1 << bit;
       if (!(avail & m)) continue;

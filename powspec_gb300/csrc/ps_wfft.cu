@@ -306,6 +306,135 @@ void launch_c_w_mom(const PassCArgs& a, cudaStream_t s) {
   }
 }
 
+// ---- Ng = 2048: a pair of warps per line.  A line of 2048 complex values
+// needs 64 values a lane in one warp; two warps share it instead, 64 lanes
+// of 32 values, lane p holding x[p + 64 m]:
+//
+//   X[k1 + 32 k2] = sum_p W_64^(p k2) W_2048^(p k1) sum_m x[p + 64 m] W_32^(m k1)
+//
+//   1. a 32-point DFT over m in registers, then the twiddles W_2048^(p k1)
+//      from the host table twl[k1 64 + p];
+//   2. a transpose through the pair's shared memory S[k1][p] (rows of 66,
+//      so that the reads below fall in distinct banks);
+//   3. the 64-point DFTs over p by lane pairs: lane q takes k1 = q / 2 and
+//      the even (q even) or odd (q odd) p, a 32-point DFT of them, the odd
+//      half times W_64^k2 (table entries 2048 + k2), and the radix-2
+//      butterfly with its neighbour through one shuffle per value: lane q
+//      ends with X[k1 + 32 (k2 + 32 (q & 1))], k2 = 0..31.
+//
+// The pair synchronises on its own named barrier (id 1 + pair, 64
+// threads), reached by both warps on the same pair-uniform path.
+constexpr int kLine2k = 2112;  // line buffer of 2048 (+ 1/32 padding), and the 32 x 66 transpose
+__device__ __forceinline__ void pair_sync(int pair) {
+  __syncwarp();
+  asm volatile("bar.sync %0, 64;" ::"r"(1 + pair) : "memory");
+}
+
+__device__ __forceinline__ void wfft_pair2k(float2 (&v)[32], float2* S, const float2* __restrict__ twl,
+                                            int p, int pair) {
+  dft<32>(v);
+#pragma unroll
+  for (int k1 = 1; k1 < 32; k1++) v[k1] = cmul(v[k1], ldtw(&twl[k1 * 64 + p]));
+  pair_sync(pair);  // S (a line buffer) is free: its last readers have passed
+#pragma unroll
+  for (int k1 = 0; k1 < 32; k1++) S[k1 * 66 + p] = v[k1];
+  pair_sync(pair);
+  const int k1 = p >> 1, h = p & 1;
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = S[k1 * 66 + 2 * i + h];
+  pair_sync(pair);  // S is read; the caller writes the transformed line over it
+  dft<32>(v);
+  if (h) {
+#pragma unroll
+    for (int k2 = 1; k2 < 32; k2++) v[k2] = cmul(v[k2], ldtw(&twl[2048 + k2]));
+  }
+#pragma unroll
+  for (int k2 = 0; k2 < 32; k2++) {
+    const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, v[k2].x, 1),
+                                 __shfl_xor_sync(0xffffffffu, v[k2].y, 1));
+    // lane h = 0 holds E, its neighbour W O: X = E + W O; lane h = 1: E - W O
+    v[k2] = h ? csub(o, v[k2]) : cadd(v[k2], o);
+  }
+}
+
+// x transform + combine + window + binning at Ng = 2048: a work item of a
+// pair is one (ky, kz); each field's line is loaded (lane p: x[p + 64 m]),
+// transformed and stored into the pair's line buffer in the padded layout
+// of bin_lines, which then bins the item with the pair's 64 threads.  The
+// tile sums are merged every kMergeEvery steps, as k_pass_c_w does.
+template <int NSPEC, int MOM>
+__global__ void __launch_bounds__(512) k_pass_c_w2k(const __grid_constant__ PassCArgs a) {
+  constexpr int N = 2048;
+  extern __shared__ __align__(16) float2 wsm[];
+  __shared__ int srange[2];
+  const int pair = threadIdx.x >> 6, p = threadIdx.x & 63, npair = blockDim.x >> 6;
+  const int nfield = a.nfield;
+  float2* X = wsm + (size_t)pair * nfield * kLine2k;  // this pair's lines [field][kLine2k]
+  float* tacc = reinterpret_cast<float*>(wsm + (size_t)npair * nfield * kLine2k);
+  const ModeGeom& gm = a.geom;
+  const int nacc = NSPEC * gm.npole;
+  const int nkey = gm.nbin * gm.nmu;
+  double* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
+  for (int e = threadIdx.x; e < tile_accs<NSPEC, MOM>(gm) * nkey; e += blockDim.x) tacc[e] = 0.f;
+  if (threadIdx.x == 0) {
+    srange[0] = 0x7fffffff;
+    srange[1] = -1;
+  }
+  __syncthreads();
+  const int nitem = (N / 2 + 1) * N;  // (kz, ky)
+  const int nstep = (nitem + (int)gridDim.x * npair - 1) / ((int)gridDim.x * npair);
+  const int merge_every = max(1, kMergeEvery * 2 / npair);
+  int nacc_steps = 0;
+  for (int st = 0; st < nstep; st++) {
+    const int item = (st * (int)gridDim.x + (int)blockIdx.x) * npair + pair;
+    int lo = 0x7fffffff, hi = -1;
+    if (item < nitem) {  // pair-uniform
+      const int kz = item / N, ky = item - kz * N;
+      for (int f = 0; f < nfield; f++) {
+        const float2* src = a.in[f] + ((size_t)kz * N + ky) * N + p;
+        float2 v[32];
+#pragma unroll
+        for (int m = 0; m < 32; m++) v[m] = __ldcs(src + 64 * m);
+        float2* line = X + f * kLine2k;
+        wfft_pair2k(v, line, a.twl, p, pair);
+        const int k1 = p >> 1, h = p & 1;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; k2++) {
+          const int kx = k1 + 32 * (k2 + 32 * h);
+          line[kx + (kx >> 5)] = v[k2];
+        }
+      }
+      pair_sync(pair);  // every line of the item is stored
+      bin_lines<NSPEC, true, MOM>(a, X, kLine2k, kz, ky, 1, tacc, lo, hi, p, 64);
+    }
+    note_range(srange, lo, hi);
+    if (++nacc_steps == merge_every) {
+      merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
+      nacc_steps = 0;
+    } else {
+      __syncthreads();
+    }
+  }
+  if (nacc_steps) merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
+}
+
+template <int NSPEC, int MOM>
+void launch_c_w2k(const PassCArgs& a, cudaStream_t s) {
+  const size_t smem = pass_c_w_smem(2048, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
+                                    a.geom.nbin * a.geom.nmu, a.wpc);
+  cudaFuncSetAttribute(k_pass_c_w2k<NSPEC, MOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_pass_c_w2k<NSPEC, MOM><<<(unsigned)a.grid, 32 * a.wpc, smem, s>>>(a);
+}
+
+template <int MOM>
+void launch_c_w2k_ns(const PassCArgs& a, cudaStream_t s) {
+  switch (a.nspec) {
+    case 1: launch_c_w2k<1, MOM>(a, s); break;
+    case 2: launch_c_w2k<2, MOM>(a, s); break;
+    default: launch_c_w2k<3, MOM>(a, s); break;
+  }
+}
+
 }  // namespace
 
 bool wfft_supported(int ng, int pass) {
@@ -315,6 +444,7 @@ bool wfft_supported(int ng, int pass) {
 
 void wfft_shape(int n, int* L, int* V) {
   switch (n) {
+    case 2048: *L = 64; *V = 32; break;  // the pair-of-warps x pass (k_pass_c_w2k)
     case 128: *L = WShape<128>::L; *V = WShape<128>::V; break;
     case 256: *L = WShape<256>::L; *V = WShape<256>::V; break;
     case 512: *L = WShape<512>::L; *V = WShape<512>::V; break;
@@ -324,6 +454,10 @@ void wfft_shape(int n, int* L, int* V) {
 }
 
 size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey, int wpc) {
+  if (ng == 2048) {  // wpc / 2 pairs, each with its nfield (<= 2) line buffers
+    if (wpc < 2 || wpc > 16 || wpc % 2 || nfield > 2) return 0;
+    return (size_t)(wpc / 2) * nfield * kLine2k * sizeof(float2) + (size_t)nacc * nkey * sizeof(float);
+  }
   int wel = 0;
   switch (ng) {
     case 256: wel = wc_warp_elems<256>(nfield); break;
@@ -373,6 +507,15 @@ int launch_pass_b_w(const PassBArgs& a, cudaStream_t s) {
 }
 
 int launch_pass_c_w(const PassCArgs& a, cudaStream_t s) {
+  if (a.ng == 2048) {
+    switch (a.mom) {
+      case 2: launch_c_w2k_ns<2>(a, s); break;
+      case 3: launch_c_w2k_ns<3>(a, s); break;
+      case 4: launch_c_w2k_ns<4>(a, s); break;
+      default: launch_c_w2k_ns<0>(a, s); break;
+    }
+    return 1;
+  }
   switch (a.ng) {
     case 256: launch_c_w_mom<256>(a, s); return 1;
     case 512: launch_c_w_mom<512>(a, s); return 1;
