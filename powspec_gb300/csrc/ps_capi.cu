@@ -304,10 +304,10 @@ void plan_pipes(ps_gpu_ctx* c) {
 // many CTAs per SM as fit.  Pipelined kernel (power-of-two Ng): the largest
 // tile (rows per field) that lets two CTAs share an SM, else one CTA.
 // Passes with a warp-register form for the context (ps_gpu_set_warp_fft's
-// mask): z (bit 0), y (bit 1) and x (bit 2); at Ng = 2048 only z and x.
+// mask): z (bit 0), y (bit 1) and x (bit 2, when its CTAs fit).
 int warp_avail(const ps_gpu_ctx* c) {
   int m = c->d_twl_half ? 1 : 0;
-  if (c->d_twl_full && c->grid_cw > 0) m |= (c->ng == 2048) ? 4 : 6;
+  if (c->d_twl_full) m |= 2 | (c->grid_cw > 0 ? 4 : 0);
   return m;
 }
 
@@ -515,9 +515,9 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   if (wfft_supported(ng, 1)) {
     if ((rc = upload(c, &c->d_twl_full, warp_twiddles(ng)))) return rc;
     c->wfft |= 2 | 4;
-  } else if (ng == 2048 && c->nfield <= 2) {  // the x pass only, by pairs of warps
+  } else if (ng == 2048) {  // the y pass, and with <= 2 fields the x pass, by pairs of warps
     if ((rc = upload(c, &c->d_twl_full, warp_twiddles(ng)))) return rc;
-    c->wfft |= 4;
+    c->wfft |= 2 | (c->nfield <= 2 ? 4 : 0);
   }
 
   ModeGeom& g = c->geom;

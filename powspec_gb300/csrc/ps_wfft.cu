@@ -418,6 +418,37 @@ __global__ void __launch_bounds__(512) k_pass_c_w2k(const __grid_constant__ Pass
   if (nacc_steps) merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
 }
 
+// y transform at Ng = 2048 by pairs of warps: pair c of the CTA transforms
+// the line (x0 + c, kz) of A[x][kz][y]; the CTA stores B[kz][ky][x0 ..
+// x0 + 6) through a shared [ky][7] tile, in runs over x.
+constexpr int kPairsB2k = 6;
+__global__ void __launch_bounds__(64 * kPairsB2k) k_pass_b_w2k(const __grid_constant__ PassBArgs a) {
+  constexpr int N = 2048, ngk = N / 2 + 1, TP = kPairsB2k + 1;
+  constexpr int ntx = (N + kPairsB2k - 1) / kPairsB2k;
+  extern __shared__ __align__(16) float2 wsm[];
+  float2* T = wsm;                                    // [N][TP]
+  const int pair = threadIdx.x >> 6, p = threadIdx.x & 63;
+  float2* S = wsm + (size_t)N * TP + (size_t)pair * kLine2k;  // the pair's transpose area
+  const int kz = blockIdx.x / ntx, x0 = (blockIdx.x - kz * ntx) * kPairsB2k;
+  const int ncol = min(kPairsB2k, N - x0);
+  if (pair < ncol) {  // pair-uniform
+    const float2* src = a.in + ((size_t)(x0 + pair) * ngk + kz) * N + p;
+    float2 v[32];
+#pragma unroll
+    for (int m = 0; m < 32; m++) v[m] = __ldcs(src + 64 * m);
+    wfft_pair2k(v, S, a.twl, p, pair);
+    const int k1 = p >> 1, h = p & 1;
+#pragma unroll
+    for (int k2 = 0; k2 < 32; k2++) T[(k1 + 32 * (k2 + 32 * h)) * TP + pair] = v[k2];
+  }
+  __syncthreads();
+  float2* dst = a.out + (size_t)kz * N * N + x0;
+  for (int e = threadIdx.x; e < N * ncol; e += blockDim.x) {
+    const int ky = e / ncol, xl = e - ky * ncol;
+    dst[(size_t)ky * N + xl] = T[ky * TP + xl];
+  }
+}
+
 template <int NSPEC, int MOM>
 void launch_c_w2k(const PassCArgs& a, cudaStream_t s) {
   const size_t smem = pass_c_w_smem(2048, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
@@ -501,6 +532,14 @@ int launch_pass_b_w(const PassBArgs& a, cudaStream_t s) {
     case 256: PS_B_W(256)
     case 512: PS_B_W(512)
     case 1024: PS_B_W(1024)
+    case 2048: {
+      constexpr int N = 2048;
+      const size_t smem = ((size_t)N * (kPairsB2k + 1) + (size_t)kPairsB2k * kLine2k) * sizeof(float2);
+      cudaFuncSetAttribute(k_pass_b_w2k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_pass_b_w2k<<<(unsigned)((N / 2 + 1) * ((N + kPairsB2k - 1) / kPairsB2k)), 64 * kPairsB2k, smem,
+                     s>>>(a);
+      return 1;
+    }
     default: return 0;
   }
 #undef PS_B_W
