@@ -763,6 +763,7 @@ GatherArgs gather_args(ps_gpu_ctx* c, int cat, size_t n) {
   g.rec = c->d_rec;
   for (int m = 0; m < c->mpc; m++) g.out[m] = (float*)c->grid[cat * c->mpc + m];
   g.wsum = c->d_wsum + 2 * cat;
+  g.moff_scale = 4294967296.0 / ((double)c->ng * c->ng * c->ng);
   g.moff = reinterpret_cast<long long*>(c->d_wsum + 4) + cat;
   g.wpart = c->d_wpart;
   g.err = c->d_err + cat;

@@ -34,27 +34,56 @@ constexpr int kGatherThreads = 512;  // 16 warps; 3 CTAs per SM fit (registers, 
 constexpr int kMeshPad = 8;  // words between the two meshes' accumulators (bank offset)
 constexpr float kEdge = 4e-6f;
 
-// wsum[0..1] = sums of the per-block partials: lane l adds blocks l, l + 32,
-// ... in order, then a fixed shuffle tree (same order every run).  *moff =
-// the mean cell value in fixed point (0 with nomean), computed once here:
-// FP64 division is slow on this GPU, and the gather kernels' threads would
-// each repeat it.
-__global__ void k_wsum(const double* __restrict__ wpart, int nblocks, double* wsum,
-                       long long* moff, int ng, int nomean) {
-  double t0 = 0, t1 = 0;
-  for (int b = threadIdx.x; b < nblocks; b += 32) {
-    t0 += wpart[2 * b];
-    t1 += wpart[2 * b + 1];
+// s += a + b as an unevaluated FP32 pair (hi, lo), renormalised after
+// each add: TwoSum of hi and a (exact), the low parts added, then hi + lo
+// recombined (Fast2Sum).  Each add loses about 2^-48 of the running sum.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float a, float b) {
+  const float t = hi + a, bp = t - hi;
+  const float err = (hi - (t - bp)) + (a - bp);
+  const float l = lo + err + b;
+  hi = t + l;
+  lo = l - (hi - t);
+}
+
+// wsum[0..1] = sums of the per-block partials (k_classify: the signed sum as
+// an FP32 pair, the sum of |w| in FP32): thread t adds blocks t, t + 256,
+// ... in order, then a fixed tree (same order every run); FP64 once at the
+// end (this GPU's FP64 pipe is narrow).  *moff = the mean cell value in
+// fixed point, W * scale rounded (0 with nomean), computed once here for
+// the gather kernels.
+constexpr int kWsumThreads = 256;
+__global__ void __launch_bounds__(kWsumThreads) k_wsum(const float4* __restrict__ wpart, int nblocks,
+                                                       double* wsum, long long* moff, double scale,
+                                                       int nomean) {
+  __shared__ float sh[kWsumThreads / 32][3];
+  float h = 0.f, l = 0.f, ab = 0.f;
+  for (int b = threadIdx.x; b < nblocks; b += kWsumThreads) {
+    const float4 v = wpart[b];
+    df_add(h, l, v.x, v.y);
+    ab += v.z;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    t0 += __shfl_xor_sync(0xffffffffu, t0, o);
-    t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+    const float oh = __shfl_down_sync(0xffffffffu, h, o), ol = __shfl_down_sync(0xffffffffu, l, o);
+    ab += __shfl_down_sync(0xffffffffu, ab, o);
+    df_add(h, l, oh, ol);
   }
+  if ((threadIdx.x & 31) == 0) {
+    sh[threadIdx.x >> 5][0] = h;
+    sh[threadIdx.x >> 5][1] = l;
+    sh[threadIdx.x >> 5][2] = ab;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    wsum[0] = t0;
-    wsum[1] = t1;
-    *moff = nomean ? 0 : __double2ll_rn(t0 * 4294967296.0 / ((double)ng * ng * ng));
+    float th = 0.f, tl = 0.f, ta = 0.f;
+    for (int k = 0; k < kWsumThreads / 32; k++) {
+      df_add(th, tl, sh[k][0], sh[k][1]);
+      ta += sh[k][2];
+    }
+    const double w = (double)th + (double)tl;
+    wsum[0] = w;
+    wsum[1] = (double)ta;
+    *moff = nomean ? 0 : __double2ll_rn(w * scale);
   }
 }
 
@@ -395,17 +424,6 @@ __device__ __forceinline__ bool region_key(const Particle& q, const GatherArgs& 
   return true;
 }
 
-// s += a + b as an unevaluated FP32 pair (hi, lo), renormalised after
-// each add: TwoSum of hi and a (exact), the low parts added, then hi + lo
-// recombined (Fast2Sum).  Each add loses about 2^-48 of the running sum.
-__device__ __forceinline__ void df_add(float& hi, float& lo, float a, float b) {
-  const float t = hi + a, bp = t - hi;
-  const float err = (hi - (t - bp)) + (a - bp);
-  const float l = lo + err + b;
-  hi = t + l;
-  lo = l - (hi - t);
-}
-
 __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ GatherArgs g, Particles p) {
   // weight sums: the signed one as an FP32 pair (the per-particle FP64 add
   // would load this GPU's narrow FP64 pipe), |w| in FP32 (only compared
@@ -460,8 +478,7 @@ __global__ void __launch_bounds__(256) k_classify(const __grid_constant__ Gather
       df_add(th, tl, sws[k][0], sws[k][1]);
       ta += swa[k];
     }
-    g.wpart[2 * blockIdx.x] = (double)th + (double)tl;
-    g.wpart[2 * blockIdx.x + 1] = (double)ta;
+    reinterpret_cast<float4*>(g.wpart)[blockIdx.x] = make_float4(th, tl, ta, 0.f);
   }
   if (bad) atomicOr(g.err, 1);
 }
@@ -1307,12 +1324,12 @@ __global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ Gath
         const unsigned t0 = tb + tz;
         const bool f0 = g.regflag[t0] != 0;
         long long v0[2 * NM], v1[2 * NM];
-        load_pair<NM>(rb + ((size_t)t0 * RP + row + uz - of + 1) * NM, v0);
+        load_pair<NM>(rb + ((size_t)t0 * RP + (size_t)(row + uz - of + 1)) * NM, v0);
         bool f1 = false;
         if (tz2 >= 0) {
           const unsigned t1 = tb + tz2;
           f1 = g.regflag[t1] != 0;
-          load_pair<NM>(rb + ((size_t)t1 * RP + row + cz2) * NM, v1);
+          load_pair<NM>(rb + ((size_t)t1 * RP + (size_t)(row + cz2)) * NM, v1);
         }
         if (f0) {
 #pragma unroll
@@ -1379,7 +1396,8 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
     if (blocks < 1) blocks = 1;
     k_classify<<<(unsigned)blocks, 256, 0, s>>>(g, p);
     n++;
-    k_wsum<<<1, 32, 0, s>>>(g.wpart, (int)blocks, g.wsum, g.moff, g.ng, g.nomean);
+    k_wsum<<<1, kWsumThreads, 0, s>>>(reinterpret_cast<const float4*>(g.wpart), (int)blocks, g.wsum,
+                                      g.moff, g.moff_scale, g.nomean);
     n++;
     const int nb = (int)((nkeys + kScanBlock - 1) / kScanBlock);
     k_scan_reduce<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum);

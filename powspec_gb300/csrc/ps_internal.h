@@ -41,7 +41,8 @@ struct GatherArgs {
   long long* out64[2];     // or exact fixed-point meshes (diagnostics)
   double* wsum;            // [2]
   long long* moff;         // mean cell value in fixed point (0 with nomean), set by k_wsum
-  double* wpart;           // [2 * kAssignMaxBlocks]
+  double* wpart;           // [2 * kAssignMaxBlocks]: per block (sum w as an FP32 pair, sum |w|, 0)
+  double moff_scale;       // 2^32 / Ng^3: the mean cell value in fixed point per unit of W
   int* err;                // bit 0: particle outside [0, L); bit 1: region index out of range
   int threads;             // CTA size of the gather: 256, 512 or 0 (by density)
   unsigned sparse_max;     // tiles with at most this many records: lane groups, rows flagged;
