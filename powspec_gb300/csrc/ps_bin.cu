@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kFftThreads) k_pass_c(const __grid_constant__ 
   float2* sm2 = sm + tile_elems;  // second FFT buffer (ping-pong)
   float* tacc = reinterpret_cast<float*>(sm + 2 * tile_elems);
   __shared__ int srange[2];
-  double* part = STORE ? nullptr : a.partials + (size_t)blockIdx.x * nacc * nkey;
+  float2* part = STORE ? nullptr : a.partials + (size_t)blockIdx.x * nacc * nkey;
   if (!STORE) {
     for (int e = threadIdx.x; e < tile_accs<NSPEC, MOM>(g) * nkey; e += blockDim.x) tacc[e] = 0.f;
     if (threadIdx.x == 0) {
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_c_tma(const __grid_cons
   stage[1] = stage[0] + selems;
   float2* F = stage[1] + selems;
   float* tacc = reinterpret_cast<float*>(F + selems);
-  double* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
+  float2* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
   for (int e = threadIdx.x; e < tile_accs<NSPEC, MOM>(g) * nkey; e += blockDim.x) tacc[e] = 0.f;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kFftThreads) k_bin_fields(const __grid_constan
   const int nacc = g.npole;
   float* tacc = smf;
   __shared__ int srange[2];
-  double* part = a.partials + (size_t)blockIdx.x * nacc * g.nbin;
+  float2* part = a.partials + (size_t)blockIdx.x * nacc * g.nbin;
   for (int e = threadIdx.x; e < nacc * g.nbin; e += blockDim.x) tacc[e] = 0.f;
   if (threadIdx.x == 0) {
     srange[0] = 0x7fffffff;
@@ -303,10 +303,32 @@ __global__ void __launch_bounds__(256) k_geometry(const __grid_constant__ GeomAr
 
 // out[j] = sum over the grid rows of part[row][j], in a fixed order: warp w
 // of a block adds rows w, w + 16, ... of 32 consecutive columns (coalesced
-// 256-byte rows), then the 16 warp sums are added in warp order.
+// 256-byte rows), then the 16 warp sums are added in warp order.  The
+// binning partials are FP32 pairs, added as pairs (FP64 once per column);
+// FP64 partials (k_dc_sum) are added in FP64.
 constexpr int kReduceWarps = 16;
-__global__ void __launch_bounds__(32 * kReduceWarps) k_reduce(const double* __restrict__ part, int grid,
+__global__ void __launch_bounds__(32 * kReduceWarps) k_reduce(const float2* __restrict__ part, int grid,
                                                              int width, double* __restrict__ out) {
+  __shared__ float2 sh[kReduceWarps][33];
+  const int j = blockIdx.x * 32 + threadIdx.x, w = threadIdx.y;
+  float h = 0.f, l = 0.f;
+  if (j < width) {
+#pragma unroll 4
+    for (int gi = w; gi < grid; gi += kReduceWarps) {
+      const float2 v = __ldg(&part[(size_t)gi * width + j]);
+      df_add(h, l, v.x, v.y);
+    }
+  }
+  sh[w][threadIdx.x] = make_float2(h, l);
+  __syncthreads();
+  if (w == 0 && j < width) {
+    float th = sh[0][threadIdx.x].x, tl = sh[0][threadIdx.x].y;
+    for (int q = 1; q < kReduceWarps; q++) df_add(th, tl, sh[q][threadIdx.x].x, sh[q][threadIdx.x].y);
+    out[j] = (double)th + (double)tl;
+  }
+}
+__global__ void __launch_bounds__(32 * kReduceWarps) k_reduce_f64(const double* __restrict__ part, int grid,
+                                                                 int width, double* __restrict__ out) {
   __shared__ double sh[kReduceWarps][33];
   const int j = blockIdx.x * 32 + threadIdx.x, w = threadIdx.y;
   double s = 0.0;
@@ -430,7 +452,12 @@ int launch_geometry(const GeomArgs& a, cudaStream_t s) {
   return 1;
 }
 
-int launch_reduce(const double* part, int grid, int width, double* out, cudaStream_t s) {
+int launch_reduce_f64(const double* part, int grid, int width, double* out, cudaStream_t s) {
+  k_reduce_f64<<<(width + 31) / 32, dim3(32, kReduceWarps), 0, s>>>(part, grid, width, out);
+  return 1;
+}
+
+int launch_reduce(const float2* part, int grid, int width, double* out, cudaStream_t s) {
   k_reduce<<<(width + 31) / 32, dim3(32, kReduceWarps), 0, s>>>(part, grid, width, out);
   return 1;
 }

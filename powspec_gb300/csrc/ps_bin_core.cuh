@@ -79,9 +79,10 @@ __device__ __forceinline__ void note_range(int* srange, int lo, int hi) {
   }
 }
 
-// Merge the FP32 accumulators of the touched bin range into the CTA's FP64
-// slice and clear them.  Starts and ends with a barrier.
-__device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int nbin) {
+// Merge the FP32 accumulators of the touched bin range into the CTA's
+// slice of FP32-pair partials (hi + lo, about 48 bits: FP64 adds are slow
+// on this GPU) and clear them.  Starts and ends with a barrier.
+__device__ void merge_tile(float* tacc, int* srange, float2* part, int nacc, int nbin) {
   __syncthreads();
   const int blo = srange[0], bhi = srange[1];
   if (bhi >= blo) {
@@ -89,7 +90,9 @@ __device__ void merge_tile(float* tacc, int* srange, double* part, int nacc, int
     for (int e = threadIdx.x; e < nacc * w; e += blockDim.x) {
       const int q = e / w;
       const int idx = q * nbin + blo + (e - q * w);
-      part[idx] += (double)tacc[idx];
+      float2 pv = part[idx];
+      df_add(pv.x, pv.y, tacc[idx], 0.f);
+      part[idx] = pv;
       tacc[idx] = 0.f;
     }
   }
@@ -153,7 +156,7 @@ __device__ __forceinline__ void mom_add(MomAcc<NSPEC, MOM>& ra, int b, int nkey,
 // Merge of moment tile sums: the Legendre sums of the touched keys are added
 // into the CTA's FP64 slice [NSPEC][npole][nkey], the moments cleared.
 template <int NSPEC, int MOM>
-__device__ void merge_tile_mom(float* tacc, int* srange, double* part, const ModeGeom& g,
+__device__ void merge_tile_mom(float* tacc, int* srange, float2* part, const ModeGeom& g,
                                int nkey) {
   __syncthreads();
   const int blo = srange[0], bhi = srange[1];
@@ -172,12 +175,15 @@ __device__ void merge_tile_mom(float* tacc, int* srange, double* part, const Mod
       }
       if (!any) continue;  // a key of the range that no mode reached
       // the combination in FP32 (FP64 arithmetic is slow on this GPU; the
-      // moments are FP32 sums already), added into the FP64 partials
+      // moments are FP32 sums already), added into the FP32-pair partials
       for (int l = 0; l < g.npole; l++) {
         float v = 0.f;
 #pragma unroll
         for (int j = 0; j < MOM; j++) v = fmaf(g.lc[l][j], m[j], v);
-        part[(s * g.npole + l) * nkey + key] += (double)v;
+        float2& q = part[(s * g.npole + l) * nkey + key];
+        float h = q.x, lo = q.y;
+        df_add(h, lo, v, 0.f);
+        q = make_float2(h, lo);
       }
     }
   }
@@ -190,7 +196,7 @@ __device__ void merge_tile_mom(float* tacc, int* srange, double* part, const Mod
 }
 
 template <int NSPEC, int MOM>
-__device__ __forceinline__ void merge_any(float* tacc, int* srange, double* part,
+__device__ __forceinline__ void merge_any(float* tacc, int* srange, float2* part,
                                           const ModeGeom& g, int nkey) {
   if (MOM > 0) merge_tile_mom<NSPEC, (MOM > 0 ? MOM : 1)>(tacc, srange, part, g, nkey);
   else merge_tile(tacc, srange, part, NSPEC * g.npole, nkey);

@@ -902,12 +902,12 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
   pc.tw_full = c->d_tw_full;
   pc.plan_full = c->plan_full;
   pc.geom = c->geom;
-  pc.partials = c->d_part;
+  pc.partials = reinterpret_cast<float2*>(c->d_part);
   pc.grid = grid_c;
   c->launches += launch_pass_c(pc, s);
   CU(cudaGetLastError());
   if (events) CU(cudaEventRecord(c->ev[3], s));
-  c->launches += launch_reduce(c->d_part, grid_c, nacc * nkey, sums_dst, s);
+  c->launches += launch_reduce(reinterpret_cast<const float2*>(c->d_part), grid_c, nacc * nkey, sums_dst, s);
   CU(cudaGetLastError());
   if (events) CU(cudaEventRecord(c->ev[4], s));
   return 0;
@@ -1213,7 +1213,7 @@ void bin_pair(ps_gpu_ctx* c, const float2* f1, const float2* f2) {
   b.geom.npole = 1;  // l = 0 weights: the multipole is in the fields
   for (int q = 0; q < 4; q++) b.geom.lc[0][q] = q == 0 ? 1.f : 0.f;
   b.geom.lodd = 0;
-  b.partials = c->d_part;
+  b.partials = reinterpret_cast<float2*>(c->d_part);
   b.grid = c->grid_c;
   launch_bin_fields(b, c->stream);
   c->launches++;
@@ -1293,7 +1293,7 @@ int enqueue_survey_multipoles(ps_gpu_ctx* c) {
         bin_pair(c, f0[a], fl[b]);
         if (a != b) bin_pair(c, f0[b], fl[a]);
       }
-      launch_reduce(c->d_part, c->grid_c, nbin, c->d_sums + ((size_t)sp * npole + l) * nbin, s);
+      launch_reduce(reinterpret_cast<const float2*>(c->d_part), c->grid_c, nbin, c->d_sums + ((size_t)sp * npole + l) * nbin, s);
       c->launches++;
     }
   }
@@ -1568,10 +1568,10 @@ int ps_gpu_bin_fields_host(ps_gpu_ctx* c, const float* f1, const float* f2, doub
   b.f2 = d2;
   b.geom = c->geom;
   b.geom.nmu = 1;
-  b.partials = c->d_part;
+  b.partials = reinterpret_cast<float2*>(c->d_part);
   b.grid = c->grid_c;
   launch_bin_fields(b, s);
-  launch_reduce(c->d_part, c->grid_c, npole * nbin, c->d_sums, s);
+  launch_reduce(reinterpret_cast<const float2*>(c->d_part), c->grid_c, npole * nbin, c->d_sums, s);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(pl, c->d_sums, sizeof(double) * (size_t)npole * nbin, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));

@@ -443,6 +443,17 @@ __device__ __forceinline__ float2* fft_lines_pp(float2* a, float2* b, const FftP
 
 // Fixed-point cell (minus a constant offset) -> float.  d = hi * 2^32 + lo,
 // value = d * 2^-32 = hi + lo * 2^-32, using two 32-bit conversions.
+// s += a + b as an unevaluated FP32 pair (hi, lo), renormalised after
+// each add: TwoSum of hi and a (exact), the low parts added, then hi + lo
+// recombined (Fast2Sum).  Each add loses about 2^-48 of the running sum.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float a, float b) {
+  const float t = hi + a, bp = t - hi;
+  const float err = (hi - (t - bp)) + (a - bp);
+  const float l = lo + err + b;
+  hi = t + l;
+  lo = l - (hi - t);
+}
+
 __device__ __forceinline__ float fix_to_float(long long d) {
   const int hi = (int)(d >> 32);
   const unsigned lo = (unsigned)(d & 0xffffffffull);

@@ -34,17 +34,6 @@ constexpr int kGatherThreads = 512;  // 16 warps; 3 CTAs per SM fit (registers, 
 constexpr int kMeshPad = 8;  // words between the two meshes' accumulators (bank offset)
 constexpr float kEdge = 4e-6f;
 
-// s += a + b as an unevaluated FP32 pair (hi, lo), renormalised after
-// each add: TwoSum of hi and a (exact), the low parts added, then hi + lo
-// recombined (Fast2Sum).  Each add loses about 2^-48 of the running sum.
-__device__ __forceinline__ void df_add(float& hi, float& lo, float a, float b) {
-  const float t = hi + a, bp = t - hi;
-  const float err = (hi - (t - bp)) + (a - bp);
-  const float l = lo + err + b;
-  hi = t + l;
-  lo = l - (hi - t);
-}
-
 // wsum[0..1] = sums of the per-block partials (k_classify: the signed sum as
 // an FP32 pair, the sum of |w| in FP32): thread t adds blocks t, t + 256,
 // ... in order, then a fixed tree (same order every run); FP64 once at the

@@ -169,7 +169,7 @@ struct PassCArgs {
   const float2* tw_full;
   FftPlan plan_full;
   ModeGeom geom;
-  double* partials;             // [grid][nspec*npole*nbin] FP64
+  float2* partials;             // [grid][nspec*npole*nbin] FP32 pairs (hi + lo)
   int grid;                     // persistent CTAs (bin mode)
   int pipe;                     // power-of-two Ng: the cp.async.bulk-pipelined kernel
   int mom;                      // 0: pole sums; 2..4: mu^2 moments (even poles, lmax = 2 (mom - 1))
@@ -213,7 +213,7 @@ struct BinFieldArgs {
   const float2* f1;
   const float2* f2;
   ModeGeom geom;
-  double* partials;             // [grid][npole*nbin]
+  float2* partials;             // [grid][npole*nbin] FP32 pairs (hi + lo)
   int grid;
 };
 int launch_bin_fields(const BinFieldArgs& a, cudaStream_t s);
@@ -232,7 +232,8 @@ struct GeomArgs {
 int launch_geometry(const GeomArgs& a, cudaStream_t s);
 
 // Deterministic reduction of per-CTA partials: out[j] = sum_g part[g][j].
-int launch_reduce(const double* part, int grid, int width, double* out, cudaStream_t s);
+int launch_reduce(const float2* part, int grid, int width, double* out, cudaStream_t s);
+int launch_reduce_f64(const double* part, int grid, int width, double* out, cudaStream_t s);
 
 // Minimum shared memory per CTA the passes need (bytes).
 size_t pass_c_smem(int ng, int ty, int nfield, int nacc, int nbin, bool pow2);

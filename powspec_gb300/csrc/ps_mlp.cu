@@ -502,20 +502,25 @@ __global__ void k_learned_features(const ps::LearnedArgs a) {
 
 // P_l = (2l + 1) (sum_j c_j A_jl - shot lcnt_l / cnt), l = 0, 2, 4, the
 // cells summed in j order.
+// One thread per (pole, bin): the per-cell sums times the corrections in
+// FP64, then one division by the bin's normalisation (FP64 division is slow
+// on this GPU: one per pole and bin, not per cell).
 __global__ void k_learned_combine(const ps::LearnedArgs a) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= a.nbin) return;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.npole * a.nbin) return;
+  const int l = e / a.nbin, b = e - l * a.nbin;
   const double W = a.wsum[0], norm = W * W / a.volume, shot = a.volume / W;
   const double cb = a.cnt[b], safe = fmax(cb, 1.0);
   const int nkey = a.nbin * a.nmu;
-  for (int l = 0; l < a.npole; l++) {
-    double s = 0.0;
-    if (cb > 0)
-      for (int j = 0; j < a.nmu; j++)
-        s += (double)a.c[(size_t)b * a.nmu + j] * (a.sums[(size_t)l * nkey + (size_t)b * a.nmu + j] / (norm * safe));
-    const double B = (cb > 0) ? shot * a.lcnt[(size_t)l * a.nbin + b] / safe : 0.0;
-    a.out[(size_t)l * a.nbin + b] = (4.0 * l + 1.0) * (s - B);
+  double s = 0.0, B = 0.0;
+  if (cb > 0) {
+    const float* c = a.c + (size_t)b * a.nmu;
+    const double* sm = a.sums + (size_t)l * nkey + (size_t)b * a.nmu;
+    for (int j = 0; j < a.nmu; j++) s = fma((double)c[j], sm[j], s);
+    s /= norm * safe;
+    B = shot * a.lcnt[(size_t)l * a.nbin + b] / safe;
   }
+  a.out[(size_t)l * a.nbin + b] = (4.0 * l + 1.0) * (s - B);
 }
 
 }  // namespace
@@ -542,7 +547,7 @@ int learned_enqueue(::ps_mlp* m, const LearnedArgs& a, cudaStream_t s) {
   cudaError_t e = cudaFuncSetAttribute(k_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return PS_GPU_ERR_CUDA;
   k_mlp<<<(n + kRows - 1) / kRows, 256, smem, s>>>(t);
-  k_learned_combine<<<(a.nbin + 127) / 128, 128, 0, s>>>(a);
+  k_learned_combine<<<(a.npole * a.nbin + 127) / 128, 128, 0, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : PS_GPU_ERR_CUDA;
 }
 

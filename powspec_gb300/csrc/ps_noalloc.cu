@@ -24,7 +24,7 @@ namespace {
 constexpr int kNoAllocMaxCtas = 160;     // partial-sum rows (one per CTA)
 constexpr int kNoAllocMaxWidth = 3200;   // npole * nbin
 constexpr size_t kNoAllocScratchBytes =  // 4,096,000 bytes
-    (size_t)kNoAllocMaxCtas * kNoAllocMaxWidth * sizeof(double);
+    (size_t)kNoAllocMaxCtas * kNoAllocMaxWidth * sizeof(float2);
 
 // Per-CTA partial sums [grid][npole * nbin] of every call on this device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -79,9 +79,9 @@ extern "C" int ps_gpu_bin_fields_noalloc(ps_gpu_ctx* c, const float* f1, const f
     return ctx_fail(c, PS_GPU_ERR_CUDA, "bin_fields_noalloc set-up: %s", cudaGetErrorString(e));
   const int grid = nsm < kNoAllocMaxCtas ? nsm : kNoAllocMaxCtas;
   cudaStream_t s = (cudaStream_t)stream;
-  double* part = (double*)scratch;
+  float2* part = (float2*)scratch;  // FP32-pair partials
   // the kernel adds its tile sums into the partials: they start at zero
-  e = cudaMemsetAsync(part, 0, (size_t)grid * width * sizeof(double), s);
+  e = cudaMemsetAsync(part, 0, (size_t)grid * width * sizeof(float2), s);
   if (e != cudaSuccess)
     return ctx_fail(c, PS_GPU_ERR_CUDA, "bin_fields_noalloc memset: %s", cudaGetErrorString(e));
   BinFieldArgs b;

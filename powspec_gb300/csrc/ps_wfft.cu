@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(32 * WPC, WPC == 4 ? 0 : 2) k_pass_c_w(const _
   const ModeGeom& gm = a.geom;
   const int nacc = NSPEC * gm.npole;
   const int nkey = gm.nbin * gm.nmu;
-  double* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
+  float2* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
   for (int e = threadIdx.x; e < tile_accs<NSPEC, MOM>(gm) * nkey; e += blockDim.x) tacc[e] = 0.f;
   if (threadIdx.x == 0) {
     srange[0] = 0x7fffffff;
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(512) k_pass_c_w2k(const __grid_constant__ Pass
   const ModeGeom& gm = a.geom;
   const int nacc = NSPEC * gm.npole;
   const int nkey = gm.nbin * gm.nmu;
-  double* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
+  float2* part = a.partials + (size_t)blockIdx.x * nacc * nkey;
   for (int e = threadIdx.x; e < tile_accs<NSPEC, MOM>(gm) * nkey; e += blockDim.x) tacc[e] = 0.f;
   if (threadIdx.x == 0) {
     srange[0] = 0x7fffffff;

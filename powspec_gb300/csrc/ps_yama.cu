@@ -348,7 +348,7 @@ int launch_dc_sum(const float* mesh, int ng, int ell, const double* org, const d
   a.wsum = wsum;
   a.ncat = ncat;
   k_dc_sum<<<grid, 256, 0, s>>>(a);
-  launch_reduce(part, grid, 1, part + grid, s);
+  launch_reduce_f64(part, grid, 1, part + grid, s);
   k_dc_select<<<1, 1, 0, s>>>(part + grid, dc32, wsum, ncat, out);
   return 3;
 }
