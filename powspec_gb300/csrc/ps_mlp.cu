@@ -248,11 +248,26 @@ __global__ void __launch_bounds__(256, 1) k_mlp(const __grid_constant__ TrainArg
   extern __shared__ __align__(16) unsigned char smraw[];
   Smem& s = *reinterpret_cast<Smem*>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // weights
+  // weights, in 16-byte pieces (all loads of a thread in flight at once);
+  // inference needs only the forward images (w1t, w2t, w3t)
   {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(p.bw);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(&s.w);
-    for (int e = threadIdx.x; e < (int)(sizeof(BfWeights) / 4); e += blockDim.x) dst[e] = src[e];
+    static_assert(sizeof(BfWeights) % 16 == 0 && offsetof(BfWeights, w2t) % 16 == 0 &&
+                      offsetof(BfWeights, w3t) % 16 == 0 && (kH * kK1 * sizeof(bf16)) % 16 == 0 &&
+                      (kH * kH * sizeof(bf16)) % 16 == 0,
+                  "16-byte weight pieces");
+    auto copy = [&](const bf16* g, bf16* d, int n) {
+      const uint4* src = reinterpret_cast<const uint4*>(g);
+      uint4* dst = reinterpret_cast<uint4*>(d);
+      for (int e = threadIdx.x; e < n * (int)sizeof(bf16) / 16; e += blockDim.x) dst[e] = src[e];
+    };
+    if (p.train) {
+      copy(reinterpret_cast<const bf16*>(p.bw), reinterpret_cast<bf16*>(&s.w),
+           (int)(sizeof(BfWeights) / sizeof(bf16)));
+    } else {
+      copy(p.bw->w1t, s.w.w1t, kH * kK1);
+      copy(p.bw->w2t, s.w.w2t, kH * kH);
+      copy(p.bw->w3t, s.w.w3t, kH * kH);
+    }
     for (int e = threadIdx.x; e < kH; e += blockDim.x) {
       s.w4[e] = p.params[ow4 + e];
       s.b[0][e] = p.params[ob1 + e];
