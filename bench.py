@@ -409,16 +409,20 @@ def run_reference(args, world, rank):
     return 0
 
 
-def timed(stream, steps, fn):
-    """Device time (CUDA events on the context stream) of `steps` calls."""
+def timed(stream, steps, fn, many=None):
+    """Device time (CUDA events on the context stream) of `steps` calls, or
+    of one call many(steps) that runs them back to back."""
     import torch
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     ev0.record(stream)
     out = None
-    for _ in range(steps):
-        out = fn()
+    if many is not None:
+        out = many(steps)
+    else:
+        for _ in range(steps):
+            out = fn()
     ev1.record(stream)
     torch.cuda.synchronize()
     return ev0.elapsed_time(ev1), out
@@ -474,10 +478,21 @@ def run_gpu(args, world, rank, local):
             launches[0] += le.est.launches() + 2  # + feature cast and network kernels
             return out
 
+        def step_many(k):
+            # k evaluations back to back: each next assignment enqueued before
+            # the previous results are waited for (LearnedEstimator.run_many);
+            # the phase times are the last evaluation's (the assignment's from
+            # the last one run alone)
+            res = le.run_many([d_cat.data_ptr()] * k, nreal)
+            phases[:] += le.est.timings() * k
+            launches[0] += (le.est.launches() + 2) * k
+            return res[-1]
+
         def e2e_stream(k):
             return le.run_stream(itertools.repeat(host_arr, k))
     else:
         le = None
+        step_many = None
         stream, phases, launches = s_plain, phases_plain, [0]
 
         def step():
@@ -498,7 +513,7 @@ def run_gpu(args, world, rank, local):
 
     with ClockSampler(local) as clk:
         barrier(world)
-        dev_ms, out = timed(stream, args.steps, step)
+        dev_ms, out = timed(stream, args.steps, step, many=step_many)
         barrier(world)
     clocks = clk.summary()
     ph = phases / args.steps

@@ -68,6 +68,16 @@ int ps_mlp_infer(ps_mlp *m, const float *x, int n, float *c);
  * train it meanwhile. */
 int ps_gpu_execute_learned(ps_gpu_ctx *ctx, ps_mlp *m, ps_gpu_result *res, double *pl_corr);
 
+/* ps_gpu_execute_learned in two halves (no counterpart in the reference),
+ * for evaluating many catalogues back to back: launch enqueues the passes,
+ * the network and the copy back, and returns; the next catalogue may then
+ * be assigned (its assignment runs on the GPU after this evaluation) before
+ * finish waits for this evaluation's results and fills res and pl_corr as
+ * ps_gpu_execute_learned does.  One evaluation may be pending at a time;
+ * ps_gpu_execute is refused meanwhile. */
+int ps_gpu_learned_launch(ps_gpu_ctx *ctx, ps_mlp *m);
+int ps_gpu_learned_finish(ps_gpu_ctx *ctx, ps_gpu_result *res, double *pl_corr);
+
 /* Checkpoint with parameters, Adam moments and step count; load resumes. */
 int ps_mlp_save(ps_mlp *m, const char *path);
 int ps_mlp_load(ps_mlp *m, const char *path);

@@ -37,7 +37,7 @@ EXPORTED = [
     "ps_gpu_set_mu_bins", "ps_gpu_read_kmu", "ps_gpu_bin_fields_noalloc",
     "ps_gpu_batch_create", "ps_gpu_batch_launch", "ps_gpu_batch_wait", "ps_gpu_batch_result",
     "ps_gpu_batch_launches", "ps_gpu_batch_destroy", "ps_gpu_autotune", "ps_gpu_set_tuning",
-    "ps_gpu_execute_learned", "ps_gpu_stage_aos", "ps_gpu_assign_staged", "ps_gpu_set_survey",
+    "ps_gpu_execute_learned", "ps_gpu_learned_launch", "ps_gpu_learned_finish", "ps_gpu_stage_aos", "ps_gpu_assign_staged", "ps_gpu_set_survey",
     "ps_gpu_debug_fail_alloc", "ps_gpu_set_warp_fft", "ps_gpu_debug_stall_pipeline",
     "ps_gpu_ensemble_create", "ps_gpu_ensemble_launch", "ps_gpu_ensemble_wait",
     "ps_gpu_ensemble_destroy",

@@ -216,6 +216,12 @@ struct ps_gpu_ctx {
   int assigned[2] = {0, 0};
   size_t npart[2] = {0, 0};
   cudaEvent_t ev[8] = {};
+  // a learned evaluation launched and not yet finished (ps_gpu_learned_launch)
+  cudaEvent_t ev_done = nullptr;  // its results are on the host
+  bool learned_pending = false;
+  size_t npart_pending[2] = {0, 0};
+  bool assign_timed_pending = false;  // its assignment's events can be read at finish
+  unsigned assign_gen = 0, assign_gen_pending = 0;  // assignments started
   bool assign_started = false;
   float timings[6] = {0, 0, 0, 0, 0, 0};
   int launches = 0;
@@ -467,6 +473,7 @@ int ps_gpu_create(const ps_gpu_params* params, ps_gpu_ctx** out) {
   CU(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, p.device));
   CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   for (auto& e : c->ev) CU(cudaEventCreate(&e));
+  CU(cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming));
   // place ps_gpu_bin_fields_noalloc's static scratch now, not on its first
   // call; a failure here is cleared and reported by that entry point
   if (noalloc_prepare(p.device) != cudaSuccess) (void)cudaGetLastError();
@@ -666,6 +673,7 @@ void ps_gpu_destroy(ps_gpu_ctx* c) {
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  if (c->ev_done) cudaEventDestroy(c->ev_done);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -801,6 +809,7 @@ int assign_common(ps_gpu_ctx* c, int cat, Particles pt) {
     CU(cudaEventRecord(c->ev[6], c->stream));
     c->assign_started = true;
     c->launches = 0;
+    c->assign_gen++;
   }
   {
     int rc = ensure_gather_capacity(c, pt.n);
@@ -1316,6 +1325,7 @@ extern "C" {
 
 int ps_gpu_execute(ps_gpu_ctx* c, ps_gpu_result* r) {
   if (!c || !r) return fail(c, PS_GPU_ERR_ARG, "null argument");
+  if (c->learned_pending) return fail(c, PS_GPU_ERR_STATE, "a learned evaluation is pending: finish it first");
   const ps_gpu_params& p = c->p;
   for (int k = 0; k < p.ncat; k++)
     if (!c->assigned[k]) return fail(c, PS_GPU_ERR_STATE, "catalogue %d not assigned", k);
@@ -1363,8 +1373,9 @@ int ps_gpu_set_survey(ps_gpu_ctx* c, int cat, double shot, double norm, const do
   return 0;
 }
 
-int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* pl_corr) {
-  if (!c || !m || !r || !pl_corr) return fail(c, PS_GPU_ERR_ARG, "null argument");
+int ps_gpu_learned_launch(ps_gpu_ctx* c, ps_mlp* m) {
+  if (!c || !m) return fail(c, PS_GPU_ERR_ARG, "null argument");
+  if (c->learned_pending) return fail(c, PS_GPU_ERR_STATE, "a learned evaluation is pending: finish it first");
   const ps_gpu_params& p = c->p;
   if (p.ncat != 1 || p.npole != 3 || p.poles[0] != 0 || p.poles[1] != 2 || p.poles[2] != 4 ||
       p.logscale || c->survey[0])
@@ -1429,18 +1440,44 @@ int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* p
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey + 4, c->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(c->h_lout, c->d_lout, sizeof(double) * (size_t)nacc * nbin, cudaMemcpyDeviceToHost, s));
-  CU(cudaStreamSynchronize(s));
+  CU(cudaEventRecord(c->ev_done, s));
+  // the next catalogue may be assigned before the finish: keep what it
+  // would overwrite
+  c->npart_pending[0] = c->npart[0];
+  c->npart_pending[1] = c->npart[1];
+  c->assign_timed_pending = c->assign_started;
+  c->assign_gen_pending = c->assign_gen;
+  c->assign_started = false;
+  c->assigned[0] = c->assigned[1] = 0;
+  c->learned_pending = true;
+  return 0;
+}
+
+int ps_gpu_learned_finish(ps_gpu_ctx* c, ps_gpu_result* r, double* pl_corr) {
+  if (!c || !r || !pl_corr) return fail(c, PS_GPU_ERR_ARG, "null argument");
+  if (!c->learned_pending) return fail(c, PS_GPU_ERR_STATE, "no learned evaluation was launched");
+  DeviceScope dev_scope_(c->p.device);
+  CU(dev_scope_.err);
+  c->learned_pending = false;
+  CU(cudaEventSynchronize(c->ev_done));
   float t = 0;
-  if (c->assign_started && cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess) c->timings[0] = t;
+  // the assignment's events, unless a later assignment has recorded them again
+  if (c->assign_timed_pending && c->assign_gen == c->assign_gen_pending &&
+      cudaEventElapsedTime(&t, c->ev[6], c->ev[7]) == cudaSuccess)
+    c->timings[0] = t;
   for (int i = 0; i < 4; i++)
     if (cudaEventElapsedTime(&t, c->ev[i], c->ev[i + 1]) == cudaSuccess) c->timings[1 + i] = t;
   if (cudaEventElapsedTime(&t, c->ev[0], c->ev[4]) == cudaSuccess) c->timings[5] = t + c->timings[0];
-  c->assign_started = false;
-  c->assigned[0] = c->assigned[1] = 0;
-  rc = finish(c, h, c->npart, r, true);
+  const int rc = finish(c, c->h_out, c->npart_pending, r, true);
   if (rc) return rc;
-  memcpy(pl_corr, c->h_lout, sizeof(double) * (size_t)nacc * nbin);
+  memcpy(pl_corr, c->h_lout, sizeof(double) * (size_t)c->p.npole * c->nbin);
   return 0;
+}
+
+int ps_gpu_execute_learned(ps_gpu_ctx* c, ps_mlp* m, ps_gpu_result* r, double* pl_corr) {
+  if (!c || !m || !r || !pl_corr) return fail(c, PS_GPU_ERR_ARG, "null argument");
+  const int rc = ps_gpu_learned_launch(c, m);
+  return rc ? rc : ps_gpu_learned_finish(c, r, pl_corr);
 }
 
 int ps_gpu_set_mu_bins(ps_gpu_ctx* c, int nmu) {

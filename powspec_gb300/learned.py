@@ -53,6 +53,8 @@ def _mlp_lib():
         L.ps_mlp_save.argtypes = [vp, ctypes.c_char_p]
         L.ps_mlp_load.argtypes = [vp, ctypes.c_char_p]
         L.ps_gpu_execute_learned.argtypes = [vp, vp, vp, vp]
+        L.ps_gpu_learned_launch.argtypes = [vp, vp]
+        L.ps_gpu_learned_finish.argtypes = [vp, vp, vp]
         L._mlp_ready = True
     return L
 
@@ -450,12 +452,50 @@ class LearnedEstimator:
             return (self.run(c) for c in cats)
         return self.est.run_stream(cats, execute=self._execute)
 
+    def run_many(self, device_ptrs, n):
+        """run() over catalogues already on the device (32-byte aligned AoS
+        records, n each), back to back: each catalogue's assignment is
+        enqueued before the previous evaluation's results are waited for
+        (ps_gpu_learned_launch / ps_gpu_learned_finish), so the GPU does not
+        idle between evaluations.  Returns one (k, pc, trusted) per catalogue.
+        A configuration that needs the fine-mesh fallback runs them one at a
+        time."""
+        ptrs = list(device_ptrs)
+        if self.fine is not None or not ptrs:
+            return [self.run(device_ptr=p, n=n) for p in ptrs]
+        out = []
+        self.est.assign(0, ptrs[0], on_device=True, n=n)
+        self._launch()
+        for i in range(len(ptrs)):
+            if i + 1 < len(ptrs):
+                self.est.assign(0, ptrs[i + 1], on_device=True, n=n)
+            out.append(self._finish())
+            if i + 1 < len(ptrs):
+                self._launch()
+        return out
+
+    def _launch(self):
+        rc = _mlp_lib().ps_gpu_learned_launch(self.est._ctx, self.mlp._m)
+        if rc:
+            raise PowspecError(rc, lib().ps_gpu_last_error(self.est._ctx).decode())
+
+    def _finish(self):
+        r, out = self.est._result()
+        pc = np.zeros((len(POLES), self.est.nbin))
+        rc = _mlp_lib().ps_gpu_learned_finish(self.est._ctx, ctypes.byref(r), _ptr(pc))
+        if rc:
+            raise PowspecError(rc, lib().ps_gpu_last_error(self.est._ctx).decode())
+        return self._post(r, out, pc)
+
     def _execute(self):
         r, out = self.est._result()
         pc = np.zeros((len(POLES), self.est.nbin))
         rc = _mlp_lib().ps_gpu_execute_learned(self.est._ctx, self.mlp._m, ctypes.byref(r), _ptr(pc))
         if rc:
             raise PowspecError(rc, lib().ps_gpu_last_error(self.est._ctx).decode())
+        return self._post(r, out, pc)
+
+    def _post(self, r, out, pc):
         spec = Estimator._spectrum(r, out)
         self._last = spec
         if self._trusted is None:

@@ -212,3 +212,21 @@ def test_fallback_replaces_the_disabled_bins(gpu_lib):
     print(f"Ng=256 CIC noil: uncorrected {e_plain:.4f}, learned + fallback {e_learned:.4f}")
     assert e_learned < 0.01, e_learned
     assert e_plain > 0.01
+
+
+def test_run_many_matches_run(gpu_lib):
+    """LearnedEstimator.run_many (each next assignment enqueued before the
+    previous evaluation is finished) gives each catalogue's run() result."""
+    import torch
+    from powspec_gb300 import catalog, learned
+    cats = [catalog.lognormal(300_000, box=1000.0, seed=s, ngen=64) for s in (3, 4, 5)]
+    n = min(len(c) for c in cats)
+    dev = [torch.from_numpy(np.ascontiguousarray(c[:n])).cuda() for c in cats]
+    with learned.LearnedEstimator(ng=256, assign=3, interlace=True) as le:
+        one = [le.run(device_ptr=d.data_ptr(), n=n) for d in dev]
+        many = le.run_many([d.data_ptr() for d in dev], n)
+    assert len(many) == len(one)
+    for (k1, p1, t1), (k2, p2, t2) in zip(one, many):
+        assert np.array_equal(k1, k2) and np.array_equal(t1, t2)
+        # the same kernels; the binning's FP32 adds may differ in order
+        assert np.abs(p1 - p2).max() <= 5e-6 * np.abs(p1[0]).max()
