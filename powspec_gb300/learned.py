@@ -445,12 +445,36 @@ class LearnedEstimator:
         return self._execute()
 
     def run_stream(self, cats):
-        """run() over host catalogues, the copy of each overlapping the
-        evaluation of the one before (two staging slots).  A configuration
-        that needs the fine-mesh fallback evaluates them one at a time."""
+        """run() over host catalogues: the copy of each next catalogue (two
+        staging slots) and its assignment are enqueued before the previous
+        evaluation's results are waited for, so copies, assignments and
+        evaluations follow each other without the GPU idling.  A
+        configuration that needs the fine-mesh fallback evaluates them one
+        at a time."""
         if self.fine is not None:
             return (self.run(c) for c in cats)
-        return self.est.run_stream(cats, execute=self._execute)
+        return self._stream(cats)
+
+    def _stream(self, cats):
+        est = self.est
+        it = iter(cats)
+        cur = next(it, None)
+        if cur is None:
+            return
+        slot = 0
+        est.stage(slot, cur)
+        est.assign_staged(0, slot)
+        self._launch()
+        while True:
+            nxt = next(it, None)
+            if nxt is not None:
+                est.stage(1 - slot, nxt)
+                est.assign_staged(0, 1 - slot)
+            yield self._finish()
+            if nxt is None:
+                break
+            self._launch()
+            slot = 1 - slot
 
     def run_many(self, device_ptrs, n):
         """run() over catalogues already on the device (32-byte aligned AoS

@@ -31,11 +31,16 @@ def test_stream_matches_single_evaluations(gpu_lib):
         assert (np.abs(g.pl[0] - r.pl[0])[:, use] / scale[use]).max() <= 5e-6
 
 
-def test_learned_stream_matches_run(gpu_lib):
+@pytest.mark.parametrize("ng", [128, 256])
+def test_learned_stream_matches_run(gpu_lib, ng):
+    """Ng = 256 PCS: no fine-mesh fallback, so the stream enqueues each next
+    copy and assignment before the previous results are waited for."""
     torch = pytest.importorskip("torch")
     from powspec_gb300 import learned
     cats = [torch.from_numpy(c).pin_memory().numpy() for c in _cats()[:3]]
-    with learned.LearnedEstimator(ng=128, assign=3, interlace=True) as le:
+    with learned.LearnedEstimator(ng=ng, assign=3, interlace=True) as le:
+        if ng == 256:
+            assert le.fine is None
         got = list(le.run_stream(cats))
         ref = [le.run(c) for c in cats]
     for (k1, p1, t1), (k2, p2, t2) in zip(got, ref):
