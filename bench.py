@@ -475,7 +475,7 @@ def run_gpu(args, world, rank, local):
         def step():
             out = le.run(device_ptr=d_cat.data_ptr(), n=nreal)
             phases[:] += le.est.timings()
-            launches[0] += le.est.launches() + 2  # + feature cast and network kernels
+            launches[0] += le.est.launches()  # passes, features, network, combine
             return out
 
         def step_many(k):
@@ -485,7 +485,7 @@ def run_gpu(args, world, rank, local):
             # the last one run alone)
             res = le.run_many([d_cat.data_ptr()] * k, nreal)
             phases[:] += le.est.timings() * k
-            launches[0] += (le.est.launches() + 2) * k
+            launches[0] += le.est.launches() * k
             return res[-1]
 
         def e2e_stream(k):

@@ -1434,7 +1434,7 @@ int ps_gpu_learned_launch(ps_gpu_ctx* c, ps_mlp* m) {
   a.c = c->d_lc;
   a.out = c->d_lout;
   if ((rc = learned_enqueue(m, a, s))) return fail(c, rc, "learned correction launch failed");
-  c->launches += 4;
+  c->launches += 3;  // features, network, combine
   double* h = c->h_out;
   CU(cudaMemcpyAsync(h, c->d_sums, sizeof(double) * (size_t)nacc * nkey, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(h + (size_t)nacc * nkey, c->d_wsum, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));

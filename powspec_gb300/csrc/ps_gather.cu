@@ -396,8 +396,8 @@ __device__ __forceinline__ bool make_record(const Particle& q, const GatherArgs&
 }
 
 // Key of a particle for the region gather, which takes every record of its
-// home tile (the tile of the plain grid's base node) from one bucket: class
-// 0 of that tile, from the plain grid alone.  The same tile as make_record's.
+// home tile (the tile of the plain grid's base node) from one bucket: the
+// tile's index, from the plain grid alone.  The same tile as make_record's.
 __device__ __forceinline__ bool region_key(const Particle& q, const GatherArgs& g, unsigned& key) {
   if (!q.ok) return false;
   int tile[3];
@@ -409,7 +409,7 @@ __device__ __forceinline__ bool region_key(const Particle& q, const GatherArgs& 
                                g.s_hi[a], g.s_lo[a], g.box[a], g.ng, i, d);
     tile[a] = tile_of(a0.base, g);
   }
-  key = (((unsigned)tile[0] * g.nt + tile[1]) * g.nt + tile[2]) * 27u;
+  key = ((unsigned)tile[0] * g.nt + tile[1]) * g.nt + tile[2];
   return true;
 }
 
@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(32 * kScatterWarps, 4) k_scatter(const __grid_
       Rec r;
       unsigned key;
       make_record(q, g, r, key);
-      if (g.region) key -= key % 27u;  // one bucket per home tile (region_key)
+      if (g.region) key /= 27u;  // one bucket per home tile (region_key)
       slot = g.hist[key] + rk;
       if (g.assign >= 2)
         stage[w][lane] = weighted_record(r, g);
@@ -1056,7 +1056,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
   __shared__ float bound_sum[2];
   const int nt = g.nt;
   const unsigned tile = ((unsigned)blockIdx.z * nt + blockIdx.y) * nt + blockIdx.x;
-  const unsigned beg = g.hist[tile * 27u], end = g.hist[tile * 27u + 27u];
+  const unsigned beg = g.hist[tile], end = g.hist[tile + 1];  // one bucket per tile
   if (beg == end) {  // k_region_sum skips tiles without records
     if (threadIdx.x == 0) g.regflag[tile] = 0;
     return;
@@ -1375,9 +1375,32 @@ size_t gather_keys(int ng) {
   return nt * nt * nt * 27;
 }
 
+// The same for nkeys <= kScanBlock (the region gather's one bucket per
+// tile): one block, the total into hist[n].
+__global__ void __launch_bounds__(256) k_scan_one(unsigned* hist, size_t n) {
+  __shared__ unsigned sh[8];
+  const size_t base = (size_t)threadIdx.x * kScanPer;
+  unsigned v[kScanPer];
+  unsigned s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++) {
+    v[k] = (base + k < n) ? hist[base + k] : 0;
+    s += v[k];
+  }
+  unsigned total;
+  unsigned run = block_exclusive(s, sh, total);
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++) {
+    if (base + k < n) hist[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) hist[n] = total;
+}
+
 int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool int64_out) {
   int n = 0;
-  const size_t nkeys = gather_keys(g.ng);
+  // buckets: (tile, reach class) for the tile gather, one per tile for the region gather
+  const size_t nkeys = g.region ? gather_keys(g.ng) / 27 : gather_keys(g.ng);
   if (!int64_out) {
     cudaMemsetAsync(g.hist, 0, (nkeys + 1) * sizeof(unsigned), s);
     size_t blocks = (p.n + 255) / 256;
@@ -1389,10 +1412,15 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
                                       g.moff, g.moff_scale, g.nomean);
     n++;
     const int nb = (int)((nkeys + kScanBlock - 1) / kScanBlock);
-    k_scan_reduce<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum);
-    k_scan_blocks<<<1, 256, 0, s>>>(g.bsum, nb);
-    k_scan_apply<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum, nb);
-    n += 3;
+    if (nb == 1) {
+      k_scan_one<<<1, 256, 0, s>>>(g.hist, nkeys);
+      n++;
+    } else {
+      k_scan_reduce<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum);
+      k_scan_blocks<<<1, 256, 0, s>>>(g.bsum, nb);
+      k_scan_apply<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum, nb);
+      n += 3;
+    }
     k_scatter<<<(unsigned)blocks, 32 * kScatterWarps, 0, s>>>(g, p);
     n++;
   }

@@ -63,7 +63,7 @@ struct LearnedArgs {
   double volume, kny;
   float assign3, interlace;  // features: scheme / 3, 0 or 1
   int nbin, nmu, npole;      // npole 3: l = 0, 2, 4
-  float* x;                  // [nbin * nmu][16] feature rows
+  float* x;                  // [nbin * nmu][16] feature rows (FP32; not written on the device path)
   void* xb;                  // [nbin * nmu][16] BF16 copy
   float* c;                  // [nbin * nmu] corrections exp(y)
   double* out;               // [npole][nbin] corrected P_l

@@ -501,17 +501,18 @@ __global__ void k_learned_features(const ps::LearnedArgs a) {
   }
   __syncthreads();
   const double q = a.kcen[b] / a.kny;
+  // the rows as the network reads them: FP32 features rounded to BF16
   for (int j = threadIdx.x; j < a.nmu; j += blockDim.x) {
     const double mu = (j + 0.5) / a.nmu;
-    float* xr = a.x + ((size_t)b * a.nmu + j) * kK1;
-    xr[0] = (float)q;
-    xr[1] = (float)(q * q);
-    xr[2] = (float)(mu * mu);
-    xr[3] = a.assign3;
-    xr[4] = a.interlace;
-    xr[5] = (float)s_ratio;
+    bf16* xr = reinterpret_cast<bf16*>(a.xb) + ((size_t)b * a.nmu + j) * kK1;
+    xr[0] = __float2bfloat16((float)q);
+    xr[1] = __float2bfloat16((float)(q * q));
+    xr[2] = __float2bfloat16((float)(mu * mu));
+    xr[3] = __float2bfloat16(a.assign3);
+    xr[4] = __float2bfloat16(a.interlace);
+    xr[5] = __float2bfloat16((float)s_ratio);
 #pragma unroll
-    for (int k = kIn; k < kK1; k++) xr[k] = 0.f;
+    for (int k = kIn; k < kK1; k++) xr[k] = __float2bfloat16(0.f);
   }
 }
 
@@ -550,7 +551,6 @@ int learned_enqueue(::ps_mlp* m, const LearnedArgs& a, cudaStream_t s) {
   if (!m || a.nmu < 1 || a.nmu > 64 || a.npole != 3) return PS_GPU_ERR_ARG;
   const int n = a.nbin * a.nmu;
   k_learned_features<<<a.nbin, 64, 0, s>>>(a);
-  k_to_bf16<<<(unsigned)(((size_t)n * kK1 + 255) / 256), 256, 0, s>>>(a.x, (bf16*)a.xb, (size_t)n * kK1);
   TrainArgs t{};
   t.x = (bf16*)a.xb;
   t.params = m->d_params;
