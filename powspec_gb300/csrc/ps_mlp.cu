@@ -425,6 +425,91 @@ __global__ void k_adam(float* params, float* m, float* v, float* grad, BfWeights
   }
 }
 
+// Inference only (the learned evaluation's c = exp(y) per cell): 4 warps
+// of 16 rows per CTA, the forward weight images and two activation buffers
+// in 35 KB of shared memory (no pre-activations kept), so many CTAs share
+// an SM; the same arithmetic as k_mlp's forward.
+constexpr int kInfWarps = 4;
+struct SmemInf {
+  bf16 w1t[kH * kK1], w2t[kH * kH], w3t[kH * kH];
+  bf16 x[kInfWarps * kGroup * kK1];
+  bf16 h[2][kInfWarps * kGroup * kH];
+  float w4[kH];
+  float b[3][kH];
+  float b4;
+};
+template <int KIN>
+__device__ __forceinline__ void layer_fwd_inf(const bf16* in, const bf16* wt, const float* bias,
+                                              bf16* out, int r0) {
+  const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+  float acc[8][4];
+#pragma unroll
+  for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[nt][q] = 0.f;
+#pragma unroll
+  for (int k0 = 0; k0 < KIN; k0 += 16) {
+    uint32_t a[4];
+    frag_a(in, KIN, r0, k0, a);
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+      uint32_t b[2];
+      frag_b(wt, KIN, nt * 8, k0, b);
+      mma16816(acc[nt], a, b);
+    }
+  }
+#pragma unroll
+  for (int nt = 0; nt < 8; nt++) {
+    const int n = nt * 8 + 2 * t;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int row = r0 + g + ((q & 2) ? 8 : 0);
+      const int col = n + (q & 1);
+      out[row * kH + col] = __float2bfloat16(gelu(acc[nt][q] + bias[col]));
+    }
+  }
+}
+__global__ void __launch_bounds__(32 * kInfWarps) k_mlp_infer(const __grid_constant__ TrainArgs p) {
+  __shared__ __align__(16) SmemInf s;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto copy = [&](const bf16* g, bf16* d, int n) {
+    const uint4* src = reinterpret_cast<const uint4*>(g);
+    uint4* dst = reinterpret_cast<uint4*>(d);
+    for (int e = threadIdx.x; e < n * (int)sizeof(bf16) / 16; e += blockDim.x) dst[e] = src[e];
+  };
+  copy(p.bw->w1t, s.w1t, kH * kK1);
+  copy(p.bw->w2t, s.w2t, kH * kH);
+  copy(p.bw->w3t, s.w3t, kH * kH);
+  for (int e = threadIdx.x; e < kH; e += blockDim.x) {
+    s.w4[e] = p.params[ow4 + e];
+    s.b[0][e] = p.params[ob1 + e];
+    s.b[1][e] = p.params[ob2 + e];
+    s.b[2][e] = p.params[ob3 + e];
+  }
+  if (threadIdx.x == 0) s.b4 = p.params[ob4];
+  const int r0 = warp * kGroup;
+  const int row0 = blockIdx.x * (kInfWarps * kGroup) + r0;
+  for (int e = lane; e < kGroup * kK1; e += 32) {
+    const int rl = e / kK1, c = e % kK1;
+    const int gr = row0 + rl;
+    s.x[(r0 + rl) * kK1 + c] = (gr < p.nrows) ? p.x[(size_t)gr * kK1 + c] : __float2bfloat16(0.f);
+  }
+  __syncthreads();
+  layer_fwd_inf<kK1>(s.x, s.w1t, s.b[0], s.h[0], r0);
+  __syncwarp();
+  layer_fwd_inf<kH>(s.h[0], s.w2t, s.b[1], s.h[1], r0);
+  __syncwarp();
+  layer_fwd_inf<kH>(s.h[1], s.w3t, s.b[2], s.h[0], r0);
+  __syncwarp();
+  if (lane < kGroup && row0 + lane < p.nrows) {
+    const int row = r0 + lane;
+    float y = s.b4;
+#pragma unroll 8
+    for (int n = 0; n < kH; n++) y += __bfloat162float(s.h[0][row * kH + n]) * s.w4[n];
+    p.out[row0 + lane] = __expf(y);
+  }
+}
+
 __global__ void k_to_bf16(const float* x, bf16* y, size_t n) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) y[i] = __float2bfloat16(x[i]);
@@ -558,10 +643,7 @@ int learned_enqueue(::ps_mlp* m, const LearnedArgs& a, cudaStream_t s) {
   t.train = 0;
   t.out = a.c;
   t.nrows = n;
-  const size_t smem = sizeof(Smem);
-  cudaError_t e = cudaFuncSetAttribute(k_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return PS_GPU_ERR_CUDA;
-  k_mlp<<<(n + kRows - 1) / kRows, 256, smem, s>>>(t);
+  k_mlp_infer<<<(n + kInfWarps * kGroup - 1) / (kInfWarps * kGroup), 32 * kInfWarps, 0, s>>>(t);
   k_learned_combine<<<(a.npole * a.nbin + 127) / 128, 128, 0, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : PS_GPU_ERR_CUDA;
 }
@@ -759,8 +841,8 @@ int ps_mlp_infer(ps_mlp* m, const float* x, int n, float* c) {
   a.train = 0;
   a.out = m->d_inf_c;
   a.nrows = n;
-  int rc = launch_mlp(m, a, (n + kRows - 1) / kRows);
-  if (rc) return rc;
+  k_mlp_infer<<<(n + kInfWarps * kGroup - 1) / (kInfWarps * kGroup), 32 * kInfWarps, 0, m->stream>>>(a);
+  MCU(cudaGetLastError());
   MCU(cudaMemcpyAsync(c, m->d_inf_c, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
   MCU(cudaStreamSynchronize(m->stream));
   return 0;
