@@ -415,9 +415,40 @@ class LearnedEstimator:
         self._last = None
         self._x = None
         self._trusted = None
+        self._ctor = dict(ng=ng, box=box, assign=assign, interlace=interlace, poles=POLES, dk=dk,
+                          device=device)
+        self._tuning = None
+        self._lane2 = None  # a second context for run_many(lanes=2)
+
+    def autotune(self, device_ptr, n):
+        """The context's autotuner (Estimator.autotune), its choice kept for
+        the second context of run_many(lanes=2)."""
+        self._tuning = self.est.autotune(device_ptr, n)
+        if self._lane2 is not None:
+            self._apply_tuning(self._lane2)
+        return self._tuning
+
+    def _apply_tuning(self, e):
+        t = dict(self._tuning or {})
+        mask = t.pop("warp_fft", None)
+        if t:
+            e.set_tuning(**t)
+        e.warp_fft(self.est.warp_fft() if mask is None else mask)
+
+    def _lane(self, i):
+        if i == 0:
+            return self.est
+        if self._lane2 is None:
+            e = Estimator(**self._ctor)
+            e.set_mu_bins(NMU)
+            self._apply_tuning(e)
+            self._lane2 = e
+        return self._lane2
 
     def close(self):
         self.est.close()
+        if self._lane2 is not None:
+            self._lane2.close()
         self.mlp.close()
         if self.fine is not None:
             self.fine.close()
@@ -476,39 +507,59 @@ class LearnedEstimator:
             self._launch()
             slot = 1 - slot
 
-    def run_many(self, device_ptrs, n):
+    def run_many(self, device_ptrs, n, lanes=1):
         """run() over catalogues already on the device (32-byte aligned AoS
         records, n each), back to back: each catalogue's assignment is
         enqueued before the previous evaluation's results are waited for
         (ps_gpu_learned_launch / ps_gpu_learned_finish), so the GPU does not
-        idle between evaluations.  Returns one (k, pc, trusted) per catalogue.
-        A configuration that needs the fine-mesh fallback runs them one at a
-        time."""
+        idle between evaluations.  lanes=2 alternates the catalogues between
+        this context and a second one (same configuration and tuning, its own
+        stream and buffers), so that two evaluations are in flight and one's
+        kernels fill the other's gaps and tails.  Returns one (k, pc,
+        trusted) per catalogue, in order.  A configuration that needs the
+        fine-mesh fallback runs them one at a time."""
         ptrs = list(device_ptrs)
         if self.fine is not None or not ptrs:
             return [self.run(device_ptr=p, n=n) for p in ptrs]
-        out = []
-        self.est.assign(0, ptrs[0], on_device=True, n=n)
-        self._launch()
+        ests = [self._lane(k) for k in range(max(1, min(2, int(lanes))))]
+        L = len(ests)
+        out = [None] * len(ptrs)
+
+        def start(i):
+            e = ests[i % L]
+            e.assign(0, ptrs[i], on_device=True, n=n)
+            self._launch(e)
+
+        if L == 1:
+            start(0)
+            for i in range(len(ptrs)):
+                if i + 1 < len(ptrs):
+                    self.est.assign(0, ptrs[i + 1], on_device=True, n=n)
+                out[i] = self._finish()
+                if i + 1 < len(ptrs):
+                    self._launch()
+            return out
+        for i in range(min(L, len(ptrs))):
+            start(i)
         for i in range(len(ptrs)):
-            if i + 1 < len(ptrs):
-                self.est.assign(0, ptrs[i + 1], on_device=True, n=n)
-            out.append(self._finish())
-            if i + 1 < len(ptrs):
-                self._launch()
+            out[i] = self._finish(ests[i % L])
+            if i + L < len(ptrs):
+                start(i + L)
         return out
 
-    def _launch(self):
-        rc = _mlp_lib().ps_gpu_learned_launch(self.est._ctx, self.mlp._m)
+    def _launch(self, est=None):
+        est = est or self.est
+        rc = _mlp_lib().ps_gpu_learned_launch(est._ctx, self.mlp._m)
         if rc:
-            raise PowspecError(rc, lib().ps_gpu_last_error(self.est._ctx).decode())
+            raise PowspecError(rc, lib().ps_gpu_last_error(est._ctx).decode())
 
-    def _finish(self):
-        r, out = self.est._result()
-        pc = np.zeros((len(POLES), self.est.nbin))
-        rc = _mlp_lib().ps_gpu_learned_finish(self.est._ctx, ctypes.byref(r), _ptr(pc))
+    def _finish(self, est=None):
+        est = est or self.est
+        r, out = est._result()
+        pc = np.zeros((len(POLES), est.nbin))
+        rc = _mlp_lib().ps_gpu_learned_finish(est._ctx, ctypes.byref(r), _ptr(pc))
         if rc:
-            raise PowspecError(rc, lib().ps_gpu_last_error(self.est._ctx).decode())
+            raise PowspecError(rc, lib().ps_gpu_last_error(est._ctx).decode())
         return self._post(r, out, pc)
 
     def _execute(self):

@@ -225,8 +225,12 @@ def test_run_many_matches_run(gpu_lib):
     with learned.LearnedEstimator(ng=256, assign=3, interlace=True) as le:
         one = [le.run(device_ptr=d.data_ptr(), n=n) for d in dev]
         many = le.run_many([d.data_ptr() for d in dev], n)
-    assert len(many) == len(one)
-    for (k1, p1, t1), (k2, p2, t2) in zip(one, many):
+        two = le.run_many([d.data_ptr() for d in dev] * 2, n, lanes=2)  # two contexts, in order
+    assert len(many) == len(one) and len(two) == 2 * len(one)
+    for (k1, p1, t1), (k2, p2, t2) in zip(one + one, many + two[len(one):]):
         assert np.array_equal(k1, k2) and np.array_equal(t1, t2)
         # the same kernels; the binning's FP32 adds may differ in order
+        assert np.abs(p1 - p2).max() <= 5e-6 * np.abs(p1[0]).max()
+    for (k1, p1, t1), (k2, p2, t2) in zip(one, two[:len(one)]):
+        assert np.array_equal(k1, k2) and np.array_equal(t1, t2)
         assert np.abs(p1 - p2).max() <= 5e-6 * np.abs(p1[0]).max()
