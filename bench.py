@@ -490,7 +490,7 @@ def run_gpu(args, world, rank, local):
             return res[-1]
 
         def e2e_stream(k):
-            return le.run_stream(itertools.repeat(host_arr, k))
+            return le.run_stream(itertools.repeat(host_arr, k), lanes=LEARNED_LANES)
     else:
         le = None
         step_many = None
@@ -579,7 +579,7 @@ def run_gpu(args, world, rank, local):
     # End to end through the public API with host (pinned) buffers: every
     # step copies its catalogue in (staged, overlapping the step before) and
     # reads its result back.  Staging slots allocated untimed first.
-    for _ in e2e_stream(2):
+    for _ in e2e_stream(4):  # both slots of up to two contexts
         pass
     barrier(world)
     torch.cuda.synchronize()

@@ -475,16 +475,53 @@ class LearnedEstimator:
                 self.fine.assign(0, cat)
         return self._execute()
 
-    def run_stream(self, cats):
+    def run_stream(self, cats, lanes=1):
         """run() over host catalogues: the copy of each next catalogue (two
         staging slots) and its assignment are enqueued before the previous
         evaluation's results are waited for, so copies, assignments and
-        evaluations follow each other without the GPU idling.  A
+        evaluations follow each other without the GPU idling.  lanes=2
+        alternates the catalogues between two contexts (as run_many), each
+        with its own staging slots.  Results come in catalogue order.  A
         configuration that needs the fine-mesh fallback evaluates them one
         at a time."""
         if self.fine is not None:
             return (self.run(c) for c in cats)
+        if int(lanes) >= 2:
+            return self._stream2(cats)
         return self._stream(cats)
+
+    def _stream2(self, cats):
+        ests = [self._lane(0), self._lane(1)]
+        slots = [0, 0]
+        it = iter(cats)
+        order = []  # lanes with an evaluation in flight, oldest first
+
+        def begin(k, c):  # copy, assign and launch on lane k
+            e = ests[k]
+            e.stage(slots[k], c)
+            e.assign_staged(0, slots[k])
+            slots[k] ^= 1
+            self._launch(e)
+            order.append(k)
+
+        for k in range(2):
+            c = next(it, None)
+            if c is None:
+                break
+            begin(k, c)
+        while order:
+            k = order.pop(0)
+            e = ests[k]
+            c = next(it, None)
+            if c is not None:  # the lane's next catalogue, before waiting for its results
+                e.stage(slots[k], c)
+                e.assign_staged(0, slots[k])
+                slots[k] ^= 1
+            res = self._finish(e)
+            if c is not None:
+                self._launch(e)
+                order.append(k)
+            yield res
 
     def _stream(self, cats):
         est = self.est

@@ -31,8 +31,8 @@ def test_stream_matches_single_evaluations(gpu_lib):
         assert (np.abs(g.pl[0] - r.pl[0])[:, use] / scale[use]).max() <= 5e-6
 
 
-@pytest.mark.parametrize("ng", [128, 256])
-def test_learned_stream_matches_run(gpu_lib, ng):
+@pytest.mark.parametrize("ng,lanes", [(128, 1), (256, 1), (256, 2)])
+def test_learned_stream_matches_run(gpu_lib, ng, lanes):
     """Ng = 256 PCS: no fine-mesh fallback, so the stream enqueues each next
     copy and assignment before the previous results are waited for."""
     torch = pytest.importorskip("torch")
@@ -41,7 +41,7 @@ def test_learned_stream_matches_run(gpu_lib, ng):
     with learned.LearnedEstimator(ng=ng, assign=3, interlace=True) as le:
         if ng == 256:
             assert le.fine is None
-        got = list(le.run_stream(cats))
+        got = list(le.run_stream(cats, lanes=lanes))
         ref = [le.run(c) for c in cats]
     for (k1, p1, t1), (k2, p2, t2) in zip(got, ref):
         assert np.array_equal(k1, k2) and np.array_equal(t1, t2)
