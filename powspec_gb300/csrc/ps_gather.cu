@@ -1375,6 +1375,7 @@ size_t gather_keys(int ng) {
   return nt * nt * nt * 27;
 }
 
+namespace {
 // The same for nkeys <= kScanBlock (the region gather's one bucket per
 // tile): one block, the total into hist[n].
 __global__ void __launch_bounds__(256) k_scan_one(unsigned* hist, size_t n) {
@@ -1396,6 +1397,7 @@ __global__ void __launch_bounds__(256) k_scan_one(unsigned* hist, size_t n) {
   }
   if (threadIdx.x == 0) hist[n] = total;
 }
+}  // namespace
 
 int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool int64_out) {
   int n = 0;
