@@ -852,10 +852,8 @@ int enqueue_passes(ps_gpu_ctx* c, double* sums_dst, bool events) {
     a.pipe_grid = pipe ? (c->radix32_a ? 1 : 2) * c->nsm : 0;
     a.radix32 = c->radix32_a ? 1 : 0;
     a.err = c->d_err + 2;
-    a.grid = nullptr;
     a.fgrid = (const float*)c->grid[f];
     a.out = c->cbuf[f];
-    a.wsum = c->d_wsum + 2 * (f / c->mpc);
     a.tw_half = c->d_tw_half;
     a.tw_full = c->d_tw_full;
     a.plan_half = c->plan_half;
@@ -1544,10 +1542,8 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   memset(&a, 0, sizeof a);
   a.ng = ng;
   a.ty = c->ty_a;
-  a.grid = nullptr;
   a.fgrid = d_in;
   a.out = c->cbuf[0];
-  a.wsum = nullptr;
   a.tw_half = c->d_tw_half;
   a.tw_full = c->d_tw_full;
   a.plan_half = c->plan_half;

@@ -35,27 +35,15 @@ __global__ void __launch_bounds__(kFftThreads, 2) k_pass_a(const __grid_constant
   const int y0 = (blockIdx.x - x * nty) * a.ty;
   const int nl = min(a.ty, ng - y0);
 
-  if (a.grid) {
-    // Mean cell value in fixed point (any constant works: it only moves k = 0).
-    const double W = *a.wsum;
-    const long long off = __double2ll_rn(W * 4294967296.0 / ((double)ng * ng * ng));
-    const long long* base = a.grid + ((size_t)x * ng + y0) * ng;
-    for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
-      const int r = e / M, m = e - r * M;
-      const longlong2 q = __ldcs(reinterpret_cast<const longlong2*>(base + (size_t)r * ng) + m);
-      sm[r * ls + lidx<P2>(m)] = make_float2(fix_to_float(q.x - off), fix_to_float(q.y - off));
+  const float* base = a.fgrid + ((size_t)x * ng + y0) * ng;
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+    const int r = e / M, m = e - r * M;
+    float2 v = __ldcs(reinterpret_cast<const float2*>(base + (size_t)r * ng) + m);
+    if (a.yw) {
+      v.x *= cell_harmonic(a, x, y0 + r, 2 * m);
+      v.y *= cell_harmonic(a, x, y0 + r, 2 * m + 1);
     }
-  } else {
-    const float* base = a.fgrid + ((size_t)x * ng + y0) * ng;
-    for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
-      const int r = e / M, m = e - r * M;
-      float2 v = __ldcs(reinterpret_cast<const float2*>(base + (size_t)r * ng) + m);
-      if (a.yw) {
-        v.x *= cell_harmonic(a, x, y0 + r, 2 * m);
-        v.y *= cell_harmonic(a, x, y0 + r, 2 * m + 1);
-      }
-      sm[r * ls + lidx<P2>(m)] = v;
-    }
+    sm[r * ls + lidx<P2>(m)] = v;
   }
   __syncthreads();
   if (P2)
@@ -294,13 +282,13 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma
 }  // namespace
 
 int launch_pass_a(const PassAArgs& a, cudaStream_t s) {
-  if (a.twl && !a.grid && !a.yw && launch_pass_a_w(a, s)) return 1;
+  if (a.twl && !a.yw && launch_pass_a_w(a, s)) return 1;
   const int M = a.ng / 2;
   const bool p2 = a.plan_half.logn >= 0;
   const size_t smem = (size_t)a.ty * line_stride(M + 1, p2) * sizeof(float2);
   const int nty = (a.ng + a.ty - 1) / a.ty;
   const unsigned grid = (unsigned)(a.ng * nty);
-  if (p2 && !a.grid && a.pipe_grid > 0) {
+  if (p2 && a.pipe_grid > 0) {
     const size_t sm2 = 128 + 3 * ((((size_t)a.ty * line_stride(M + 1, true)) + 1) & ~(size_t)1) * 8;
     if (a.radix32) {
       cudaFuncSetAttribute(k_pass_a_tma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);

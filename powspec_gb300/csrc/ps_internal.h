@@ -106,10 +106,8 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
 struct PassAArgs {
   int ng;
   int ty;                       // y rows per CTA
-  const long long* grid;        // fixed-point input, or NULL
-  const float* fgrid;           // FP32 input when grid == NULL
+  const float* fgrid;           // FP32 input mesh
   float2* out;
-  const double* wsum;           // mean offset source: wsum[0] = W
   const float2* tw_half;        // length ng/2 twiddles
   const float2* tw_full;        // length ng twiddles (r2c split)
   FftPlan plan_half;
