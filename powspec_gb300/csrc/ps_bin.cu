@@ -10,7 +10,7 @@
 // |k| grows monotonically, and keeps the run's sums in registers while the
 // bin stays the same; on a bin change it adds them to FP32 per-tile
 // accumulators in shared memory.  After each tile the touched bins are added
-// into this CTA's FP64 slice of a partial-sum array in global memory, which
+// into this CTA's slice of a partial-sum array in global memory (FP32 pairs), which
 // a final kernel reduces over CTAs in a fixed order.
 #include "ps_bin_core.cuh"
 

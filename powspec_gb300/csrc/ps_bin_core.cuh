@@ -5,7 +5,8 @@
 // |k| grows monotonically, and keeps the run's sums in registers while the
 // bin stays the same; on a bin change it adds them to FP32 per-tile
 // accumulators in shared memory.  After every few tiles the touched bins are
-// added into the CTA's FP64 slice of a partial-sum array in global memory,
+// added into the CTA's slice of a partial-sum array in global memory (FP32
+// pairs),
 // which a final kernel reduces over CTAs in a fixed order.
 //
 // Reference: dens_k0's interlace combine (src/multipole.c:462-487) and
@@ -110,7 +111,7 @@ __device__ void merge_tile(float* tacc, int* srange, float2* part, int nacc, int
 // instead of a Horner evaluation per pole.  The merge turns them into the
 // Legendre sums, sum p L_l(mu) = sum_j c_lj M_j with the exact coefficients
 // of L_l in mu^2 (math/legpoly.h:47-62), combined in FP32 and added into
-// the FP64 partials.
+// the FP32-pair partials.
 template <int NSPEC, int MOM>
 struct MomAcc {
   int bin;
@@ -154,7 +155,7 @@ __device__ __forceinline__ void mom_add(MomAcc<NSPEC, MOM>& ra, int b, int nkey,
 }
 
 // Merge of moment tile sums: the Legendre sums of the touched keys are added
-// into the CTA's FP64 slice [NSPEC][npole][nkey], the moments cleared.
+// into the CTA's FP32-pair slice [NSPEC][npole][nkey], the moments cleared.
 template <int NSPEC, int MOM>
 __device__ void merge_tile_mom(float* tacc, int* srange, float2* part, const ModeGeom& g,
                                int nkey) {

@@ -195,10 +195,10 @@ constexpr int kMaxWarpsC = 16;  // warps per CTA of the x pass: 4 or 16 (host's 
 // x transform + combine + window + binning.  A work item of a warp is NP
 // consecutive ky at one kz (NP > 1 when a transform holds more lines than
 // there are fields); every CTA step gives one item to each warp, and the
-// tile sums are merged into the CTA's FP64 partials every kMergeEvery steps
-// of 4 warps' items (fewer steps with more warps).  Large tile sums (|mu|
-// sub-bins) take the CTA's shared memory: then 8 or 16 warps share them, so
-// that more warps are resident.
+// tile sums are merged into the CTA's FP32-pair partials every kMergeEvery
+// steps of 4 warps' items (fewer steps with more warps).  Large tile sums
+// (|mu| sub-bins) take the CTA's shared memory: then 16 warps share them,
+// so that more warps are resident.
 template <int N, int NSPEC, int MOM, int WPC>
 __global__ void __launch_bounds__(32 * WPC, WPC == 4 ? 0 : 2) k_pass_c_w(const __grid_constant__ PassCArgs a) {
   using S = WF<N>;
