@@ -6,8 +6,7 @@
 // bin stays the same; on a bin change it adds them to FP32 per-tile
 // accumulators in shared memory.  After every few tiles the touched bins are
 // added into the CTA's slice of a partial-sum array in global memory (FP32
-// pairs),
-// which a final kernel reduces over CTAs in a fixed order.
+// pairs), which a final kernel reduces over CTAs in a fixed order.
 //
 // Reference: dens_k0's interlace combine (src/multipole.c:462-487) and
 // count_mode_sim_lin/_log (src/multipole.c:778-1031).
