@@ -1172,6 +1172,7 @@ void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* o
   a.tw_half = c->d_tw_half;
   a.tw_full = c->d_tw_full;
   a.plan_half = c->plan_half;
+  a.twl = (c->wfft & 1) ? c->d_twl_half : nullptr;
   a.err = c->d_err + 2;
   launch_pass_a(a, s);
   PassBArgs b;
@@ -1184,6 +1185,7 @@ void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* o
   b.out = a2;
   b.tw_full = c->d_tw_full;
   b.plan_full = c->plan_full;
+  b.twl = (c->wfft & 2) ? c->d_twl_full : nullptr;
   b.err = c->d_err + 2;
   launch_pass_b(b, s);
   PassCArgs pc;

@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kFftThreads, MAXLOG == 4 ? 2 : 1) k_pass_b_tma
 }  // namespace
 
 int launch_pass_a(const PassAArgs& a, cudaStream_t s) {
-  if (a.twl && !a.yw && launch_pass_a_w(a, s)) return 1;
+  if (a.twl && launch_pass_a_w(a, s)) return 1;
   const int M = a.ng / 2;
   const bool p2 = a.plan_half.logn >= 0;
   const size_t smem = (size_t)a.ty * line_stride(M + 1, p2) * sizeof(float2);

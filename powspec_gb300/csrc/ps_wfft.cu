@@ -114,6 +114,17 @@ __global__ void __launch_bounds__(32 * kWarpsAB) k_pass_a_w(const __grid_constan
   float2 v[S::V];
 #pragma unroll
   for (int m = 0; m < S::V; m++) v[m] = __ldcs(src + m * S::L);
+  if (a.yw && (x != 0 || y0 + r != 0)) {
+    // survey harmonic: cell (x, y, z) weighted by Y_lm of its position,
+    // the (x, y) part once per line (1 on the row x = y = 0, as in k_pass_a)
+    const YlmRow w = ylm_row(a.yc, (x + a.org[0]) * a.len[0], (y0 + r + a.org[1]) * a.len[1]);
+#pragma unroll
+    for (int m = 0; m < S::V; m++) {
+      const int z = 2 * (l + S::L * m);
+      v[m].x *= ylm_cell(a.yc, w, (z + a.org[2]) * a.len[2]);
+      v[m].y *= ylm_cell(a.yc, w, (z + 1 + a.org[2]) * a.len[2]);
+    }
+  }
   wfft<M>(v, scr, a.twl, lane);
 #pragma unroll
   for (int j = 0; j < S::R; j++)
