@@ -425,6 +425,7 @@ void launch_c_p(const PassCArgs& a, cudaStream_t s) {
 
 int launch_pass_c(const PassCArgs& a, cudaStream_t s) {
   if (a.twl && !a.store && launch_pass_c_w(a, s)) return 1;
+  if (a.twl && a.store && launch_pass_c_ws(a, s)) return 1;
   if (a.plan_full.logn >= 0)
     launch_c_p<true>(a, s);
   else

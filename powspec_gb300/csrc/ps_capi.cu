@@ -1206,6 +1206,7 @@ void r2c_store(ps_gpu_ctx* c, const float* in, float2* a1, float2* a2, float2* o
   pc.tw_full = c->d_tw_full;
   pc.plan_full = c->plan_full;
   pc.geom = c->geom;
+  pc.twl = (c->wfft & 4) ? c->d_twl_full : nullptr;
   launch_pass_c(pc, s);
   c->launches += 3;
 }
@@ -1579,6 +1580,7 @@ int ps_gpu_fft_r2c_host(ps_gpu_ctx* c, const float* in, float* out) {
   pc.tw_full = c->d_tw_full;
   pc.plan_full = c->plan_full;
   pc.geom = c->geom;
+  pc.twl = (c->wfft & 4) ? c->d_twl_full : nullptr;
   launch_pass_c(pc, s);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(out, c->cbuf[0], c->ncx * sizeof(float2), cudaMemcpyDeviceToHost, s));

@@ -202,6 +202,8 @@ void wfft_shape(int n, int* L, int* V);
 int launch_pass_a_w(const PassAArgs& a, cudaStream_t s);  // 0: shape not supported
 int launch_pass_b_w(const PassBArgs& a, cudaStream_t s);
 int launch_pass_c_w(const PassCArgs& a, cudaStream_t s);
+// The store-mode x pass (one field, survey harmonic terms); 0 without a warp form.
+int launch_pass_c_ws(const PassCArgs& a, cudaStream_t s);
 // Dynamic shared memory and block size of the warp x pass (persistent CTAs).
 size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey, int wpc);
 

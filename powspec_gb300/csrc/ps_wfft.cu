@@ -184,6 +184,59 @@ __global__ void __launch_bounds__(32 * kWarpsAB) k_pass_b_w(const __grid_constan
   }
 }
 
+// x transform in store mode (survey harmonic terms): a CTA takes 8 lines
+// of consecutive kz at one ky (one field), each warp transforms G of them,
+// and through a shared [kx][9] tile (over the transpose areas, after a CTA
+// barrier) the CTA writes F[x][y][kz] in runs of 8 kz: out = X (acc_mode 0), X * Y_lm(k^) (1) or out + X * Y_lm(k^) (2),
+// Y_lm = 1 for k_x = k_y = 0 (src/mp_template.c:118-121), as k_pass_c.
+constexpr int kStoreKz = 8;
+template <int N>
+__global__ void __launch_bounds__(32 * (kStoreKz / WF<N>::G)) k_pass_c_ws(const __grid_constant__ PassCArgs a) {
+  using S = WF<N>;
+  constexpr int ngk = N / 2 + 1, TP = kStoreKz + 1;
+  constexpr int nkt = (ngk + kStoreKz - 1) / kStoreKz;
+  extern __shared__ float2 wsm[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane / S::L, l = lane - g * S::L;
+  float2* T = wsm;  // [N][TP], over the warps' transpose areas once they are done
+  float2* scr = wsm + w * S::SWARP;
+  const int ky = blockIdx.x / nkt, kz0 = (blockIdx.x - ky * nkt) * kStoreKz;
+  const int nl = min(kStoreKz, ngk - kz0);
+  const int r = w * S::G + g;  // this group's line: kz0 + r
+  const bool live = r < nl;
+  const float2* src = a.in[0] + ((size_t)(live ? kz0 + r : kz0) * N + ky) * N + l;
+  float2 v[S::V];
+#pragma unroll
+  for (int m = 0; m < S::V; m++) v[m] = __ldcs(src + m * S::L);
+  wfft<N>(v, scr, a.twl, lane);
+  __syncthreads();
+  if (live) {
+#pragma unroll
+    for (int j = 0; j < S::R; j++)
+#pragma unroll
+      for (int k2 = 0; k2 < S::L; k2++) T[((l * S::R + j) + S::V * k2) * TP + r] = v[j * S::L + k2];
+  }
+  __syncthreads();
+  const int jp = dsigned(ky, N);
+  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
+    const int i = e / nl, rr = e - i * nl;
+    const size_t idx = ((size_t)i * N + ky) * ngk + kz0 + rr;
+    float2 x = T[i * TP + rr];
+    if (a.acc_mode) {
+      const int ip = dsigned(i, N);
+      const float y = (ip == 0 && jp == 0)
+                          ? 1.f
+                          : ylm_eval(a.yk, ip * a.kinv[0], jp * a.kinv[1], (kz0 + rr) * a.kinv[2]);
+      x = make_float2(x.x * y, x.y * y);
+      if (a.acc_mode == 2) {
+        const float2 o = a.store[idx];
+        x = make_float2(x.x + o.x, x.y + o.y);
+      }
+    }
+    a.store[idx] = x;
+  }
+}
+
 // Complex values per warp of the x pass: NP positions x nfield lines in the
 // padded layout, plus what the transpose area needs beyond G lines.
 template <int N>
@@ -554,6 +607,25 @@ int launch_pass_b_w(const PassBArgs& a, cudaStream_t s) {
     default: return 0;
   }
 #undef PS_B_W
+}
+
+int launch_pass_c_ws(const PassCArgs& a, cudaStream_t s) {
+  if (a.nfield != 1 || !a.store) return 0;
+#define PS_C_WS(N)                                                                                \
+  {                                                                                               \
+    constexpr int W = kStoreKz / WF<N>::G;                                                        \
+    const size_t smem = std::max((size_t)(N) * (kStoreKz + 1), (size_t)W * WF<N>::SWARP) * sizeof(float2); \
+    cudaFuncSetAttribute(k_pass_c_ws<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    k_pass_c_ws<N><<<(unsigned)((N) * (((N) / 2 + 1 + kStoreKz - 1) / kStoreKz)), 32 * W, smem, s>>>(a); \
+    return 1;                                                                                     \
+  }
+  switch (a.ng) {
+    case 256: PS_C_WS(256)
+    case 512: PS_C_WS(512)
+    case 1024: PS_C_WS(1024)
+    default: return 0;
+  }
+#undef PS_C_WS
 }
 
 int launch_pass_c_w(const PassCArgs& a, cudaStream_t s) {
