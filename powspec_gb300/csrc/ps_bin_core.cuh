@@ -318,6 +318,100 @@ __device__ __forceinline__ void bin_lines_pair(const PassCArgs& a, const float2*
   }
 }
 
+// The +-k_y pairing of bin_lines_pair, for a warp that holds one line per
+// field at a time (line ky, then line Ng - ky, at one kz): with the line of
+// sight along z the four modes (+-k_x, +-k_y, k_z) share |k|, mu, the bin
+// and the |mu| sub-bin, so the geometry is evaluated once for the four.
+// Each lane keeps the windowed, combined powers of its runs of |k_x| in
+// registers between the two lines (ypair_powers), then walks the geometry
+// (ypair_bin); runs as in bin_lines_pair, the last one taking k_x = Ng/2.
+template <int N>
+struct YPairRuns {
+  static constexpr int RP = (N / 64 < kRun) ? N / 64 : kRun;  // modes per run
+  static constexpr int NC = (N / 2) / RP / 32;                // runs per lane
+};
+
+template <int N, int NSPEC>
+__device__ __forceinline__ void ypair_powers(
+    const PassCArgs& a, const float2* X, int ls, int kz, int ky,
+    float (&pw)[YPairRuns<N>::NC][YPairRuns<N>::RP + 1][NSPEC], bool add, int lane,
+    const int (&spec_a)[NSPEC], const int (&spec_b)[NSPEC]) {
+  using Y = YPairRuns<N>;
+  constexpr int half = N / 2;
+  const ModeGeom& g = a.geom;
+  const int jp = dsigned(ky, N);
+  const bool twice = !(kz == 0 || 2 * kz == N);
+  const float wjk = __ldg(&g.win[N + ky]) * __ldg(&g.win[2 * N + kz]) * (twice ? 2.f : 1.f);
+#pragma unroll
+  for (int c = 0; c < Y::NC; c++) {
+    const int i0 = (lane + 32 * c) * Y::RP;
+#pragma unroll
+    for (int k = 0; k <= Y::RP; k++) {
+      const int i = i0 + k;
+      if (k == Y::RP && i != half) continue;  // only the last run takes k_x = Ng/2
+      float p[NSPEC];
+      mode_power<NSPEC, true>(a, X, ls, 1, 0, i, i, jp, kz, wjk, spec_a, spec_b, p);
+      if (i != 0 && i != half) {  // the mode at -k_x
+        float q[NSPEC];
+        mode_power<NSPEC, true>(a, X, ls, 1, 0, N - i, -i, jp, kz, wjk, spec_a, spec_b, q);
+#pragma unroll
+        for (int s = 0; s < NSPEC; s++) p[s] += q[s];
+      }
+#pragma unroll
+      for (int s = 0; s < NSPEC; s++) pw[c][k][s] = add ? pw[c][k][s] + p[s] : p[s];
+    }
+  }
+}
+
+template <int N, int NSPEC, int MOM>
+__device__ __forceinline__ void ypair_bin(
+    const PassCArgs& a, int kz, int kyp,
+    const float (&pw)[YPairRuns<N>::NC][YPairRuns<N>::RP + 1][NSPEC], float* tacc, int& lo,
+    int& hi, int lane) {
+  using Y = YPairRuns<N>;
+  constexpr int half = N / 2;
+  const ModeGeom& g = a.geom;
+  const int nkey = g.nbin * g.nmu;
+  const float kzf = g.vec[2] * (float)kz;
+  const float kyf = g.vec[1] * (float)kyp;
+  const float mu_yz = kyf * g.los[1] + kzf * g.los[2];  // los[1] = 0: the same for -k_y
+  const float k2_yz = kyf * kyf + kzf * kzf;
+  const int n_yz = kyp * kyp + kz * kz;
+#pragma unroll
+  for (int c = 0; c < Y::NC; c++) {
+    const int i0 = (lane + 32 * c) * Y::RP;
+    MomAcc<NSPEC, MOM> rm;
+    rm.bin = -1;
+#pragma unroll
+    for (int s = 0; s < NSPEC; s++)
+#pragma unroll
+      for (int j = 0; j < MOM; j++) rm.v[s][j] = 0.f;
+#pragma unroll
+    for (int k = 0; k <= Y::RP; k++) {
+      const int i = i0 + k;
+      if (k == Y::RP && i != half) continue;
+      const int n = i * i + n_yz;
+      if (n == 0) continue;  // DC (src/multipole.c:806)
+      const float kxf = g.vec[0] * (float)i;
+      const float rq = rsqrtf(kxf * kxf + k2_yz);
+      int b;
+      if (g.fastbin) {
+        const float t = (fmaf(kxf, kxf, k2_yz) * rq - g.k0f) * g.inv_dkf;
+        const float fl = floorf(t), fr = t - fl;
+        b = (fr > g.eps_t && fr < 1.f - g.eps_t) ? ((fl < 0.f || fl >= (float)g.nbin) ? -1 : (int)fl)
+                                                 : mode_bin(g, i, kyp, kz, n);
+      } else {
+        b = mode_bin(g, i, kyp, kz, n);
+      }
+      if (b < 0) continue;
+      const float mu = mu_yz * rq;
+      const int key = (g.nmu == 1) ? b : b * g.nmu + min(g.nmu - 1, (int)(fabsf(mu) * g.nmu));
+      mom_add<NSPEC, MOM>(rm, key, nkey, pw[c][k], mu, tacc, lo, hi);
+    }
+    mom_flush<NSPEC, MOM>(rm, tacc, nkey, lo, hi);
+  }
+}
+
 template <int NSPEC, bool P2, int MOM>
 __device__ __forceinline__ void bin_lines(const PassCArgs& a, const float2* X, int ls, int kz,
                                           int ky0, int nl, float* tacc, int& lo, int& hi,

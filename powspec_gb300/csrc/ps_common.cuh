@@ -441,8 +441,6 @@ __device__ __forceinline__ float2* fft_lines_pp(float2* a, float2* b, const FftP
   return a;
 }
 
-// Fixed-point cell (minus a constant offset) -> float.  d = hi * 2^32 + lo,
-// value = d * 2^-32 = hi + lo * 2^-32, using two 32-bit conversions.
 // s += a + b as an unevaluated FP32 pair (hi, lo), renormalised after
 // each add: TwoSum of hi and a (exact), the low parts added, then hi + lo
 // recombined (Fast2Sum).  Each add loses about 2^-48 of the running sum.
@@ -454,6 +452,8 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float a, float b) {
   lo = l - (hi - t);
 }
 
+// Fixed-point cell (minus a constant offset) -> float.  d = hi * 2^32 + lo,
+// value = d * 2^-32 = hi + lo * 2^-32, using two 32-bit conversions.
 __device__ __forceinline__ float fix_to_float(long long d) {
   const int hi = (int)(d >> 32);
   const unsigned lo = (unsigned)(d & 0xffffffffull);

@@ -1036,6 +1036,36 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// FP32 form of a region (the FP32 meshes): word (row, rem) of the region's
+// [R][R][RG][NM] layout (row = x * R + y, rem = z * NM + mesh) as FP32, the
+// mean cell value subtracted in fixed point from the tile's own cells
+// (region index [1 - of, T + 1 - of) on every axis), so that a cell's sum
+// over its regions carries the mean once.  NM == 2: four words per 16-byte
+// store, NM == 1: two per 8-byte store.  word(row, rem) -> fixed-point sum.
+template <int S, int NM, class Word>
+__device__ __forceinline__ void region_out_f32(const GatherArgs& g, unsigned tile, Word word) {
+  constexpr int R = RegGeom<S>::R, RG = RegGeom<S>::RG, RP = RegGeom<S>::RP;
+  constexpr int T = kRegT, of = (S >= 3) ? -1 : 0, ROW = RG * NM, V = 2 * NM;
+  static_assert((NM * RP) % V == 0, "whole stores per region");
+  const long long off = *g.moff;
+  float* o = reinterpret_cast<float*>(g.regbuf) + (size_t)tile * NM * RP;
+  for (int e = threadIdx.x; e < NM * RP / V; e += blockDim.x) {
+    float v[V];
+#pragma unroll
+    for (int j = 0; j < V; j++) {
+      const int wi = V * e + j, row = wi / ROW, rem = wi - row * ROW;
+      const int ux = row / R, uy = row - ux * R, uz = rem / NM;
+      const bool home = (unsigned)(ux - 1 + of) < (unsigned)T && (unsigned)(uy - 1 + of) < (unsigned)T &&
+                        (unsigned)(uz - 1 + of) < (unsigned)T;
+      v[j] = fix_to_float(word(row, rem) - (home ? off : 0ll));
+    }
+    if constexpr (NM == 2)
+      *reinterpret_cast<float4*>(o + V * e) = make_float4(v[0], v[1], v[2], v[3]);
+    else
+      *reinterpret_cast<float2*>(o + V * e) = make_float2(v[0], v[1]);
+  }
+}
+
 // ---- region gather.  One CTA per home tile (the tile of the plain grid's
 // base node): each record is added once, into shared-memory accumulators
 // that cover every node its stencils reach, local cells [of - 1, T + of +
@@ -1169,6 +1199,43 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     const float room = 2147483648.f * (float)(65536u - nrec);  // 2^47 - n 2^31, exact
     split = bound_sum[0] < room && bound_sum[1] < room;
     if (split) {
+      if constexpr (NM == 2) {
+        if (g.reg_f32) {
+          // FP32 regions (see region_out_f32): four words, two cells of both
+          // meshes, per thread and step, from 16-byte loads of each array
+          constexpr int T = kRegT, of = (S >= 3) ? -1 : 0, ROW = RG * NM;
+          static_assert(ROW % 4 == 0 && (RZ * NM) % 4 == 0 && HW % 4 == 0, "16-byte groups");
+          const long long off = *g.moff;
+          float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(g.regbuf) + (size_t)tile * NM * RP);
+          for (int e = threadIdx.x; e < NM * RP / 4; e += blockDim.x) {
+            const int row = (4 * e) / ROW, rem = 4 * e - row * ROW;
+            const int ux = row / R, uy = row - ux * R, uz = rem / NM;
+            const bool hxy = (unsigned)(ux - 1 + of) < (unsigned)T && (unsigned)(uy - 1 + of) < (unsigned)T;
+            const long long o0 = (hxy && (unsigned)(uz - 1 + of) < (unsigned)T) ? off : 0ll;
+            const long long o1 = (hxy && (unsigned)(uz + of) < (unsigned)T) ? off : 0ll;
+            const int w = row * RZ * NM + rem;
+            const uint4 lo = *reinterpret_cast<const uint4*>(w32 + w);
+            const int4 hi = *reinterpret_cast<const int4*>(w32 + HW + w);
+            auto join = [](unsigned l, int h) {
+              return ((long long)h << 16) + (long long)(l - ((unsigned)h << 16));
+            };
+            o[e] = make_float4(fix_to_float(join(lo.x, hi.x) - o0), fix_to_float(join(lo.y, hi.y) - o0),
+                               fix_to_float(join(lo.z, hi.z) - o1), fix_to_float(join(lo.w, hi.w) - o1));
+          }
+          if (threadIdx.x == 0) g.regflag[tile] = 1;
+          return;
+        }
+      }
+      if (g.reg_f32) {
+        region_out_f32<S, NM>(g, tile, [&](int row, int rem) {
+          const int w = row * RZ * NM + rem;
+          const unsigned lo = w32[w];
+          const int hi = reinterpret_cast<const int*>(w32 + HW)[w];
+          return ((long long)hi << 16) + (long long)(lo - ((unsigned)hi << 16));
+        });
+        if (threadIdx.x == 0) g.regflag[tile] = 1;
+        return;
+      }
       // out as [R][R][RG][NM] (meshes interleaved): a pair of words per
       // thread and step, one 16-byte store; the padding column z = R reads
       // zeros
@@ -1209,6 +1276,13 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     records(proc);
   }
   __syncthreads();
+  if (g.reg_f32) {
+    region_out_f32<S, NM>(g, tile, [&](int row, int rem) {
+      return (long long)acc[(rem % NM) * SM + row * RZ + rem / NM];
+    });
+    if (threadIdx.x == 0) g.regflag[tile] = 1;
+    return;
+  }
   // out as [R][R][RG][NM], as above
   longlong2* o = reinterpret_cast<longlong2*>(g.regbuf + (size_t)tile * NM * RP);
   constexpr int ROW = RG * NM;
@@ -1264,10 +1338,26 @@ __device__ __forceinline__ void load_pair(const unsigned long long* p, long long
   }
 }
 
+template <int NM>
+__device__ __forceinline__ void load_pair_f32(const float* p, float (&v)[2 * NM]) {
+  if constexpr (NM == 2) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+  } else {
+    const float2 q = *reinterpret_cast<const float2*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+  }
+}
+
 // Mesh from the regions: a pair of consecutive z cells of every mesh per
-// thread (a warp reads 32 consecutive pairs: whole sectors), the FP32 value
-// minus the mean cell value (or the exact fixed-point sum).  Regions are
-// [R][R][RG][NM] words; a cell pair starts on an even region cell.  A tile
+// thread (a warp reads 32 consecutive pairs: whole sectors), the FP32 sum
+// of the FP32 regions, or from int64 regions the exact fixed-point sum
+// (INT64) or its FP32 value minus the mean.  Regions are [R][R][RG][NM]
+// words; a cell pair starts on an even region cell.  A tile
 // without records wrote neither its region nor a flag of 1, and its words
 // (loaded alongside the flag) are dropped.
 template <int S, int NM, bool INT64>
@@ -1284,6 +1374,8 @@ __global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ Gath
   const size_t work = (size_t)ng * ng * nh;
   const long long off = INT64 ? 0 : *g.moff;  // mean cell value (k_wsum)
   const unsigned long long* const rb = g.regbuf;
+  const float* const rbf = reinterpret_cast<const float*>(g.regbuf);  // FP32 regions
+  const float mean_neg = fix_to_float(-off);  // a cell whose home tile has no records
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < work;
        e += (size_t)gridDim.x * blockDim.x) {
     const int zh = (int)(e % (size_t)nh);
@@ -1303,40 +1395,72 @@ __global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ Gath
       tz2 = (tz == nt - 1) ? 0 : tz + 1;
       cz2 = uz - T - of + 1;
     }
-    long long s[2 * NM];
+    if (!INT64 && g.reg_f32) {
+      // FP32 regions, the home tile's (which carries the mean) first
+      float s[2 * NM];
 #pragma unroll
-    for (int k = 0; k < 2 * NM; k++) s[k] = 0;
-    for (int a = 0; a < nx; a++)
-      for (int b = 0; b < ny; b++) {
-        const unsigned tb = ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt;
-        const int row = (ix[a] * R + iy[b]) * RG;
-        const unsigned t0 = tb + tz;
-        const bool f0 = g.regflag[t0] != 0;
-        long long v0[2 * NM], v1[2 * NM];
-        load_pair<NM>(rb + ((size_t)t0 * RP + (size_t)(row + uz - of + 1)) * NM, v0);
-        bool f1 = false;
-        if (tz2 >= 0) {
-          const unsigned t1 = tb + tz2;
-          f1 = g.regflag[t1] != 0;
-          load_pair<NM>(rb + ((size_t)t1 * RP + (size_t)(row + cz2)) * NM, v1);
-        }
-        if (f0) {
+      for (int k = 0; k < 2 * NM; k++) s[k] = 0.f;
+      for (int a = 0; a < nx; a++)
+        for (int b = 0; b < ny; b++) {
+          const unsigned tb = ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt;
+          const int row = (ix[a] * R + iy[b]) * RG;
+          const unsigned t0 = tb + tz;
+          const bool f0 = g.regflag[t0] != 0;
+          float v0[2 * NM], v1[2 * NM];
+          load_pair_f32<NM>(rbf + ((size_t)t0 * RP + (size_t)(row + uz - of + 1)) * NM, v0);
+          bool f1 = false;
+          if (tz2 >= 0) {
+            const unsigned t1 = tb + tz2;
+            f1 = g.regflag[t1] != 0;
+            load_pair_f32<NM>(rbf + ((size_t)t1 * RP + (size_t)(row + cz2)) * NM, v1);
+          }
 #pragma unroll
-          for (int k = 0; k < 2 * NM; k++) s[k] += v0[k];
-        }
-        if (f1) {
+          for (int k = 0; k < 2 * NM; k++) s[k] += f0 ? v0[k] : ((a == 0 && b == 0) ? mean_neg : 0.f);
+          if (f1) {
 #pragma unroll
-          for (int k = 0; k < 2 * NM; k++) s[k] += v1[k];
+            for (int k = 0; k < 2 * NM; k++) s[k] += v1[k];
+          }
         }
+      const size_t cell = ((size_t)x * ng + y) * ng + z;
+#pragma unroll
+      for (int m = 0; m < NM; m++)
+        *reinterpret_cast<float2*>(g.out[m] + cell) = make_float2(s[m], s[NM + m]);
+    } else {
+      long long s[2 * NM];
+#pragma unroll
+      for (int k = 0; k < 2 * NM; k++) s[k] = 0;
+      for (int a = 0; a < nx; a++)
+        for (int b = 0; b < ny; b++) {
+          const unsigned tb = ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt;
+          const int row = (ix[a] * R + iy[b]) * RG;
+          const unsigned t0 = tb + tz;
+          const bool f0 = g.regflag[t0] != 0;
+          long long v0[2 * NM], v1[2 * NM];
+          load_pair<NM>(rb + ((size_t)t0 * RP + (size_t)(row + uz - of + 1)) * NM, v0);
+          bool f1 = false;
+          if (tz2 >= 0) {
+            const unsigned t1 = tb + tz2;
+            f1 = g.regflag[t1] != 0;
+            load_pair<NM>(rb + ((size_t)t1 * RP + (size_t)(row + cz2)) * NM, v1);
+          }
+          if (f0) {
+#pragma unroll
+            for (int k = 0; k < 2 * NM; k++) s[k] += v0[k];
+          }
+          if (f1) {
+#pragma unroll
+            for (int k = 0; k < 2 * NM; k++) s[k] += v1[k];
+          }
+        }
+      const size_t cell = ((size_t)x * ng + y) * ng + z;
+#pragma unroll
+      for (int m = 0; m < NM; m++) {
+        if (INT64)
+          *reinterpret_cast<longlong2*>(g.out64[m] + cell) = make_longlong2(s[m], s[NM + m]);
+        else
+          *reinterpret_cast<float2*>(g.out[m] + cell) =
+              make_float2(fix_to_float(s[m] - off), fix_to_float(s[NM + m] - off));
       }
-    const size_t cell = ((size_t)x * ng + y) * ng + z;
-#pragma unroll
-    for (int m = 0; m < NM; m++) {
-      if (INT64)
-        *reinterpret_cast<longlong2*>(g.out64[m] + cell) = make_longlong2(s[m], s[NM + m]);
-      else
-        *reinterpret_cast<float2*>(g.out[m] + cell) =
-            make_float2(fix_to_float(s[m] - off), fix_to_float(s[NM + m] - off));
     }
   }
 }
@@ -1401,6 +1525,10 @@ __global__ void __launch_bounds__(256) k_scan_one(unsigned* hist, size_t n) {
 
 int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool int64_out) {
   int n = 0;
+  // FP32 regions for the FP32 meshes of a periodic box; exact int64 ones for
+  // the int64 meshes and for survey meshes (data minus alpha randoms), whose
+  // cells cancel to a small fraction of their terms
+  g.reg_f32 = (int64_out || g.nomean) ? 0 : 1;
   // buckets: (tile, reach class) for the tile gather, one per tile for the region gather
   const size_t nkeys = g.region ? gather_keys(g.ng) / 27 : gather_keys(g.ng);
   if (!int64_out) {

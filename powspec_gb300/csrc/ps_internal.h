@@ -49,6 +49,8 @@ struct GatherArgs {
                            // more: one record per warp (TSC/PCS)
   int region;              // 1: each record once, into its home tile's region (TSC/PCS, T = 16)
   unsigned long long* regbuf;  // [tiles][gather_region_words()][meshes] region sums
+  int reg_f32;                 // 1: regions as FP32 words (home cells minus the mean);
+                               // 0: exact int64 words (int64 meshes, survey meshes)
   unsigned char* regflag;      // [tiles] 1: the tile wrote its region (it has records)
   int nomean;                  // 1: FP32 meshes keep their mean (survey catalogues)
 };

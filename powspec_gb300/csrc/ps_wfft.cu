@@ -263,8 +263,12 @@ constexpr int kMaxWarpsC = 16;  // warps per CTA of the x pass: 4 or 16 (host's 
 // steps of 4 warps' items (fewer steps with more warps).  Large tile sums
 // (|mu| sub-bins) take the CTA's shared memory: then 16 warps share them,
 // so that more warps are resident.
-template <int N, int NSPEC, int MOM, int WPC>
-__global__ void __launch_bounds__(32 * WPC, WPC == 4 ? 0 : 2) k_pass_c_w(const __grid_constant__ PassCArgs a) {
+// PY: items are (kz, |ky|) and a warp transforms line ky, then line Ng - ky,
+// binned together (ypair_powers / ypair_bin; line of sight along z, moment
+// form, one line per field in a transform).
+template <int N, int NSPEC, int MOM, int WPC, bool PY>
+__global__ void __launch_bounds__(32 * WPC, WPC == 4 ? (PY && N == 512 ? 3 : 0) : 2)
+    k_pass_c_w(const __grid_constant__ PassCArgs a) {
   using S = WF<N>;
   constexpr int LS = wc_line<N>();
   extern __shared__ __align__(16) float2 wsm[];
@@ -289,13 +293,50 @@ __global__ void __launch_bounds__(32 * WPC, WPC == 4 ? 0 : 2) k_pass_c_w(const _
     srange[1] = -1;
   }
   __syncthreads();
-  const int nitem = (N / 2 + 1) * (N / NP);  // (kz, ky0) with ky0 a multiple of NP
+  // (kz, ky0) with ky0 a multiple of NP; with PY (kz, |ky|)
+  const int nitem = PY ? (N / 2 + 1) * (N / 2 + 1) : (N / 2 + 1) * (N / NP);
   const int nstep = (nitem + (int)gridDim.x * nwc - 1) / ((int)gridDim.x * nwc);
   int nacc_steps = 0;
   for (int st = 0; st < nstep; st++) {
     const int item = (st * (int)gridDim.x + (int)blockIdx.x) * nwc + w;
     int lo = 0x7fffffff, hi = -1;
-    if (item < nitem) {
+    if (PY && item < nitem) {
+      if constexpr (PY) {
+        const int kz = item / (N / 2 + 1), kyp = item - kz * (N / 2 + 1);
+        int spec_a[NSPEC], spec_b[NSPEC];
+#pragma unroll
+        for (int s = 0; s < NSPEC; s++) {
+          spec_a[s] = a.spec_a[s];
+          spec_b[s] = a.spec_b[s];
+        }
+        float pw[YPairRuns<N>::NC][YPairRuns<N>::RP + 1][NSPEC];
+        const int nly = (kyp == 0 || 2 * kyp == N) ? 1 : 2;
+        for (int t = 0; t < nly; t++) {
+          const int ky = t ? N - kyp : kyp;
+          // field f of line ky, G at a time (nfield >= G here)
+          for (int f0 = 0; f0 < nfield; f0 += S::G) {
+            const int f = f0 + g;
+            const float2* src = a.in[f] + ((size_t)kz * N + ky) * N + l;
+            float2 v[S::V];
+#pragma unroll
+            for (int m = 0; m < S::V; m++) v[m] = __ldcs(src + m * S::L);
+            wfft<N>(v, X + f0 * LS, a.twl, lane);
+            float2* out = X + f * LS;
+#pragma unroll
+            for (int j = 0; j < S::R; j++)
+#pragma unroll
+              for (int k2 = 0; k2 < S::L; k2++) {
+                const int kx = (l * S::R + j) + S::V * k2;
+                out[kx + (kx >> 5)] = v[j * S::L + k2];
+              }
+            __syncwarp();
+          }
+          ypair_powers<N, NSPEC>(a, X, LS, kz, ky, pw, t > 0, lane, spec_a, spec_b);
+          __syncwarp();  // the next line's transform overwrites X
+        }
+        ypair_bin<N, NSPEC, MOM>(a, kz, kyp, pw, tacc, lo, hi, lane);
+      }
+    } else if (item < nitem) {
       const int kz = item / (N / NP), ky0 = (item - kz * (N / NP)) * NP;
       // lines e = pos * nfield + f, G at a time; line e -> buffer f * NP + pos
       for (int e0 = 0; e0 < nline; e0 += S::G) {
@@ -328,13 +369,27 @@ __global__ void __launch_bounds__(32 * WPC, WPC == 4 ? 0 : 2) k_pass_c_w(const _
   if (nacc_steps) merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
 }
 
+template <int N, int NSPEC, int MOM, int WPC, bool PY>
+void launch_c_w_py(const PassCArgs& a, size_t smem, cudaStream_t s) {
+  cudaFuncSetAttribute(k_pass_c_w<N, NSPEC, MOM, WPC, PY>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_pass_c_w<N, NSPEC, MOM, WPC, PY><<<(unsigned)a.grid, 32 * WPC, smem, s>>>(a);
+}
+
 template <int N, int NSPEC, int MOM, int WPC>
 void launch_c_w_at(const PassCArgs& a, cudaStream_t s) {
   const size_t smem = pass_c_w_smem(a.ng, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
                                     a.geom.nbin * a.geom.nmu, WPC);
-  cudaFuncSetAttribute(k_pass_c_w<N, NSPEC, MOM, WPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  k_pass_c_w<N, NSPEC, MOM, WPC><<<(unsigned)a.grid, 32 * WPC, smem, s>>>(a);
+  // the +-k_y pairing: one spectrum, moment form, line of sight along z,
+  // every transform holding lines of one ky only
+  if constexpr (NSPEC == 1 && MOM > 0 && WPC == 4) {
+    if (a.geom.los[0] == 0.f && a.geom.los[1] == 0.f && wc_np<N>(a.nfield) == 1 &&
+        a.nfield % WF<N>::G == 0) {
+      launch_c_w_py<N, NSPEC, MOM, WPC, true>(a, smem, s);
+      return;
+    }
+  }
+  launch_c_w_py<N, NSPEC, MOM, WPC, false>(a, smem, s);
 }
 
 // 16 warps per CTA only at Ng = 256 for one spectrum of the poles 0, 2, 4

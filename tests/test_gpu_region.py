@@ -1,9 +1,11 @@
 """The region gather (each TSC/PCS record added once, into its home tile's
 region, then the regions summed per cell) against the tile gather (each tile
 replays the records that reach it, one per warp or in lane groups): the
-fixed-point meshes are the same to the bit, for particles on the box faces, across the interlaced grid's
-periodic wrap, with weights large enough for the 64-bit node conversion, and
-with most tiles empty."""
+fixed-point meshes (int64 regions) are the same to the bit, for particles on
+the box faces, across the interlaced grid's periodic wrap, with weights large
+enough for the 64-bit node conversion, and with most tiles empty.  The FP32
+meshes the spectra use sum FP32 regions, a few FP32 roundings per cell, so
+their spectra are compared within the FP32 binning bar."""
 import numpy as np
 import pytest
 
