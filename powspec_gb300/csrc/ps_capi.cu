@@ -340,11 +340,10 @@ int plan_pass_c(ps_gpu_ctx* c) {
       c->grid_ct = std::min(c->ngk * ((ng + ty - 1) / ty), c->nsm * per);
     }
   }
-  // warp x pass: as many persistent CTAs per SM as shared memory and 2048
-  // threads allow, of the CTA size (4 warps, or 16 sharing the tile sums:
-  // one spectrum of the poles 0, 2, 4 at Ng = 256) that keeps the most warps resident
-  // (the smaller on a tie).  16-warp CTAs are built for two per SM (64
-  // registers a thread).
+  // warp x pass: as many persistent CTAs per SM as are resident (shared
+  // memory and registers of the instance the launch picks), of the CTA size
+  // (4 warps, or 16 sharing the tile sums: one spectrum of the poles 0, 2,
+  // 4 at Ng = 256) that keeps the most warps resident (the larger on a tie).
   c->grid_cw = 0;
   c->wpc_cw = 4;
   if (c->d_twl_full && ng == 2048) {
@@ -358,15 +357,30 @@ int plan_pass_c(ps_gpu_ctx* c) {
       }
     }
   } else if (c->d_twl_full) {
-    const bool big_ok = ng == 256 && c->nspec == 1 && pass_c_moments(c->p.poles, c->p.npole) == 3;
+    const int mom = pass_c_moments(c->p.poles, c->p.npole);
+    const bool big_ok = ng == 256 && c->nspec == 1 && mom == 3;
     int best = 0;
     for (int wpc : {4, 16}) {
       if (wpc == 16 && !big_ok) continue;
       const size_t smw = pass_c_w_smem(ng, c->nfield, nacc, nkey, wpc);
       if (!smw || smw > 227 * 1024) continue;
-      int per = std::max(1, (int)((228 * 1024) / (smw + 1024)));
-      per = std::min(per, wpc == 16 ? 2 : 2048 / (32 * wpc));
-      if (per * wpc > best) {
+      // resident CTAs of the instance the launch will pick (its registers
+      // and shared memory); the shared-memory estimate without a device
+      PassCArgs q;
+      memset(&q, 0, sizeof q);
+      q.ng = ng;
+      q.nfield = c->nfield;
+      q.nspec = c->nspec;
+      q.mom = mom;
+      q.wpc = wpc;
+      q.geom = c->geom;
+      q.geom.nmu = c->nmu;
+      int per = pass_c_w_per_sm(q);
+      if (per < 1) {
+        per = std::max(1, (int)((228 * 1024) / (smw + 1024)));
+        per = std::min(per, wpc == 16 ? 2 : 2048 / (32 * wpc));
+      }
+      if (per * wpc >= best) {  // the larger CTA on a tie: fewer partial slices
         best = per * wpc;
         c->wpc_cw = wpc;
         c->grid_cw = c->nsm * per;

@@ -204,6 +204,10 @@ void wfft_shape(int n, int* L, int* V);
 int launch_pass_a_w(const PassAArgs& a, cudaStream_t s);  // 0: shape not supported
 int launch_pass_b_w(const PassBArgs& a, cudaStream_t s);
 int launch_pass_c_w(const PassCArgs& a, cudaStream_t s);
+// Resident CTAs per SM of the warp x pass launch_pass_c_w would run for these
+// arguments (ng, nfield, nspec, mom, wpc, geom.npole/nbin/nmu/los), by the
+// chosen instance's registers and shared memory; 0 without a warp form.
+int pass_c_w_per_sm(const PassCArgs& a);
 // The store-mode x pass (one field, survey harmonic terms); 0 without a warp form.
 int launch_pass_c_ws(const PassCArgs& a, cudaStream_t s);
 // Dynamic shared memory and block size of the warp x pass (persistent CTAs).

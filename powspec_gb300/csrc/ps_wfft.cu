@@ -267,7 +267,7 @@ constexpr int kMaxWarpsC = 16;  // warps per CTA of the x pass: 4 or 16 (host's 
 // binned together (ypair_powers / ypair_bin; line of sight along z, moment
 // form, one line per field in a transform).
 template <int N, int NSPEC, int MOM, int WPC, bool PY>
-__global__ void __launch_bounds__(32 * WPC, WPC == 4 ? (PY && N == 512 ? 3 : 0) : 2)
+__global__ void __launch_bounds__(32 * WPC, WPC == 4 ? (PY && N == 512 ? 3 : 0) : (PY ? 1 : 2))
     k_pass_c_w(const __grid_constant__ PassCArgs a) {
   using S = WF<N>;
   constexpr int LS = wc_line<N>();
@@ -369,59 +369,58 @@ __global__ void __launch_bounds__(32 * WPC, WPC == 4 ? (PY && N == 512 ? 3 : 0) 
   if (nacc_steps) merge_any<NSPEC, MOM>(tacc, srange, part, gm, nkey);
 }
 
-template <int N, int NSPEC, int MOM, int WPC, bool PY>
-void launch_c_w_py(const PassCArgs& a, size_t smem, cudaStream_t s) {
-  cudaFuncSetAttribute(k_pass_c_w<N, NSPEC, MOM, WPC, PY>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_pass_c_w<N, NSPEC, MOM, WPC, PY><<<(unsigned)a.grid, 32 * WPC, smem, s>>>(a);
-}
+using CwKernel = void (*)(const PassCArgs);
 
+// The warp x pass's instance for these arguments.  The +-k_y pairing: one
+// spectrum, moment form, line of sight along z, every transform holding
+// lines of one ky only.
 template <int N, int NSPEC, int MOM, int WPC>
-void launch_c_w_at(const PassCArgs& a, cudaStream_t s) {
-  const size_t smem = pass_c_w_smem(a.ng, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
-                                    a.geom.nbin * a.geom.nmu, WPC);
-  // the +-k_y pairing: one spectrum, moment form, line of sight along z,
-  // every transform holding lines of one ky only
-  if constexpr (NSPEC == 1 && MOM > 0 && WPC == 4) {
+CwKernel pick_c_w_at(const PassCArgs& a) {
+  if constexpr (NSPEC == 1 && MOM > 0) {
     if (a.geom.los[0] == 0.f && a.geom.los[1] == 0.f && wc_np<N>(a.nfield) == 1 &&
-        a.nfield % WF<N>::G == 0) {
-      launch_c_w_py<N, NSPEC, MOM, WPC, true>(a, smem, s);
-      return;
-    }
+        a.nfield % WF<N>::G == 0)
+      return k_pass_c_w<N, NSPEC, MOM, WPC, true>;
   }
-  launch_c_w_py<N, NSPEC, MOM, WPC, false>(a, smem, s);
+  return k_pass_c_w<N, NSPEC, MOM, WPC, false>;
 }
 
 // 16 warps per CTA only at Ng = 256 for one spectrum of the poles 0, 2, 4
-// (the learned form's |mu| sub-bins; larger transforms would spill at the
-// 64 registers two such CTAs an SM allow); the host plans by the same rule
+// (the learned form's |mu| sub-bins, whose tile sums the CTA's warps share;
+// larger transforms would spill); the host plans by the same rule
 template <int N, int NSPEC, int MOM>
-void launch_c_w(const PassCArgs& a, cudaStream_t s) {
+CwKernel pick_c_w(const PassCArgs& a) {
   if constexpr (N == 256 && NSPEC == 1 && MOM == 3) {
-    if (a.wpc == kMaxWarpsC) {
-      launch_c_w_at<N, NSPEC, MOM, kMaxWarpsC>(a, s);
-      return;
-    }
+    if (a.wpc == kMaxWarpsC) return pick_c_w_at<N, NSPEC, MOM, kMaxWarpsC>(a);
   }
-  launch_c_w_at<N, NSPEC, MOM, 4>(a, s);
+  return pick_c_w_at<N, NSPEC, MOM, 4>(a);
 }
 
 template <int N, int MOM>
-void launch_c_w_ns(const PassCArgs& a, cudaStream_t s) {
+CwKernel pick_c_w_ns(const PassCArgs& a) {
   switch (a.nspec) {
-    case 1: launch_c_w<N, 1, MOM>(a, s); break;
-    case 2: launch_c_w<N, 2, MOM>(a, s); break;
-    default: launch_c_w<N, 3, MOM>(a, s); break;
+    case 1: return pick_c_w<N, 1, MOM>(a);
+    case 2: return pick_c_w<N, 2, MOM>(a);
+    default: return pick_c_w<N, 3, MOM>(a);
   }
 }
 
 template <int N>
-void launch_c_w_mom(const PassCArgs& a, cudaStream_t s) {
+CwKernel pick_c_w_mom(const PassCArgs& a) {
   switch (a.mom) {
-    case 2: launch_c_w_ns<N, 2>(a, s); break;
-    case 3: launch_c_w_ns<N, 3>(a, s); break;
-    case 4: launch_c_w_ns<N, 4>(a, s); break;
-    default: launch_c_w_ns<N, 0>(a, s); break;
+    case 2: return pick_c_w_ns<N, 2>(a);
+    case 3: return pick_c_w_ns<N, 3>(a);
+    case 4: return pick_c_w_ns<N, 4>(a);
+    default: return pick_c_w_ns<N, 0>(a);
+  }
+}
+
+// Ng = 256 ... 1024 (nullptr otherwise); a.wpc: 4 or 16 warps per CTA
+CwKernel pick_c_w_any(const PassCArgs& a) {
+  switch (a.ng) {
+    case 256: return pick_c_w_mom<256>(a);
+    case 512: return pick_c_w_mom<512>(a);
+    case 1024: return pick_c_w_mom<1024>(a);
+    default: return nullptr;
   }
 }
 
@@ -693,12 +692,33 @@ int launch_pass_c_w(const PassCArgs& a, cudaStream_t s) {
     }
     return 1;
   }
-  switch (a.ng) {
-    case 256: launch_c_w_mom<256>(a, s); return 1;
-    case 512: launch_c_w_mom<512>(a, s); return 1;
-    case 1024: launch_c_w_mom<1024>(a, s); return 1;
-    default: return 0;
+  const CwKernel k = pick_c_w_any(a);
+  if (!k) return 0;
+  const int wpc = (a.wpc == kMaxWarpsC) ? kMaxWarpsC : 4;
+  const size_t smem = pass_c_w_smem(a.ng, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
+                                    a.geom.nbin * a.geom.nmu, wpc);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k<<<(unsigned)a.grid, 32 * wpc, smem, s>>>(a);
+  return 1;
+}
+
+int pass_c_w_per_sm(const PassCArgs& a) {
+  if (a.ng == 2048) return 0;
+  const CwKernel k = pick_c_w_any(a);
+  if (!k) return 0;
+  const int wpc = (a.wpc == kMaxWarpsC) ? kMaxWarpsC : 4;
+  const size_t smem = pass_c_w_smem(a.ng, a.nfield, a.nspec * pass_c_accs(a.geom.npole, a.mom),
+                                    a.geom.nbin * a.geom.nmu, wpc);
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
   }
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 32 * wpc, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return nb;
 }
 
 }  // namespace ps
