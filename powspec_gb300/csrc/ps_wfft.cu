@@ -104,8 +104,8 @@ __global__ void __launch_bounds__(32 * kWarpsAB) k_pass_a_w(const __grid_constan
   extern __shared__ float2 wsm[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int g = lane / S::L, l = lane - g * S::L;
-  float2* T = wsm;                                  // [TY][TL]
-  float2* scr = wsm + TY * TL + w * S::SWARP;
+  float2* T = wsm;                    // [TY][TL], over the transpose areas once they are done
+  float2* scr = wsm + w * S::SWARP;
   constexpr int nty = NG / TY;
   const int x = blockIdx.x / nty, y0 = (blockIdx.x - x * nty) * TY;
   const int r = w * S::G + g;
@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(32 * kWarpsAB) k_pass_a_w(const __grid_constan
     }
   }
   wfft<M>(v, scr, a.twl, lane);
+  __syncthreads();  // every warp's transform is done with its transpose area
 #pragma unroll
   for (int j = 0; j < S::R; j++)
 #pragma unroll
@@ -163,8 +164,8 @@ __global__ void __launch_bounds__(32 * kWarpsAB) k_pass_b_w(const __grid_constan
   extern __shared__ float2 wsm[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int g = lane / S::L, l = lane - g * S::L;
-  float2* T = wsm;                                  // [N][TP]
-  float2* scr = wsm + N * TP + w * S::SWARP;
+  float2* T = wsm;                    // [N][TP], over the transpose areas once they are done
+  float2* scr = wsm + w * S::SWARP;
   const int kz = blockIdx.x / ntx, x0 = (blockIdx.x - kz * ntx) * TX;
   const int col = w * S::G + g;
   const float2* src = a.in + ((size_t)(x0 + col) * ngk + kz) * N + l;
@@ -172,6 +173,7 @@ __global__ void __launch_bounds__(32 * kWarpsAB) k_pass_b_w(const __grid_constan
 #pragma unroll
   for (int m = 0; m < S::V; m++) v[m] = __ldcs(src + m * S::L);
   wfft<N>(v, scr, a.twl, lane);
+  __syncthreads();  // every warp's transform is done with its transpose area
 #pragma unroll
   for (int j = 0; j < S::R; j++)
 #pragma unroll
@@ -622,7 +624,7 @@ int launch_pass_a_w(const PassAArgs& a, cudaStream_t s) {
 #define PS_A_W(NG)                                                                              \
   {                                                                                             \
     constexpr int M = (NG) / 2, TY = kWarpsAB * WF<M>::G;                                       \
-    const size_t smem = ((size_t)TY * (M + 1) + (size_t)kWarpsAB * WF<M>::SWARP) * sizeof(float2); \
+    const size_t smem = std::max((size_t)TY * (M + 1), (size_t)kWarpsAB * WF<M>::SWARP) * sizeof(float2); \
     cudaFuncSetAttribute(k_pass_a_w<NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     k_pass_a_w<NG><<<(unsigned)((NG) * ((NG) / TY)), 32 * kWarpsAB, smem, s>>>(a);              \
     return 1;                                                                                   \
@@ -641,7 +643,7 @@ int launch_pass_b_w(const PassBArgs& a, cudaStream_t s) {
 #define PS_B_W(N)                                                                               \
   {                                                                                             \
     constexpr int TX = kWarpsAB * WF<N>::G;                                                     \
-    const size_t smem = ((size_t)(N) * (TX + 1) + (size_t)kWarpsAB * WF<N>::SWARP) * sizeof(float2); \
+    const size_t smem = std::max((size_t)(N) * (TX + 1), (size_t)kWarpsAB * WF<N>::SWARP) * sizeof(float2); \
     cudaFuncSetAttribute(k_pass_b_w<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     k_pass_b_w<N><<<(unsigned)(((N) / 2 + 1) * ((N) / TX)), 32 * kWarpsAB, smem, s>>>(a);       \
     return 1;                                                                                   \
