@@ -540,31 +540,32 @@ __global__ void __launch_bounds__(512) k_pass_c_w2k(const __grid_constant__ Pass
 
 // y transform at Ng = 2048 by pairs of warps: pair c of the CTA transforms
 // the line (x0 + c, kz) of A[x][kz][y]; the CTA stores B[kz][ky][x0 ..
-// x0 + 6) through a shared [ky][7] tile, in runs over x.
-constexpr int kPairsB2k = 6;
+// x0 + 4) through a shared [ky][5] tile, in runs of 4 x (whole 32-byte
+// sectors).  The tile lies over the pairs' transpose areas, so that two
+// CTAs fit an SM.
+constexpr int kPairsB2k = 4;
 __global__ void __launch_bounds__(64 * kPairsB2k) k_pass_b_w2k(const __grid_constant__ PassBArgs a) {
   constexpr int N = 2048, ngk = N / 2 + 1, TP = kPairsB2k + 1;
-  constexpr int ntx = (N + kPairsB2k - 1) / kPairsB2k;
+  constexpr int ntx = N / kPairsB2k;
+  static_assert(N % kPairsB2k == 0, "whole tiles of x");
   extern __shared__ __align__(16) float2 wsm[];
-  float2* T = wsm;                                    // [N][TP]
+  float2* T = wsm;  // [N][TP], over the pairs' transpose areas once they are done
   const int pair = threadIdx.x >> 6, p = threadIdx.x & 63;
-  float2* S = wsm + (size_t)N * TP + (size_t)pair * kLine2k;  // the pair's transpose area
+  float2* S = wsm + (size_t)pair * kLine2k;  // the pair's transpose area
   const int kz = blockIdx.x / ntx, x0 = (blockIdx.x - kz * ntx) * kPairsB2k;
-  const int ncol = min(kPairsB2k, N - x0);
-  if (pair < ncol) {  // pair-uniform
-    const float2* src = a.in + ((size_t)(x0 + pair) * ngk + kz) * N + p;
-    float2 v[32];
+  const float2* src = a.in + ((size_t)(x0 + pair) * ngk + kz) * N + p;
+  float2 v[32];
 #pragma unroll
-    for (int m = 0; m < 32; m++) v[m] = __ldcs(src + 64 * m);
-    wfft_pair2k(v, S, a.twl, p, pair);
-    const int k1 = p >> 1, h = p & 1;
+  for (int m = 0; m < 32; m++) v[m] = __ldcs(src + 64 * m);
+  wfft_pair2k(v, S, a.twl, p, pair);
+  __syncthreads();  // every pair's transform is done with its transpose area
+  const int k1 = p >> 1, h = p & 1;
 #pragma unroll
-    for (int k2 = 0; k2 < 32; k2++) T[(k1 + 32 * (k2 + 32 * h)) * TP + pair] = v[k2];
-  }
+  for (int k2 = 0; k2 < 32; k2++) T[(k1 + 32 * (k2 + 32 * h)) * TP + pair] = v[k2];
   __syncthreads();
   float2* dst = a.out + (size_t)kz * N * N + x0;
-  for (int e = threadIdx.x; e < N * ncol; e += blockDim.x) {
-    const int ky = e / ncol, xl = e - ky * ncol;
+  for (int e = threadIdx.x; e < N * kPairsB2k; e += blockDim.x) {
+    const int ky = e / kPairsB2k, xl = e - ky * kPairsB2k;
     dst[(size_t)ky * N + xl] = T[ky * TP + xl];
   }
 }
@@ -654,9 +655,9 @@ int launch_pass_b_w(const PassBArgs& a, cudaStream_t s) {
     case 1024: PS_B_W(1024)
     case 2048: {
       constexpr int N = 2048;
-      const size_t smem = ((size_t)N * (kPairsB2k + 1) + (size_t)kPairsB2k * kLine2k) * sizeof(float2);
+      const size_t smem = std::max((size_t)N * (kPairsB2k + 1), (size_t)kPairsB2k * kLine2k) * sizeof(float2);
       cudaFuncSetAttribute(k_pass_b_w2k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_pass_b_w2k<<<(unsigned)((N / 2 + 1) * ((N + kPairsB2k - 1) / kPairsB2k)), 64 * kPairsB2k, smem,
+      k_pass_b_w2k<<<(unsigned)((N / 2 + 1) * (N / kPairsB2k)), 64 * kPairsB2k, smem,
                      s>>>(a);
       return 1;
     }
