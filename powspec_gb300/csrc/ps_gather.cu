@@ -1355,12 +1355,12 @@ __device__ __forceinline__ void load_pair_f32(const float* p, float (&v)[2 * NM]
 
 // Mesh from the regions: a pair of consecutive z cells of every mesh per
 // thread (a warp reads 32 consecutive pairs: whole sectors), the FP32 sum
-// of the FP32 regions, or from int64 regions the exact fixed-point sum
-// (INT64) or its FP32 value minus the mean.  Regions are [R][R][RG][NM]
+// of the FP32 regions (F32R), or from int64 regions the exact fixed-point
+// sum (INT64) or its FP32 value minus the mean.  Regions are [R][R][RG][NM]
 // words; a cell pair starts on an even region cell.  A tile
 // without records wrote neither its region nor a flag of 1, and its words
 // (loaded alongside the flag) are dropped.
-template <int S, int NM, bool INT64>
+template <int S, int NM, bool INT64, bool F32R>
 __global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ GatherArgs g) {
   constexpr int T = kRegT, R = RegGeom<S>::R, RG = RegGeom<S>::RG, RP = RegGeom<S>::RP;
   constexpr int of = (S >= 3) ? -1 : 0;
@@ -1395,32 +1395,49 @@ __global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ Gath
       tz2 = (tz == nt - 1) ? 0 : tz + 1;
       cz2 = uz - T - of + 1;
     }
-    if (!INT64 && g.reg_f32) {
-      // FP32 regions, the home tile's (which carries the mean) first
+    if constexpr (F32R) {
+      // FP32 regions: the (x, y) sources q = 2a + b (a < nx, b < ny), the
+      // home tile's (which carries the mean) first; every source's flags
+      // and words are loaded before any is added, so that a thread has all
+      // its loads in flight at once
+      unsigned t0q[4], t1q[4];
+      int rowq[4];
+      bool onq[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int a = q >> 1, b = q & 1;
+        onq[q] = a < nx && b < ny;
+        const unsigned tb = onq[q] ? ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt : 0u;
+        rowq[q] = onq[q] ? (ix[a] * R + iy[b]) * RG : 0;
+        t0q[q] = tb + tz;
+        t1q[q] = tb + (tz2 >= 0 ? tz2 : 0);
+      }
+      float v0[4][2 * NM], v1[4][2 * NM];
+      bool f0[4], f1[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        f0[q] = f1[q] = false;
+        if (onq[q]) {
+          f0[q] = g.regflag[t0q[q]] != 0;
+          load_pair_f32<NM>(rbf + ((size_t)t0q[q] * RP + (size_t)(rowq[q] + uz - of + 1)) * NM, v0[q]);
+          if (tz2 >= 0) {
+            f1[q] = g.regflag[t1q[q]] != 0;
+            load_pair_f32<NM>(rbf + ((size_t)t1q[q] * RP + (size_t)(rowq[q] + cz2)) * NM, v1[q]);
+          }
+        }
+      }
       float s[2 * NM];
 #pragma unroll
       for (int k = 0; k < 2 * NM; k++) s[k] = 0.f;
-      for (int a = 0; a < nx; a++)
-        for (int b = 0; b < ny; b++) {
-          const unsigned tb = ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt;
-          const int row = (ix[a] * R + iy[b]) * RG;
-          const unsigned t0 = tb + tz;
-          const bool f0 = g.regflag[t0] != 0;
-          float v0[2 * NM], v1[2 * NM];
-          load_pair_f32<NM>(rbf + ((size_t)t0 * RP + (size_t)(row + uz - of + 1)) * NM, v0);
-          bool f1 = false;
-          if (tz2 >= 0) {
-            const unsigned t1 = tb + tz2;
-            f1 = g.regflag[t1] != 0;
-            load_pair_f32<NM>(rbf + ((size_t)t1 * RP + (size_t)(row + cz2)) * NM, v1);
-          }
 #pragma unroll
-          for (int k = 0; k < 2 * NM; k++) s[k] += f0 ? v0[k] : ((a == 0 && b == 0) ? mean_neg : 0.f);
-          if (f1) {
+      for (int q = 0; q < 4; q++) {
 #pragma unroll
-            for (int k = 0; k < 2 * NM; k++) s[k] += v1[k];
-          }
+        for (int k = 0; k < 2 * NM; k++) s[k] += f0[q] ? v0[q][k] : ((q == 0) ? mean_neg : 0.f);
+        if (f1[q]) {
+#pragma unroll
+          for (int k = 0; k < 2 * NM; k++) s[k] += v1[q][k];
         }
+      }
       const size_t cell = ((size_t)x * ng + y) * ng + z;
 #pragma unroll
       for (int m = 0; m < NM; m++)
@@ -1429,6 +1446,8 @@ __global__ void __launch_bounds__(256) k_region_sum(const __grid_constant__ Gath
       long long s[2 * NM];
 #pragma unroll
       for (int k = 0; k < 2 * NM; k++) s[k] = 0;
+      // int64 regions, one source after another (the exact sums, in 98
+      // registers with every load in flight, ran slower)
       for (int a = 0; a < nx; a++)
         for (int b = 0; b < ny; b++) {
           const unsigned tb = ((unsigned)tx[a] * nt + (unsigned)ty[b]) * nt;
@@ -1572,13 +1591,17 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
     k_gather_region<SS, 1><<<ntile, 512, smem, s>>>(g);                                        \
   }                                                                                            \
   if (int64_out && nm == 2)                                                                    \
-    k_region_sum<SS, 2, true><<<sblocks, 256, 0, s>>>(g);                                      \
+    k_region_sum<SS, 2, true, false><<<sblocks, 256, 0, s>>>(g);                               \
   else if (int64_out)                                                                          \
-    k_region_sum<SS, 1, true><<<sblocks, 256, 0, s>>>(g);                                      \
+    k_region_sum<SS, 1, true, false><<<sblocks, 256, 0, s>>>(g);                               \
+  else if (nm == 2 && g.reg_f32)                                                               \
+    k_region_sum<SS, 2, false, true><<<sblocks, 256, 0, s>>>(g);                               \
   else if (nm == 2)                                                                            \
-    k_region_sum<SS, 2, false><<<sblocks, 256, 0, s>>>(g);                                     \
+    k_region_sum<SS, 2, false, false><<<sblocks, 256, 0, s>>>(g);                              \
+  else if (g.reg_f32)                                                                          \
+    k_region_sum<SS, 1, false, true><<<sblocks, 256, 0, s>>>(g);                               \
   else                                                                                         \
-    k_region_sum<SS, 1, false><<<sblocks, 256, 0, s>>>(g);
+    k_region_sum<SS, 1, false, false><<<sblocks, 256, 0, s>>>(g);
     if (g.assign == 2) {
       PS_REGION(3)
     } else {
