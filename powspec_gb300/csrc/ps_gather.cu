@@ -1087,6 +1087,13 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
   const int nt = g.nt;
   const unsigned tile = ((unsigned)blockIdx.z * nt + blockIdx.y) * nt + blockIdx.x;
   const unsigned beg = g.hist[tile], end = g.hist[tile + 1];  // one bucket per tile
+  auto zero = [&]() {
+    ulonglong2* a2 = reinterpret_cast<ulonglong2*>(acc);
+    for (int e = threadIdx.x; e < NM * SM / 2; e += blockDim.x) a2[e] = make_ulonglong2(0ull, 0ull);
+  };
+  // the accumulators are zeroed while the bucket offsets are in flight (in
+  // vain for a tile without records)
+  zero();
   if (beg == end) {  // k_region_sum skips tiles without records
     if (threadIdx.x == 0) g.regflag[tile] = 0;
     return;
@@ -1109,18 +1116,19 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
   constexpr int Q = 4;
   unsigned char* const ring =
       reinterpret_cast<unsigned char*>(acc + NM * SM) + warp * (2 * Q * sizeof(WRec));
-  auto records = [&](auto&& proc) {
-    const unsigned w0 = beg + (unsigned)(warp * Q), step = (unsigned)(nw * Q);
-    const unsigned K = (w0 < end) ? (end - w0 + step - 1) / step : 0u;
-    const int cj = lane / 7, part = lane - 7 * cj;  // copy lanes 0-27: record cj, 16-byte part
-    const unsigned char* src = reinterpret_cast<const unsigned char*>(g.rec) + part * 16;
-    auto issue = [&](unsigned k) {
-      const unsigned i = w0 + k * step + (unsigned)cj;
-      if (k < K && lane < 7 * Q && i < end)
-        cp_async16(ring + ((k & 1) * Q + cj) * sizeof(WRec) + part * 16, src + (size_t)i * sizeof(WRec));
-      cp_async_commit();
-    };
-    issue(0);
+  const unsigned w0 = beg + (unsigned)(warp * Q), step = (unsigned)(nw * Q);
+  const unsigned K = (w0 < end) ? (end - w0 + step - 1) / step : 0u;
+  const int cj = lane / 7, part = lane - 7 * cj;  // copy lanes 0-27: record cj, 16-byte part
+  const unsigned char* src = reinterpret_cast<const unsigned char*>(g.rec) + part * 16;
+  auto issue = [&](unsigned k) {
+    const unsigned i = w0 + k * step + (unsigned)cj;
+    if (k < K && lane < 7 * Q && i < end)
+      cp_async16(ring + ((k & 1) * Q + cj) * sizeof(WRec) + part * 16, src + (size_t)i * sizeof(WRec));
+    cp_async_commit();
+  };
+  // primed: the first stage was issued already (before a CTA barrier)
+  auto records = [&](auto&& proc, bool primed) {
+    if (!primed) issue(0);
     for (unsigned k = 0; k < K; k++) {
       __syncwarp();  // the stage refilled next was read in step k - 1
       issue(k + 1);
@@ -1151,10 +1159,6 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
     cp_async_wait<0>();
     __syncwarp();
   };
-  auto zero = [&]() {
-    ulonglong2* a2 = reinterpret_cast<ulonglong2*>(acc);
-    for (int e = threadIdx.x; e < NM * SM / 2; e += blockDim.x) a2[e] = make_ulonglong2(0ull, 0ull);
-  };
   // Split path.  With q = 2^16 h + l (0 <= l < 2^16), H = sum h and
   // L = sum l: at most 65535 records put at most 65535 terms in a cell, so
   // 0 <= L < 2^32 and L = (sum q - 2^16 H) mod 2^32.  A record whose node
@@ -1166,8 +1170,8 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
   const unsigned nrec = end - beg;
   bool split = nrec <= 65535u;
   if (split) {
-    zero();
     if (threadIdx.x < 2) bound_sum[threadIdx.x] = 0.f;
+    issue(0);  // the first stage's copies overlap the barrier
     __syncthreads();
     float bsum = 0.f;  // sum of 2^e over this lane's large-value records (exact: powers >= 2^31)
     const int lbase = (yy * RZ + zz) * NM + m;
@@ -1193,7 +1197,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
         }
       }
     };
-    records(proc);
+    records(proc, true);
     if (lane == 0 || lane == 16) atomicAdd(&bound_sum[(NM == 2) ? half : 0], bsum);
     __syncthreads();
     const float room = 2147483648.f * (float)(65536u - nrec);  // 2^47 - n 2^31, exact
@@ -1273,7 +1277,7 @@ __global__ void __launch_bounds__(NM == 2 ? 1024 : 512, 1) k_gather_region(const
           atomicAdd(A + x * R * RZ, (unsigned long long)round_fix(wxs[x] * wyz));
       }
     };
-    records(proc);
+    records(proc, false);
   }
   __syncthreads();
   if (g.reg_f32) {
