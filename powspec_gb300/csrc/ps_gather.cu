@@ -1546,6 +1546,24 @@ __global__ void __launch_bounds__(256) k_scan_one(unsigned* hist, size_t n) {
 }
 }  // namespace
 
+namespace {
+// CTAs of a grid-stride assignment kernel over n particles: the resident
+// CTAs of all SMs (the occupancy query; 2048 without a device), at most one
+// per 256 particles and at most kAssignMaxBlocks (the weight partials).
+size_t assign_grid(size_t n, const void* kernel, int threads, size_t smem) {
+  size_t cap = kAssignMaxBlocks;
+  int dev = 0, nsm = 0, per = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) == cudaSuccess &&
+      nsm > 0 && per > 0)
+    cap = std::min(cap, (size_t)nsm * (size_t)per);
+  else
+    cudaGetLastError();
+  return std::max<size_t>(1, std::min(cap, (n + 255) / 256));
+}
+}  // namespace
+
 int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool int64_out) {
   int n = 0;
   // FP32 regions for the FP32 meshes of a periodic box; exact int64 ones for
@@ -1556,9 +1574,9 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
   const size_t nkeys = g.region ? gather_keys(g.ng) / 27 : gather_keys(g.ng);
   if (!int64_out) {
     cudaMemsetAsync(g.hist, 0, (nkeys + 1) * sizeof(unsigned), s);
-    size_t blocks = (p.n + 255) / 256;
-    if (blocks > (size_t)kAssignMaxBlocks) blocks = kAssignMaxBlocks;
-    if (blocks < 1) blocks = 1;
+    // grid-stride kernels: one wave of resident CTAs (a partial last wave
+    // of a larger grid would run at part occupancy)
+    const size_t blocks = assign_grid(p.n, reinterpret_cast<const void*>(k_classify), 256, 0);
     k_classify<<<(unsigned)blocks, 256, 0, s>>>(g, p);
     n++;
     k_wsum<<<1, kWsumThreads, 0, s>>>(reinterpret_cast<const float4*>(g.wpart), (int)blocks, g.wsum,
@@ -1574,7 +1592,8 @@ int launch_gather_assign(const Particles& p, GatherArgs g, cudaStream_t s, bool 
       k_scan_apply<<<nb, 256, 0, s>>>(g.hist, nkeys, g.bsum, nb);
       n += 3;
     }
-    k_scatter<<<(unsigned)blocks, 32 * kScatterWarps, 0, s>>>(g, p);
+    const size_t scatter_blocks = assign_grid(p.n, reinterpret_cast<const void*>(k_scatter), 32 * kScatterWarps, 0);
+    k_scatter<<<(unsigned)scatter_blocks, 32 * kScatterWarps, 0, s>>>(g, p);
     n++;
   }
   if (g.region) {
