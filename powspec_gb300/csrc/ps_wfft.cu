@@ -186,11 +186,14 @@ __global__ void __launch_bounds__(32 * kWarpsAB) k_pass_b_w(const __grid_constan
   }
 }
 
-// x transform in store mode (survey harmonic terms): a CTA takes 8 lines
-// of consecutive kz at one ky (one field), each warp transforms G of them,
-// and through a shared [kx][9] tile (over the transpose areas, after a CTA
-// barrier) the CTA writes F[x][y][kz] in runs of 8 kz: out = X (acc_mode 0), X * Y_lm(k^) (1) or out + X * Y_lm(k^) (2),
-// Y_lm = 1 for k_x = k_y = 0 (src/mp_template.c:118-121), as k_pass_c.
+// x transform in store mode (survey harmonic terms, the host r2c): a CTA
+// takes 8 lines of consecutive kz at one ky (one field), each warp
+// transforms G of them, and through a shared [kx][9] tile (over the
+// transpose areas, after a CTA barrier) the CTA writes F[x][y][kz] in runs
+// of 8 kz: out = X (acc_mode 0), X * Y_lm(k^) (1) or out + X * Y_lm(k^)
+// (2), with Y_lm = 1 for k_x = k_y = 0 (src/mp_template.c:118-121), as
+// k_pass_c does.  The last kz tile holds fewer lines: its idle groups
+// transform line kz0 again and store nothing.
 constexpr int kStoreKz = 8;
 template <int N>
 __global__ void __launch_bounds__(32 * (kStoreKz / WF<N>::G)) k_pass_c_ws(const __grid_constant__ PassCArgs a) {
