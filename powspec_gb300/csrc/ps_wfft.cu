@@ -92,15 +92,21 @@ __device__ __forceinline__ void wfft(float2 (&x)[WF<N>::V], float2* S,
   }
 }
 
-constexpr int kWarpsAB = 4;  // warps per CTA of the z and y passes
+constexpr int kWarpsAB = 4;  // warps per CTA of the y pass (and of the z pass but below)
+// warps per CTA of the z pass: 8 at Ng = 512 and 2048, so that its
+// transposed stores A[x][kz][y] run over 8 G consecutive y (128 and 64
+// bytes) instead of 4 G (z pass 0.425 -> 0.369 ms at 512, 35.1 -> 30.3 ms at
+// 2048, two meshes); at 1024 eight warps measured slower (3.55 -> 3.81 ms)
+template <int NG>
+__host__ __device__ constexpr int warps_a() { return (NG == 512 || NG == 2048) ? 8 : kWarpsAB; }
 
 // z transform: real rows of the FP32 mesh (minus its mean) -> A[x][kz][y].
 template <int NG>
-__global__ void __launch_bounds__(32 * kWarpsAB) k_pass_a_w(const __grid_constant__ PassAArgs a) {
+__global__ void __launch_bounds__(32 * warps_a<NG>()) k_pass_a_w(const __grid_constant__ PassAArgs a) {
   constexpr int M = NG / 2;
   using S = WF<M>;
-  constexpr int TY = kWarpsAB * S::G;  // y rows per tile
-  constexpr int TL = M + 1;            // tile line (odd)
+  constexpr int TY = warps_a<NG>() * S::G;  // y rows per tile
+  constexpr int TL = M + 1;                 // tile line (odd)
   extern __shared__ float2 wsm[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int g = lane / S::L, l = lane - g * S::L;
@@ -627,10 +633,10 @@ size_t pass_c_w_smem(int ng, int nfield, int nacc, int nkey, int wpc) {
 int launch_pass_a_w(const PassAArgs& a, cudaStream_t s) {
 #define PS_A_W(NG)                                                                              \
   {                                                                                             \
-    constexpr int M = (NG) / 2, TY = kWarpsAB * WF<M>::G;                                       \
-    const size_t smem = std::max((size_t)TY * (M + 1), (size_t)kWarpsAB * WF<M>::SWARP) * sizeof(float2); \
+    constexpr int M = (NG) / 2, TY = warps_a<NG>() * WF<M>::G;                                  \
+    const size_t smem = std::max((size_t)TY * (M + 1), (size_t)warps_a<NG>() * WF<M>::SWARP) * sizeof(float2); \
     cudaFuncSetAttribute(k_pass_a_w<NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    k_pass_a_w<NG><<<(unsigned)((NG) * ((NG) / TY)), 32 * kWarpsAB, smem, s>>>(a);              \
+    k_pass_a_w<NG><<<(unsigned)((NG) * ((NG) / TY)), 32 * warps_a<NG>(), smem, s>>>(a);         \
     return 1;                                                                                   \
   }
   switch (a.ng) {
