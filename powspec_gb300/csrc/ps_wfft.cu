@@ -92,13 +92,19 @@ __device__ __forceinline__ void wfft(float2 (&x)[WF<N>::V], float2* S,
   }
 }
 
-constexpr int kWarpsAB = 4;  // warps per CTA of the y pass (and of the z pass but below)
+constexpr int kWarpsAB = 4;  // warps per CTA of the z and y passes but below
 // warps per CTA of the z pass: 8 at Ng = 512 and 2048, so that its
 // transposed stores A[x][kz][y] run over 8 G consecutive y (128 and 64
 // bytes) instead of 4 G (z pass 0.425 -> 0.369 ms at 512, 35.1 -> 30.3 ms at
 // 2048, two meshes); at 1024 eight warps measured slower (3.55 -> 3.81 ms)
 template <int NG>
 __host__ __device__ constexpr int warps_a() { return (NG == 512 || NG == 2048) ? 8 : kWarpsAB; }
+// warps per CTA of the y pass: 8 at Ng = 1024, whose 4-warp tile stored
+// runs of 4 x (32 bytes) at 5 CTAs per SM (y pass 3.95 -> 3.52 ms, two
+// meshes); at 512 eight warps measured slower (0.459 -> 0.501 ms), at 256
+// the same
+template <int N>
+__host__ __device__ constexpr int warps_b() { return N == 1024 ? 8 : kWarpsAB; }
 
 // z transform: real rows of the FP32 mesh (minus its mean) -> A[x][kz][y].
 template <int NG>
@@ -161,9 +167,9 @@ __global__ void __launch_bounds__(32 * warps_a<NG>()) k_pass_a_w(const __grid_co
 
 // y transform: A[x][kz][y] -> B[kz][ky][x].
 template <int N>
-__global__ void __launch_bounds__(32 * kWarpsAB) k_pass_b_w(const __grid_constant__ PassBArgs a) {
+__global__ void __launch_bounds__(32 * warps_b<N>()) k_pass_b_w(const __grid_constant__ PassBArgs a) {
   using S = WF<N>;
-  constexpr int TX = kWarpsAB * S::G;  // x lines per tile
+  constexpr int TX = warps_b<N>() * S::G;  // x lines per tile
   constexpr int TP = TX + 1;           // tile row (odd)
   constexpr int ngk = N / 2 + 1;
   constexpr int ntx = N / TX;
@@ -652,10 +658,10 @@ int launch_pass_a_w(const PassAArgs& a, cudaStream_t s) {
 int launch_pass_b_w(const PassBArgs& a, cudaStream_t s) {
 #define PS_B_W(N)                                                                               \
   {                                                                                             \
-    constexpr int TX = kWarpsAB * WF<N>::G;                                                     \
-    const size_t smem = std::max((size_t)(N) * (TX + 1), (size_t)kWarpsAB * WF<N>::SWARP) * sizeof(float2); \
+    constexpr int TX = warps_b<N>() * WF<N>::G;                                                 \
+    const size_t smem = std::max((size_t)(N) * (TX + 1), (size_t)warps_b<N>() * WF<N>::SWARP) * sizeof(float2); \
     cudaFuncSetAttribute(k_pass_b_w<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    k_pass_b_w<N><<<(unsigned)(((N) / 2 + 1) * ((N) / TX)), 32 * kWarpsAB, smem, s>>>(a);       \
+    k_pass_b_w<N><<<(unsigned)(((N) / 2 + 1) * ((N) / TX)), 32 * warps_b<N>(), smem, s>>>(a);  \
     return 1;                                                                                   \
   }
   switch (a.ng) {
